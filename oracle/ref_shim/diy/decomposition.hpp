@@ -1,0 +1,3 @@
+// Single-process DIY stand-in (test oracle only); all declarations live in types.hpp.
+#pragma once
+#include "types.hpp"
