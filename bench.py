@@ -1,0 +1,421 @@
+"""Benchmark: DTFE density of 2,097,152 particles onto a 512^3 grid.
+
+Workload (default): 50% uniform + 50% from 256 Gaussian clumps (sigma 0.01,
+Dirichlet(1) weights) in [0,1)^3, float32, unit mass, split into 2x2x2 DIY
+blocks with a 0.05 ghost zone; host Qhull tets per block (scipy "Qt", one
+process per block); DTFE, mixed precision (FP32 + FP64 fix-up), onto a 512^3
+float32 grid.  A step is one full DTFE pass over all blocks: star volumes,
+vertex densities, grid zeroing, tet rasterisation (+ FP64 fix-up pass).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value: grid points/s with particles and tets resident in HBM (tessgpu_batch_dense);
+e2e:   the same metric through the host-buffer call tessgpu_dense, host->device
+       copies of particles/tets/vert_to_tet from pinned memory and the grid
+       device->host copy inside the timed region.
+--impl reference times the reference's own estimator (DENSE_TESS, restated
+bit-exactly in oracle/) on the host cores, one process per block, on a sample
+of cells per block.
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DTFE grid pts/s, 2M pts->512^3, mixed vs FP64 at rel-L2<=1e-6"
+UNIT = "grid_pts/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--particles", type=int, default=2097152)
+    ap.add_argument("--grid", type=int, default=512)
+    ap.add_argument("--blocks", type=int, default=2, help="blocks per axis")
+    ap.add_argument("--ghost", type=float, default=0.05)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the FP64-mode and DENSE_TESS comparison runs")
+    return ap.parse_args()
+
+
+def prepare(args):
+    from tess2_gb300 import host
+    t0 = time.time()
+    pts = host.mixture_particles(args.particles, args.seed, frac_uniform=0.5, n_clumps=256, sigma=0.01)
+    blocks = host.decompose(pts, (args.blocks,) * 3, args.ghost)
+    blocks = host.tessellate(blocks, processes=min(len(blocks), os.cpu_count() or 1))
+    return blocks, time.time() - t0
+
+
+def workload_config(args, blocks):
+    T = sum(int(b["tets"].shape[0]) for b in blocks)
+    N = sum(int(b["particles"].shape[0]) for b in blocks)
+    G = args.grid ** 3
+    return dict(workload=f"DTFE {args.particles} particles (50% uniform + 50% 256 clumps sigma 0.01) -> "
+                         f"{args.grid}^3 float32, {args.blocks}x{args.blocks}x{args.blocks} blocks, ghost {args.ghost}",
+                particles=args.particles, particles_with_ghosts=N, tets=T, grid=[args.grid] * 3,
+                blocks=args.blocks ** 3, ghost=args.ghost, seed=args.seed, mode="mixed FP32 + FP64 fix-up",
+                l2="inputs and grid larger than L2 (tets+grid > 1 GB vs 126 MB L2); no flush")
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.device = device
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return dict(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), reasons=sorted(reasons), samples=len(sm))
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle: restated reference estimator and FP64 DTFE)
+# ---------------------------------------------------------------------------
+_W = {}
+
+
+def _worker_init(block, data6, gni):
+    _W["block"] = block
+    _W["data6"] = data6
+    _W["gni"] = gni
+
+
+def _tess_sample(ncells):
+    from oracle.oracle import Restated
+    b = dict(_W["block"])
+    b["num_orig"] = min(ncells, b["num_orig"])
+    t0 = time.perf_counter()
+    Restated().dense(0, [b], _W["gni"], data6=_W["data6"])
+    return time.perf_counter() - t0, b["num_orig"]
+
+
+def data_bounds6(blocks):
+    mn = np.min([b["bounds_min"] for b in blocks], axis=0)
+    mx = np.max([b["bounds_max"] for b in blocks], axis=0)
+    return np.concatenate([mn, mx]).astype(np.float32)
+
+
+def dtfe_cpu_baseline(blocks, gni, stride=16):
+    """FP64 DTFE oracle, one core, block 0, every stride-th tet rasterised;
+    extrapolated to the full workload."""
+    from oracle.oracle import Restated
+    O = Restated()
+    b0 = blocks[0]
+    d6 = data_bounds6(blocks)
+    t0 = time.perf_counter()
+    O.dtfe([b0], gni, want_owner=False, want_rho=False, data6=d6, raster_stride=10 ** 9)
+    t_w = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.dtfe([b0], gni, want_owner=False, want_rho=False, data6=d6, raster_stride=stride)
+    t_s = time.perf_counter() - t0
+    per_block = t_w + max(t_s - t_w, 0.0) * stride
+    total_tets = sum(b["tets"].shape[0] for b in blocks)
+    full = per_block * total_tets / b0["tets"].shape[0]
+    G = float(np.prod(gni))
+    return dict(value=G / full, unit=UNIT, cores=1, kind="port",
+                sample=f"FP64 DTFE oracle on block 0 ({b0['tets'].shape[0]} tets), star volumes over all tets, "
+                       f"every {stride}th tet rasterised; {t_w + t_s:.1f} s measured, {full:.0f} s extrapolated "
+                       f"for all {len(blocks)} blocks")
+
+
+def run_reference(args):
+    """--impl reference: the reference's DENSE_TESS (restated bit-exactly in
+    oracle/) on the host cores, one process per block, a sample of cells each."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    blocks, prep_s = prepare(args)
+    gni = [args.grid] * 3
+    d6 = data_bounds6(blocks)
+    cores = min(len(blocks), os.cpu_count() or 1)
+    total_cells = sum(b["num_orig"] for b in blocks)
+    sample_cells = max(200, min(4000, total_cells // (len(blocks) * 50)))
+    ctx = mp.get_context("spawn")
+    pools = [ctx.Pool(1, initializer=_worker_init, initargs=(b, d6, gni)) for b in blocks]
+    try:
+        def step():
+            t0 = time.perf_counter()
+            rs = [p.apply_async(_tess_sample, (sample_cells,)) for p in pools]
+            out = [r.get() for r in rs]
+            wall = time.perf_counter() - t0
+            done = sum(n for _, n in out)
+            return wall, done
+
+        for _ in range(args.warmup):
+            step()
+        walls = []
+        done = 0
+        for _ in range(args.steps):
+            w, done = step()
+            walls.append(w)
+    finally:
+        for p in pools:
+            p.close()
+            p.join()
+    wall = statistics.mean(walls)
+    # the blocks run in parallel (one process each); scale to all cells
+    t_full = wall * total_cells / done
+    G = float(np.prod(gni))
+    value = G / t_full
+    line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
+                ms_per_step=1e3 * t_full, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+                data="synthetic", impl="reference", config=workload_config(args, blocks),
+                cpu_baseline=dict(value=value, unit=UNIT, cores=cores, kind="port",
+                                  sample=f"reference DENSE_TESS estimator (restated bit-exactly), first {sample_cells} "
+                                         f"cells of each of {len(blocks)} blocks in parallel processes per step, "
+                                         f"scaled to all {total_cells} cells"),
+                e2e=dict(value=value, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                note="the reference has no DTFE; its own estimator for this path (dense() DENSE_TESS) is timed")
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    # host Qhull in spawned processes before the first CUDA call
+    blocks, prep_s = prepare(args)
+    import torch
+    from tess2_gb300 import build as tbuild
+    tbuild.build()
+    from tess2_gb300.api import DENSE_DTFE, DENSE_TESS, MODE_FP64, MODE_MIXED, Context
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    gni = [args.grid] * 3
+    G = int(np.prod(gni))
+    cfg = workload_config(args, blocks)
+    T, N = cfg["tets"], cfg["particles_with_ghosts"]
+
+    ctx = Context(local)
+    batch = ctx.upload(blocks)
+    grid = torch.empty(G, dtype=torch.float32, device=f"cuda:{local}")
+    gptr = grid.data_ptr()
+
+    def step(mode=MODE_MIXED):
+        batch.dense(DENSE_DTFE, gni, gptr, mode=mode, want_info=False)
+
+    # untimed warm-up
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx.set_timing(True)
+    launches0 = ctx.launches()
+    stage_sum = {}
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    ev0.record()
+    for _ in range(args.steps):
+        step()
+        for name, ms in ctx.stage_times():
+            stage_sum[name] = stage_sum.get(name, 0.0) + ms
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier()
+    launches = ctx.launches() - launches0
+    ctx.set_timing(False)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    stage_ms = {k: v / args.steps for k, v in stage_sum.items()}
+    value = world * G / (ms * 1e-3)
+
+    # the step's DTFE accounting (one more untimed call with info)
+    info = batch.dense(DENSE_DTFE, gni, gptr, mode=MODE_MIXED, want_info=True)
+    mixed = grid.clone()
+
+    extra = {}
+    if not args.no_extra:
+        # plain FP64 GPU path: the comparison target, and the judge at full size
+        for _ in range(2):
+            step(MODE_FP64)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        k64 = max(2, args.steps // 3)
+        e0.record()
+        for _ in range(k64):
+            step(MODE_FP64)
+        e1.record()
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1) / k64
+        info64 = batch.dense(DENSE_DTFE, gni, gptr, mode=MODE_FP64, want_info=True)
+        d = (mixed.double() - grid.double()).norm() / grid.double().norm()
+        extra["fp64_mode"] = dict(value=G / (ms64 * 1e-3), unit=UNIT, ms_per_step=ms64,
+                                  grid_pts_assigned=info64["grid_pts_assigned"])
+        extra["mixed_speedup_vs_fp64"] = ms64 / ms
+        extra["mixed_vs_fp64_rel_l2"] = float(d)
+        extra["owners_identical"] = info64["grid_pts_assigned"] == info["grid_pts_assigned"]
+        # the reference's estimator on the GPU (DENSE_TESS), same blocks and grid
+        batch.dense(DENSE_TESS, gni, gptr, want_info=False)
+        torch.cuda.synchronize()
+        e0.record()
+        kt = 2
+        for _ in range(kt):
+            batch.dense(DENSE_TESS, gni, gptr, want_info=False)
+        e1.record()
+        torch.cuda.synchronize()
+        mst = e0.elapsed_time(e1) / kt
+        extra["dense_tess_gpu"] = dict(value=G / (mst * 1e-3), unit=UNIT, ms_per_step=mst)
+
+    # roofline of the dominant kernel: the mixed rasteriser
+    # algorithmic bytes per launch: tet vertices 16 B/tet, particle positions
+    # 16 B and densities 4 B per particle (each read once), 4 B per grid point written
+    assigned = info["grid_pts_assigned"]
+    raster_bytes = 16.0 * T + 20.0 * N + 4.0 * assigned
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    r_ms = stage_ms.get("raster", float("nan"))
+    achieved = raster_bytes / (r_ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "dtfe_raster_traffic.json")))
+        if prof.get("grid") == args.grid and prof.get("particles") == args.particles:
+            traffic = prof.get("dram_bytes_per_launch")
+    except Exception:
+        pass
+    roofline = dict(bound="hbm", kernel="k_raster<float,true> (mixed DTFE rasteriser)", achieved=achieved, peak=hbm,
+                    unit="GB/s", frac=achieved / hbm, traffic=traffic, algorithmic_bytes=raster_bytes,
+                    kernel_ms=r_ms, peak_source=peak_src + " MEASURED_PEAKS.json hbm_gbs" if peak_src == "measured"
+                    else "fallback 6.8 TB/s")
+    # the whole step against the same peak: 32 B/tet + 64 B/particle + 8 B/grid point
+    step_bytes = 32.0 * T + 64.0 * N + 8.0 * G
+    step_roof = dict(algorithmic_bytes=step_bytes, achieved=step_bytes / (ms * 1e-3) / 1e9, frac=
+                     step_bytes / (ms * 1e-3) / 1e9 / hbm)
+
+    # end to end through the host-buffer call
+    e2e = None
+    if not args.no_e2e:
+        pinned = []
+        hblocks = []
+        for b in blocks:
+            nb = dict(b)
+            for k in ("particles", "tets", "vert_to_tet"):
+                a = np.ascontiguousarray(b[k])
+                t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0]).dtype, pin_memory=True)
+                t.numpy()[...] = a
+                pinned.append(t)
+                nb[k] = t.numpy()
+            hblocks.append(nb)
+        out = torch.empty((args.grid,) * 3, dtype=torch.float32, pin_memory=True).numpy()
+        for _ in range(2):
+            ctx.dense(DENSE_DTFE, hblocks, gni, out=out)
+        ke = max(2, args.steps // 2)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            ctx.dense(DENSE_DTFE, hblocks, gni, out=out)
+        te = (time.perf_counter() - t0) / ke
+        h2d = sum(b["particles"].nbytes + b["tets"].nbytes + b["vert_to_tet"].nbytes for b in blocks)
+        e2e = dict(value=G / te, unit=UNIT, ms_per_step=te * 1e3, h2d_bytes_per_step=int(h2d),
+                   d2h_bytes_per_step=int(4 * G), api="tessgpu_dense (host buffers)")
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = dtfe_cpu_baseline(blocks, gni)
+        except Exception as e:  # the baseline is reported, never the product path
+            cpu = dict(value=None, unit=UNIT, cores=1, kind="port", sample=f"failed: {e}")
+
+    if rank == 0:
+        line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
+                    ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+                    data="synthetic", config=cfg, roofline=roofline, cpu_baseline=cpu, e2e=e2e,
+                    gpu_launches=int(launches), clocks=clk, particles_per_s=world * args.particles / (ms * 1e-3),
+                    stage_ms=stage_ms, step_roofline=step_roof, fp64_fixup_tets=info["fp64_tets"],
+                    exact_tests=info["exact_tests"], grid_pts_assigned=assigned, host_prep_s=prep_s, **extra)
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

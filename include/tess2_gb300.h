@@ -1,0 +1,209 @@
+/*
+ * tess2_gb300 — GB300 (sm_103a) implementation of tess2's post-Delaunay
+ * geometry and density-estimation path, behind a plain C ABI.
+ *
+ * Everything here takes plain pointers and sizes.  Two families:
+ *
+ *  - Host-buffer entry points (tessgpu_fill_vert_to_tet, ..., tessgpu_dense):
+ *    the calls a tess2 caller makes where it calls the reference today.  They
+ *    take the same arrays as the reference functions they replace (cited on
+ *    each), copy them to the GPU, run, and copy results back.
+ *
+ *  - Device-resident batches (tessgpu_batch_*): blocks whose particles and
+ *    tets already live in GPU memory, for in-situ callers and for timing
+ *    the kernels without host copies.
+ *
+ * Tets use tess2's tet_t layout (include/tess/tet.h:4-7 in the reference):
+ * int verts[4]; int tets[4]; where tets[i] is the neighbour opposite
+ * verts[i] and -1 marks the convex hull.  Particles are float x,y,z triples.
+ * Density grids are float32, x fastest, as WriteGrid writes them
+ * (src/dense.cpp:831-850).
+ *
+ * Errors: every call returns a tessgpu_status; tessgpu_last_error() gives a
+ * message.  Device-side failures (a star or edge ring larger than the
+ * kernel's bound, malformed adjacency) are reported through a status word the
+ * kernels write; kernels never trap and every device loop is bounded.
+ */
+#ifndef TESS2_GB300_H
+#define TESS2_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tessgpu_status
+{
+    TESSGPU_OK                 = 0,
+    TESSGPU_ERR_INVALID        = 1,   /* bad argument */
+    TESSGPU_ERR_CUDA           = 2,   /* CUDA runtime error (message in tessgpu_last_error) */
+    TESSGPU_ERR_NO_DEVICE      = 3,
+    TESSGPU_ERR_STAR_OVERFLOW  = 4,   /* a vertex star exceeded TESSGPU_MAX_STAR tets */
+    TESSGPU_ERR_FACE_OVERFLOW  = 5,   /* a Voronoi cell exceeded TESSGPU_MAX_FACES faces */
+    TESSGPU_ERR_LINK_OVERFLOW  = 6,   /* an edge ring exceeded TESSGPU_MAX_LINK tets */
+    TESSGPU_ERR_BAD_MESH       = 7,   /* an index out of range or a broken adjacency */
+    TESSGPU_ERR_UNSUPPORTED    = 8
+} tessgpu_status;
+
+/* bounds of the device loops; larger inputs report the overflow codes */
+#define TESSGPU_MAX_STAR   512
+#define TESSGPU_MAX_FACES  128
+#define TESSGPU_MAX_LINK   256
+
+/* density estimators: DENSE_TESS and DENSE_CIC keep the reference's enum
+   values (include/tess/dense.hpp:33-38); DTFE is the tet-linear estimator */
+typedef enum tessgpu_alg
+{
+    TESSGPU_DENSE_TESS = 0,
+    TESSGPU_DENSE_CIC  = 1,
+    TESSGPU_DENSE_DTFE = 2
+} tessgpu_alg;
+
+/* arithmetic of the DTFE path */
+typedef enum tessgpu_mode
+{
+    TESSGPU_MODE_MIXED = 0,   /* FP32 geometry, FP64 fix-up of ill-conditioned tets */
+    TESSGPU_MODE_FP64  = 1    /* every geometric quantity in FP64 */
+} tessgpu_mode;
+
+typedef struct tessgpu_ctx tessgpu_ctx;
+typedef struct tessgpu_batch tessgpu_batch;
+
+/* One DIY block: dblock_t (include/tess/delaunay.h:38-63) plus the DBlock
+   bounds (include/tess/delaunay.hpp:18-23).  Pointers are host memory for
+   the host-buffer calls and device memory for tessgpu_batch_wrap_device. */
+typedef struct tessgpu_block
+{
+    int          gid;
+    float        bounds_min[3], bounds_max[3];       /* DBlock::bounds */
+    float        data_min[3], data_max[3];           /* DBlock::data_bounds */
+    int          num_orig_particles;
+    int          num_particles;
+    const float* particles;                          /* 3 * num_particles */
+    int          num_tets;
+    const int*   tets;                               /* 8 * num_tets (tet_t) */
+    const int*   vert_to_tet;                        /* num_particles, or NULL: computed on the GPU */
+} tessgpu_block;
+
+/* Grid and estimator parameters of dense() (src/dense.cpp:30-44). */
+typedef struct tessgpu_dense_params
+{
+    int   alg;                  /* tessgpu_alg */
+    int   mode;                 /* tessgpu_mode (DTFE only) */
+    int   num_given_bounds;     /* 0..3 */
+    float given_mins[3], given_maxs[3];
+    float mass;                 /* mass of one particle */
+    float eps;                  /* floating point tolerance (the reference's drivers use 1e-4) */
+    int   glo_num_idx[3];       /* global grid points per axis */
+} tessgpu_dense_params;
+
+/* Outputs of dense() besides the grid (src/dense.cpp:37-43, 1294-1300). */
+typedef struct tessgpu_dense_info
+{
+    float  data_mins[3], data_maxs[3];
+    float  grid_phys_mins[3], grid_phys_maxs[3], grid_step_size[3];
+    double max_dense;           /* largest grid density */
+    double tot_mass;            /* total deposited mass */
+    double check_mass;          /* cells that deposited (DENSE_TESS) or particles (DENSE_CIC) */
+    long long grid_pts_assigned;/* DTFE: grid points inside some tet */
+    long long fp64_tets;        /* DTFE mixed: tets recomputed in FP64 */
+    long long exact_tests;      /* DTFE: point-in-tet tests decided by exact arithmetic */
+} tessgpu_dense_info;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Create a context on a CUDA device; stream may be NULL (the legacy default
+   stream) or a cudaStream_t the caller owns. */
+tessgpu_status tessgpu_create(int device, void* stream, tessgpu_ctx** out);
+void           tessgpu_destroy(tessgpu_ctx* ctx);
+const char*    tessgpu_last_error(const tessgpu_ctx* ctx);
+tessgpu_status tessgpu_sync(tessgpu_ctx* ctx);
+/* number of kernel launches issued by this context so far */
+long long      tessgpu_launch_count(const tessgpu_ctx* ctx);
+
+/* Stage timing: when on, every dense call records CUDA events on the
+   context's stream between its stages; tessgpu_stage_times then returns up to
+   cap (name, milliseconds) pairs of the last call (after it has finished). */
+tessgpu_status tessgpu_set_timing(tessgpu_ctx* ctx, int on);
+int            tessgpu_stage_times(tessgpu_ctx* ctx, const char** names, float* ms, int cap);
+
+/* ---- host-buffer entry points ----------------------------------------- */
+
+/* replaces fill_vert_to_tet (src/tess.cpp:767-787): for each vertex the
+   highest-numbered tet that contains it, -1 for none */
+tessgpu_status tessgpu_fill_vert_to_tet(tessgpu_ctx* ctx, int num_particles, const int* tets,
+                                        int num_tets, int* vert_to_tet);
+
+/* replaces fill_circumcenters (src/volume.cpp:6-11) and circumcenter
+   (src/tet.cpp:37-66): 3 floats per tet, bit-identical to the reference */
+tessgpu_status tessgpu_fill_circumcenters(tessgpu_ctx* ctx, const float* particles, int num_particles,
+                                          const int* tets, int num_tets, float* circumcenters);
+
+/* replaces complete (src/tet.cpp:337-378) for vertices [0, n): 1 finite
+   Voronoi cell, 0 cell on the hull, -1 where vert_to_tet is -1 */
+tessgpu_status tessgpu_complete_all(tessgpu_ctx* ctx, const float* particles, int num_particles,
+                                    const int* tets, int num_tets, const int* vert_to_tet,
+                                    int n, int* out);
+
+/* replaces volume (src/volume.cpp:13-54) for vertices [0, n): Voronoi cell
+   volume bit-identical to the reference, -1 for infinite cells or vertices
+   in no tet.  areas (optional, may be NULL) receives the Voronoi cell's total
+   face area. */
+tessgpu_status tessgpu_volumes(tessgpu_ctx* ctx, const float* particles, int num_particles,
+                               const int* tets, int num_tets, const int* vert_to_tet,
+                               int n, float* volumes, float* areas);
+
+/* FP64 Voronoi cell volumes for vertices [0, n) (-1 for infinite cells). */
+tessgpu_status tessgpu_volumes_f64(tessgpu_ctx* ctx, const float* particles, int num_particles,
+                                   const int* tets, int num_tets, const int* vert_to_tet,
+                                   int n, double* volumes);
+
+/* replaces dense (src/dense.cpp:30-103) over nblocks blocks.  global_grid
+   (may be NULL) receives the whole grid, glo_num_idx[0]*[1]*[2] floats, x
+   fastest (what WriteGrid writes).  block_density (may be NULL) is an array of
+   nblocks host pointers; block b's array must hold
+   tessgpu_block_grid_points(...) floats and receives that block's density as
+   init_dense/est_dense/recvd_pts leave it.  info may be NULL. */
+tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tessgpu_block* blocks,
+                             const tessgpu_dense_params* params, float* global_grid,
+                             float** block_density, tessgpu_dense_info* info);
+
+/* BlockGridParams (src/dense.cpp:575-648) of block b for the grid that
+   dense() derives from params; writes min_idx[3], max_idx[3], num_idx[3] to
+   out9 and returns the block's number of grid points. */
+long long      tessgpu_block_grid_points(int nblocks, const tessgpu_block* blocks, int b,
+                                         const tessgpu_dense_params* params, int* out9);
+
+/* ---- device-resident batches ------------------------------------------ */
+
+/* Copy nblocks host blocks to the GPU once (particles, tets, vert_to_tet). */
+tessgpu_status tessgpu_batch_upload(tessgpu_ctx* ctx, int nblocks, const tessgpu_block* blocks,
+                                    tessgpu_batch** out);
+/* Wrap blocks whose particles/tets (and optionally vert_to_tet) pointers are
+   device memory; nothing is copied and the caller keeps ownership. */
+tessgpu_status tessgpu_batch_wrap_device(tessgpu_ctx* ctx, int nblocks, const tessgpu_block* blocks,
+                                         tessgpu_batch** out);
+void           tessgpu_batch_free(tessgpu_batch* batch);
+
+/* dense() on a device batch into a device grid (d_grid: glo_num_idx product
+   floats, x fastest).  Nothing is copied to or from the host except info. */
+tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* batch,
+                                   const tessgpu_dense_params* params, float* d_grid,
+                                   tessgpu_dense_info* info);
+
+/* Validation outputs of the last tessgpu_batch_dense call, copied to host:
+   cell_counts (DENSE_TESS: per original particle of every block in order,
+   the reference's CellGridPts result, -1 for a skipped cell), owner (DTFE:
+   the block-local tet index that holds each grid point, -1 for none),
+   rho (DTFE: per particle of every block in order).  Each may be NULL;
+   sizes are the caller's to know.  Requires tessgpu_batch_keep_debug(batch, 1)
+   before the tessgpu_batch_dense call. */
+tessgpu_status tessgpu_batch_keep_debug(tessgpu_batch* batch, int on);
+tessgpu_status tessgpu_batch_debug_outputs(tessgpu_ctx* ctx, tessgpu_batch* batch, int* cell_counts,
+                                           int* owner, float* rho);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

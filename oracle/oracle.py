@@ -121,8 +121,9 @@ class Oracle:
             raise ValueError("neighbor_edges overflow")
         return pairs[:2 * n].reshape(n, 2).copy(), bool(fin.value)
 
-    def dense(self, alg, blocks, glo_num_idx, mass=1.0, eps=1e-4, given=None, cell_counts=False):
-        """dense() into a global grid (z, y, x order, x fastest)."""
+    def dense(self, alg, blocks, glo_num_idx, mass=1.0, eps=1e-4, given=None, cell_counts=False, data6=None):
+        """dense() into a global grid (z, y, x order, x fastest).  data6 (restated
+        oracle only) fixes the data bounds, as DataBounds' all-reduce would."""
         arr, keep = make_blocks(blocks)
         gni = np.ascontiguousarray(glo_num_idx, dtype=np.int32)
         grid = np.zeros((gni[2], gni[1], gni[0]), np.float32)
@@ -139,9 +140,10 @@ class Oracle:
         if self.which == "oracle":
             total = sum(int(b["num_orig"]) for b in blocks)
             cc = np.zeros(max(total, 1), np.int32) if cell_counts else None
-            fn = self._l.f("dense")
+            fn = self._l.f("dense_bounds")
             fn.restype = ctypes.c_long
-            lost = fn(ctypes.c_int(alg), ctypes.c_int(len(blocks)), arr, ctypes.c_int(ngiven), _ptr(gmin),
+            db = None if data6 is None else np.ascontiguousarray(data6, np.float32)
+            lost = fn(ctypes.c_int(alg), ctypes.c_int(len(blocks)), arr, _ptr(db), ctypes.c_int(ngiven), _ptr(gmin),
                       _ptr(gmax), ctypes.c_float(mass), ctypes.c_float(eps), _ptr(gni), _ptr(grid),
                       _ptr(g6), _ptr(d6), _ptr(st), _ptr(cc))
             res["lost"] = int(lost)
@@ -208,7 +210,8 @@ class Restated(Oracle):
         p = np.ascontiguousarray(p, np.float32)
         return bool(self._l.f("tet_contains")(_ptr(particles), _ptr(tet), _ptr(p)))
 
-    def dtfe(self, blocks, glo_num_idx, mass=1.0, eps=1e-4, given=None, want_owner=True, want_rho=True):
+    def dtfe(self, blocks, glo_num_idx, mass=1.0, eps=1e-4, given=None, want_owner=True, want_rho=True,
+             data6=None, raster_stride=1):
         arr, keep = make_blocks(blocks)
         gni = np.ascontiguousarray(glo_num_idx, dtype=np.int32)
         grid = np.zeros((gni[2], gni[1], gni[0]), np.float32)
@@ -222,10 +225,12 @@ class Restated(Oracle):
             ngiven = 3
             gmin = np.ascontiguousarray(given[0], dtype=np.float32)
             gmax = np.ascontiguousarray(given[1], dtype=np.float32)
-        fn = self._l.f("dtfe_f64")
+        fn = self._l.f("dtfe_f64_sample")
         fn.restype = ctypes.c_long
-        n = fn(ctypes.c_int(len(blocks)), arr, ctypes.c_int(ngiven), _ptr(gmin), _ptr(gmax),
-               ctypes.c_float(mass), ctypes.c_float(eps), _ptr(gni), _ptr(grid), _ptr(rho), _ptr(owner), _ptr(g6))
+        db = None if data6 is None else np.ascontiguousarray(data6, np.float32)
+        n = fn(ctypes.c_int(len(blocks)), arr, _ptr(db), ctypes.c_int(ngiven), _ptr(gmin), _ptr(gmax),
+               ctypes.c_float(mass), ctypes.c_float(eps), _ptr(gni), ctypes.c_int(raster_stride), _ptr(grid),
+               _ptr(rho), _ptr(owner), _ptr(g6))
         del keep
         return dict(grid=grid, owner=owner, rho=rho[:nv] if rho is not None else None, assigned=int(n),
                     grid_min=g6[:3].copy(), grid_step=g6[3:].copy())

@@ -816,8 +816,20 @@ long orc_dense(int alg, int nblocks, const orc_block* blocks,
                float* global_grid, float* grid_out6, float* data_out6, double* stats3,
                int* cell_counts)
 {
+    return orc_dense_bounds(alg, nblocks, blocks, NULL, num_given_bounds, given_mins, given_maxs, mass, eps,
+                            glo_num_idx, global_grid, grid_out6, data_out6, stats3, cell_counts);
+}
+
+long orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float* data6,
+                      int num_given_bounds, const float* given_mins, const float* given_maxs,
+                      float mass, float eps, const int* glo_num_idx,
+                      float* global_grid, float* grid_out6, float* data_out6, double* stats3,
+                      int* cell_counts)
+{
     float data_mins[3], data_maxs[3], gmin[3], gmax[3], step[3];
     orc_data_bounds(nblocks, blocks, data_mins, data_maxs);
+    if (data6)
+        for (int i = 0; i < 3; ++i) { data_mins[i] = data6[i]; data_maxs[i] = data6[3 + i]; }
     orc_grid_step_params(num_given_bounds, given_mins, given_maxs, data_mins, data_maxs,
                          gmin, gmax, step, glo_num_idx);
     float max_dense = 0.0f, check_mass = 0.0f;
@@ -1191,8 +1203,21 @@ long orc_dtfe_f64(int nblocks, const orc_block* blocks,
                   float mass, float eps, const int* glo_num_idx,
                   float* global_grid, double* rho_out, int* owner_out, float* grid_out6)
 {
+    return orc_dtfe_f64_sample(nblocks, blocks, NULL, num_given_bounds, given_mins, given_maxs, mass, eps,
+                               glo_num_idx, 1, global_grid, rho_out, owner_out, grid_out6);
+}
+
+long orc_dtfe_f64_sample(int nblocks, const orc_block* blocks, const float* data6,
+                         int num_given_bounds, const float* given_mins, const float* given_maxs,
+                         float mass, float eps, const int* glo_num_idx, int raster_stride,
+                         float* global_grid, double* rho_out, int* owner_out, float* grid_out6)
+{
     float data_mins[3], data_maxs[3], gmin[3], gmax[3], step[3];
     orc_data_bounds(nblocks, blocks, data_mins, data_maxs);
+    if (data6)
+        for (int i = 0; i < 3; ++i) { data_mins[i] = data6[i]; data_maxs[i] = data6[3 + i]; }
+    if (raster_stride < 1)
+        raster_stride = 1;
     orc_grid_step_params(num_given_bounds, given_mins, given_maxs, data_mins, data_maxs,
                          gmin, gmax, step, glo_num_idx);
     size_t nx = glo_num_idx[0], ny = glo_num_idx[1], nz = glo_num_idx[2];
@@ -1230,7 +1255,7 @@ long orc_dtfe_f64(int nblocks, const orc_block* blocks,
         for (int v = 0; v < b->num_particles; ++v)
             rho[v] = W[v] > 0 ? 4.0 * (double)mass / W[v] : 0.0;
 
-        for (int t = 0; t < b->num_tets; ++t)
+        for (int t = 0; t < b->num_tets; t += raster_stride)
         {
             const orc_tet* tt = &b->tets[t];
             const float* a[4];

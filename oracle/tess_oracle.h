@@ -82,6 +82,14 @@ long  orc_dense(int alg, int nblocks, const orc_block* blocks,
                 float mass, float eps, const int* glo_num_idx,
                 float* global_grid, float* grid_out6, float* data_out6, double* stats3,
                 int* cell_counts);
+/* orc_dense with the data bounds given (data6: mins[3], maxs[3]), as every
+   rank sees them after DataBounds' all-reduce when one process holds one
+   block of a larger decomposition. */
+long  orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float* data6,
+                       int num_given_bounds, const float* given_mins, const float* given_maxs,
+                       float mass, float eps, const int* glo_num_idx,
+                       float* global_grid, float* grid_out6, float* data_out6, double* stats3,
+                       int* cell_counts);
 
 /* ---- part 2: FP64 judges ---- */
 void  orc_fill_circumcenters_f64(const float* particles, const orc_tet* tets, int num_tets, double* out);
@@ -104,6 +112,12 @@ long  orc_dtfe_f64(int nblocks, const orc_block* blocks,
                    int num_given_bounds, const float* given_mins, const float* given_maxs,
                    float mass, float eps, const int* glo_num_idx,
                    float* global_grid, double* rho_out, int* owner_out, float* grid_out6);
+/* orc_dtfe_f64 with explicit data bounds (may be NULL) that rasterises only
+   every raster_stride-th tet (a bounded sample for CPU timing). */
+long  orc_dtfe_f64_sample(int nblocks, const orc_block* blocks, const float* data6,
+                          int num_given_bounds, const float* given_mins, const float* given_maxs,
+                          float mass, float eps, const int* glo_num_idx, int raster_stride,
+                          float* global_grid, double* rho_out, int* owner_out, float* grid_out6);
 
 #ifdef __cplusplus
 }

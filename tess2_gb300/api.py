@@ -1,0 +1,317 @@
+"""Python mirror of tess2's geometry/density interface over the C ABI
+(include/tess2_gb300.h).  Names and argument meanings follow the reference:
+
+  fill_vert_to_tet   src/tess.cpp:767-787
+  fill_circumcenters src/volume.cpp:6-11      (circumcenter, src/tet.cpp:37-66)
+  complete           src/tet.cpp:337-378      (all vertices at once)
+  volume             src/volume.cpp:13-54     (all vertices at once)
+  dense              src/dense.cpp:30-103     (DENSE_TESS, DENSE_CIC, plus DENSE_DTFE)
+
+Everything runs in libtess2_gb300.so on the GPU; there is no CPU fallback.
+If the library is missing the calls raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+DENSE_TESS, DENSE_CIC, DENSE_DTFE = 0, 1, 2
+MODE_MIXED, MODE_FP64 = 0, 1
+
+_STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no CUDA device", 4: "star overflow",
+           5: "face overflow", 6: "edge ring overflow", 7: "malformed mesh", 8: "unsupported"}
+
+
+class TessGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"tessgpu status {code} ({_STATUS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Block(ctypes.Structure):
+    """tessgpu_block"""
+    _fields_ = [("gid", ctypes.c_int),
+                ("bounds_min", ctypes.c_float * 3), ("bounds_max", ctypes.c_float * 3),
+                ("data_min", ctypes.c_float * 3), ("data_max", ctypes.c_float * 3),
+                ("num_orig_particles", ctypes.c_int), ("num_particles", ctypes.c_int),
+                ("particles", ctypes.c_void_p), ("num_tets", ctypes.c_int),
+                ("tets", ctypes.c_void_p), ("vert_to_tet", ctypes.c_void_p)]
+
+
+class DenseParams(ctypes.Structure):
+    """tessgpu_dense_params"""
+    _fields_ = [("alg", ctypes.c_int), ("mode", ctypes.c_int), ("num_given_bounds", ctypes.c_int),
+                ("given_mins", ctypes.c_float * 3), ("given_maxs", ctypes.c_float * 3),
+                ("mass", ctypes.c_float), ("eps", ctypes.c_float), ("glo_num_idx", ctypes.c_int * 3)]
+
+
+class DenseInfo(ctypes.Structure):
+    """tessgpu_dense_info"""
+    _fields_ = [("data_mins", ctypes.c_float * 3), ("data_maxs", ctypes.c_float * 3),
+                ("grid_phys_mins", ctypes.c_float * 3), ("grid_phys_maxs", ctypes.c_float * 3),
+                ("grid_step_size", ctypes.c_float * 3),
+                ("max_dense", ctypes.c_double), ("tot_mass", ctypes.c_double), ("check_mass", ctypes.c_double),
+                ("grid_pts_assigned", ctypes.c_longlong), ("fp64_tets", ctypes.c_longlong),
+                ("exact_tests", ctypes.c_longlong)]
+
+    def as_dict(self):
+        return dict(data_mins=np.array(self.data_mins[:], np.float32), data_maxs=np.array(self.data_maxs[:], np.float32),
+                    grid_phys_mins=np.array(self.grid_phys_mins[:], np.float32),
+                    grid_phys_maxs=np.array(self.grid_phys_maxs[:], np.float32),
+                    grid_step_size=np.array(self.grid_step_size[:], np.float32),
+                    max_dense=self.max_dense, tot_mass=self.tot_mass, check_mass=self.check_mass,
+                    grid_pts_assigned=self.grid_pts_assigned, fp64_tets=self.fp64_tets,
+                    exact_tests=self.exact_tests)
+
+
+_LIB = None
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """The loaded libtess2_gb300.so (raises when it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path} is missing: build it with tess2_gb300.build.build()")
+        L = ctypes.CDLL(path)
+        sig = {
+            "tessgpu_create": (_I, [_I, _VP, ctypes.POINTER(_VP)]),
+            "tessgpu_destroy": (None, [_VP]),
+            "tessgpu_last_error": (ctypes.c_char_p, [_VP]),
+            "tessgpu_sync": (_I, [_VP]),
+            "tessgpu_launch_count": (ctypes.c_longlong, [_VP]),
+            "tessgpu_fill_vert_to_tet": (_I, [_VP, _I, _VP, _I, _VP]),
+            "tessgpu_fill_circumcenters": (_I, [_VP, _VP, _I, _VP, _I, _VP]),
+            "tessgpu_complete_all": (_I, [_VP, _VP, _I, _VP, _I, _VP, _I, _VP]),
+            "tessgpu_volumes": (_I, [_VP, _VP, _I, _VP, _I, _VP, _I, _VP, _VP]),
+            "tessgpu_volumes_f64": (_I, [_VP, _VP, _I, _VP, _I, _VP, _I, _VP]),
+            "tessgpu_dense": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP]),
+            "tessgpu_block_grid_points": (ctypes.c_longlong, [_I, _VP, _I, _VP, _VP]),
+            "tessgpu_batch_upload": (_I, [_VP, _I, _VP, ctypes.POINTER(_VP)]),
+            "tessgpu_batch_wrap_device": (_I, [_VP, _I, _VP, ctypes.POINTER(_VP)]),
+            "tessgpu_batch_free": (None, [_VP]),
+            "tessgpu_batch_dense": (_I, [_VP, _VP, _VP, _VP, _VP]),
+            "tessgpu_batch_keep_debug": (_I, [_VP, _I]),
+            "tessgpu_batch_debug_outputs": (_I, [_VP, _VP, _VP, _VP, _VP]),
+            "tessgpu_set_timing": (_I, [_VP, _I]),
+            "tessgpu_stage_times": (_I, [_VP, _VP, _VP, _I]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def make_blocks(blocks):
+    """blocks: dicts with particles (N,3) f32, tets (T,8) i32, optional
+    vert_to_tet (N,) i32, num_orig, bounds_min/max, data_min/max, gid."""
+    arr = (Block * len(blocks))()
+    keep = []
+    for i, b in enumerate(blocks):
+        p = np.ascontiguousarray(b["particles"], dtype=np.float32)
+        t = np.ascontiguousarray(b["tets"], dtype=np.int32).reshape(-1, 8)
+        v = b.get("vert_to_tet")
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.int32)
+        keep += [p, t, v]
+        blk = arr[i]
+        blk.gid = int(b.get("gid", i))
+        for d in range(3):
+            blk.bounds_min[d] = b["bounds_min"][d]
+            blk.bounds_max[d] = b["bounds_max"][d]
+            blk.data_min[d] = b.get("data_min", b["bounds_min"])[d]
+            blk.data_max[d] = b.get("data_max", b["bounds_max"])[d]
+        blk.num_orig_particles = int(b.get("num_orig", p.shape[0]))
+        blk.num_particles = int(p.shape[0])
+        blk.particles = p.ctypes.data
+        blk.num_tets = int(t.shape[0])
+        blk.tets = t.ctypes.data
+        blk.vert_to_tet = None if v is None else v.ctypes.data
+    return arr, keep
+
+
+def make_params(alg, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None):
+    p = DenseParams()
+    p.alg = int(alg)
+    p.mode = int(mode)
+    if given is not None:
+        p.num_given_bounds = 3
+        for d in range(3):
+            p.given_mins[d] = given[0][d]
+            p.given_maxs[d] = given[1][d]
+    p.mass = mass
+    p.eps = eps
+    for d in range(3):
+        p.glo_num_idx[d] = int(glo_num_idx[d])
+    return p
+
+
+class Context:
+    """tessgpu_ctx on one CUDA device; stream is a cudaStream_t handle or None."""
+
+    def __init__(self, device=0, stream=None):
+        self._h = _VP()
+        s = lib().tessgpu_create(device, stream, ctypes.byref(self._h))
+        if s != 0:
+            raise TessGpuError(s, "tessgpu_create failed")
+
+    def close(self):
+        if self._h:
+            lib().tessgpu_destroy(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, s):
+        if s != 0:
+            raise TessGpuError(s, lib().tessgpu_last_error(self._h).decode())
+
+    @property
+    def handle(self):
+        return self._h
+
+    def launches(self):
+        return lib().tessgpu_launch_count(self._h)
+
+    def set_timing(self, on=True):
+        self._check(lib().tessgpu_set_timing(self._h, 1 if on else 0))
+
+    def stage_times(self):
+        """[(stage, ms)] of the last dense call (CUDA events on the context's stream)."""
+        names = (ctypes.c_char_p * 32)()
+        ms = (ctypes.c_float * 32)()
+        n = lib().tessgpu_stage_times(self._h, names, ms, 32)
+        return [(names[i].decode(), float(ms[i])) for i in range(n)]
+
+    # --- reference-named calls -------------------------------------------
+    def fill_vert_to_tet(self, num_particles, tets):
+        tets = np.ascontiguousarray(tets, np.int32)
+        out = np.empty(num_particles, np.int32)
+        self._check(lib().tessgpu_fill_vert_to_tet(self._h, num_particles, _p(tets), tets.shape[0], _p(out)))
+        return out
+
+    def fill_circumcenters(self, tets, particles):
+        tets = np.ascontiguousarray(tets, np.int32)
+        particles = np.ascontiguousarray(particles, np.float32)
+        out = np.empty((tets.shape[0], 3), np.float32)
+        self._check(lib().tessgpu_fill_circumcenters(self._h, _p(particles), particles.shape[0], _p(tets),
+                                                     tets.shape[0], _p(out)))
+        return out
+
+    def complete(self, tets, vert_to_tet, particles, n=None):
+        tets = np.ascontiguousarray(tets, np.int32)
+        v = np.ascontiguousarray(vert_to_tet, np.int32)
+        particles = np.ascontiguousarray(particles, np.float32)
+        n = v.shape[0] if n is None else n
+        out = np.empty(n, np.int32)
+        self._check(lib().tessgpu_complete_all(self._h, _p(particles), particles.shape[0], _p(tets), tets.shape[0],
+                                               _p(v), n, _p(out)))
+        return out
+
+    def volume(self, vert_to_tet, tets, particles, n=None, areas=False):
+        tets = np.ascontiguousarray(tets, np.int32)
+        v = np.ascontiguousarray(vert_to_tet, np.int32)
+        particles = np.ascontiguousarray(particles, np.float32)
+        n = v.shape[0] if n is None else n
+        out = np.empty(n, np.float32)
+        ar = np.empty(n, np.float32) if areas else None
+        self._check(lib().tessgpu_volumes(self._h, _p(particles), particles.shape[0], _p(tets), tets.shape[0], _p(v),
+                                          n, _p(out), _p(ar)))
+        return (out, ar) if areas else out
+
+    def volume_f64(self, vert_to_tet, tets, particles, n=None):
+        tets = np.ascontiguousarray(tets, np.int32)
+        v = np.ascontiguousarray(vert_to_tet, np.int32)
+        particles = np.ascontiguousarray(particles, np.float32)
+        n = v.shape[0] if n is None else n
+        out = np.empty(n, np.float64)
+        self._check(lib().tessgpu_volumes_f64(self._h, _p(particles), particles.shape[0], _p(tets), tets.shape[0],
+                                              _p(v), n, _p(out)))
+        return out
+
+    def dense(self, alg, blocks, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, block_arrays=False,
+              global_grid=True, out=None):
+        """dense() over host blocks.  Returns dict(grid=(nz,ny,nx) float32, info=..., blocks=[...])."""
+        arr, keep = make_blocks(blocks)
+        p = make_params(alg, glo_num_idx, mass, eps, mode, given)
+        grid = None
+        if global_grid:
+            grid = out if out is not None else np.empty((glo_num_idx[2], glo_num_idx[1], glo_num_idx[0]), np.float32)
+        bd = None
+        barrays = None
+        if block_arrays:
+            barrays = []
+            ptrs = (ctypes.c_void_p * len(blocks))()
+            for i in range(len(blocks)):
+                n = lib().tessgpu_block_grid_points(len(blocks), arr, i, ctypes.byref(p), None)
+                a = np.empty(max(n, 0), np.float32)
+                barrays.append(a)
+                ptrs[i] = a.ctypes.data
+            bd = ptrs
+        info = DenseInfo()
+        self._check(lib().tessgpu_dense(self._h, len(blocks), arr, ctypes.byref(p), _p(grid), bd, ctypes.byref(info)))
+        del keep
+        return dict(grid=grid, info=info.as_dict(), blocks=barrays)
+
+    def upload(self, blocks):
+        return Batch(self, blocks, device=False)
+
+
+class Batch:
+    """tessgpu_batch: blocks resident on the GPU."""
+
+    def __init__(self, ctx, blocks, device=False):
+        self.ctx = ctx
+        self._arr, self._keep = make_blocks(blocks) if not device else blocks
+        self._h = _VP()
+        f = lib().tessgpu_batch_wrap_device if device else lib().tessgpu_batch_upload
+        ctx._check(f(ctx.handle, len(self._arr), self._arr, ctypes.byref(self._h)))
+        if not device:
+            self._keep = None   # host arrays were copied
+
+    def free(self):
+        if self._h:
+            lib().tessgpu_batch_free(self._h)
+            self._h = _VP()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def keep_debug(self, on=True):
+        self.ctx._check(lib().tessgpu_batch_keep_debug(self._h, 1 if on else 0))
+
+    def dense(self, alg, glo_num_idx, d_grid, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, want_info=True):
+        """dense() into the device grid at address d_grid (an int, e.g. torch tensor.data_ptr())."""
+        p = make_params(alg, glo_num_idx, mass, eps, mode, given)
+        info = DenseInfo() if want_info else None
+        self.ctx._check(lib().tessgpu_batch_dense(self.ctx.handle, self._h, ctypes.byref(p), ctypes.c_void_p(d_grid),
+                                                  ctypes.byref(info) if info is not None else None))
+        return info.as_dict() if info is not None else None
+
+    def debug_outputs(self, cells=None, grid_points=None, particles=None):
+        cc = np.empty(cells, np.int32) if cells else None
+        ow = np.empty(grid_points, np.int32) if grid_points else None
+        rh = np.empty(particles, np.float32) if particles else None
+        self.ctx._check(lib().tessgpu_batch_debug_outputs(self.ctx.handle, self._h, _p(cc), _p(ow), _p(rh)))
+        return cc, ow, rh

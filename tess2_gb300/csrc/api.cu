@@ -1,0 +1,879 @@
+// C ABI of tess2_gb300 (include/tess2_gb300.h): contexts, device batches,
+// host-buffer entry points that replace the reference's calls, and the host
+// side of dense() (grid parameters and block grid ranges).
+//
+// Host code here must evaluate GridStepParams/BlockGridParams with the
+// reference's FP32 rounding, so this file is built with
+// -Xcompiler -ffp-contract=off (gcc on aarch64 would otherwise fuse a*b+c).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include "kernels.h"
+
+using namespace tg;
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct tessgpu_ctx
+{
+    int          device = 0;
+    cudaStream_t stream = nullptr;
+    std::string  err;
+    long long    launches = 0;
+    Status*      d_status = nullptr;
+    Status*      h_status = nullptr;     // pinned
+    float*       d_max = nullptr;
+    // grow-only buffers reused by the host-buffer entry points
+    std::vector<std::pair<void*, size_t>> pool;
+    // stage timing
+    bool                     timing = false;
+    std::vector<cudaEvent_t> events;
+    std::vector<const char*> marks;
+    int                      nmarks = 0;
+};
+
+static void mark(tessgpu_ctx* c, const char* name)
+{
+    if (!c->timing) return;
+    if (c->nmarks >= (int)c->events.size())
+    {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c->events.push_back(e);
+        c->marks.push_back(nullptr);
+    }
+    cudaEventRecord(c->events[c->nmarks], c->stream);
+    c->marks[c->nmarks] = name;
+    c->nmarks++;
+}
+
+extern "C" tessgpu_status tessgpu_set_timing(tessgpu_ctx* ctx, int on)
+{
+    if (!ctx) return TESSGPU_ERR_INVALID;
+    ctx->timing = on != 0;
+    return TESSGPU_OK;
+}
+
+extern "C" int tessgpu_stage_times(tessgpu_ctx* ctx, const char** names, float* ms, int cap)
+{
+    if (!ctx || ctx->nmarks < 2) return 0;
+    cudaEventSynchronize(ctx->events[ctx->nmarks - 1]);
+    int n = 0;
+    for (int i = 1; i < ctx->nmarks && n < cap; ++i, ++n)
+    {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, ctx->events[i - 1], ctx->events[i]);
+        if (names) names[n] = ctx->marks[i];
+        if (ms) ms[n] = t;
+    }
+    return n;
+}
+
+static tessgpu_status set_err(tessgpu_ctx* c, tessgpu_status code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+static tessgpu_status cuda_check(tessgpu_ctx* c, cudaError_t e, const char* what)
+{
+    if (e == cudaSuccess)
+        return TESSGPU_OK;
+    return set_err(c, TESSGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                                        \
+    do {                                                                \
+        tessgpu_status _s = cuda_check(ctx, (call), #call);            \
+        if (_s != TESSGPU_OK) return _s;                                \
+    } while (0)
+
+static void* pool_get(tessgpu_ctx* c, int slot, size_t bytes, cudaError_t* e)
+{
+    if ((int)c->pool.size() <= slot)
+        c->pool.resize(slot + 1, { nullptr, 0 });
+    auto& p = c->pool[slot];
+    *e = cudaSuccess;
+    if (p.second < bytes)
+    {
+        if (p.first) cudaFree(p.first);
+        p.first = nullptr;
+        p.second = 0;
+        *e = cudaMalloc(&p.first, bytes ? bytes : 16);
+        if (*e != cudaSuccess)
+            return nullptr;
+        p.second = bytes;
+    }
+    return p.first;
+}
+
+extern "C" tessgpu_status tessgpu_create(int device, void* stream, tessgpu_ctx** out)
+{
+    if (!out) return TESSGPU_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0)
+    {
+        cudaGetLastError();
+        return TESSGPU_ERR_NO_DEVICE;
+    }
+    tessgpu_ctx* ctx = new tessgpu_ctx;
+    ctx->device = device;
+    ctx->stream = (cudaStream_t)stream;
+    tessgpu_status s;
+    if ((s = cuda_check(ctx, cudaSetDevice(device), "cudaSetDevice")) != TESSGPU_OK ||
+        (s = cuda_check(ctx, cudaMalloc(&ctx->d_status, sizeof(Status)), "cudaMalloc")) != TESSGPU_OK ||
+        (s = cuda_check(ctx, cudaMalloc(&ctx->d_max, sizeof(float)), "cudaMalloc")) != TESSGPU_OK ||
+        (s = cuda_check(ctx, cudaMallocHost(&ctx->h_status, sizeof(Status)), "cudaMallocHost")) != TESSGPU_OK)
+    {
+        tessgpu_destroy(ctx);
+        return s;
+    }
+    *out = ctx;
+    return TESSGPU_OK;
+}
+
+extern "C" void tessgpu_destroy(tessgpu_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    for (auto& p : ctx->pool)
+        if (p.first) cudaFree(p.first);
+    for (cudaEvent_t e : ctx->events)
+        cudaEventDestroy(e);
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->d_max) cudaFree(ctx->d_max);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    delete ctx;
+}
+
+extern "C" const char* tessgpu_last_error(const tessgpu_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+extern "C" long long tessgpu_launch_count(const tessgpu_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" tessgpu_status tessgpu_sync(tessgpu_ctx* ctx)
+{
+    if (!ctx) return TESSGPU_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return TESSGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dense() grid parameters on the host, in the reference's FP32 order
+// ---------------------------------------------------------------------------
+// DataBounds (src/dense.cpp:1221-1275)
+static void data_bounds(int nb, const tessgpu_block* b, float* mn, float* mx)
+{
+    for (int i = 0; i < nb; ++i)
+        for (int d = 0; d < 3; ++d)
+        {
+            if (i == 0 || b[i].bounds_min[d] < mn[d]) mn[d] = b[i].bounds_min[d];
+            if (i == 0 || b[i].bounds_max[d] > mx[d]) mx[d] = b[i].bounds_max[d];
+        }
+}
+
+// GridStepParams (src/dense.cpp:1712-1767)
+static void grid_step_params(const tessgpu_dense_params* p, const float* dmin, const float* dmax, float* gmin,
+                             float* gmax, float* step)
+{
+    float mds = dmax[0] - dmin[0];
+    if (dmax[1] - dmin[1] > mds) mds = dmax[1] - dmin[1];
+    if (dmax[2] - dmin[2] > mds) mds = dmax[2] - dmin[2];
+    for (int i = 0; i < 3; ++i)
+    {
+        gmin[i] = dmin[i] - (mds - (dmax[i] - dmin[i])) / 2.0;
+        gmax[i] = dmax[i] + (mds - (dmax[i] - dmin[i])) / 2.0;
+    }
+    for (int i = 0; i < 3 && i < p->num_given_bounds; ++i)
+    {
+        gmin[i] = p->given_mins[i];
+        gmax[i] = p->given_maxs[i];
+    }
+    for (int i = 0; i < 3; ++i)
+        step[i] = (gmax[i] - gmin[i]) / (p->glo_num_idx[i] - 1);
+}
+
+static void h_idx2phys(const int* gi, float* pos, const float* step, const float* gmin)
+{
+    for (int i = 0; i < 3; ++i)
+        pos[i] = gi[i] * step[i] + gmin[i];
+}
+static void h_phys2idx(const float* pos, int* gi, const float* step, const float* gmin)
+{
+    for (int i = 0; i < 3; ++i)
+        gi[i] = (int)((pos[i] - gmin[i]) / step[i]);
+}
+
+// BlockGridParams (src/dense.cpp:575-648)
+static void block_grid_params(const tessgpu_block& b, const float* gmin, const float* step, float eps,
+                              const float* dmin, const float* dmax, const int* gni, int* mn, int* mx, int* num)
+{
+    float pos[3];
+    h_phys2idx(b.bounds_min, mn, step, gmin);
+    h_idx2phys(mn, pos, step, gmin);
+    for (int i = 0; i < 3; ++i)
+        if (pos[i] < b.bounds_min[i]) mn[i]++;
+    h_phys2idx(b.bounds_max, mx, step, gmin);
+    h_idx2phys(mx, pos, step, gmin);
+    for (int i = 0; i < 3; ++i)
+        if (pos[i] + step[i] <= b.bounds_max[i]) mx[i]++;
+    for (int i = 0; i < 3; ++i)
+        if (std::fabs(dmin[i] + mx[i] * step[i] - b.bounds_max[i]) < eps &&
+            std::fabs(b.bounds_max[i] - dmax[i]) > step[i])
+            mx[i]--;
+    for (int i = 0; i < 3; ++i)
+        if (std::fabs(b.bounds_min[i] - dmin[i]) < step[i]) mn[i] = 0;
+    for (int i = 0; i < 3; ++i)
+        if (std::fabs(b.bounds_max[i] - dmax[i]) < step[i]) mx[i] = gni[i] - 1;
+    for (int i = 0; i < 3; ++i)
+        num[i] = mx[i] - mn[i] + 1;
+}
+
+static bool valid_params(const tessgpu_dense_params* p)
+{
+    if (!p) return false;
+    if (p->alg < 0 || p->alg > 2 || p->mode < 0 || p->mode > 1) return false;
+    if (p->num_given_bounds < 0 || p->num_given_bounds > 3) return false;
+    for (int i = 0; i < 3; ++i)
+        if (p->glo_num_idx[i] < 2) return false;
+    long long g = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
+    return g < (1LL << 40);
+}
+
+extern "C" long long tessgpu_block_grid_points(int nblocks, const tessgpu_block* blocks, int b,
+                                               const tessgpu_dense_params* p, int* out9)
+{
+    if (nblocks <= 0 || !blocks || b < 0 || b >= nblocks || !valid_params(p)) return -1;
+    float dmin[3], dmax[3], gmin[3], gmax[3], step[3];
+    data_bounds(nblocks, blocks, dmin, dmax);
+    grid_step_params(p, dmin, dmax, gmin, gmax, step);
+    int mn[3], mx[3], num[3];
+    block_grid_params(blocks[b], gmin, step, p->eps, dmin, dmax, p->glo_num_idx, mn, mx, num);
+    if (out9)
+        for (int i = 0; i < 3; ++i) { out9[i] = mn[i]; out9[3 + i] = mx[i]; out9[6 + i] = num[i]; }
+    return (long long)num[0] * num[1] * num[2];
+}
+
+// ---------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------
+struct tessgpu_batch
+{
+    tessgpu_ctx*           ctx = nullptr;
+    bool                   pooled = false;   // buffers belong to the context pool
+    int                    nb = 0;
+    std::vector<tessgpu_block> blocks;       // host copy of the descriptors (pointers not owned)
+    std::vector<BlockDesc> hb;
+    std::vector<int>       hc_off;
+    long long              N = 0, T = 0, C = 0;
+    BlockDesc*             d_blocks = nullptr;
+    int*                   d_c_off = nullptr;
+    float4*                pos = nullptr;
+    int4*                  tv = nullptr;
+    int4*                  tn = nullptr;
+    int*                   v2t = nullptr;
+    float4*                cc = nullptr;
+    double*                cc64 = nullptr;
+    bool                   cc_ok = false, cc64_ok = false;
+    // DTFE scratch
+    double*                W = nullptr;
+    float*                 rho32 = nullptr;
+    double*                rho64 = nullptr;
+    int*                   fix_list = nullptr;
+    int*                   fix_count = nullptr;
+    // validation outputs
+    bool                   keep_debug = false;
+    int*                   d_cell_counts = nullptr;
+    int*                   d_owner = nullptr;
+    long long              owner_n = 0;
+    int                    last_alg = -1;
+    std::vector<void*>     owned;            // device allocations to free (non-pooled)
+};
+
+enum PoolSlot
+{
+    SLOT_BLOCKS, SLOT_COFF, SLOT_POS, SLOT_TV, SLOT_TN, SLOT_V2T, SLOT_CC, SLOT_CC64, SLOT_W, SLOT_RHO32,
+    SLOT_RHO64, SLOT_FIX, SLOT_FIXN, SLOT_STAGE, SLOT_RAWPTR, SLOT_RAWV2T, SLOT_GRID, SLOT_CELLS, SLOT_OUT,
+    SLOT_OUT2, SLOT_COUNT
+};
+
+static cudaError_t balloc(tessgpu_batch* bt, int slot, size_t bytes, void** out)
+{
+    cudaError_t e;
+    if (bt->pooled)
+    {
+        *out = pool_get(bt->ctx, slot, bytes, &e);
+        return e;
+    }
+    e = cudaMalloc(out, bytes ? bytes : 16);
+    if (e == cudaSuccess)
+        bt->owned.push_back(*out);
+    return e;
+}
+#define BALLOC(slot, bytes, ptr)                                                            \
+    do {                                                                                    \
+        void* _p = nullptr;                                                                 \
+        tessgpu_status _s = cuda_check(ctx, balloc(bt, (slot), (bytes), &_p), "cudaMalloc"); \
+        if (_s != TESSGPU_OK) return _s;                                                    \
+        *(void**)&(ptr) = _p;                                                               \
+    } while (0)
+
+extern "C" void tessgpu_batch_free(tessgpu_batch* bt)
+{
+    if (!bt) return;
+    cudaSetDevice(bt->ctx->device);
+    for (void* p : bt->owned)
+        cudaFree(p);
+    delete bt;
+}
+
+__global__ void k_pack_pos(const float* const* raw, const BlockDesc* blocks, int nb, int total, float4* pos)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < total; p += gridDim.x * blockDim.x)
+    {
+        int lo = 0, hi = nb - 1;
+        while (lo < hi)
+        {
+            int mid = (lo + hi + 1) >> 1;
+            if (blocks[mid].p_off <= p) lo = mid; else hi = mid - 1;
+        }
+        const float* r = raw[lo] + 3 * (size_t)(p - blocks[lo].p_off);
+        pos[p] = make_float4(r[0], r[1], r[2], 0.0f);
+    }
+}
+
+static int grid_small(long long n)
+{
+    long long g = (n + 255) / 256;
+    return (int)(g < 1 ? 1 : (g > 4096 ? 4096 : g));
+}
+
+// build the device layout; device_ptrs says whether block pointers are device memory
+static tessgpu_status batch_build(tessgpu_ctx* ctx, int nb, const tessgpu_block* blocks, bool device_ptrs,
+                                  bool pooled, tessgpu_batch** out)
+{
+    if (!ctx || !out || nb <= 0 || !blocks) return set_err(ctx, TESSGPU_ERR_INVALID, "bad batch arguments");
+    for (int i = 0; i < nb; ++i)
+        if (blocks[i].num_particles < 0 || blocks[i].num_tets < 0 || blocks[i].num_orig_particles < 0 ||
+            blocks[i].num_orig_particles > blocks[i].num_particles ||
+            (blocks[i].num_particles && !blocks[i].particles) || (blocks[i].num_tets && !blocks[i].tets))
+            return set_err(ctx, TESSGPU_ERR_INVALID, "block " + std::to_string(i) + " is malformed");
+    CK(cudaSetDevice(ctx->device));
+    tessgpu_batch* bt = new tessgpu_batch;
+    *out = bt;
+    bt->ctx = ctx;
+    bt->pooled = pooled;
+    bt->nb = nb;
+    bt->blocks.assign(blocks, blocks + nb);
+    bt->hb.resize(nb);
+    bt->hc_off.resize(nb);
+    long long N = 0, T = 0, C = 0;
+    for (int i = 0; i < nb; ++i)
+    {
+        BlockDesc& d = bt->hb[i];
+        std::memset(&d, 0, sizeof(d));
+        d.gid = blocks[i].gid;
+        for (int k = 0; k < 3; ++k) { d.bmin[k] = blocks[i].bounds_min[k]; d.bmax[k] = blocks[i].bounds_max[k]; }
+        d.p_off = (int)N; d.np = blocks[i].num_particles; d.norig = blocks[i].num_orig_particles;
+        d.t_off = (int)T; d.nt = blocks[i].num_tets;
+        d.c_off = (int)C;
+        bt->hc_off[i] = (int)C;
+        N += blocks[i].num_particles;
+        T += blocks[i].num_tets;
+        C += blocks[i].num_orig_particles;
+    }
+    if (N >= (1LL << 31) || T >= (1LL << 31))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "batch larger than 2^31 particles or tets");
+    bt->N = N; bt->T = T; bt->C = C;
+    BALLOC(SLOT_BLOCKS, sizeof(BlockDesc) * nb, bt->d_blocks);
+    BALLOC(SLOT_COFF, sizeof(int) * nb, bt->d_c_off);
+    BALLOC(SLOT_POS, sizeof(float4) * N, bt->pos);
+    BALLOC(SLOT_TV, sizeof(int4) * T, bt->tv);
+    BALLOC(SLOT_TN, sizeof(int4) * T, bt->tn);
+    BALLOC(SLOT_V2T, sizeof(int) * N, bt->v2t);
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(bt->d_c_off, bt->hc_off.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+
+    // raw pointer tables (device pointers to each block's particles / tet_t / vert_to_tet)
+    std::vector<const void*> raw_pos(nb), raw_tets(nb), raw_v2t(nb);
+    bool have_v2t = true;
+    for (int i = 0; i < nb; ++i)
+        if (blocks[i].num_particles && !blocks[i].vert_to_tet) have_v2t = false;
+    float* stage_pos = nullptr;
+    int* stage_tets = nullptr;
+    int* stage_v2t = nullptr;
+    if (!device_ptrs)
+    {
+        // one staging buffer: xyz, then tet_t, then vert_to_tet
+        size_t bytes = sizeof(float) * 3 * N + sizeof(int) * 8 * T + (have_v2t ? sizeof(int) * N : 0);
+        char* stage;
+        BALLOC(SLOT_STAGE, bytes, stage);
+        stage_pos = (float*)stage;
+        stage_tets = (int*)(stage + sizeof(float) * 3 * N);
+        stage_v2t = (int*)(stage + sizeof(float) * 3 * N + sizeof(int) * 8 * T);
+        for (int i = 0; i < nb; ++i)
+        {
+            const BlockDesc& d = bt->hb[i];
+            if (d.np)
+                CK(cudaMemcpyAsync(stage_pos + 3 * (size_t)d.p_off, blocks[i].particles, sizeof(float) * 3 * d.np,
+                                   cudaMemcpyHostToDevice, s));
+            if (d.nt)
+                CK(cudaMemcpyAsync(stage_tets + 8 * (size_t)d.t_off, blocks[i].tets, sizeof(int) * 8 * d.nt,
+                                   cudaMemcpyHostToDevice, s));
+            if (have_v2t && d.np)
+                CK(cudaMemcpyAsync(stage_v2t + d.p_off, blocks[i].vert_to_tet, sizeof(int) * d.np,
+                                   cudaMemcpyHostToDevice, s));
+            raw_pos[i] = stage_pos + 3 * (size_t)d.p_off;
+            raw_tets[i] = stage_tets + 8 * (size_t)d.t_off;
+            raw_v2t[i] = stage_v2t + d.p_off;
+        }
+    }
+    else
+    {
+        for (int i = 0; i < nb; ++i)
+        {
+            raw_pos[i] = blocks[i].particles;
+            raw_tets[i] = blocks[i].tets;
+            raw_v2t[i] = blocks[i].vert_to_tet;
+        }
+    }
+    const void** d_raw;
+    BALLOC(SLOT_RAWPTR, sizeof(void*) * 3 * nb, d_raw);
+    std::vector<const void*> tbl(3 * nb);
+    for (int i = 0; i < nb; ++i) { tbl[i] = raw_pos[i]; tbl[nb + i] = raw_tets[i]; tbl[2 * nb + i] = raw_v2t[i]; }
+    CK(cudaMemcpyAsync(d_raw, tbl.data(), sizeof(void*) * 3 * nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
+    if (N)
+    {
+        k_pack_pos<<<grid_small(N), 256, 0, s>>>((const float* const*)d_raw, bt->d_blocks, nb, (int)N, bt->pos);
+        ctx->launches++;
+    }
+    launch_ingest((const int* const*)(d_raw + nb), bt->d_blocks, nb, (int)T, bt->tv, bt->tn, ctx->d_status, s);
+    ctx->launches += T ? 1 : 0;
+    if (have_v2t)
+    {
+        launch_v2t_from_local((const int* const*)(d_raw + 2 * nb), bt->d_blocks, nb, (int)N, bt->v2t,
+                              ctx->d_status, s);
+        ctx->launches += N ? 1 : 0;
+    }
+    else
+    {
+        CK(cudaMemsetAsync(bt->v2t, 0xff, sizeof(int) * N, s));
+        launch_vert_to_tet(bt->tv, (int)T, bt->v2t, s);
+        ctx->launches += T ? 1 : 0;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (ctx->h_status->code)
+        return set_err(ctx, (tessgpu_status)ctx->h_status->code,
+                       "malformed mesh at item " + std::to_string(ctx->h_status->detail));
+    return TESSGPU_OK;
+}
+
+extern "C" tessgpu_status tessgpu_batch_upload(tessgpu_ctx* ctx, int nb, const tessgpu_block* blocks,
+                                               tessgpu_batch** out)
+{
+    tessgpu_status s = batch_build(ctx, nb, blocks, false, false, out);
+    if (s != TESSGPU_OK && out && *out) { tessgpu_batch_free(*out); *out = nullptr; }
+    return s;
+}
+
+extern "C" tessgpu_status tessgpu_batch_wrap_device(tessgpu_ctx* ctx, int nb, const tessgpu_block* blocks,
+                                                    tessgpu_batch** out)
+{
+    tessgpu_status s = batch_build(ctx, nb, blocks, true, false, out);
+    if (s != TESSGPU_OK && out && *out) { tessgpu_batch_free(*out); *out = nullptr; }
+    return s;
+}
+
+extern "C" tessgpu_status tessgpu_batch_keep_debug(tessgpu_batch* bt, int on)
+{
+    if (!bt) return TESSGPU_ERR_INVALID;
+    bt->keep_debug = on != 0;
+    return TESSGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dense on a batch
+// ---------------------------------------------------------------------------
+static tessgpu_status finish_status(tessgpu_ctx* ctx)
+{
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const Status& st = *ctx->h_status;
+    if (st.code)
+    {
+        static const char* names[] = { "ok", "invalid", "cuda", "no device", "vertex star larger than TESSGPU_MAX_STAR",
+                                       "Voronoi cell with more than TESSGPU_MAX_FACES faces",
+                                       "edge ring longer than TESSGPU_MAX_LINK", "malformed mesh", "unsupported" };
+        const char* nm = (st.code > 0 && st.code < 9) ? names[st.code] : "error";
+        return set_err(ctx, (tessgpu_status)st.code, std::string(nm) + " at item " + std::to_string(st.detail));
+    }
+    return TESSGPU_OK;
+}
+
+static const float kTau = 4.0e-5f;   // mixed DTFE: FP64 for tets whose FP32 bound exceeds tau*|6V|
+
+extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* bt, const tessgpu_dense_params* p,
+                                              float* d_grid, tessgpu_dense_info* info)
+{
+    if (!ctx || !bt || !d_grid || !valid_params(p))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad dense arguments");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int nb = bt->nb;
+    float dmin[3], dmax[3], gmin[3], gmax[3], step[3];
+    data_bounds(nb, bt->blocks.data(), dmin, dmax);
+    grid_step_params(p, dmin, dmax, gmin, gmax, step);
+    GridDesc g;
+    for (int i = 0; i < 3; ++i)
+    {
+        g.gmin[i] = gmin[i]; g.step[i] = step[i]; g.dmin[i] = dmin[i]; g.dmax[i] = dmax[i];
+        g.n[i] = p->glo_num_idx[i];
+    }
+    g.eps = p->eps;
+    g.mass = p->mass;
+    g.div = step[0] * step[1] * step[2];   // src/dense.cpp:241-242
+    for (int i = 0; i < nb; ++i)
+    {
+        BlockDesc& d = bt->hb[i];
+        block_grid_params(bt->blocks[i], gmin, step, p->eps, dmin, dmax, p->glo_num_idx, d.gmin_idx, d.gmax_idx,
+                          d.gnum_idx);
+        // kernels write only inside the grid, whatever the block bounds
+        for (int k = 0; k < 3; ++k)
+        {
+            d.gmin_idx[k] = std::max(d.gmin_idx[k], 0);
+            d.gmax_idx[k] = std::min(d.gmax_idx[k], p->glo_num_idx[k] - 1);
+        }
+    }
+    CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
+    const long long G = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
+    ctx->nmarks = 0;
+    mark(ctx, "start");
+    CK(cudaMemsetAsync(d_grid, 0, sizeof(float) * G, s));
+    mark(ctx, "grid_zero");
+    bt->last_alg = p->alg;
+
+    if (p->alg == TESSGPU_DENSE_TESS)
+    {
+        if (!bt->cc_ok)
+        {
+            BALLOC(SLOT_CC, sizeof(float4) * bt->T, bt->cc);
+            launch_circumcenters(bt->pos, bt->tv, (int)bt->T, bt->cc, s);
+            ctx->launches += bt->T ? 1 : 0;
+            bt->cc_ok = !bt->pooled;
+            mark(ctx, "circumcenters");
+        }
+        int* counts = nullptr;
+        if (bt->keep_debug)
+        {
+            BALLOC(SLOT_CELLS, sizeof(int) * (bt->C ? bt->C : 1), bt->d_cell_counts);
+            counts = bt->d_cell_counts;
+        }
+        launch_cells(CELL_DENSE_TESS, bt->d_blocks, bt->d_c_off, nb, (int)bt->C, bt->pos, bt->tv, bt->tn, bt->v2t,
+                     bt->cc, nullptr, g, d_grid, nullptr, nullptr, nullptr, nullptr, counts, ctx->d_status, s);
+        ctx->launches += bt->C ? 1 : 0;
+        mark(ctx, "cells_dense_tess");
+    }
+    else if (p->alg == TESSGPU_DENSE_CIC)
+    {
+        launch_cic(bt->d_blocks, bt->d_c_off, nb, (int)bt->C, bt->pos, g, d_grid, ctx->d_status, s);
+        ctx->launches += bt->C ? 1 : 0;
+        mark(ctx, "cic");
+    }
+    else
+    {
+        BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
+        BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
+        BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
+        BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
+        BALLOC(SLOT_FIXN, sizeof(int), bt->fix_count);
+        int* owner = nullptr;
+        if (bt->keep_debug)
+        {
+            BALLOC(SLOT_OUT, sizeof(int) * G, bt->d_owner);
+            CK(cudaMemsetAsync(bt->d_owner, 0xff, sizeof(int) * G, s));
+            bt->owner_n = G;
+            owner = bt->d_owner;
+        }
+        CK(cudaMemsetAsync(bt->W, 0, sizeof(double) * bt->N, s));
+        CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
+        launch_star_volumes(p->mode, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->W, kTau, ctx->d_status, s);
+        mark(ctx, "star_volumes");
+        launch_densities(bt->W, (int)bt->N, p->mass, bt->rho32, bt->rho64, s);
+        mark(ctx, "densities");
+        launch_raster(p->mode, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, kTau, d_grid,
+                      owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
+        mark(ctx, "raster");
+        if (p->mode != TESSGPU_MODE_FP64)
+        {
+            launch_raster_fix(bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, d_grid, owner,
+                              bt->fix_list, bt->fix_count, ctx->d_status, s);
+            mark(ctx, "raster_fp64_fixup");
+        }
+        ctx->launches += (bt->T ? 1 : 0) + (bt->N ? 1 : 0) + (bt->T ? (p->mode == TESSGPU_MODE_FP64 ? 1 : 2) : 0);
+    }
+    double max_dense = 0.0;
+    if (info || p->alg != TESSGPU_DENSE_DTFE)
+    {
+        CK(cudaMemsetAsync(ctx->d_max, 0, sizeof(float), s));
+        launch_grid_max(d_grid, G, ctx->d_max, s);
+        ctx->launches++;
+        mark(ctx, "grid_max");
+    }
+    tessgpu_status st = finish_status(ctx);
+    if (info)
+    {
+        float mx = 0.0f;
+        CK(cudaMemcpy(&mx, ctx->d_max, sizeof(float), cudaMemcpyDeviceToHost));
+        max_dense = mx;
+        std::memset(info, 0, sizeof(*info));
+        for (int i = 0; i < 3; ++i)
+        {
+            info->data_mins[i] = dmin[i]; info->data_maxs[i] = dmax[i];
+            info->grid_phys_mins[i] = gmin[i]; info->grid_phys_maxs[i] = gmax[i]; info->grid_step_size[i] = step[i];
+        }
+        info->max_dense = max_dense;
+        info->tot_mass = ctx->h_status->tot_mass;
+        info->check_mass = (double)ctx->h_status->check_mass;
+        info->grid_pts_assigned = (long long)ctx->h_status->assigned;
+        info->fp64_tets = (long long)ctx->h_status->fp64_tets;
+        info->exact_tests = (long long)ctx->h_status->exact_tests;
+    }
+    return st;
+}
+
+extern "C" tessgpu_status tessgpu_batch_debug_outputs(tessgpu_ctx* ctx, tessgpu_batch* bt, int* cell_counts,
+                                                      int* owner, float* rho)
+{
+    if (!ctx || !bt) return TESSGPU_ERR_INVALID;
+    if (cell_counts)
+    {
+        if (!bt->d_cell_counts) return set_err(ctx, TESSGPU_ERR_INVALID, "no DENSE_TESS debug output kept");
+        CK(cudaMemcpy(cell_counts, bt->d_cell_counts, sizeof(int) * bt->C, cudaMemcpyDeviceToHost));
+    }
+    if (owner)
+    {
+        if (!bt->d_owner) return set_err(ctx, TESSGPU_ERR_INVALID, "no DTFE debug output kept");
+        CK(cudaMemcpy(owner, bt->d_owner, sizeof(int) * bt->owner_n, cudaMemcpyDeviceToHost));
+    }
+    if (rho)
+    {
+        if (!bt->rho32) return set_err(ctx, TESSGPU_ERR_INVALID, "no DTFE run on this batch");
+        CK(cudaMemcpy(rho, bt->rho32, sizeof(float) * bt->N, cudaMemcpyDeviceToHost));
+    }
+    return TESSGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// host-buffer entry points
+// ---------------------------------------------------------------------------
+static tessgpu_block single_block(const float* particles, int np, const int* tets, int nt, const int* v2t)
+{
+    tessgpu_block b;
+    std::memset(&b, 0, sizeof(b));
+    b.num_orig_particles = np;
+    b.num_particles = np;
+    b.particles = particles;
+    b.num_tets = nt;
+    b.tets = tets;
+    b.vert_to_tet = v2t;
+    for (int i = 0; i < 3; ++i) { b.bounds_max[i] = 1; b.data_max[i] = 1; }
+    return b;
+}
+
+extern "C" tessgpu_status tessgpu_fill_vert_to_tet(tessgpu_ctx* ctx, int num_particles, const int* tets, int num_tets,
+                                                   int* vert_to_tet)
+{
+    if (!ctx || num_particles < 0 || num_tets < 0 || (num_particles && !vert_to_tet) || (num_tets && !tets))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    if (!num_particles) return TESSGPU_OK;
+    // particles are not read by this call; a zero stand-in keeps the batch layout
+    std::vector<float> zero(3 * (size_t)num_particles, 0.0f);
+    tessgpu_block b = single_block(zero.data(), num_particles, tets, num_tets, nullptr);
+    tessgpu_batch* bt = nullptr;
+    tessgpu_status s = batch_build(ctx, 1, &b, false, true, &bt);
+    if (s == TESSGPU_OK)
+        s = cuda_check(ctx, cudaMemcpy(vert_to_tet, bt->v2t, sizeof(int) * num_particles, cudaMemcpyDeviceToHost),
+                       "cudaMemcpy");
+    tessgpu_batch_free(bt);
+    return s;
+}
+
+extern "C" tessgpu_status tessgpu_fill_circumcenters(tessgpu_ctx* ctx, const float* particles, int num_particles,
+                                                     const int* tets, int num_tets, float* out)
+{
+    if (!ctx || num_particles < 0 || num_tets < 0 || (num_tets && (!tets || !out || !particles)))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    if (!num_tets) return TESSGPU_OK;
+    std::vector<int> none(num_particles ? num_particles : 1, -1);
+    tessgpu_block b = single_block(particles, num_particles, tets, num_tets, none.data());
+    tessgpu_batch* bt = nullptr;
+    tessgpu_status s = batch_build(ctx, 1, &b, false, true, &bt);
+    if (s == TESSGPU_OK)
+    {
+        cudaError_t e;
+        float4* cc = (float4*)pool_get(ctx, SLOT_CC, sizeof(float4) * num_tets, &e);
+        s = cuda_check(ctx, e, "cudaMalloc");
+        if (s == TESSGPU_OK)
+        {
+            launch_circumcenters(bt->pos, bt->tv, num_tets, cc, ctx->stream);
+            ctx->launches++;
+            // float4 -> 3 floats per tet
+            s = cuda_check(ctx, cudaMemcpy2D(out, 3 * sizeof(float), cc, sizeof(float4), 3 * sizeof(float), num_tets,
+                                             cudaMemcpyDeviceToHost), "cudaMemcpy2D");
+        }
+    }
+    tessgpu_batch_free(bt);
+    return s;
+}
+
+static tessgpu_status cells_call(tessgpu_ctx* ctx, int mode, const float* particles, int num_particles,
+                                 const int* tets, int num_tets, const int* v2t, int n, int* out_i, float* out_f,
+                                 float* out_area, double* out_d)
+{
+    if (!ctx || n < 0 || n > num_particles || num_tets < 0 || (num_tets && !tets) || (num_particles && !particles))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    if (!n) return TESSGPU_OK;
+    tessgpu_block b = single_block(particles, num_particles, tets, num_tets, v2t);
+    b.num_orig_particles = n;
+    tessgpu_batch* bt = nullptr;
+    tessgpu_status s = batch_build(ctx, 1, &b, false, true, &bt);
+    if (s != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
+    cudaError_t e = cudaSuccess;
+    void* d_out = pool_get(ctx, SLOT_OUT, sizeof(double) * n, &e);
+    void* d_area = out_area ? pool_get(ctx, SLOT_OUT2, sizeof(float) * n, &e) : nullptr;
+    if ((s = cuda_check(ctx, e, "cudaMalloc")) != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
+    GridDesc g;
+    std::memset(&g, 0, sizeof(g));
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), ctx->stream));
+    if (mode == CELL_VOLUME || mode == CELL_DENSE_TESS)
+    {
+        float4* cc = (float4*)pool_get(ctx, SLOT_CC, sizeof(float4) * (num_tets ? num_tets : 1), &e);
+        if ((s = cuda_check(ctx, e, "cudaMalloc")) != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
+        launch_circumcenters(bt->pos, bt->tv, num_tets, cc, ctx->stream);
+        bt->cc = cc;
+        ctx->launches++;
+    }
+    if (mode == CELL_VOLUME_F64)
+    {
+        double* cc64 = (double*)pool_get(ctx, SLOT_CC64, sizeof(double) * 3 * (num_tets ? num_tets : 1), &e);
+        if ((s = cuda_check(ctx, e, "cudaMalloc")) != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
+        launch_circumcenters_f64(bt->pos, bt->tv, num_tets, cc64, ctx->stream);
+        bt->cc64 = cc64;
+        ctx->launches++;
+    }
+    launch_cells(mode, bt->d_blocks, bt->d_c_off, 1, n, bt->pos, bt->tv, bt->tn, bt->v2t, bt->cc, bt->cc64, g,
+                 nullptr, (int*)d_out, (float*)d_out, (float*)d_area, (double*)d_out, nullptr, ctx->d_status,
+                 ctx->stream);
+    ctx->launches++;
+    s = finish_status(ctx);
+    if (s == TESSGPU_OK)
+    {
+        size_t bytes = mode == CELL_VOLUME_F64 ? sizeof(double) * n : sizeof(int) * n;
+        void* host = mode == CELL_COMPLETE ? (void*)out_i : mode == CELL_VOLUME ? (void*)out_f : (void*)out_d;
+        s = cuda_check(ctx, cudaMemcpy(host, d_out, bytes, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (s == TESSGPU_OK && out_area)
+            s = cuda_check(ctx, cudaMemcpy(out_area, d_area, sizeof(float) * n, cudaMemcpyDeviceToHost), "cudaMemcpy");
+    }
+    tessgpu_batch_free(bt);
+    return s;
+}
+
+extern "C" tessgpu_status tessgpu_complete_all(tessgpu_ctx* ctx, const float* particles, int num_particles,
+                                               const int* tets, int num_tets, const int* v2t, int n, int* out)
+{
+    if (n && !out) return set_err(ctx, TESSGPU_ERR_INVALID, "null output");
+    return cells_call(ctx, CELL_COMPLETE, particles, num_particles, tets, num_tets, v2t, n, out, nullptr, nullptr,
+                      nullptr);
+}
+
+extern "C" tessgpu_status tessgpu_volumes(tessgpu_ctx* ctx, const float* particles, int num_particles, const int* tets,
+                                          int num_tets, const int* v2t, int n, float* volumes, float* areas)
+{
+    if (n && !volumes) return set_err(ctx, TESSGPU_ERR_INVALID, "null output");
+    return cells_call(ctx, CELL_VOLUME, particles, num_particles, tets, num_tets, v2t, n, nullptr, volumes, areas,
+                      nullptr);
+}
+
+extern "C" tessgpu_status tessgpu_volumes_f64(tessgpu_ctx* ctx, const float* particles, int num_particles,
+                                              const int* tets, int num_tets, const int* v2t, int n, double* volumes)
+{
+    if (n && !volumes) return set_err(ctx, TESSGPU_ERR_INVALID, "null output");
+    return cells_call(ctx, CELL_VOLUME_F64, particles, num_particles, tets, num_tets, v2t, n, nullptr, nullptr,
+                      nullptr, volumes);
+}
+
+__global__ void k_extract_box(const float* grid, int nx, int ny, const int* mn, const int* num, float* out)
+{
+    const long long n = (long long)num[0] * num[1] * num[2];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    {
+        const int x = (int)(i % num[0]);
+        const int y = (int)((i / num[0]) % num[1]);
+        const int z = (int)(i / ((long long)num[0] * num[1]));
+        out[i] = grid[((size_t)(mn[2] + z) * ny + (mn[1] + y)) * nx + (mn[0] + x)];
+    }
+}
+
+extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tessgpu_block* blocks,
+                                        const tessgpu_dense_params* p, float* global_grid, float** block_density,
+                                        tessgpu_dense_info* info)
+{
+    if (!ctx || nblocks <= 0 || !blocks || !valid_params(p))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad dense arguments");
+    tessgpu_batch* bt = nullptr;
+    tessgpu_status s = batch_build(ctx, nblocks, blocks, false, true, &bt);
+    if (s != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
+    const long long G = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
+    cudaError_t e;
+    float* d_grid = (float*)pool_get(ctx, SLOT_GRID, sizeof(float) * G, &e);
+    if ((s = cuda_check(ctx, e, "cudaMalloc")) != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
+    s = tessgpu_batch_dense(ctx, bt, p, d_grid, info);
+    if (s == TESSGPU_OK && global_grid)
+        s = cuda_check(ctx, cudaMemcpyAsync(global_grid, d_grid, sizeof(float) * G, cudaMemcpyDeviceToHost, ctx->stream),
+                       "cudaMemcpy");
+    if (s == TESSGPU_OK && block_density)
+    {
+        for (int i = 0; i < nblocks && s == TESSGPU_OK; ++i)
+        {
+            if (!block_density[i]) continue;
+            int out9[9];
+            long long n = tessgpu_block_grid_points(nblocks, blocks, i, p, out9);
+            if (n <= 0) continue;
+            bool inside = true;
+            for (int k = 0; k < 3; ++k)
+                if (out9[k] < 0 || out9[3 + k] >= p->glo_num_idx[k]) inside = false;
+            if (!inside)
+            {
+                s = set_err(ctx, TESSGPU_ERR_UNSUPPORTED,
+                            "block " + std::to_string(i) + "'s grid box reaches outside the grid");
+                break;
+            }
+            int* d_box = (int*)pool_get(ctx, SLOT_COUNT, sizeof(int) * 9, &e);
+            float* d_tmp = (float*)pool_get(ctx, SLOT_OUT2, sizeof(float) * n, &e);
+            if ((s = cuda_check(ctx, e, "cudaMalloc")) != TESSGPU_OK) break;
+            int box[6] = { out9[0], out9[1], out9[2], out9[6], out9[7], out9[8] };
+            CK(cudaMemcpyAsync(d_box, box, sizeof(box), cudaMemcpyHostToDevice, ctx->stream));
+            k_extract_box<<<grid_small(n), 256, 0, ctx->stream>>>(d_grid, p->glo_num_idx[0], p->glo_num_idx[1], d_box,
+                                                                  d_box + 3, d_tmp);
+            ctx->launches++;
+            s = cuda_check(ctx, cudaMemcpyAsync(block_density[i], d_tmp, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                                                ctx->stream), "cudaMemcpy");
+            if (s == TESSGPU_OK)
+                s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+        }
+    }
+    if (s == TESSGPU_OK)
+        s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    tessgpu_batch_free(bt);
+    return s;
+}

@@ -1,0 +1,39 @@
+// Host-side launchers of the tess2_gb300 kernels (one .cu per family).
+#pragma once
+#include <cuda_runtime.h>
+#include "common.cuh"
+
+namespace tg {
+
+// geometry.cu  (reference-order FP32, built with -fmad=false)
+void launch_ingest(const int* const* d_raw_tets, const BlockDesc* d_blocks, int nb, int total_tets,
+                   int4* tv, int4* tn, Status* st, cudaStream_t s);
+void launch_vert_to_tet(const int4* tv, int total_tets, int* v2t, cudaStream_t s);
+void launch_v2t_from_local(const int* const* d_raw_v2t, const BlockDesc* d_blocks, int nb, int total_particles,
+                           int* v2t, Status* st, cudaStream_t s);
+void launch_circumcenters(const float4* pos, const int4* tv, int total_tets, float4* cc, cudaStream_t s);
+void launch_circumcenters_f64(const float4* pos, const int4* tv, int total_tets, double* cc3, cudaStream_t s);
+
+enum CellMode { CELL_COMPLETE = 0, CELL_VOLUME = 1, CELL_DENSE_TESS = 2, CELL_VOLUME_F64 = 3 };
+// one warp per cell (the original particles of every block)
+void launch_cells(int mode, const BlockDesc* d_blocks, const int* d_cell_off, int nb, int total_cells,
+                  const float4* pos, const int4* tv, const int4* tn, const int* v2t, const float4* cc,
+                  const double* cc64, const GridDesc& g, float* grid, int* out_i, float* out_f, float* out_area,
+                  double* out_d, int* cell_counts, Status* st, cudaStream_t s);
+void launch_cic(const BlockDesc* d_blocks, const int* d_cell_off, int nb, int total_cells, const float4* pos,
+                const GridDesc& g, float* grid, Status* st, cudaStream_t s);
+void launch_grid_max(const float* grid, long long n, float* d_max, cudaStream_t s);
+
+// dtfe.cu  (built with -fmad=false; FMAs only where written)
+void launch_star_volumes(int mode, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos,
+                         const int4* tv, double* W, float tau, Status* st, cudaStream_t s);
+void launch_densities(const double* W, int total_particles, float mass, float* rho32, double* rho64,
+                      cudaStream_t s);
+void launch_raster(int mode, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos, const int4* tv,
+                   const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid, int* owner,
+                   int* fix_list, int* fix_count, Status* st, cudaStream_t s);
+void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos, const int4* tv,
+                       const float* rho32, const double* rho64, const GridDesc& g, float* grid, int* owner,
+                       const int* fix_list, const int* fix_count, Status* st, cudaStream_t s);
+
+}
