@@ -109,6 +109,8 @@ typedef struct tessgpu_dense_info
     long long grid_pts_assigned;/* DTFE: grid points inside some tet */
     long long fp64_tets;        /* DTFE mixed: tets recomputed in FP64 */
     long long exact_tests;      /* DTFE: point-in-tet tests decided by exact arithmetic */
+    long long rows_visited;     /* DTFE: grid rows the rasteriser examined */
+    long long points_tested;    /* DTFE: grid points the rasteriser classified */
 } tessgpu_dense_info;
 
 /* ---- context ---------------------------------------------------------- */

@@ -54,7 +54,8 @@ class DenseInfo(ctypes.Structure):
                 ("grid_step_size", ctypes.c_float * 3),
                 ("max_dense", ctypes.c_double), ("tot_mass", ctypes.c_double), ("check_mass", ctypes.c_double),
                 ("grid_pts_assigned", ctypes.c_longlong), ("fp64_tets", ctypes.c_longlong),
-                ("exact_tests", ctypes.c_longlong)]
+                ("exact_tests", ctypes.c_longlong), ("rows_visited", ctypes.c_longlong),
+                ("points_tested", ctypes.c_longlong)]
 
     def as_dict(self):
         return dict(data_mins=np.array(self.data_mins[:], np.float32), data_maxs=np.array(self.data_maxs[:], np.float32),
@@ -63,7 +64,8 @@ class DenseInfo(ctypes.Structure):
                     grid_step_size=np.array(self.grid_step_size[:], np.float32),
                     max_dense=self.max_dense, tot_mass=self.tot_mass, check_mass=self.check_mass,
                     grid_pts_assigned=self.grid_pts_assigned, fp64_tets=self.fp64_tets,
-                    exact_tests=self.exact_tests)
+                    exact_tests=self.exact_tests, rows_visited=self.rows_visited,
+                    points_tested=self.points_tested)
 
 
 _LIB = None

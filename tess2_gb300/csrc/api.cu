@@ -566,7 +566,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     {
         if (!bt->cc_ok)
         {
-            BALLOC(SLOT_CC, sizeof(float4) * bt->T, bt->cc);
+            if (!bt->cc || bt->pooled)
+                BALLOC(SLOT_CC, sizeof(float4) * bt->T, bt->cc);
             launch_circumcenters(bt->pos, bt->tv, (int)bt->T, bt->cc, s);
             ctx->launches += bt->T ? 1 : 0;
             bt->cc_ok = !bt->pooled;
@@ -575,7 +576,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         int* counts = nullptr;
         if (bt->keep_debug)
         {
-            BALLOC(SLOT_CELLS, sizeof(int) * (bt->C ? bt->C : 1), bt->d_cell_counts);
+            if (!bt->d_cell_counts || bt->pooled)
+                BALLOC(SLOT_CELLS, sizeof(int) * (bt->C ? bt->C : 1), bt->d_cell_counts);
             counts = bt->d_cell_counts;
         }
         launch_cells(CELL_DENSE_TESS, bt->d_blocks, bt->d_c_off, nb, (int)bt->C, bt->pos, bt->tv, bt->tn, bt->v2t,
@@ -591,24 +593,37 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     }
     else
     {
-        BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
-        BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
-        BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
-        BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
-        BALLOC(SLOT_FIXN, sizeof(int), bt->fix_count);
+        if (!bt->W || bt->pooled)
+        {
+            BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
+            BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
+            BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
+            BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
+            BALLOC(SLOT_FIXN, sizeof(int), bt->fix_count);
+        }
         int* owner = nullptr;
         if (bt->keep_debug)
         {
-            BALLOC(SLOT_OUT, sizeof(int) * G, bt->d_owner);
+            if (!bt->d_owner || bt->owner_n < G || bt->pooled)
+                BALLOC(SLOT_OUT, sizeof(int) * G, bt->d_owner);
             CK(cudaMemsetAsync(bt->d_owner, 0xff, sizeof(int) * G, s));
             bt->owner_n = G;
             owner = bt->d_owner;
         }
-        CK(cudaMemsetAsync(bt->W, 0, sizeof(double) * bt->N, s));
+        CK(cudaMemsetAsync(bt->W, 0, sizeof(unsigned long long) * bt->N, s));
         CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
-        launch_star_volumes(p->mode, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->W, kTau, ctx->d_status, s);
+        // fixed-point scale of the star-volume sums: any star volume is below
+        // the volume of the particles' bounding box; allow 8x the data box
+        double vbox = 8.0;
+        for (int i = 0; i < 3; ++i)
+            vbox *= std::max((double)dmax[i] - (double)dmin[i], 1e-30);
+        const int bits = 61 - (int)std::ceil(std::log2(vbox));
+        const double scale = std::ldexp(1.0, bits);
+        launch_star_volumes(p->mode, (int)bt->T, bt->pos, bt->tv, (unsigned long long*)bt->W, scale, kTau,
+                            ctx->d_status, s);
         mark(ctx, "star_volumes");
-        launch_densities(bt->W, (int)bt->N, p->mass, bt->rho32, bt->rho64, s);
+        launch_densities((const unsigned long long*)bt->W, (int)bt->N, p->mass, 1.0 / scale, bt->rho32, bt->rho64,
+                         ctx->d_status, s);
         mark(ctx, "densities");
         launch_raster(p->mode, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, kTau, d_grid,
                       owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
@@ -619,7 +634,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
                               bt->fix_list, bt->fix_count, ctx->d_status, s);
             mark(ctx, "raster_fp64_fixup");
         }
-        ctx->launches += (bt->T ? 1 : 0) + (bt->N ? 1 : 0) + (bt->T ? (p->mode == TESSGPU_MODE_FP64 ? 1 : 2) : 0);
+        ctx->launches += (bt->T ? (p->mode == TESSGPU_MODE_FP64 ? 2 : 3) : 0) + (bt->N ? 1 : 0);
     }
     double max_dense = 0.0;
     if (info || p->alg != TESSGPU_DENSE_DTFE)
@@ -647,6 +662,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         info->grid_pts_assigned = (long long)ctx->h_status->assigned;
         info->fp64_tets = (long long)ctx->h_status->fp64_tets;
         info->exact_tests = (long long)ctx->h_status->exact_tests;
+        info->rows_visited = (long long)ctx->h_status->rows;
+        info->points_tested = (long long)ctx->h_status->candidates;
     }
     return st;
 }

@@ -41,6 +41,8 @@ struct Status
     unsigned long long assigned;
     double tot_mass;
     unsigned long long check_mass;
+    unsigned long long rows;        // DTFE: grid rows visited
+    unsigned long long candidates;  // DTFE: grid points tested
 };
 
 __device__ __forceinline__ void fail(Status* st, int code, int detail)

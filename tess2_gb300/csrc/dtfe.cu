@@ -193,8 +193,13 @@ __device__ __forceinline__ float tet_vol6_f32(float3 a0, float3 a1, float3 a2, f
     return det;
 }
 
-__global__ void k_star_volumes(int mode, const BlockDesc* blocks, int nb, int total, const float4* pos,
-                               const int4* tv, double* W, float tau, Status* st)
+// Star volumes W_v are sums of the volumes of v's tets.  Each volume is
+// rounded once to a multiple of 2^-scale_bits and added with 64-bit integer
+// atomics: the sum is exact and independent of the order of the additions,
+// so W (and rho) is bit-reproducible.  scale_bits keeps any star volume below
+// 2^62 (the host derives it from the data bounds).
+__global__ void k_star_volumes(int mode, int total, const float4* pos, const int4* tv, unsigned long long* W,
+                               double scale, float tau, Status* st)
 {
     unsigned long long nfix = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
@@ -216,11 +221,11 @@ __global__ void k_star_volumes(int mode, const BlockDesc* blocks, int nb, int to
             else
                 vol = (double)(fabsf(d) / 6.0f);
         }
-        // FP64 sums in L2: the float32 terms add exactly for the usual exponent spread
-        atomicAdd(&W[vi.x], vol);
-        atomicAdd(&W[vi.y], vol);
-        atomicAdd(&W[vi.z], vol);
-        atomicAdd(&W[vi.w], vol);
+        const unsigned long long q = (unsigned long long)__double2ll_rn(vol * scale);
+        atomicAdd(&W[vi.x], q);
+        atomicAdd(&W[vi.y], q);
+        atomicAdd(&W[vi.z], q);
+        atomicAdd(&W[vi.w], q);
     }
     for (int o = 16; o > 0; o >>= 1)
         nfix += __shfl_xor_sync(FULL, nfix, o);
@@ -228,11 +233,16 @@ __global__ void k_star_volumes(int mode, const BlockDesc* blocks, int nb, int to
         atomicAdd(&st->fp64_tets, nfix);
 }
 
-__global__ void k_densities(const double* W, int n, float mass, float* rho32, double* rho64)
+// rho_v = (D+1) m / W_v = 4 m / W_v, 0 for a vertex in no tet
+__global__ void k_densities(const unsigned long long* W, int n, float mass, double inv_scale, float* rho32,
+                            double* rho64, Status* st)
 {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
     {
-        const double w = W[v];
+        const long long wi = (long long)W[v];
+        if (wi < 0)
+            fail(st, TESSGPU_ERR_UNSUPPORTED, v);   // star volume past the fixed-point range
+        const double w = (double)wi * inv_scale;
         const double r = w > 0.0 ? 4.0 * (double)mass / w : 0.0;
         rho32[v] = (float)r;
         rho64[v] = r;
@@ -336,174 +346,319 @@ __device__ __noinline__ bool inside_exact(float a00, float a01, float a02, float
     return true;
 }
 
-// One thread per tet.  Tets come from [0, total) or, when list is given,
-// from list[0 .. *list_count).
-// MIXED (T = float): FP32 classification and values; a tet whose summed
-//   bounds exceed tau * |6V| is appended to fix_list instead and left to the
-//   FP64 pass.
-// !MIXED (T = double): classification and values in FP64 (FP64 mode, and
-//   the fix-up pass over fix_list).
-template <typename T, bool MIXED>
-__global__ void __launch_bounds__(256)
+// Work decomposition: a warp takes 32 tets.  Each lane sets up one tet
+// (bounding box in grid indices, orientation, the four numerator planes with
+// their error bounds, interpolation weights) into shared memory; then the
+// warp walks the concatenated list of the 32 tets' grid rows (y, z pairs of
+// their boxes), one row per lane, so a tet spanning thousands of rows is
+// spread over the lanes instead of serialising one.  A row finds the x range
+// its four planes allow, tests those points with the filter (exact
+// arithmetic when it cannot decide) and writes the interpolated density of
+// every point inside.
+//
+// Instances:
+//   T=float,  VAL64=false, LIST=false  mixed main pass: FP32 classification and
+//       values; an ill-conditioned tet (summed bounds > tau * |6V|) is only
+//       appended to fix_list
+//   T=float,  VAL64=true,  LIST=true   mixed fix-up pass over fix_list: the same
+//       exact classification, values from an FP64 evaluation
+//   T=double, VAL64=true,  LIST=false  FP64 mode: everything in FP64
+constexpr int RW = 4;   // warps per block
+
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { typedef float4 type; };
+template <> struct Vec4<double> { typedef double4 type; };
+
+template <typename T, bool VAL64>
+struct __align__(16) RasterSmem
+{
+    typedef typename Vec4<T>::type T4;
+    float4 A0[32], A1[32], A2[32], A3[32];   // vertices; A0.w = bbox x lo, A1.w = bbox x hi
+    T4     C[4][32];                         // c_k.x, c_k.y, c_k.z, B_k
+    T4     W[32];                            // rho_k / 6V
+    float4 IC[32];                           // 1 / (s c_kx), 0 where c_kx == 0
+    int4   I0[32];                           // ix0, ix1, iy0, ny
+    int4   I1[32];                           // iz0, s, local tet index, unused
+    int    pre[33];
+    double C64[VAL64 && sizeof(T) == 4 ? 12 : 1][32];   // FP64 values for the fix-up pass
+    double W64[VAL64 && sizeof(T) == 4 ? 4 : 1][32];
+};
+
+template <typename T> __device__ __forceinline__ T comp4(const typename Vec4<T>::type& v, int i)
+{
+    return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
+}
+
+template <typename T, bool VAL64, bool LIST>
+__global__ void __launch_bounds__(RW * 32, 4)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
          int* fix_list, int* fix_count, Status* st)
 {
-    unsigned long long nexact = 0, nassigned = 0, nfix = 0;
-    const int n = list ? *list_count : total;
-    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < n; it += gridDim.x * blockDim.x)
+    typedef typename Vec4<T>::type T4;
+    __shared__ RasterSmem<T, VAL64> smem[RW];
+    constexpr bool F32 = sizeof(T) == 4;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    RasterSmem<T, VAL64>& S = smem[wid];
+    unsigned long long nexact = 0, nassigned = 0, nfix = 0, nrows = 0, ncand = 0;
+    const int n = LIST ? *list_count : total;
+    const int nchunks = (n + 31) / 32;
+    for (int chunk = blockIdx.x * RW + wid; chunk < nchunks; chunk += gridDim.x * RW)
     {
-        const int t = list ? list[it] : it;
-        const int b = find_blk(blocks, nb, t);
-        const int4 vi = __ldg(&tv[t]);
-        const int vid[4] = { vi.x, vi.y, vi.z, vi.w };
-        float a[4][3];
+        // ---- phase A: one tet per lane
+        const int it = chunk * 32 + lane;
+        int rows = 0;
+        if (it < n)
+        {
+            const int t = LIST ? list[it] : it;
+            const int b = find_blk(blocks, nb, t);
+            const int4 vi = __ldg(&tv[t]);
+            const int vid[4] = { vi.x, vi.y, vi.z, vi.w };
+            float a[4][3];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-        {
-            const float4 p4 = __ldg(&pos[vid[k]]);
-            a[k][0] = p4.x; a[k][1] = p4.y; a[k][2] = p4.z;
-        }
-        // index box: grid positions in [lo, hi) per axis (the perturbation
-        // moves points up, so a point on an upper bbox face is outside)
-        int ilo[3], ihi[3];
-        bool empty = false;
-        float lo[3], hi[3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-        {
-            lo[d] = fminf(fminf(a[0][d], a[1][d]), fminf(a[2][d], a[3][d]));
-            hi[d] = fmaxf(fmaxf(a[0][d], a[1][d]), fmaxf(a[2][d], a[3][d]));
-            const int olo = blocks[b].gmin_idx[d], ohi = blocks[b].gmax_idx[d];
-            ilo[d] = first_at_or_above(lo[d], g.gmin[d], g.step[d], olo, ohi);
-            ihi[d] = first_at_or_above(hi[d], g.gmin[d], g.step[d], olo, ohi + 1) - 1;
-            if (ihi[d] > ohi) ihi[d] = ohi;
-            if (ilo[d] > ihi[d]) empty = true;
-        }
-        if (empty)
-            continue;
-
-        // orientation s = sign(6V): filtered, exact when uncertain
-        const float3 A0 = make_float3(a[0][0], a[0][1], a[0][2]), A1 = make_float3(a[1][0], a[1][1], a[1][2]);
-        const float3 A2 = make_float3(a[2][0], a[2][1], a[2][2]), A3 = make_float3(a[3][0], a[3][1], a[3][2]);
-        int s;
-        T v6;
-        if (MIXED)
-        {
-            float vb;
-            const float v6f = tet_vol6_f32(A0, A1, A2, A3, vb);
-            v6 = v6f;
-            if (v6f > vb) s = 1;
-            else if (v6f < -vb) s = -1;
-            else s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1], a[2][2],
-                              a[3][0], a[3][1], a[3][2]);
-        }
-        else
-        {
-            v6 = (T)tet_vol6_f64(A0, A1, A2, A3);
-            s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1], a[2][2],
-                         a[3][0], a[3][1], a[3][2]);
-        }
-        if (s == 0)
-            continue;   // flat tet: no interior
-
-        T c[4][3], Bk[4];
-        numerators_setup<T>(a, lo, hi, c, Bk);
-        if (MIXED && (float)(Bk[0] + Bk[1] + Bk[2] + Bk[3]) > tau * fabsf((float)v6))
-        {
-            fix_list[atomicAdd(fix_count, 1)] = t;
-            nfix++;
-            continue;
-        }
-        T w[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            w[k] = (MIXED ? (T)__ldg(&rho32[vid[k]]) : (T)__ldg(&rho64[vid[k]])) / v6;
-
-        const T sf = (T)s;
-        const int t_local = t - blocks[b].t_off;
-        for (int zi = ilo[2]; zi <= ihi[2]; ++zi)
-        {
-            const float pzf = zi * g.step[2] + g.gmin[2];
-            for (int yi = ilo[1]; yi <= ihi[1]; ++yi)
+            for (int k = 0; k < 4; ++k)
             {
-                const float pyf = yi * g.step[1] + g.gmin[1];
-                // row constants and the x range that can hold inside points
-                T R[4];
-                T xmin = lo[0], xmax = hi[0];
-                bool row_empty = false;
+                const float4 p4 = __ldg(&pos[vid[k]]);
+                a[k][0] = p4.x; a[k][1] = p4.y; a[k][2] = p4.z;
+            }
+            int ilo[3], ihi[3];
+            bool empty = false;
+            float lo[3], hi[3];
 #pragma unroll
-                for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d)
+            {
+                lo[d] = fminf(fminf(a[0][d], a[1][d]), fminf(a[2][d], a[3][d]));
+                hi[d] = fmaxf(fmaxf(a[0][d], a[1][d]), fmaxf(a[2][d], a[3][d]));
+                const int olo = blocks[b].gmin_idx[d], ohi = blocks[b].gmax_idx[d];
+                ilo[d] = first_at_or_above(lo[d], g.gmin[d], g.step[d], olo, ohi);
+                ihi[d] = first_at_or_above(hi[d], g.gmin[d], g.step[d], olo, ohi + 1) - 1;
+                if (ihi[d] > ohi) ihi[d] = ohi;
+                if (ilo[d] > ihi[d]) empty = true;
+            }
+            int s = 0;
+            T v6 = 0;
+            if (!empty)
+            {
+                const float3 A0 = make_float3(a[0][0], a[0][1], a[0][2]), A1 = make_float3(a[1][0], a[1][1], a[1][2]);
+                const float3 A2 = make_float3(a[2][0], a[2][1], a[2][2]), A3 = make_float3(a[3][0], a[3][1], a[3][2]);
+                if (F32)
                 {
-                    const int base = k == 0 ? 1 : 0;
-                    const T qy = (T)pyf - (T)a[base][1], qz = (T)pzf - (T)a[base][2];
-                    R[k] = Real<T>::fma_(c[k][1], qy, c[k][2] * qz);
-                    const T cx = sf * c[k][0];
-                    const T rhs = -Bk[k] - sf * R[k];        // inside needs cx*qx >= rhs, up to rounding
-                    if (cx > 0)
-                        xmin = fmax(xmin, (T)a[base][0] + rhs / cx);
-                    else if (cx < 0)
-                        xmax = fmin(xmax, (T)a[base][0] + rhs / cx);
-                    else if (rhs > 0)
-                        row_empty = true;
+                    float vb;
+                    const float v6f = tet_vol6_f32(A0, A1, A2, A3, vb);
+                    v6 = v6f;
+                    if (v6f > vb) s = 1;
+                    else if (v6f < -vb) s = -1;
+                    else s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1],
+                                      a[2][2], a[3][0], a[3][1], a[3][2]);
                 }
-                const float slack = 2.0f * g.step[0];
-                if (row_empty || (float)xmin > hi[0] + slack || (float)xmax < lo[0] - slack)
-                    continue;
-                int i0 = ilo[0], i1 = ihi[0];
-                if ((float)xmin - slack > lo[0])
-                    i0 = max(i0, (int)floorf(((float)xmin - slack - g.gmin[0]) / g.step[0]));
-                if ((float)xmax + slack < hi[0])
-                    i1 = min(i1, (int)ceilf(((float)xmax + slack - g.gmin[0]) / g.step[0]));
-                const size_t row = ((size_t)zi * g.n[1] + yi) * g.n[0];
-                for (int xi = i0; xi <= i1; ++xi)
+                else
                 {
-                    const float pxf = xi * g.step[0] + g.gmin[0];
-                    const T px = pxf;
-                    T N[4];
-                    N[0] = Real<T>::fma_(c[0][0], px - (T)a[1][0], R[0]);
-                    const T qx = px - (T)a[0][0];
-                    N[1] = Real<T>::fma_(c[1][0], qx, R[1]);
-                    N[2] = Real<T>::fma_(c[2][0], qx, R[2]);
-                    N[3] = Real<T>::fma_(c[3][0], qx, R[3]);
-                    bool in = true, out = false;
-                    unsigned open = 0;
+                    v6 = (T)tet_vol6_f64(A0, A1, A2, A3);
+                    s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1], a[2][2],
+                                 a[3][0], a[3][1], a[3][2]);
+                }
+            }
+            if (!empty && s != 0)
+            {
+                T c[4][3], Bk[4];
+                numerators_setup<T>(a, lo, hi, c, Bk);
+                bool keep = true;
+                if (F32 && !VAL64 && fix_list &&
+                    (float)(Bk[0] + Bk[1] + Bk[2] + Bk[3]) > tau * fabsf((float)v6))
+                {
+                    fix_list[atomicAdd(fix_count, 1)] = t;   // values need FP64: the fix-up pass
+                    nfix++;
+                    keep = false;
+                }
+                if (keep)
+                {
+                    S.A0[lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
+                    S.A1[lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
+                    S.A2[lane] = make_float4(a[2][0], a[2][1], a[2][2], 0.0f);
+                    S.A3[lane] = make_float4(a[3][0], a[3][1], a[3][2], 0.0f);
+                    T w[4];
+                    float ic[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
                     {
-                        const T sn = sf * N[k];
-                        const bool ik = sn > Bk[k];
-                        in = in && ik;
-                        out = out || (sn < -Bk[k]);
-                        open |= (ik ? 0u : 1u) << k;
+                        T4 ck;
+                        ck.x = c[k][0]; ck.y = c[k][1]; ck.z = c[k][2]; ck.w = Bk[k];
+                        S.C[k][lane] = ck;
+                        w[k] = (F32 ? (T)__ldg(&rho32[vid[k]]) : (T)__ldg(&rho64[vid[k]])) / v6;
+                        const float cx = (float)((T)s * c[k][0]);
+                        ic[k] = cx != 0.0f ? 1.0f / cx : 0.0f;
                     }
-                    if (out)
-                        continue;
-                    if (!in)
+                    T4 w4;
+                    w4.x = w[0]; w4.y = w[1]; w4.z = w[2]; w4.w = w[3];
+                    S.W[lane] = w4;
+                    S.IC[lane] = make_float4(ic[0], ic[1], ic[2], ic[3]);
+                    if (VAL64 && F32)
                     {
-                        nexact++;
-                        if (!inside_exact(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1],
-                                          a[2][2], a[3][0], a[3][1], a[3][2], pxf, pyf, pzf, s, open))
-                            continue;
+                        double e[3][3], f1[3], f2[3];
+                        for (int k = 0; k < 3; ++k)
+                            for (int d = 0; d < 3; ++d)
+                                e[k][d] = (double)a[k + 1][d] - (double)a[0][d];
+                        for (int d = 0; d < 3; ++d)
+                        {
+                            f1[d] = (double)a[3][d] - (double)a[1][d];
+                            f2[d] = (double)a[2][d] - (double)a[1][d];
+                        }
+                        double cc[4][3];
+                        for (int j = 0; j < 3; ++j)
+                        {
+                            const int ja = (j + 1) % 3, jb = (j + 2) % 3;
+                            cc[0][j] = f1[ja] * f2[jb] - f1[jb] * f2[ja];
+                            cc[1][j] = e[1][ja] * e[2][jb] - e[1][jb] * e[2][ja];
+                            cc[2][j] = e[2][ja] * e[0][jb] - e[2][jb] * e[0][ja];
+                            cc[3][j] = e[0][ja] * e[1][jb] - e[0][jb] * e[1][ja];
+                        }
+                        const double v6d = e[0][0] * cc[1][0] + e[0][1] * cc[1][1] + e[0][2] * cc[1][2];
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            for (int j = 0; j < 3; ++j)
+                                S.C64[3 * k + j][lane] = cc[k][j];
+                            S.W64[k][lane] = __ldg(&rho64[vid[k]]) / v6d;
+                        }
                     }
-                    const T f = Real<T>::fma_(N[0], w[0], Real<T>::fma_(N[1], w[1],
-                                              Real<T>::fma_(N[2], w[2], N[3] * w[3])));
-                    grid[row + xi] = (float)f;
-                    if (owner)
-                        owner[row + xi] = t_local;
-                    nassigned++;
+                    S.I0[lane] = make_int4(ilo[0], ihi[0], ilo[1], ihi[1] - ilo[1] + 1);
+                    S.I1[lane] = make_int4(ilo[2], s, t - blocks[b].t_off, 0);
+                    rows = (ihi[1] - ilo[1] + 1) * (ihi[2] - ilo[2] + 1);
                 }
             }
         }
+        // exclusive prefix of the row counts
+        int incl = rows;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
+        }
+        S.pre[lane + 1] = incl;
+        if (lane == 0) S.pre[0] = 0;
+        __syncwarp();
+        const int R = S.pre[32];
+
+        // ---- phase B: one grid row per lane; each lane's tet index only grows
+        int j = 0;
+        for (int r = lane; r < R; r += 32)
+        {
+            while (S.pre[j + 1] <= r) ++j;
+            const int rr = r - S.pre[j];
+            const int4 I0 = S.I0[j];
+            const int4 I1 = S.I1[j];
+            const int ny = I0.w;
+            int zo = (int)(((float)rr + 0.5f) / (float)ny);
+            if (zo * ny > rr) --zo;
+            else if ((zo + 1) * ny <= rr) ++zo;
+            const int yi = I0.z + (rr - zo * ny);
+            const int zi = I1.x + zo;
+            const float pyf = yi * g.step[1] + g.gmin[1];
+            const float pzf = zi * g.step[2] + g.gmin[2];
+            const int s = I1.y;
+            const T sf = (T)s;
+            const float4 A0 = S.A0[j], A1 = S.A1[j];
+            const float4 IC = S.IC[j];
+            T R4[4], Bk[4], cx[4];
+            float xmin = A0.w, xmax = A1.w;
+            bool row_empty = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                const T4 ck = S.C[k][j];
+                const float by = k == 0 ? A1.y : A0.y, bz = k == 0 ? A1.z : A0.z, bx = k == 0 ? A1.x : A0.x;
+                const T qy = (T)pyf - (T)by, qz = (T)pzf - (T)bz;
+                R4[k] = Real<T>::fma_(ck.y, qy, ck.z * qz);
+                Bk[k] = ck.w;
+                cx[k] = ck.x;
+                const float rhs = (float)(-Bk[k] - sf * R4[k]);   // inside needs s*c_kx*qx >= rhs
+                const float ic = comp4<float>(IC, k);
+                if (ic > 0.0f)
+                    xmin = fmaxf(xmin, bx + rhs * ic);
+                else if (ic < 0.0f)
+                    xmax = fminf(xmax, bx + rhs * ic);
+                else if (rhs > 0.0f)
+                    row_empty = true;
+            }
+            const float slack = 2.0f * g.step[0];
+            nrows++;
+            if (row_empty || xmin > A1.w + slack || xmax < A0.w - slack || xmin > xmax + 2.0f * slack)
+                continue;
+            int i0 = I0.x, i1 = I0.y;
+            if (xmin - slack > A0.w)
+                i0 = max(i0, (int)floorf((xmin - slack - g.gmin[0]) / g.step[0]));
+            if (xmax + slack < A1.w)
+                i1 = min(i1, (int)ceilf((xmax + slack - g.gmin[0]) / g.step[0]));
+            const T4 W4 = S.W[j];
+            const size_t row = ((size_t)zi * g.n[1] + yi) * g.n[0];
+            ncand += i1 >= i0 ? i1 - i0 + 1 : 0;
+            for (int xi = i0; xi <= i1; ++xi)
+            {
+                const float pxf = xi * g.step[0] + g.gmin[0];
+                const T px = pxf;
+                T N[4];
+                N[0] = Real<T>::fma_(cx[0], px - (T)A1.x, R4[0]);
+                const T qx = px - (T)A0.x;
+                N[1] = Real<T>::fma_(cx[1], qx, R4[1]);
+                N[2] = Real<T>::fma_(cx[2], qx, R4[2]);
+                N[3] = Real<T>::fma_(cx[3], qx, R4[3]);
+                bool in = true, out = false;
+                unsigned open = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                {
+                    const T sn = sf * N[k];
+                    const bool ik = sn > Bk[k];
+                    in = in && ik;
+                    out = out || (sn < -Bk[k]);
+                    open |= (ik ? 0u : 1u) << k;
+                }
+                if (out)
+                    continue;
+                if (!in)
+                {
+                    nexact++;
+                    const float4 A2 = S.A2[j], A3 = S.A3[j];
+                    if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf,
+                                      pyf, pzf, s, open))
+                        continue;
+                }
+                float f;
+                if (!VAL64 || !F32)
+                    f = (float)Real<T>::fma_(N[0], W4.x, Real<T>::fma_(N[1], W4.y,
+                                             Real<T>::fma_(N[2], W4.z, N[3] * W4.w)));
+                else
+                {
+                    const double q1[3] = { (double)pxf - A1.x, (double)pyf - A1.y, (double)pzf - A1.z };
+                    const double q0[3] = { (double)pxf - A0.x, (double)pyf - A0.y, (double)pzf - A0.z };
+                    double acc = 0.0;
+                    for (int k = 0; k < 4; ++k)
+                    {
+                        const double* q = k == 0 ? q1 : q0;
+                        acc += (q[0] * S.C64[3 * k][j] + q[1] * S.C64[3 * k + 1][j] + q[2] * S.C64[3 * k + 2][j]) *
+                               S.W64[k][j];
+                    }
+                    f = (float)acc;
+                }
+                grid[row + xi] = f;
+                if (owner)
+                    owner[row + xi] = I1.z;
+                nassigned++;
+            }
+        }
+        __syncwarp();
     }
     for (int o = 16; o > 0; o >>= 1)
     {
         nexact += __shfl_xor_sync(FULL, nexact, o);
         nassigned += __shfl_xor_sync(FULL, nassigned, o);
         nfix += __shfl_xor_sync(FULL, nfix, o);
+        nrows += __shfl_xor_sync(FULL, nrows, o);
+        ncand += __shfl_xor_sync(FULL, ncand, o);
     }
-    if ((threadIdx.x & 31) == 0)
+    if (lane == 0)
     {
+        if (nrows) atomicAdd(&st->rows, nrows);
+        if (ncand) atomicAdd(&st->candidates, ncand);
         if (nexact) atomicAdd(&st->exact_tests, nexact);
         if (nassigned) atomicAdd(&st->assigned, nassigned);
         if (nfix) atomicAdd(&st->fp64_tets, nfix);
@@ -524,17 +679,18 @@ static int grid_for(long long n, int block, int per_sm)
     return (int)(need < cap ? need : cap);
 }
 
-void launch_star_volumes(int mode, const BlockDesc* d_blocks, int nb, int total, const float4* pos,
-                         const int4* tv, double* W, float tau, Status* st, cudaStream_t s)
+void launch_star_volumes(int mode, int total, const float4* pos, const int4* tv, unsigned long long* W,
+                         double scale, float tau, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
-    k_star_volumes<<<grid_for(total, 256, 8), 256, 0, s>>>(mode, d_blocks, nb, total, pos, tv, W, tau, st);
+    k_star_volumes<<<grid_for(total, 256, 8), 256, 0, s>>>(mode, total, pos, tv, W, scale, tau, st);
 }
 
-void launch_densities(const double* W, int n, float mass, float* rho32, double* rho64, cudaStream_t s)
+void launch_densities(const unsigned long long* W, int n, float mass, double inv_scale, float* rho32, double* rho64,
+                      Status* st, cudaStream_t s)
 {
     if (n <= 0) return;
-    k_densities<<<grid_for(n, 256, 8), 256, 0, s>>>(W, n, mass, rho32, rho64);
+    k_densities<<<grid_for(n, 256, 8), 256, 0, s>>>(W, n, mass, inv_scale, rho32, rho64, st);
 }
 
 void launch_raster(int mode, const BlockDesc* d_blocks, int nb, int total, const float4* pos, const int4* tv,
@@ -542,24 +698,25 @@ void launch_raster(int mode, const BlockDesc* d_blocks, int nb, int total, const
                    int* fix_list, int* fix_count, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
-    const int nblk = grid_for(total, 256, 8);
+    const int nblk = grid_for((long long)((total + 31) / 32) * 32 * 32, RW * 32, 16);
     if (mode == TESSGPU_MODE_FP64)
-        k_raster<double, false><<<nblk, 256, 0, s>>>(d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32, rho64, g,
-                                                      tau, grid, owner, nullptr, nullptr, st);
+        k_raster<double, true, false><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
+                                                                rho64, g, tau, grid, owner, nullptr, nullptr, st);
     else
-        k_raster<float, true><<<nblk, 256, 0, s>>>(d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32, rho64, g,
-                                                    tau, grid, owner, fix_list, fix_count, st);
+        k_raster<float, false, false><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
+                                                                rho64, g, tau, grid, owner, fix_list, fix_count, st);
 }
 
-// the ill-conditioned tets the mixed pass listed, in FP64; the launch is sized
-// for the longest possible list and reads the length on the device
+// the tets the mixed pass listed, with FP64 values; sized for the longest
+// possible list, the length is read on the device
 void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total, const float4* pos, const int4* tv,
                        const float* rho32, const double* rho64, const GridDesc& g, float* grid, int* owner,
                        const int* fix_list, const int* fix_count, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
-    k_raster<double, false><<<grid_for(total / 64 + 1, 256, 2), 256, 0, s>>>(
-        d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32, rho64, g, 0.0f, grid, owner, nullptr, nullptr, st);
+    const int nblk = grid_for((long long)((total / 16 + 31) / 32) * 32 * 32, RW * 32, 4);
+    k_raster<float, true, true><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32,
+                                                          rho64, g, 0.0f, grid, owner, nullptr, nullptr, st);
 }
 
 }  // namespace tg

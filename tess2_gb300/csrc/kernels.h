@@ -25,10 +25,10 @@ void launch_cic(const BlockDesc* d_blocks, const int* d_cell_off, int nb, int to
 void launch_grid_max(const float* grid, long long n, float* d_max, cudaStream_t s);
 
 // dtfe.cu  (built with -fmad=false; FMAs only where written)
-void launch_star_volumes(int mode, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos,
-                         const int4* tv, double* W, float tau, Status* st, cudaStream_t s);
-void launch_densities(const double* W, int total_particles, float mass, float* rho32, double* rho64,
-                      cudaStream_t s);
+void launch_star_volumes(int mode, int total_tets, const float4* pos, const int4* tv, unsigned long long* W,
+                         double scale, float tau, Status* st, cudaStream_t s);
+void launch_densities(const unsigned long long* W, int total_particles, float mass, double inv_scale, float* rho32,
+                      double* rho64, Status* st, cudaStream_t s);
 void launch_raster(int mode, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos, const int4* tv,
                    const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid, int* owner,
                    int* fix_list, int* fix_count, Status* st, cudaStream_t s);

@@ -73,9 +73,9 @@ def test_dense_single_block(gpu_ctx, name, alg, tag):
     r = gpu_ctx.dense(alg, single_block(d), gni)
     ref = d[f"{tag}_grid"]
     assert rel_l2(r["grid"], ref) < 1e-5
-    # single-hit grid points match bit for bit; count the rest
-    mism = np.count_nonzero(bits(r["grid"]) != bits(ref))
-    assert mism <= max(10, ref.size // 1000)
+    # points hit by one cell match bit for bit; points hit by several differ
+    # only by the order of their float additions (a few ulps)
+    assert np.allclose(r["grid"], ref, rtol=4e-6, atol=0.0)
     st = d[f"{tag}_stats"]
     assert r["info"]["check_mass"] == st[2]
     assert abs(r["info"]["tot_mass"] - st[1]) <= 1e-6 * st[1]
