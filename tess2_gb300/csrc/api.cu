@@ -541,6 +541,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     g.eps = p->eps;
     g.mass = p->mass;
     g.div = step[0] * step[1] * step[2];   // src/dense.cpp:241-242
+    for (int i = 0; i < 3; ++i)
+        g.inv_step[i] = 1.0f / step[i];
     for (int i = 0; i < nb; ++i)
     {
         BlockDesc& d = bt->hb[i];
@@ -614,7 +616,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
         // fixed-point scale of the star-volume sums: any star volume is below
         // the volume of the particles' bounding box; allow 8x the data box
-        double vbox = 8.0;
+        double vbox = 48.0;   // 6V sums of up to 8x the data box
         for (int i = 0; i < 3; ++i)
             vbox *= std::max((double)dmax[i] - (double)dmin[i], 1e-30);
         const int bits = 61 - (int)std::ceil(std::log2(vbox));

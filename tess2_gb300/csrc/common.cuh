@@ -29,6 +29,7 @@ struct GridDesc
     float dmin[3], dmax[3];      // data bounds
     int   n[3];                  // glo_num_idx
     float eps, mass, div;        // eps, particle mass, step0*step1*step2
+    float inv_step[3];           // 1 / step (index estimates only; exact checks follow)
 };
 
 // first failure wins; detail records the offending item

@@ -193,8 +193,9 @@ __device__ __forceinline__ float tet_vol6_f32(float3 a0, float3 a1, float3 a2, f
     return det;
 }
 
-// Star volumes W_v are sums of the volumes of v's tets.  Each volume is
-// rounded once to a multiple of 2^-scale_bits and added with 64-bit integer
+// Star volumes W_v are sums of the volumes of v's tets (accumulated as 6V,
+// the orientation determinants).  Each term is rounded once to a multiple of
+// 2^-scale_bits and added with 64-bit integer
 // atomics: the sum is exact and independent of the order of the additions,
 // so W (and rho) is bit-reproducible.  scale_bits keeps any star volume below
 // 2^62 (the host derives it from the data bounds).
@@ -208,18 +209,18 @@ __global__ void k_star_volumes(int mode, int total, const float4* pos, const int
         const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
         double vol;
         if (mode == TESSGPU_MODE_FP64)
-            vol = fabs(tet_vol6_f64(a0, a1, a2, a3)) / 6.0;
+            vol = fabs(tet_vol6_f64(a0, a1, a2, a3));
         else
         {
             float bound;
             const float d = tet_vol6_f32(a0, a1, a2, a3, bound);
             if (bound > tau * fabsf(d))
             {
-                vol = fabs(tet_vol6_f64(a0, a1, a2, a3)) / 6.0;
+                vol = fabs(tet_vol6_f64(a0, a1, a2, a3));
                 nfix++;
             }
             else
-                vol = (double)(fabsf(d) / 6.0f);
+                vol = (double)fabsf(d);
         }
         const unsigned long long q = (unsigned long long)__double2ll_rn(vol * scale);
         atomicAdd(&W[vi.x], q);
@@ -233,7 +234,8 @@ __global__ void k_star_volumes(int mode, int total, const float4* pos, const int
         atomicAdd(&st->fp64_tets, nfix);
 }
 
-// rho_v = (D+1) m / W_v = 4 m / W_v, 0 for a vertex in no tet
+// rho_v = (D+1) m / W_v = 4 m / W_v, 0 for a vertex in no tet.  The sums
+// hold 6x the volumes (the determinants), so rho = 24 m / sum.
 __global__ void k_densities(const unsigned long long* W, int n, float mass, double inv_scale, float* rho32,
                             double* rho64, Status* st)
 {
@@ -243,7 +245,7 @@ __global__ void k_densities(const unsigned long long* W, int n, float mass, doub
         if (wi < 0)
             fail(st, TESSGPU_ERR_UNSUPPORTED, v);   // star volume past the fixed-point range
         const double w = (double)wi * inv_scale;
-        const double r = w > 0.0 ? 4.0 * (double)mass / w : 0.0;
+        const double r = w > 0.0 ? 24.0 * (double)mass / w : 0.0;
         rho32[v] = (float)r;
         rho64[v] = r;
     }
@@ -253,9 +255,9 @@ __global__ void k_densities(const unsigned long long* W, int n, float mass, doub
 // rasterisation, one thread per tet
 // ---------------------------------------------------------------------------
 // first grid index whose position is >= x (positions are x_i = i*step + gmin in float)
-__device__ __forceinline__ int first_at_or_above(float x, float gmin, float step, int lo, int hi)
+__device__ __forceinline__ int first_at_or_above(float x, float gmin, float step, float inv_step, int lo, int hi)
 {
-    float f = (x - gmin) / step;
+    float f = (x - gmin) * inv_step;
     f = fminf(fmaxf(f, (float)lo - 2.0f), (float)hi + 2.0f);
     int i = (int)floorf(f);
     while (i > lo && (float)(i - 1) * step + gmin >= x) --i;
@@ -376,9 +378,9 @@ struct __align__(16) RasterSmem
     float4 A0[32], A1[32], A2[32], A3[32];   // vertices; A0.w = bbox x lo, A1.w = bbox x hi
     T4     C[4][32];                         // c_k.x, c_k.y, c_k.z, B_k
     T4     W[32];                            // rho_k / 6V
-    float4 IC[32];                           // 1 / (s c_kx), 0 where c_kx == 0
+    float4 XA[32], XB[32], XG[32];           // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
     int4   I0[32];                           // ix0, ix1, iy0, ny
-    int4   I1[32];                           // iz0, s, local tet index, unused
+    int4   I1[32];                           // iz0, s, local tet index, lower-bound face mask
     int    pre[33];
     double C64[VAL64 && sizeof(T) == 4 ? 12 : 1][32];   // FP64 values for the fix-up pass
     double W64[VAL64 && sizeof(T) == 4 ? 4 : 1][32];
@@ -430,8 +432,8 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                 lo[d] = fminf(fminf(a[0][d], a[1][d]), fminf(a[2][d], a[3][d]));
                 hi[d] = fmaxf(fmaxf(a[0][d], a[1][d]), fmaxf(a[2][d], a[3][d]));
                 const int olo = blocks[b].gmin_idx[d], ohi = blocks[b].gmax_idx[d];
-                ilo[d] = first_at_or_above(lo[d], g.gmin[d], g.step[d], olo, ohi);
-                ihi[d] = first_at_or_above(hi[d], g.gmin[d], g.step[d], olo, ohi + 1) - 1;
+                ilo[d] = first_at_or_above(lo[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi);
+                ihi[d] = first_at_or_above(hi[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi + 1) - 1;
                 if (ihi[d] > ohi) ihi[d] = ohi;
                 if (ilo[d] > ihi[d]) empty = true;
             }
@@ -477,21 +479,68 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                     S.A2[lane] = make_float4(a[2][0], a[2][1], a[2][2], 0.0f);
                     S.A3[lane] = make_float4(a[3][0], a[3][1], a[3][2], 0.0f);
                     T w[4];
-                    float ic[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
                     {
                         T4 ck;
                         ck.x = c[k][0]; ck.y = c[k][1]; ck.z = c[k][2]; ck.w = Bk[k];
                         S.C[k][lane] = ck;
-                        w[k] = (F32 ? (T)__ldg(&rho32[vid[k]]) : (T)__ldg(&rho64[vid[k]])) / v6;
-                        const float cx = (float)((T)s * c[k][0]);
-                        ic[k] = cx != 0.0f ? 1.0f / cx : 0.0f;
+                        w[k] = F32 ? (T)(__ldg(&rho32[vid[k]]) * __frcp_rn((float)v6))
+                                   : (T)__ldg(&rho64[vid[k]]) / v6;
                     }
                     T4 w4;
                     w4.x = w[0]; w4.y = w[1]; w4.z = w[2]; w4.w = w[3];
                     S.W[lane] = w4;
-                    S.IC[lane] = make_float4(ic[0], ic[1], ic[2], ic[3]);
+                    // Row-wise x bounds.  Inside needs s*N_k >= -B_k, N_k = c_kx (x - bx)
+                    // + R_k(y, z); along row (dy, dz) of the box this is x >= bnd_k
+                    // (s c_kx > 0) or x <= bnd_k (s c_kx < 0) with
+                    //   bnd_k = bx - s B_k / c_kx - R_k / c_kx, affine in (dy, dz).
+                    // E_k covers the rounding of the coefficients, of the float grid
+                    // positions against the affine form, and of N_k's own evaluation,
+                    // so a point outside [max lower, min upper] fails the per-point
+                    // test for some face.  c_kx == 0 gives no x bound.
+                    {
+                        const float h1 = g.step[1], h2 = g.step[2];
+                        const float py0 = ilo[1] * h1 + g.gmin[1], pz0 = ilo[2] * h2 + g.gmin[2];
+                        const float ymx = fmaxf(fabsf(py0), fabsf(ihi[1] * h1 + g.gmin[1]));
+                        const float zmx = fmaxf(fabsf(pz0), fabsf(ihi[2] * h2 + g.gmin[2]));
+                        const float xmx = fmaxf(fabsf(lo[0]), fabsf(hi[0]));
+                        const int ny = ihi[1] - ilo[1] + 1, nz = ihi[2] - ilo[2] + 1;
+                        float xa[4], xb[4], xg[4];
+                        int lower = 0;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            const int base = k == 0 ? 1 : 0;
+                            const float bx = a[base][0], by = a[base][1], bz = a[base][2];
+                            const float cx = (float)c[k][0], cy = (float)c[k][1], cz = (float)c[k][2];
+                            const float B = (float)Bk[k];
+                            if (cx == 0.0f)
+                            {
+                                xa[k] = 0.0f; xb[k] = 0.0f; xg[k] = 0.0f;
+                                lower |= 1 << (4 + k);   // no x bound from this face
+                                continue;
+                            }
+                            const float icx = __frcp_rn(cx);
+                            const float R0 = cy * (py0 - by) + cz * (pz0 - bz);
+                            const float alpha = bx - (float)s * B * icx - R0 * icx;
+                            const float beta = -cy * h1 * icx, gamma = -cz * h2 * icx;
+                            const float E = 32.0f * EPS32 *
+                                (fabsf(bx) + xmx + fabsf(alpha) + fabsf(B * icx) + fabsf(R0 * icx) +
+                                 fabsf(beta) * ny + fabsf(gamma) * nz +
+                                 (fabsf(cy) * (ymx + fabsf(by)) + fabsf(cz) * (zmx + fabsf(bz))) * fabsf(icx)) +
+                                1e-30f;
+                            const bool lo_face = (float)s * cx > 0.0f;
+                            lower |= lo_face ? 1 << k : 0;
+                            xa[k] = lo_face ? alpha - E : alpha + E;
+                            xb[k] = beta;
+                            xg[k] = gamma;
+                        }
+                        S.XA[lane] = make_float4(xa[0], xa[1], xa[2], xa[3]);
+                        S.XB[lane] = make_float4(xb[0], xb[1], xb[2], xb[3]);
+                        S.XG[lane] = make_float4(xg[0], xg[1], xg[2], xg[3]);
+                        S.I1[lane] = make_int4(ilo[2], s, t - blocks[b].t_off, lower);
+                    }
                     if (VAL64 && F32)
                     {
                         double e[3][3], f1[3], f2[3];
@@ -521,7 +570,6 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         }
                     }
                     S.I0[lane] = make_int4(ilo[0], ihi[0], ilo[1], ihi[1] - ilo[1] + 1);
-                    S.I1[lane] = make_int4(ilo[2], s, t - blocks[b].t_off, 0);
                     rows = (ihi[1] - ilo[1] + 1) * (ihi[2] - ilo[2] + 1);
                 }
             }
@@ -547,47 +595,58 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
             const int4 I0 = S.I0[j];
             const int4 I1 = S.I1[j];
             const int ny = I0.w;
-            int zo = (int)(((float)rr + 0.5f) / (float)ny);
+            int zo = (int)(((float)rr + 0.5f) * __frcp_rn((float)ny));
             if (zo * ny > rr) --zo;
             else if ((zo + 1) * ny <= rr) ++zo;
-            const int yi = I0.z + (rr - zo * ny);
+            const int dy = rr - zo * ny;
+            const int yi = I0.z + dy;
             const int zi = I1.x + zo;
+            const float4 A0 = S.A0[j], A1 = S.A1[j];
+            // x range of this row from the four affine face bounds
+            float xmin = A0.w, xmax = A1.w;
+            {
+                const float4 XA = S.XA[j], XB = S.XB[j], XG = S.XG[j];
+                const float fdy = (float)dy, fdz = (float)zo;
+                const int m = I1.w;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                {
+                    const float bnd = fmaf(comp4<float>(XG, k), fdz, fmaf(comp4<float>(XB, k), fdy, comp4<float>(XA, k)));
+                    if ((m >> (4 + k)) & 1) continue;
+                    if ((m >> k) & 1) xmin = fmaxf(xmin, bnd);
+                    else xmax = fminf(xmax, bnd);
+                }
+            }
+            nrows++;
+            if (xmin > xmax)
+                continue;
+            // grid indices inside [xmin, xmax]: an index estimate widened by m
+            // grid steps, where m exceeds the rounding of the estimate and of the
+            // float grid positions (2 eps |pos| each), so no point in the range is
+            // dropped; an extra point at the edge is classified like any other
+            const float f0 = (xmin - g.gmin[0]) * g.inv_step[0];
+            const float f1 = (xmax - g.gmin[0]) * g.inv_step[0];
+            const float m = 1e-3f + 8.0f * EPS32 * ((fabsf(g.gmin[0]) + fmaxf(fabsf(xmin), fabsf(xmax))) *
+                                                    g.inv_step[0] + fmaxf(fabsf(f0), fabsf(f1)));
+            const int i0 = max(I0.x, (int)ceilf(fmaxf(f0 - m, (float)(I0.x - 1))));
+            const int i1 = min(I0.y, (int)floorf(fminf(f1 + m, (float)(I0.y + 1))));
+            if (i0 > i1)
+                continue;
             const float pyf = yi * g.step[1] + g.gmin[1];
             const float pzf = zi * g.step[2] + g.gmin[2];
             const int s = I1.y;
             const T sf = (T)s;
-            const float4 A0 = S.A0[j], A1 = S.A1[j];
-            const float4 IC = S.IC[j];
             T R4[4], Bk[4], cx[4];
-            float xmin = A0.w, xmax = A1.w;
-            bool row_empty = false;
 #pragma unroll
             for (int k = 0; k < 4; ++k)
             {
                 const T4 ck = S.C[k][j];
-                const float by = k == 0 ? A1.y : A0.y, bz = k == 0 ? A1.z : A0.z, bx = k == 0 ? A1.x : A0.x;
+                const float by = k == 0 ? A1.y : A0.y, bz = k == 0 ? A1.z : A0.z;
                 const T qy = (T)pyf - (T)by, qz = (T)pzf - (T)bz;
                 R4[k] = Real<T>::fma_(ck.y, qy, ck.z * qz);
                 Bk[k] = ck.w;
                 cx[k] = ck.x;
-                const float rhs = (float)(-Bk[k] - sf * R4[k]);   // inside needs s*c_kx*qx >= rhs
-                const float ic = comp4<float>(IC, k);
-                if (ic > 0.0f)
-                    xmin = fmaxf(xmin, bx + rhs * ic);
-                else if (ic < 0.0f)
-                    xmax = fminf(xmax, bx + rhs * ic);
-                else if (rhs > 0.0f)
-                    row_empty = true;
             }
-            const float slack = 2.0f * g.step[0];
-            nrows++;
-            if (row_empty || xmin > A1.w + slack || xmax < A0.w - slack || xmin > xmax + 2.0f * slack)
-                continue;
-            int i0 = I0.x, i1 = I0.y;
-            if (xmin - slack > A0.w)
-                i0 = max(i0, (int)floorf((xmin - slack - g.gmin[0]) / g.step[0]));
-            if (xmax + slack < A1.w)
-                i1 = min(i1, (int)ceilf((xmax + slack - g.gmin[0]) / g.step[0]));
             const T4 W4 = S.W[j];
             const size_t row = ((size_t)zi * g.n[1] + yi) * g.n[0];
             ncand += i1 >= i0 ? i1 - i0 + 1 : 0;
