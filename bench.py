@@ -404,7 +404,8 @@ def run_gpu(args):
                     gpu_launches=int(launches), clocks=clk, particles_per_s=world * args.particles / (ms * 1e-3),
                     stage_ms=stage_ms, step_roofline=step_roof, fp64_fixup_tets=info["fp64_tets"],
                     exact_tests=info["exact_tests"], grid_pts_assigned=assigned,
-                    rows_visited=info["rows_visited"], points_tested=info["points_tested"], host_prep_s=prep_s, **extra)
+                    rows_visited=info["rows_visited"], points_tested=info["points_tested"],
+                    raster_variant=info["raster_variant"], host_prep_s=prep_s, **extra)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

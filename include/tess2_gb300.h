@@ -111,6 +111,7 @@ typedef struct tessgpu_dense_info
     long long exact_tests;      /* DTFE: point-in-tet tests decided by exact arithmetic */
     long long rows_visited;     /* DTFE: grid rows the rasteriser examined */
     long long points_tested;    /* DTFE: grid points the rasteriser classified */
+    int       raster_variant;   /* DTFE: launch configuration the autotuner chose for this batch */
 } tessgpu_dense_info;
 
 /* ---- context ---------------------------------------------------------- */

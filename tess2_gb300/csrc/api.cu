@@ -30,6 +30,8 @@ struct tessgpu_ctx
     float*       d_max = nullptr;
     // grow-only buffers reused by the host-buffer entry points
     std::vector<std::pair<void*, size_t>> pool;
+    // rasteriser launch configuration chosen by the autotuner, per mode
+    int                      raster_variant[2] = { -1, -1 };
     // stage timing
     bool                     timing = false;
     std::vector<cudaEvent_t> events;
@@ -286,6 +288,7 @@ struct tessgpu_batch
     int*                   fix_list = nullptr;
     int*                   fix_count = nullptr;
     // validation outputs
+    int                    raster_variant[2] = { -1, -1 };   // autotuned per mode
     bool                   keep_debug = false;
     int*                   d_cell_counts = nullptr;
     int*                   d_owner = nullptr;
@@ -627,8 +630,40 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         launch_densities((const unsigned long long*)bt->W, (int)bt->N, p->mass, 1.0 / scale, bt->rho32, bt->rho64,
                          ctx->d_status, s);
         mark(ctx, "densities");
-        launch_raster(p->mode, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, kTau, d_grid,
-                      owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
+        int& var = bt->raster_variant[p->mode];
+        if (var < 0)
+            var = ctx->raster_variant[p->mode];   // a choice made on an earlier batch of this context
+        if (var < 0)
+        {
+            // autotune: time each launch-bound variant once on this batch (the
+            // grid is rewritten by every run, the fix list is reset between)
+            float best = 1e30f;
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            for (int v = 0; v < raster_variants(); ++v)
+            {
+                CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
+                cudaEventRecord(e0, s);
+                launch_raster(p->mode, v, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g,
+                              kTau, d_grid, owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
+                cudaEventRecord(e1, s);
+                ctx->launches++;
+                CK(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) { best = ms; var = v; }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            ctx->raster_variant[p->mode] = var;
+            CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
+            CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
+            CK(cudaMemsetAsync(d_grid, 0, sizeof(float) * G, s));
+            if (owner) CK(cudaMemsetAsync(owner, 0xff, sizeof(int) * G, s));
+        }
+        launch_raster(p->mode, var, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, kTau,
+                      d_grid, owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
         mark(ctx, "raster");
         if (p->mode != TESSGPU_MODE_FP64)
         {
@@ -666,6 +701,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         info->exact_tests = (long long)ctx->h_status->exact_tests;
         info->rows_visited = (long long)ctx->h_status->rows;
         info->points_tested = (long long)ctx->h_status->candidates;
+        info->raster_variant = bt->raster_variant[p->mode];
     }
     return st;
 }

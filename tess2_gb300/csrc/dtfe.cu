@@ -365,7 +365,8 @@ __device__ __noinline__ bool inside_exact(float a00, float a01, float a02, float
 //   T=float,  VAL64=true,  LIST=true   mixed fix-up pass over fix_list: the same
 //       exact classification, values from an FP64 evaluation
 //   T=double, VAL64=true,  LIST=false  FP64 mode: everything in FP64
-constexpr int RW = 4;   // warps per block
+constexpr int RW = 4;       // warps per block
+constexpr int SLICES = 8;   // tets with at most this many z slices visit only their cross-section rows
 
 template <typename T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; };
@@ -375,12 +376,14 @@ template <typename T, bool VAL64>
 struct __align__(16) RasterSmem
 {
     typedef typename Vec4<T>::type T4;
-    float4 A0[32], A1[32], A2[32], A3[32];   // vertices; A0.w = bbox x lo, A1.w = bbox x hi
+    float4 A0[32], A1[32];                   // vertices 0, 1; A0.w = bbox x lo, A1.w = bbox x hi
+    int    TG[32];                           // global tet index (the exact path reloads vertices 2, 3)
     T4     C[4][32];                         // c_k.x, c_k.y, c_k.z, B_k
     T4     W[32];                            // rho_k / 6V
     float4 XA[32], XB[32], XG[32];           // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
     int4   I0[32];                           // ix0, ix1, iy0, ny
     int4   I1[32];                           // iz0, s, local tet index, lower-bound face mask
+    int    SLC[SLICES][32];                  // per z slice: first row dy << 16 | rows (0 when the tet is not sliced)
     int    pre[33];
     double C64[VAL64 && sizeof(T) == 4 ? 12 : 1][32];   // FP64 values for the fix-up pass
     double W64[VAL64 && sizeof(T) == 4 ? 4 : 1][32];
@@ -391,8 +394,8 @@ template <typename T> __device__ __forceinline__ T comp4(const typename Vec4<T>:
     return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
 }
 
-template <typename T, bool VAL64, bool LIST>
-__global__ void __launch_bounds__(RW * 32, 4)
+template <typename T, bool VAL64, bool LIST, int MINB>
+__global__ void __launch_bounds__(RW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
          int* fix_list, int* fix_count, Status* st)
@@ -476,8 +479,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                 {
                     S.A0[lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
                     S.A1[lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
-                    S.A2[lane] = make_float4(a[2][0], a[2][1], a[2][2], 0.0f);
-                    S.A3[lane] = make_float4(a[3][0], a[3][1], a[3][2], 0.0f);
+                    S.TG[lane] = t;
                     T w[4];
 #pragma unroll
                     for (int k = 0; k < 4; ++k)
@@ -570,7 +572,72 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         }
                     }
                     S.I0[lane] = make_int4(ilo[0], ihi[0], ilo[1], ihi[1] - ilo[1] + 1);
-                    rows = (ihi[1] - ilo[1] + 1) * (ihi[2] - ilo[2] + 1);
+                    const int nyb = ihi[1] - ilo[1] + 1, nzb = ihi[2] - ilo[2] + 1;
+                    if (nzb <= SLICES)
+                    {
+                        // rows of slice z: the y range of the tet's cross-section there,
+                        // from the edges that cross the plane, widened by a rounding
+                        // margin (an extra row is only visited, a dropped row would lose
+                        // points)
+                        rows = 0;
+                        float idz[6];
+#pragma unroll
+                        for (int e = 0; e < 6; ++e)
+                        {
+                            const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
+                            const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
+                            const float dz = a[v][2] - a[u][2];
+                            idz[e] = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+                        }
+                        for (int zo = 0; zo < nzb; ++zo)
+                        {
+                            const float pz = (ilo[2] + zo) * g.step[2] + g.gmin[2];
+                            float ylo = FLT_MAX, yhi = -FLT_MAX;
+#pragma unroll
+                            for (int e = 0; e < 6; ++e)
+                            {
+                                const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
+                                const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
+                                const float za = a[u][2], zb = a[v][2];
+                                if (pz < fminf(za, zb) || pz > fmaxf(za, zb))
+                                    continue;
+                                float y0, y1;
+                                if (za == zb)
+                                {
+                                    y0 = a[u][1];
+                                    y1 = a[v][1];
+                                }
+                                else
+                                {
+                                    const float tt = fminf(fmaxf((pz - za) * idz[e], 0.0f), 1.0f);
+                                    y0 = y1 = fmaf(tt, a[v][1] - a[u][1], a[u][1]);
+                                }
+                                ylo = fminf(ylo, fminf(y0, y1));
+                                yhi = fmaxf(yhi, fmaxf(y0, y1));
+                            }
+                            int cnt = 0, d0 = 0;
+                            if (ylo <= yhi)
+                            {
+                                const float my = 64.0f * EPS32 * (fmaxf(fabsf(ylo), fabsf(yhi)) + hi[1] - lo[1]);
+                                const float f0 = (ylo - my - g.gmin[1]) * g.inv_step[1];
+                                const float f1 = (yhi + my - g.gmin[1]) * g.inv_step[1];
+                                const float mm = 1e-3f + 8.0f * EPS32 * ((fabsf(g.gmin[1]) + fmaxf(fabsf(ylo), fabsf(yhi))) *
+                                                                         g.inv_step[1] + fmaxf(fabsf(f0), fabsf(f1)));
+                                const int y0i = max(ilo[1], (int)ceilf(fmaxf(f0 - mm, (float)(ilo[1] - 1))));
+                                const int y1i = min(ihi[1], (int)floorf(fminf(f1 + mm, (float)(ihi[1] + 1))));
+                                if (y1i >= y0i)
+                                {
+                                    cnt = y1i - y0i + 1;
+                                    d0 = y0i - ilo[1];
+                                }
+                            }
+                            S.SLC[zo][lane] = (d0 << 16) | cnt;
+                            rows += cnt;
+                        }
+                        S.I1[lane].w |= 1 << 8;   // sliced
+                    }
+                    else
+                        rows = nyb * nzb;
                 }
             }
         }
@@ -594,11 +661,28 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
             const int rr = r - S.pre[j];
             const int4 I0 = S.I0[j];
             const int4 I1 = S.I1[j];
-            const int ny = I0.w;
-            int zo = (int)(((float)rr + 0.5f) * __frcp_rn((float)ny));
-            if (zo * ny > rr) --zo;
-            else if ((zo + 1) * ny <= rr) ++zo;
-            const int dy = rr - zo * ny;
+            int zo, dy;
+            if ((I1.w >> 8) & 1)
+            {
+                // sliced tet: walk the per-slice row counts
+                int q = rr;
+                zo = 0;
+                int sl = S.SLC[0][j];
+                while (q >= (sl & 0xffff))
+                {
+                    q -= sl & 0xffff;
+                    sl = S.SLC[++zo][j];
+                }
+                dy = (sl >> 16) + q;
+            }
+            else
+            {
+                const int ny = I0.w;
+                zo = (int)(((float)rr + 0.5f) * __frcp_rn((float)ny));
+                if (zo * ny > rr) --zo;
+                else if ((zo + 1) * ny <= rr) ++zo;
+                dy = rr - zo * ny;
+            }
             const int yi = I0.z + dy;
             const int zi = I1.x + zo;
             const float4 A0 = S.A0[j], A1 = S.A1[j];
@@ -607,7 +691,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
             {
                 const float4 XA = S.XA[j], XB = S.XB[j], XG = S.XG[j];
                 const float fdy = (float)dy, fdz = (float)zo;
-                const int m = I1.w;
+                const int m = I1.w & 0xff;
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
                 {
@@ -676,7 +760,8 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                 if (!in)
                 {
                     nexact++;
-                    const float4 A2 = S.A2[j], A3 = S.A3[j];
+                    const int4 vt = __ldg(&tv[S.TG[j]]);
+                    const float4 A2 = __ldg(&pos[vt.z]), A3 = __ldg(&pos[vt.w]);
                     if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf,
                                       pyf, pzf, s, open))
                         continue;
@@ -752,18 +837,46 @@ void launch_densities(const unsigned long long* W, int n, float mass, double inv
     k_densities<<<grid_for(n, 256, 8), 256, 0, s>>>(W, n, mass, inv_scale, rho32, rho64, st);
 }
 
-void launch_raster(int mode, const BlockDesc* d_blocks, int nb, int total, const float4* pos, const int4* tv,
-                   const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid, int* owner,
-                   int* fix_list, int* fix_count, Status* st, cudaStream_t s)
+// Block residency per SM trades registers against latency hiding; which
+// bound is fastest depends on the GPU and the mesh, so the caller picks it
+// (variant 0, 1, 2 = 4, 5, 6 resident blocks per SM).
+template <typename T, bool VAL64, bool LIST>
+static void raster_variant(int variant, int nblk, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
+                           const int* list, const int* list_count, const float4* pos, const int4* tv,
+                           const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
+                           int* owner, int* fix_list, int* fix_count, Status* st)
+{
+    switch (variant)
+    {
+    case 1:
+        k_raster<T, VAL64, LIST, 5><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, rho32,
+                                                              rho64, g, tau, grid, owner, fix_list, fix_count, st);
+        break;
+    case 2:
+        k_raster<T, VAL64, LIST, 6><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, rho32,
+                                                              rho64, g, tau, grid, owner, fix_list, fix_count, st);
+        break;
+    default:
+        k_raster<T, VAL64, LIST, 4><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, rho32,
+                                                              rho64, g, tau, grid, owner, fix_list, fix_count, st);
+        break;
+    }
+}
+
+int raster_variants() { return 3; }
+
+void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total, const float4* pos,
+                   const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
+                   int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
     const int nblk = grid_for((long long)((total + 31) / 32) * 32 * 32, RW * 32, 16);
     if (mode == TESSGPU_MODE_FP64)
-        k_raster<double, true, false><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                                                rho64, g, tau, grid, owner, nullptr, nullptr, st);
+        raster_variant<double, true, false>(variant, nblk, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
+                                            rho64, g, tau, grid, owner, nullptr, nullptr, st);
     else
-        k_raster<float, false, false><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                                                rho64, g, tau, grid, owner, fix_list, fix_count, st);
+        raster_variant<float, false, false>(variant, nblk, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
+                                            rho64, g, tau, grid, owner, fix_list, fix_count, st);
 }
 
 // the tets the mixed pass listed, with FP64 values; sized for the longest
@@ -774,8 +887,8 @@ void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total, const float
 {
     if (total <= 0) return;
     const int nblk = grid_for((long long)((total / 16 + 31) / 32) * 32 * 32, RW * 32, 4);
-    k_raster<float, true, true><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32,
-                                                          rho64, g, 0.0f, grid, owner, nullptr, nullptr, st);
+    raster_variant<float, true, true>(0, nblk, s, d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32, rho64, g,
+                                      0.0f, grid, owner, nullptr, nullptr, st);
 }
 
 }  // namespace tg

@@ -29,9 +29,10 @@ void launch_star_volumes(int mode, int total_tets, const float4* pos, const int4
                          double scale, float tau, Status* st, cudaStream_t s);
 void launch_densities(const unsigned long long* W, int total_particles, float mass, double inv_scale, float* rho32,
                       double* rho64, Status* st, cudaStream_t s);
-void launch_raster(int mode, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos, const int4* tv,
-                   const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid, int* owner,
-                   int* fix_list, int* fix_count, Status* st, cudaStream_t s);
+void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos,
+                   const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
+                   int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s);
+int  raster_variants();
 void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos, const int4* tv,
                        const float* rho32, const double* rho64, const GridDesc& g, float* grid, int* owner,
                        const int* fix_list, const int* fix_count, Status* st, cudaStream_t s);
