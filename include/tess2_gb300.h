@@ -206,6 +206,33 @@ tessgpu_status tessgpu_batch_keep_debug(tessgpu_batch* batch, int on);
 tessgpu_status tessgpu_batch_debug_outputs(tessgpu_ctx* ctx, tessgpu_batch* batch, int* cell_counts,
                                            int* owner, float* rho);
 
+/* ---- allocation-free entry point -------------------------------------- */
+
+/* Largest particle count tessgpu_dtfe_densities_noalloc accepts: its scratch
+   is a fixed 16 MiB array inside the library. */
+#define TESSGPU_NOALLOC_MAX_PARTICLES (1 << 21)
+
+/* DTFE vertex densities of one block (rho_v = 4 m / star volume, as the
+   DENSE_DTFE path computes them) for callers that cannot allocate GPU
+   memory, e.g. an in-situ analysis running inside a simulation whose own
+   allocator has reserved the device, or code that must not call cudaMalloc
+   / cudaFree because those can synchronise the device.  It has no
+   counterpart in the reference.
+   d_particles (3 floats per particle), d_tets (tet_t records) and d_rho
+   (one float per particle) are device memory the caller owns; bounds6 is a
+   host array {min x, y, z, max x, y, z} of the data bounds, as dense() uses;
+   mode is tessgpu_mode; stream may be NULL.  The function allocates nothing:
+   its scratch is a static device array shared by all calls, which keeps the
+   last call's contents (each call clears what it uses), so calls that
+   overlap on the GPU race and must be serialised by the caller.  The first
+   call on a device looks up that array's device address; make it before
+   any stream capture.  More than TESSGPU_NOALLOC_MAX_PARTICLES particles is
+   rejected with TESSGPU_ERR_INVALID.  Returns after the densities are
+   written (the call synchronises the stream). */
+tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particles, int num_particles, const int* d_tets,
+                                              int num_tets, const float* bounds6, float mass, int mode,
+                                              float* d_rho, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -106,6 +106,7 @@ def lib():
             "tessgpu_batch_debug_outputs": (_I, [_VP, _VP, _VP, _VP, _VP]),
             "tessgpu_set_timing": (_I, [_VP, _I]),
             "tessgpu_stage_times": (_I, [_VP, _VP, _VP, _I]),
+            "tessgpu_dtfe_densities_noalloc": (_I, [_VP, _I, _VP, _I, _VP, ctypes.c_float, _I, _VP, _VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

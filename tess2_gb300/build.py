@@ -24,6 +24,7 @@ UNITS = {
     "geometry.cu": ["-fmad=false"],
     "dtfe.cu": ["-fmad=false"],
     "api.cu": ["-fmad=false"],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 
