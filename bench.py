@@ -405,7 +405,7 @@ def run_gpu(args):
                     stage_ms=stage_ms, step_roofline=step_roof, fp64_fixup_tets=info["fp64_tets"],
                     exact_tests=info["exact_tests"], grid_pts_assigned=assigned,
                     rows_visited=info["rows_visited"], points_tested=info["points_tested"],
-                    raster_variant=info["raster_variant"], host_prep_s=prep_s, **extra)
+                    raster_variant=info["raster_variant"], raster_variant_ms=info["raster_variant_ms"], host_prep_s=prep_s, **extra)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

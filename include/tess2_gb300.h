@@ -112,6 +112,7 @@ typedef struct tessgpu_dense_info
     long long rows_visited;     /* DTFE: grid rows the rasteriser examined */
     long long points_tested;    /* DTFE: grid points the rasteriser classified */
     int       raster_variant;   /* DTFE: launch configuration the autotuner chose for this batch */
+    float     raster_variant_ms[8]; /* DTFE: the autotuner's best time of each configuration (0 if not run) */
 } tessgpu_dense_info;
 
 /* ---- context ---------------------------------------------------------- */

@@ -55,7 +55,8 @@ class DenseInfo(ctypes.Structure):
                 ("max_dense", ctypes.c_double), ("tot_mass", ctypes.c_double), ("check_mass", ctypes.c_double),
                 ("grid_pts_assigned", ctypes.c_longlong), ("fp64_tets", ctypes.c_longlong),
                 ("exact_tests", ctypes.c_longlong), ("rows_visited", ctypes.c_longlong),
-                ("points_tested", ctypes.c_longlong), ("raster_variant", ctypes.c_int)]
+                ("points_tested", ctypes.c_longlong), ("raster_variant", ctypes.c_int),
+                ("raster_variant_ms", ctypes.c_float * 8)]
 
     def as_dict(self):
         return dict(data_mins=np.array(self.data_mins[:], np.float32), data_maxs=np.array(self.data_maxs[:], np.float32),
@@ -65,7 +66,8 @@ class DenseInfo(ctypes.Structure):
                     max_dense=self.max_dense, tot_mass=self.tot_mass, check_mass=self.check_mass,
                     grid_pts_assigned=self.grid_pts_assigned, fp64_tets=self.fp64_tets,
                     exact_tests=self.exact_tests, rows_visited=self.rows_visited,
-                    points_tested=self.points_tested, raster_variant=self.raster_variant)
+                    points_tested=self.points_tested, raster_variant=self.raster_variant,
+                    raster_variant_ms=list(self.raster_variant_ms))
 
 
 _LIB = None

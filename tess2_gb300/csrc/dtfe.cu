@@ -365,7 +365,6 @@ __device__ __noinline__ bool inside_exact(float a00, float a01, float a02, float
 //   T=float,  VAL64=true,  LIST=true   mixed fix-up pass over fix_list: the same
 //       exact classification, values from an FP64 evaluation
 //   T=double, VAL64=true,  LIST=false  FP64 mode: everything in FP64
-constexpr int RW = 4;       // warps per block
 constexpr int SLICES = 8;   // tets with at most this many z slices visit only their cross-section rows
 
 template <typename T> struct Vec4;
@@ -376,15 +375,21 @@ template <typename T, bool VAL64>
 struct __align__(16) RasterSmem
 {
     typedef typename Vec4<T>::type T4;
+    // per tet of the current batch (lane = tet slot)
     float4 A0[32], A1[32];                   // vertices 0, 1; A0.w = bbox x lo, A1.w = bbox x hi
     int    TG[32];                           // global tet index (the exact path reloads vertices 2, 3)
     T4     C[4][32];                         // c_k.x, c_k.y, c_k.z, B_k
     T4     W[32];                            // rho_k / 6V
     float4 XA[32], XB[32], XG[32];           // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
     int4   I0[32];                           // ix0, ix1, iy0, ny
-    int4   I1[32];                           // iz0, s, local tet index, lower-bound face mask
-    int    SLC[SLICES][32];                  // per z slice: first row dy << 16 | rows (0 when the tet is not sliced)
-    int    pre[33];
+    int4   I1[32];                           // iz0, s, local tet index, face masks | sliced flag
+    int    SLC[SLICES][32];                  // per z slice: first row dy << 16 | rows
+    int    pre[33];                          // prefix of the tets' row counts
+    // per row of the current round (lane = row slot)
+    T      RN[4][32];                        // R_k(y, z) of the row
+    int    RJ[32], RI0[32], RY[32], RZ[32];  // tet slot, first x index, y, z
+    int    pp[33];                           // prefix of the rows' point counts
+    int    Q[64];                            // tets whose box holds grid points, waiting for a batch
     double C64[VAL64 && sizeof(T) == 4 ? 12 : 1][32];   // FP64 values for the fix-up pass
     double W64[VAL64 && sizeof(T) == 4 ? 4 : 1][32];
 };
@@ -394,402 +399,537 @@ template <typename T> __device__ __forceinline__ T comp4(const typename Vec4<T>:
     return i == 0 ? v.x : i == 1 ? v.y : i == 2 ? v.z : v.w;
 }
 
-template <typename T, bool VAL64, bool LIST, int MINB>
-__global__ void __launch_bounds__(RW * 32, MINB)
+// the tet's vertices and the index box of grid points it can hold inside its
+// block's grid box; true when that box is empty
+__device__ __forceinline__ bool tet_box(const BlockDesc* blocks, int nb, const float4* pos, const int4* tv,
+                                        const GridDesc& g, int t, int& b, int* vid, float a[4][3], float* lo,
+                                        float* hi, int* ilo, int* ihi)
+{
+    b = find_blk(blocks, nb, t);
+    const int4 vi = __ldg(&tv[t]);
+    vid[0] = vi.x; vid[1] = vi.y; vid[2] = vi.z; vid[3] = vi.w;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const float4 p4 = __ldg(&pos[vid[k]]);
+        a[k][0] = p4.x; a[k][1] = p4.y; a[k][2] = p4.z;
+    }
+    bool empty = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        lo[d] = fminf(fminf(a[0][d], a[1][d]), fminf(a[2][d], a[3][d]));
+        hi[d] = fmaxf(fmaxf(a[0][d], a[1][d]), fmaxf(a[2][d], a[3][d]));
+        const int olo = blocks[b].gmin_idx[d], ohi = blocks[b].gmax_idx[d];
+        ilo[d] = first_at_or_above(lo[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi);
+        ihi[d] = first_at_or_above(hi[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi + 1) - 1;
+        if (ihi[d] > ohi) ihi[d] = ohi;
+        if (ilo[d] > ihi[d]) empty = true;
+    }
+    return empty;
+}
+
+// one grid point of a row: classify against the tet's four numerator planes
+// (exact arithmetic when the filter cannot decide) and write the
+// interpolated density when it is inside
+template <typename T, bool VAL64>
+__device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64>& S, int j, int xi, int yi, int zi, float pyf,
+                                             float pzf, const float4& A0, const float4& A1, const int4& I1,
+                                             const T* cx, const T* RN, const T* Bk, const GridDesc& g,
+                                             const int4* tv, const float4* pos, float* grid, int* owner,
+                                             unsigned long long& nexact, unsigned long long& nassigned)
+{
+    typedef typename Vec4<T>::type T4;
+    constexpr bool F32 = sizeof(T) == 4;
+    const float pxf = xi * g.step[0] + g.gmin[0];
+    const T px = pxf;
+    const int s = I1.y;
+    const T sf = (T)s;
+    T N[4];
+    N[0] = Real<T>::fma_(cx[0], px - (T)A1.x, RN[0]);
+    const T qx = px - (T)A0.x;
+    N[1] = Real<T>::fma_(cx[1], qx, RN[1]);
+    N[2] = Real<T>::fma_(cx[2], qx, RN[2]);
+    N[3] = Real<T>::fma_(cx[3], qx, RN[3]);
+    bool in = true, out = false;
+    unsigned open = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+    {
+        const T sn = sf * N[k];
+        const bool ik = sn > Bk[k];
+        in = in && ik;
+        out = out || (sn < -Bk[k]);
+        open |= (ik ? 0u : 1u) << k;
+    }
+    if (out)
+        return;
+    if (!in)
+    {
+        nexact++;
+        const int4 vt = __ldg(&tv[S.TG[j]]);
+        const float4 A2 = __ldg(&pos[vt.z]), A3 = __ldg(&pos[vt.w]);
+        if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf, pyf, pzf, s,
+                          open))
+            return;
+    }
+    float f;
+    if (!VAL64 || !F32)
+    {
+        const T4 W4 = S.W[j];
+        f = (float)Real<T>::fma_(N[0], W4.x, Real<T>::fma_(N[1], W4.y, Real<T>::fma_(N[2], W4.z, N[3] * W4.w)));
+    }
+    else
+    {
+        const double q1[3] = { (double)pxf - A1.x, (double)pyf - A1.y, (double)pzf - A1.z };
+        const double q0[3] = { (double)pxf - A0.x, (double)pyf - A0.y, (double)pzf - A0.z };
+        double acc = 0.0;
+        for (int k = 0; k < 4; ++k)
+        {
+            const double* qq = k == 0 ? q1 : q0;
+            acc += (qq[0] * S.C64[3 * k][j] + qq[1] * S.C64[3 * k + 1][j] + qq[2] * S.C64[3 * k + 2][j]) *
+                   S.W64[k][j];
+        }
+        f = (float)acc;
+    }
+    const size_t gi = ((size_t)zi * g.n[1] + yi) * g.n[0] + xi;
+    grid[gi] = f;
+    if (owner)
+        owner[gi] = I1.z;
+    nassigned++;
+}
+
+template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, bool FLAT>
+__global__ void __launch_bounds__(NW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
          int* fix_list, int* fix_count, Status* st)
 {
     typedef typename Vec4<T>::type T4;
-    __shared__ RasterSmem<T, VAL64> smem[RW];
+    __shared__ RasterSmem<T, VAL64> smem[NW];
     constexpr bool F32 = sizeof(T) == 4;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     RasterSmem<T, VAL64>& S = smem[wid];
     unsigned long long nexact = 0, nassigned = 0, nfix = 0, nrows = 0, ncand = 0;
     const int n = LIST ? *list_count : total;
     const int nchunks = (n + 31) / 32;
-    for (int chunk = blockIdx.x * RW + wid; chunk < nchunks; chunk += gridDim.x * RW)
+    int qn = 0;   // queued tets (warp-uniform)
+    for (int chunk = blockIdx.x * NW + wid;; chunk += gridDim.x * NW)
     {
-        // ---- phase A: one tet per lane
-        const int it = chunk * 32 + lane;
-        int rows = 0;
-        if (it < n)
+        const bool more = chunk < nchunks;
+        if (COMPACT && more)
         {
-            const int t = LIST ? list[it] : it;
-            const int b = find_blk(blocks, nb, t);
-            const int4 vi = __ldg(&tv[t]);
-            const int vid[4] = { vi.x, vi.y, vi.z, vi.w };
-            float a[4][3];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
+            // ---- screen: keep the tets whose box holds grid points
+            const int it = chunk * 32 + lane;
+            bool keep = false;
+            int t = -1;
+            if (it < n)
             {
-                const float4 p4 = __ldg(&pos[vid[k]]);
-                a[k][0] = p4.x; a[k][1] = p4.y; a[k][2] = p4.z;
+                t = LIST ? list[it] : it;
+                int b, vid[4], ilo[3], ihi[3];
+                float a[4][3], lo[3], hi[3];
+                keep = !tet_box(blocks, nb, pos, tv, g, t, b, vid, a, lo, hi, ilo, ihi);
             }
-            int ilo[3], ihi[3];
-            bool empty = false;
-            float lo[3], hi[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d)
+            const unsigned m = __ballot_sync(FULL, keep);
+            if (keep)
+                S.Q[qn + __popc(m & ((1u << lane) - 1u))] = t;
+            qn += __popc(m);
+            __syncwarp();
+        }
+        if (!COMPACT && more)
+            qn = 32;   // the chunk itself is the batch
+        while (qn >= 32 || (!more && qn > 0))
+        {
+            // ---- a batch of up to 32 tets, one per lane
+            int tq;
+            if (COMPACT)
             {
-                lo[d] = fminf(fminf(a[0][d], a[1][d]), fminf(a[2][d], a[3][d]));
-                hi[d] = fmaxf(fmaxf(a[0][d], a[1][d]), fmaxf(a[2][d], a[3][d]));
-                const int olo = blocks[b].gmin_idx[d], ohi = blocks[b].gmax_idx[d];
-                ilo[d] = first_at_or_above(lo[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi);
-                ihi[d] = first_at_or_above(hi[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi + 1) - 1;
-                if (ihi[d] > ohi) ihi[d] = ohi;
-                if (ilo[d] > ihi[d]) empty = true;
+                const int take = min(qn, 32);
+                tq = lane < take ? S.Q[lane] : -1;
+                const int rest = qn - take;
+                const int carry = lane < rest ? S.Q[take + lane] : 0;
+                __syncwarp();
+                if (lane < rest)
+                    S.Q[lane] = carry;
+                qn = rest;
             }
-            int s = 0;
-            T v6 = 0;
-            if (!empty)
+            else
             {
-                const float3 A0 = make_float3(a[0][0], a[0][1], a[0][2]), A1 = make_float3(a[1][0], a[1][1], a[1][2]);
-                const float3 A2 = make_float3(a[2][0], a[2][1], a[2][2]), A3 = make_float3(a[3][0], a[3][1], a[3][2]);
-                if (F32)
-                {
-                    float vb;
-                    const float v6f = tet_vol6_f32(A0, A1, A2, A3, vb);
-                    v6 = v6f;
-                    if (v6f > vb) s = 1;
-                    else if (v6f < -vb) s = -1;
-                    else s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1],
-                                      a[2][2], a[3][0], a[3][1], a[3][2]);
-                }
-                else
-                {
-                    v6 = (T)tet_vol6_f64(A0, A1, A2, A3);
-                    s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1], a[2][2],
-                                 a[3][0], a[3][1], a[3][2]);
-                }
+                const int it = chunk * 32 + lane;
+                tq = it < n ? (LIST ? list[it] : it) : -1;
+                qn = 0;
             }
-            if (!empty && s != 0)
+            int rows = 0;
+            if (tq >= 0)
             {
-                T c[4][3], Bk[4];
-                numerators_setup<T>(a, lo, hi, c, Bk);
-                bool keep = true;
-                if (F32 && !VAL64 && fix_list &&
-                    (float)(Bk[0] + Bk[1] + Bk[2] + Bk[3]) > tau * fabsf((float)v6))
+                const int t = tq;
+                int b, vid[4], ilo[3], ihi[3];
+                float a[4][3], lo[3], hi[3];
+                const bool empty = tet_box(blocks, nb, pos, tv, g, t, b, vid, a, lo, hi, ilo, ihi);
+                int s = 0;
+                T v6 = 0;
+                if (!empty)
                 {
-                    fix_list[atomicAdd(fix_count, 1)] = t;   // values need FP64: the fix-up pass
-                    nfix++;
-                    keep = false;
-                }
-                if (keep)
-                {
-                    S.A0[lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
-                    S.A1[lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
-                    S.TG[lane] = t;
-                    T w[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
+                    const float3 A0 = make_float3(a[0][0], a[0][1], a[0][2]), A1 = make_float3(a[1][0], a[1][1], a[1][2]);
+                    const float3 A2 = make_float3(a[2][0], a[2][1], a[2][2]), A3 = make_float3(a[3][0], a[3][1], a[3][2]);
+                    if (F32)
                     {
-                        T4 ck;
-                        ck.x = c[k][0]; ck.y = c[k][1]; ck.z = c[k][2]; ck.w = Bk[k];
-                        S.C[k][lane] = ck;
-                        w[k] = F32 ? (T)(__ldg(&rho32[vid[k]]) * __frcp_rn((float)v6))
-                                   : (T)__ldg(&rho64[vid[k]]) / v6;
+                        float vb;
+                        const float v6f = tet_vol6_f32(A0, A1, A2, A3, vb);
+                        v6 = v6f;
+                        if (v6f > vb) s = 1;
+                        else if (v6f < -vb) s = -1;
+                        else s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1],
+                                          a[2][2], a[3][0], a[3][1], a[3][2]);
                     }
-                    T4 w4;
-                    w4.x = w[0]; w4.y = w[1]; w4.z = w[2]; w4.w = w[3];
-                    S.W[lane] = w4;
-                    // Row-wise x bounds.  Inside needs s*N_k >= -B_k, N_k = c_kx (x - bx)
-                    // + R_k(y, z); along row (dy, dz) of the box this is x >= bnd_k
-                    // (s c_kx > 0) or x <= bnd_k (s c_kx < 0) with
-                    //   bnd_k = bx - s B_k / c_kx - R_k / c_kx, affine in (dy, dz).
-                    // E_k covers the rounding of the coefficients, of the float grid
-                    // positions against the affine form, and of N_k's own evaluation,
-                    // so a point outside [max lower, min upper] fails the per-point
-                    // test for some face.  c_kx == 0 gives no x bound.
+                    else
                     {
-                        const float h1 = g.step[1], h2 = g.step[2];
-                        const float py0 = ilo[1] * h1 + g.gmin[1], pz0 = ilo[2] * h2 + g.gmin[2];
-                        const float ymx = fmaxf(fabsf(py0), fabsf(ihi[1] * h1 + g.gmin[1]));
-                        const float zmx = fmaxf(fabsf(pz0), fabsf(ihi[2] * h2 + g.gmin[2]));
-                        const float xmx = fmaxf(fabsf(lo[0]), fabsf(hi[0]));
-                        const int ny = ihi[1] - ilo[1] + 1, nz = ihi[2] - ilo[2] + 1;
-                        float xa[4], xb[4], xg[4];
-                        int lower = 0;
+                        v6 = (T)tet_vol6_f64(A0, A1, A2, A3);
+                        s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1], a[2][2],
+                                     a[3][0], a[3][1], a[3][2]);
+                    }
+                }
+                if (s != 0)   // s == 0: flat tet, no interior
+                {
+                    T c[4][3], Bk[4];
+                    numerators_setup<T>(a, lo, hi, c, Bk);
+                    bool keep = true;
+                    if (F32 && !VAL64 && fix_list &&
+                        (float)(Bk[0] + Bk[1] + Bk[2] + Bk[3]) > tau * fabsf((float)v6))
+                    {
+                        fix_list[atomicAdd(fix_count, 1)] = t;   // values need FP64: the fix-up pass
+                        nfix++;
+                        keep = false;
+                    }
+                    if (keep)
+                    {
+                        S.A0[lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
+                        S.A1[lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
+                        S.TG[lane] = t;
+                        T4 w4;
+                        const float r6 = F32 ? __frcp_rn((float)v6) : 0.0f;
 #pragma unroll
                         for (int k = 0; k < 4; ++k)
                         {
-                            const int base = k == 0 ? 1 : 0;
-                            const float bx = a[base][0], by = a[base][1], bz = a[base][2];
-                            const float cx = (float)c[k][0], cy = (float)c[k][1], cz = (float)c[k][2];
-                            const float B = (float)Bk[k];
-                            if (cx == 0.0f)
-                            {
-                                xa[k] = 0.0f; xb[k] = 0.0f; xg[k] = 0.0f;
-                                lower |= 1 << (4 + k);   // no x bound from this face
-                                continue;
-                            }
-                            const float icx = __frcp_rn(cx);
-                            const float R0 = cy * (py0 - by) + cz * (pz0 - bz);
-                            const float alpha = bx - (float)s * B * icx - R0 * icx;
-                            const float beta = -cy * h1 * icx, gamma = -cz * h2 * icx;
-                            const float E = 32.0f * EPS32 *
-                                (fabsf(bx) + xmx + fabsf(alpha) + fabsf(B * icx) + fabsf(R0 * icx) +
-                                 fabsf(beta) * ny + fabsf(gamma) * nz +
-                                 (fabsf(cy) * (ymx + fabsf(by)) + fabsf(cz) * (zmx + fabsf(bz))) * fabsf(icx)) +
-                                1e-30f;
-                            const bool lo_face = (float)s * cx > 0.0f;
-                            lower |= lo_face ? 1 << k : 0;
-                            xa[k] = lo_face ? alpha - E : alpha + E;
-                            xb[k] = beta;
-                            xg[k] = gamma;
+                            T4 ck;
+                            ck.x = c[k][0]; ck.y = c[k][1]; ck.z = c[k][2]; ck.w = Bk[k];
+                            S.C[k][lane] = ck;
+                            const T wk = F32 ? (T)(__ldg(&rho32[vid[k]]) * r6) : (T)__ldg(&rho64[vid[k]]) / v6;
+                            if (k == 0) w4.x = wk;
+                            else if (k == 1) w4.y = wk;
+                            else if (k == 2) w4.z = wk;
+                            else w4.w = wk;
                         }
-                        S.XA[lane] = make_float4(xa[0], xa[1], xa[2], xa[3]);
-                        S.XB[lane] = make_float4(xb[0], xb[1], xb[2], xb[3]);
-                        S.XG[lane] = make_float4(xg[0], xg[1], xg[2], xg[3]);
-                        S.I1[lane] = make_int4(ilo[2], s, t - blocks[b].t_off, lower);
-                    }
-                    if (VAL64 && F32)
-                    {
-                        double e[3][3], f1[3], f2[3];
-                        for (int k = 0; k < 3; ++k)
+                        S.W[lane] = w4;
+                        if (VAL64 && F32)
+                        {
+                            double e[3][3], f1[3], f2[3];
+                            for (int k = 0; k < 3; ++k)
+                                for (int d = 0; d < 3; ++d)
+                                    e[k][d] = (double)a[k + 1][d] - (double)a[0][d];
                             for (int d = 0; d < 3; ++d)
-                                e[k][d] = (double)a[k + 1][d] - (double)a[0][d];
-                        for (int d = 0; d < 3; ++d)
-                        {
-                            f1[d] = (double)a[3][d] - (double)a[1][d];
-                            f2[d] = (double)a[2][d] - (double)a[1][d];
+                            {
+                                f1[d] = (double)a[3][d] - (double)a[1][d];
+                                f2[d] = (double)a[2][d] - (double)a[1][d];
+                            }
+                            double cc[4][3];
+                            for (int jj = 0; jj < 3; ++jj)
+                            {
+                                const int ja = (jj + 1) % 3, jb = (jj + 2) % 3;
+                                cc[0][jj] = f1[ja] * f2[jb] - f1[jb] * f2[ja];
+                                cc[1][jj] = e[1][ja] * e[2][jb] - e[1][jb] * e[2][ja];
+                                cc[2][jj] = e[2][ja] * e[0][jb] - e[2][jb] * e[0][ja];
+                                cc[3][jj] = e[0][ja] * e[1][jb] - e[0][jb] * e[1][ja];
+                            }
+                            const double v6d = e[0][0] * cc[1][0] + e[0][1] * cc[1][1] + e[0][2] * cc[1][2];
+                            for (int k = 0; k < 4; ++k)
+                            {
+                                for (int jj = 0; jj < 3; ++jj)
+                                    S.C64[3 * k + jj][lane] = cc[k][jj];
+                                S.W64[k][lane] = __ldg(&rho64[vid[k]]) / v6d;
+                            }
                         }
-                        double cc[4][3];
-                        for (int j = 0; j < 3; ++j)
+                        // Row-wise x bounds.  Inside needs s*N_k >= -B_k, N_k = c_kx (x - bx)
+                        // + R_k(y, z); along row (dy, dz) of the box this is x >= bnd_k
+                        // (s c_kx > 0) or x <= bnd_k (s c_kx < 0) with
+                        //   bnd_k = bx - s B_k / c_kx - R_k / c_kx, affine in (dy, dz).
+                        // E_k covers the rounding of the coefficients, of the float grid
+                        // positions against the affine form, and of N_k's own evaluation,
+                        // so a point outside [max lower, min upper] fails the per-point
+                        // test for some face.  c_kx == 0 gives no x bound.
+                        const int nyb = ihi[1] - ilo[1] + 1, nzb = ihi[2] - ilo[2] + 1;
+                        int masks = 0;
                         {
-                            const int ja = (j + 1) % 3, jb = (j + 2) % 3;
-                            cc[0][j] = f1[ja] * f2[jb] - f1[jb] * f2[ja];
-                            cc[1][j] = e[1][ja] * e[2][jb] - e[1][jb] * e[2][ja];
-                            cc[2][j] = e[2][ja] * e[0][jb] - e[2][jb] * e[0][ja];
-                            cc[3][j] = e[0][ja] * e[1][jb] - e[0][jb] * e[1][ja];
-                        }
-                        const double v6d = e[0][0] * cc[1][0] + e[0][1] * cc[1][1] + e[0][2] * cc[1][2];
-                        for (int k = 0; k < 4; ++k)
-                        {
-                            for (int j = 0; j < 3; ++j)
-                                S.C64[3 * k + j][lane] = cc[k][j];
-                            S.W64[k][lane] = __ldg(&rho64[vid[k]]) / v6d;
-                        }
-                    }
-                    S.I0[lane] = make_int4(ilo[0], ihi[0], ilo[1], ihi[1] - ilo[1] + 1);
-                    const int nyb = ihi[1] - ilo[1] + 1, nzb = ihi[2] - ilo[2] + 1;
-                    if (nzb <= SLICES)
-                    {
-                        // rows of slice z: the y range of the tet's cross-section there,
-                        // from the edges that cross the plane, widened by a rounding
-                        // margin (an extra row is only visited, a dropped row would lose
-                        // points)
-                        rows = 0;
-                        float idz[6];
+                            const float h1 = g.step[1], h2 = g.step[2];
+                            const float py0 = ilo[1] * h1 + g.gmin[1], pz0 = ilo[2] * h2 + g.gmin[2];
+                            const float ymx = fmaxf(fabsf(py0), fabsf(ihi[1] * h1 + g.gmin[1]));
+                            const float zmx = fmaxf(fabsf(pz0), fabsf(ihi[2] * h2 + g.gmin[2]));
+                            const float xmx = fmaxf(fabsf(lo[0]), fabsf(hi[0]));
+                            float xa[4], xb[4], xg[4];
 #pragma unroll
-                        for (int e = 0; e < 6; ++e)
-                        {
-                            const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
-                            const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
-                            const float dz = a[v][2] - a[u][2];
-                            idz[e] = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+                            for (int k = 0; k < 4; ++k)
+                            {
+                                const int base = k == 0 ? 1 : 0;
+                                const float bx = a[base][0], by = a[base][1], bz = a[base][2];
+                                const float cx = (float)c[k][0], cy = (float)c[k][1], cz = (float)c[k][2];
+                                const float B = (float)Bk[k];
+                                if (cx == 0.0f)
+                                {
+                                    xa[k] = 0.0f; xb[k] = 0.0f; xg[k] = 0.0f;
+                                    masks |= 1 << (4 + k);   // no x bound from this face
+                                    continue;
+                                }
+                                const float icx = __frcp_rn(cx);
+                                const float R0 = cy * (py0 - by) + cz * (pz0 - bz);
+                                const float alpha = bx - (float)s * B * icx - R0 * icx;
+                                const float beta = -cy * h1 * icx, gamma = -cz * h2 * icx;
+                                const float E = 32.0f * EPS32 *
+                                    (fabsf(bx) + xmx + fabsf(alpha) + fabsf(B * icx) + fabsf(R0 * icx) +
+                                     fabsf(beta) * nyb + fabsf(gamma) * nzb +
+                                     (fabsf(cy) * (ymx + fabsf(by)) + fabsf(cz) * (zmx + fabsf(bz))) * fabsf(icx)) +
+                                    1e-30f;
+                                const bool lo_face = (float)s * cx > 0.0f;
+                                masks |= lo_face ? 1 << k : 0;
+                                xa[k] = lo_face ? alpha - E : alpha + E;
+                                xb[k] = beta;
+                                xg[k] = gamma;
+                            }
+                            S.XA[lane] = make_float4(xa[0], xa[1], xa[2], xa[3]);
+                            S.XB[lane] = make_float4(xb[0], xb[1], xb[2], xb[3]);
+                            S.XG[lane] = make_float4(xg[0], xg[1], xg[2], xg[3]);
                         }
-                        for (int zo = 0; zo < nzb; ++zo)
+                        S.I0[lane] = make_int4(ilo[0], ihi[0], ilo[1], nyb);
+                        if (nzb <= SLICES)
                         {
-                            const float pz = (ilo[2] + zo) * g.step[2] + g.gmin[2];
-                            float ylo = FLT_MAX, yhi = -FLT_MAX;
+                            // rows of slice z: the y range of the tet's cross-section there,
+                            // from the edges that cross the plane, widened by a rounding
+                            // margin (an extra row is only visited, a dropped row would lose
+                            // points)
+                            float idz[6];
 #pragma unroll
                             for (int e = 0; e < 6; ++e)
                             {
                                 const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
                                 const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
-                                const float za = a[u][2], zb = a[v][2];
-                                if (pz < fminf(za, zb) || pz > fmaxf(za, zb))
-                                    continue;
-                                float y0, y1;
-                                if (za == zb)
-                                {
-                                    y0 = a[u][1];
-                                    y1 = a[v][1];
-                                }
-                                else
-                                {
-                                    const float tt = fminf(fmaxf((pz - za) * idz[e], 0.0f), 1.0f);
-                                    y0 = y1 = fmaf(tt, a[v][1] - a[u][1], a[u][1]);
-                                }
-                                ylo = fminf(ylo, fminf(y0, y1));
-                                yhi = fmaxf(yhi, fmaxf(y0, y1));
+                                const float dz = a[v][2] - a[u][2];
+                                idz[e] = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
                             }
-                            int cnt = 0, d0 = 0;
-                            if (ylo <= yhi)
+                            for (int zo = 0; zo < nzb; ++zo)
                             {
-                                const float my = 64.0f * EPS32 * (fmaxf(fabsf(ylo), fabsf(yhi)) + hi[1] - lo[1]);
-                                const float f0 = (ylo - my - g.gmin[1]) * g.inv_step[1];
-                                const float f1 = (yhi + my - g.gmin[1]) * g.inv_step[1];
-                                const float mm = 1e-3f + 8.0f * EPS32 * ((fabsf(g.gmin[1]) + fmaxf(fabsf(ylo), fabsf(yhi))) *
-                                                                         g.inv_step[1] + fmaxf(fabsf(f0), fabsf(f1)));
-                                const int y0i = max(ilo[1], (int)ceilf(fmaxf(f0 - mm, (float)(ilo[1] - 1))));
-                                const int y1i = min(ihi[1], (int)floorf(fminf(f1 + mm, (float)(ihi[1] + 1))));
-                                if (y1i >= y0i)
+                                const float pz = (ilo[2] + zo) * g.step[2] + g.gmin[2];
+                                float ylo = FLT_MAX, yhi = -FLT_MAX;
+#pragma unroll
+                                for (int e = 0; e < 6; ++e)
                                 {
-                                    cnt = y1i - y0i + 1;
-                                    d0 = y0i - ilo[1];
+                                    const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
+                                    const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
+                                    const float za = a[u][2], zb = a[v][2];
+                                    if (pz < fminf(za, zb) || pz > fmaxf(za, zb))
+                                        continue;
+                                    float y0, y1;
+                                    if (za == zb)
+                                    {
+                                        y0 = a[u][1];
+                                        y1 = a[v][1];
+                                    }
+                                    else
+                                    {
+                                        const float tt = fminf(fmaxf((pz - za) * idz[e], 0.0f), 1.0f);
+                                        y0 = y1 = fmaf(tt, a[v][1] - a[u][1], a[u][1]);
+                                    }
+                                    ylo = fminf(ylo, fminf(y0, y1));
+                                    yhi = fmaxf(yhi, fmaxf(y0, y1));
                                 }
+                                int cnt = 0, d0 = 0;
+                                if (ylo <= yhi)
+                                {
+                                    const float my = 64.0f * EPS32 * (fmaxf(fabsf(ylo), fabsf(yhi)) + hi[1] - lo[1]);
+                                    const float f0 = (ylo - my - g.gmin[1]) * g.inv_step[1];
+                                    const float f1 = (yhi + my - g.gmin[1]) * g.inv_step[1];
+                                    const float mm = 1e-3f + 8.0f * EPS32 *
+                                        ((fabsf(g.gmin[1]) + fmaxf(fabsf(ylo), fabsf(yhi))) * g.inv_step[1] +
+                                         fmaxf(fabsf(f0), fabsf(f1)));
+                                    const int y0i = max(ilo[1], (int)ceilf(fmaxf(f0 - mm, (float)(ilo[1] - 1))));
+                                    const int y1i = min(ihi[1], (int)floorf(fminf(f1 + mm, (float)(ihi[1] + 1))));
+                                    if (y1i >= y0i)
+                                    {
+                                        cnt = y1i - y0i + 1;
+                                        d0 = y0i - ilo[1];
+                                    }
+                                }
+                                S.SLC[zo][lane] = (d0 << 16) | cnt;
+                                rows += cnt;
                             }
-                            S.SLC[zo][lane] = (d0 << 16) | cnt;
-                            rows += cnt;
+                            masks |= 1 << 8;   // sliced
                         }
-                        S.I1[lane].w |= 1 << 8;   // sliced
+                        else
+                            rows = nyb * nzb;
+                        S.I1[lane] = make_int4(ilo[2], s, t - blocks[b].t_off, masks);
+                    }
+                }
+            }
+            // exclusive prefix of the tets' row counts
+            int incl = rows;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int v = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += v;
+            }
+            S.pre[lane + 1] = incl;
+            if (lane == 0) S.pre[0] = 0;
+            __syncwarp();
+            const int R = S.pre[32];
+
+            // ---- rounds of 32 rows: a lane per row finds its x range, then the
+            // rows' points are spread over the lanes
+            int j = 0;
+            for (int rbase = 0; rbase < R; rbase += 32)
+            {
+                const int r = rbase + lane;
+                int cnt = 0;
+                if (r < R)
+                {
+                    while (S.pre[j + 1] <= r) ++j;
+                    const int rr = r - S.pre[j];
+                    const int4 I0 = S.I0[j];
+                    const int4 I1 = S.I1[j];
+                    int zo, dy;
+                    if ((I1.w >> 8) & 1)
+                    {
+                        int q = rr;
+                        zo = 0;
+                        int sl = S.SLC[0][j];
+                        while (q >= (sl & 0xffff))
+                        {
+                            q -= sl & 0xffff;
+                            sl = S.SLC[++zo][j];
+                        }
+                        dy = (sl >> 16) + q;
                     }
                     else
-                        rows = nyb * nzb;
-                }
-            }
-        }
-        // exclusive prefix of the row counts
-        int incl = rows;
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const int v = __shfl_up_sync(FULL, incl, o);
-            if (lane >= o) incl += v;
-        }
-        S.pre[lane + 1] = incl;
-        if (lane == 0) S.pre[0] = 0;
-        __syncwarp();
-        const int R = S.pre[32];
-
-        // ---- phase B: one grid row per lane; each lane's tet index only grows
-        int j = 0;
-        for (int r = lane; r < R; r += 32)
-        {
-            while (S.pre[j + 1] <= r) ++j;
-            const int rr = r - S.pre[j];
-            const int4 I0 = S.I0[j];
-            const int4 I1 = S.I1[j];
-            int zo, dy;
-            if ((I1.w >> 8) & 1)
-            {
-                // sliced tet: walk the per-slice row counts
-                int q = rr;
-                zo = 0;
-                int sl = S.SLC[0][j];
-                while (q >= (sl & 0xffff))
-                {
-                    q -= sl & 0xffff;
-                    sl = S.SLC[++zo][j];
-                }
-                dy = (sl >> 16) + q;
-            }
-            else
-            {
-                const int ny = I0.w;
-                zo = (int)(((float)rr + 0.5f) * __frcp_rn((float)ny));
-                if (zo * ny > rr) --zo;
-                else if ((zo + 1) * ny <= rr) ++zo;
-                dy = rr - zo * ny;
-            }
-            const int yi = I0.z + dy;
-            const int zi = I1.x + zo;
-            const float4 A0 = S.A0[j], A1 = S.A1[j];
-            // x range of this row from the four affine face bounds
-            float xmin = A0.w, xmax = A1.w;
-            {
-                const float4 XA = S.XA[j], XB = S.XB[j], XG = S.XG[j];
-                const float fdy = (float)dy, fdz = (float)zo;
-                const int m = I1.w & 0xff;
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                {
-                    const float bnd = fmaf(comp4<float>(XG, k), fdz, fmaf(comp4<float>(XB, k), fdy, comp4<float>(XA, k)));
-                    if ((m >> (4 + k)) & 1) continue;
-                    if ((m >> k) & 1) xmin = fmaxf(xmin, bnd);
-                    else xmax = fminf(xmax, bnd);
-                }
-            }
-            nrows++;
-            if (xmin > xmax)
-                continue;
-            // grid indices inside [xmin, xmax]: an index estimate widened by m
-            // grid steps, where m exceeds the rounding of the estimate and of the
-            // float grid positions (2 eps |pos| each), so no point in the range is
-            // dropped; an extra point at the edge is classified like any other
-            const float f0 = (xmin - g.gmin[0]) * g.inv_step[0];
-            const float f1 = (xmax - g.gmin[0]) * g.inv_step[0];
-            const float m = 1e-3f + 8.0f * EPS32 * ((fabsf(g.gmin[0]) + fmaxf(fabsf(xmin), fabsf(xmax))) *
-                                                    g.inv_step[0] + fmaxf(fabsf(f0), fabsf(f1)));
-            const int i0 = max(I0.x, (int)ceilf(fmaxf(f0 - m, (float)(I0.x - 1))));
-            const int i1 = min(I0.y, (int)floorf(fminf(f1 + m, (float)(I0.y + 1))));
-            if (i0 > i1)
-                continue;
-            const float pyf = yi * g.step[1] + g.gmin[1];
-            const float pzf = zi * g.step[2] + g.gmin[2];
-            const int s = I1.y;
-            const T sf = (T)s;
-            T R4[4], Bk[4], cx[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-            {
-                const T4 ck = S.C[k][j];
-                const float by = k == 0 ? A1.y : A0.y, bz = k == 0 ? A1.z : A0.z;
-                const T qy = (T)pyf - (T)by, qz = (T)pzf - (T)bz;
-                R4[k] = Real<T>::fma_(ck.y, qy, ck.z * qz);
-                Bk[k] = ck.w;
-                cx[k] = ck.x;
-            }
-            const T4 W4 = S.W[j];
-            const size_t row = ((size_t)zi * g.n[1] + yi) * g.n[0];
-            ncand += i1 >= i0 ? i1 - i0 + 1 : 0;
-            for (int xi = i0; xi <= i1; ++xi)
-            {
-                const float pxf = xi * g.step[0] + g.gmin[0];
-                const T px = pxf;
-                T N[4];
-                N[0] = Real<T>::fma_(cx[0], px - (T)A1.x, R4[0]);
-                const T qx = px - (T)A0.x;
-                N[1] = Real<T>::fma_(cx[1], qx, R4[1]);
-                N[2] = Real<T>::fma_(cx[2], qx, R4[2]);
-                N[3] = Real<T>::fma_(cx[3], qx, R4[3]);
-                bool in = true, out = false;
-                unsigned open = 0;
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                {
-                    const T sn = sf * N[k];
-                    const bool ik = sn > Bk[k];
-                    in = in && ik;
-                    out = out || (sn < -Bk[k]);
-                    open |= (ik ? 0u : 1u) << k;
-                }
-                if (out)
-                    continue;
-                if (!in)
-                {
-                    nexact++;
-                    const int4 vt = __ldg(&tv[S.TG[j]]);
-                    const float4 A2 = __ldg(&pos[vt.z]), A3 = __ldg(&pos[vt.w]);
-                    if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf,
-                                      pyf, pzf, s, open))
-                        continue;
-                }
-                float f;
-                if (!VAL64 || !F32)
-                    f = (float)Real<T>::fma_(N[0], W4.x, Real<T>::fma_(N[1], W4.y,
-                                             Real<T>::fma_(N[2], W4.z, N[3] * W4.w)));
-                else
-                {
-                    const double q1[3] = { (double)pxf - A1.x, (double)pyf - A1.y, (double)pzf - A1.z };
-                    const double q0[3] = { (double)pxf - A0.x, (double)pyf - A0.y, (double)pzf - A0.z };
-                    double acc = 0.0;
-                    for (int k = 0; k < 4; ++k)
                     {
-                        const double* q = k == 0 ? q1 : q0;
-                        acc += (q[0] * S.C64[3 * k][j] + q[1] * S.C64[3 * k + 1][j] + q[2] * S.C64[3 * k + 2][j]) *
-                               S.W64[k][j];
+                        const int ny = I0.w;
+                        zo = (int)(((float)rr + 0.5f) * __frcp_rn((float)ny));
+                        if (zo * ny > rr) --zo;
+                        else if ((zo + 1) * ny <= rr) ++zo;
+                        dy = rr - zo * ny;
                     }
-                    f = (float)acc;
+                    const float4 A0 = S.A0[j], A1 = S.A1[j];
+                    float xmin = A0.w, xmax = A1.w;
+                    {
+                        const float4 XA = S.XA[j], XB = S.XB[j], XG = S.XG[j];
+                        const float fdy = (float)dy, fdz = (float)zo;
+                        const int m = I1.w & 0xff;
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            const float bnd = fmaf(comp4<float>(XG, k), fdz,
+                                                   fmaf(comp4<float>(XB, k), fdy, comp4<float>(XA, k)));
+                            if ((m >> (4 + k)) & 1) continue;
+                            if ((m >> k) & 1) xmin = fmaxf(xmin, bnd);
+                            else xmax = fminf(xmax, bnd);
+                        }
+                    }
+                    nrows++;
+                    if (xmin <= xmax)
+                    {
+                        // grid indices inside [xmin, xmax]: an index estimate widened by m
+                        // grid steps, where m exceeds the rounding of the estimate and of the
+                        // float grid positions (2 eps |pos| each), so no point in the range is
+                        // dropped; an extra point at the edge is classified like any other
+                        const float f0 = (xmin - g.gmin[0]) * g.inv_step[0];
+                        const float f1 = (xmax - g.gmin[0]) * g.inv_step[0];
+                        const float mg = 1e-3f + 8.0f * EPS32 * ((fabsf(g.gmin[0]) + fmaxf(fabsf(xmin), fabsf(xmax))) *
+                                                                 g.inv_step[0] + fmaxf(fabsf(f0), fabsf(f1)));
+                        const int i0 = max(I0.x, (int)ceilf(fmaxf(f0 - mg, (float)(I0.x - 1))));
+                        const int i1 = min(I0.y, (int)floorf(fminf(f1 + mg, (float)(I0.y + 1))));
+                        if (i0 <= i1)
+                        {
+                            const int yi = I0.z + dy, zi = I1.x + zo;
+                            const float pyf = yi * g.step[1] + g.gmin[1];
+                            const float pzf = zi * g.step[2] + g.gmin[2];
+                            T RN[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                            {
+                                const T4 ck = S.C[k][j];
+                                const float by = k == 0 ? A1.y : A0.y, bz = k == 0 ? A1.z : A0.z;
+                                const T qy = (T)pyf - (T)by, qz = (T)pzf - (T)bz;
+                                RN[k] = Real<T>::fma_(ck.y, qy, ck.z * qz);
+                            }
+                            ncand += i1 - i0 + 1;
+                            if (FLAT)
+                            {
+#pragma unroll
+                                for (int k = 0; k < 4; ++k)
+                                    S.RN[k][lane] = RN[k];
+                                S.RJ[lane] = j;
+                                S.RI0[lane] = i0;
+                                S.RY[lane] = yi;
+                                S.RZ[lane] = zi;
+                                cnt = i1 - i0 + 1;
+                            }
+                            else
+                            {
+                                // this lane's row, point by point
+                                T cx[4], Bk[4];
+#pragma unroll
+                                for (int k = 0; k < 4; ++k)
+                                {
+                                    const T4 ck = S.C[k][j];
+                                    cx[k] = ck.x;
+                                    Bk[k] = ck.w;
+                                }
+                                for (int xi = i0; xi <= i1; ++xi)
+                                    raster_point<T, VAL64>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv,
+                                                           pos, grid, owner, nexact, nassigned);
+                            }
+                        }
+                    }
                 }
-                grid[row + xi] = f;
-                if (owner)
-                    owner[row + xi] = I1.z;
-                nassigned++;
+                if (FLAT)
+                {
+                    // prefix of the rows' point counts, then the points spread over the lanes
+                    int pin = cnt;
+                    for (int o = 1; o < 32; o <<= 1)
+                    {
+                        const int v = __shfl_up_sync(FULL, pin, o);
+                        if (lane >= o) pin += v;
+                    }
+                    S.pp[lane + 1] = pin;
+                    if (lane == 0) S.pp[0] = 0;
+                    __syncwarp();
+                    const int P = S.pp[32];
+                    int rs = 0;
+                    for (int q = lane; q < P; q += 32)
+                    {
+                        while (S.pp[rs + 1] <= q) ++rs;
+                        const int jj = S.RJ[rs];
+                        const int xi = S.RI0[rs] + (q - S.pp[rs]);
+                        const int yi = S.RY[rs], zi = S.RZ[rs];
+                        const float pyf = yi * g.step[1] + g.gmin[1];
+                        const float pzf = zi * g.step[2] + g.gmin[2];
+                        const float4 A0 = S.A0[jj], A1 = S.A1[jj];
+                        const int4 I1 = S.I1[jj];
+                        T cx[4], Bk[4], RN[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            const T4 ck = S.C[k][jj];
+                            cx[k] = ck.x;
+                            Bk[k] = ck.w;
+                            RN[k] = S.RN[k][rs];
+                        }
+                        raster_point<T, VAL64>(S, jj, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv, pos, grid,
+                                               owner, nexact, nassigned);
+                    }
+                }
+                __syncwarp();
             }
+            __syncwarp();
         }
-        __syncwarp();
+        if (!more)
+            break;
     }
     for (int o = 16; o > 0; o >>= 1)
     {
@@ -840,42 +980,54 @@ void launch_densities(const unsigned long long* W, int n, float mass, double inv
 // Block residency per SM trades registers against latency hiding; which
 // bound is fastest depends on the GPU and the mesh, so the caller picks it
 // (variant 0, 1, 2 = 4, 5, 6 resident blocks per SM).
+// Launch variants.  Block residency per SM trades registers against latency
+// hiding; COMPACT screens tets with empty boxes out before the setup; FLAT
+// spreads a round's points over the lanes (good when a point is expensive,
+// as in FP64, costly in shared-memory traffic when it is cheap).  The
+// fastest depends on the GPU, the mesh and the mode, so the caller times them.
+//   0..2: per-lane rows, 4/5/6 blocks per SM    3: compact, 5 blocks
+//   4..5: compact + flat, 4/5 blocks per SM
+constexpr int N_RASTER_VARIANTS = 6;
+
 template <typename T, bool VAL64, bool LIST>
-static void raster_variant(int variant, int nblk, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
+static void raster_variant(int variant, long long work, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
                            const int* list, const int* list_count, const float4* pos, const int4* tv,
                            const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                            int* owner, int* fix_list, int* fix_count, Status* st)
 {
+    // the double-precision tables need more shared memory: 3 warps per block
+    constexpr int NW = (sizeof(T) == 4 && !VAL64) ? 4 : 3;
+    const int nblk = grid_for(work, NW * 32, 16);
+#define TG_RASTER(MB, C, F)                                                                                        \
+    k_raster<T, VAL64, LIST, MB, NW, C, F><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, \
+                                                                      rho32, rho64, g, tau, grid, owner, fix_list,  \
+                                                                      fix_count, st)
     switch (variant)
     {
-    case 1:
-        k_raster<T, VAL64, LIST, 5><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, rho32,
-                                                              rho64, g, tau, grid, owner, fix_list, fix_count, st);
-        break;
-    case 2:
-        k_raster<T, VAL64, LIST, 6><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, rho32,
-                                                              rho64, g, tau, grid, owner, fix_list, fix_count, st);
-        break;
-    default:
-        k_raster<T, VAL64, LIST, 4><<<nblk, RW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, rho32,
-                                                              rho64, g, tau, grid, owner, fix_list, fix_count, st);
-        break;
+    case 1: TG_RASTER(5, false, false); break;
+    case 2: TG_RASTER(6, false, false); break;
+    case 3: TG_RASTER(5, true, false); break;
+    case 4: TG_RASTER(4, true, true); break;
+    case 5: TG_RASTER(5, true, true); break;
+    default: TG_RASTER(4, false, false); break;
     }
+#undef TG_RASTER
 }
 
-int raster_variants() { return 3; }
+int raster_variants() { return N_RASTER_VARIANTS; }
+
 
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                    int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
-    const int nblk = grid_for((long long)((total + 31) / 32) * 32 * 32, RW * 32, 16);
+    const long long work = (long long)((total + 31) / 32) * 32 * 32;
     if (mode == TESSGPU_MODE_FP64)
-        raster_variant<double, true, false>(variant, nblk, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
+        raster_variant<double, true, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
                                             rho64, g, tau, grid, owner, nullptr, nullptr, st);
     else
-        raster_variant<float, false, false>(variant, nblk, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
+        raster_variant<float, false, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
                                             rho64, g, tau, grid, owner, fix_list, fix_count, st);
 }
 
@@ -886,8 +1038,8 @@ void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total, const float
                        const int* fix_list, const int* fix_count, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
-    const int nblk = grid_for((long long)((total / 16 + 31) / 32) * 32 * 32, RW * 32, 4);
-    raster_variant<float, true, true>(0, nblk, s, d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32, rho64, g,
+    const long long work = (long long)((total / 16 + 31) / 32) * 32 * 32;
+    raster_variant<float, true, true>(0, work, s, d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32, rho64, g,
                                       0.0f, grid, owner, nullptr, nullptr, st);
 }
 
