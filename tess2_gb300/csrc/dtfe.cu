@@ -365,13 +365,13 @@ __device__ __noinline__ bool inside_exact(float a00, float a01, float a02, float
 //   T=float,  VAL64=true,  LIST=true   mixed fix-up pass over fix_list: the same
 //       exact classification, values from an FP64 evaluation
 //   T=double, VAL64=true,  LIST=false  FP64 mode: everything in FP64
-constexpr int SLICES = 8;   // tets with at most this many z slices visit only their cross-section rows
+constexpr int SLICES = 16;  // tets with at most this many z slices visit only their cross-section rows
 
 template <typename T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; };
 template <> struct Vec4<double> { typedef double4 type; };
 
-template <typename T, bool VAL64>
+template <typename T, bool VAL64, bool FLAT, bool COMPACT>
 struct __align__(16) RasterSmem
 {
     typedef typename Vec4<T>::type T4;
@@ -386,10 +386,10 @@ struct __align__(16) RasterSmem
     int    SLC[SLICES][32];                  // per z slice: first row dy << 16 | rows
     int    pre[33];                          // prefix of the tets' row counts
     // per row of the current round (lane = row slot)
-    T      RN[4][32];                        // R_k(y, z) of the row
-    int    RJ[32], RI0[32], RY[32], RZ[32];  // tet slot, first x index, y, z
+    T      RN[4][FLAT ? 32 : 1];             // R_k(y, z) of the row
+    int    RJ[FLAT ? 32 : 1], RI0[FLAT ? 32 : 1], RY[FLAT ? 32 : 1], RZ[FLAT ? 32 : 1];  // tet slot, first x, y, z
     int    pp[33];                           // prefix of the rows' point counts
-    int    Q[64];                            // tets whose box holds grid points, waiting for a batch
+    int    Q[COMPACT ? 64 : 1];              // tets whose box holds grid points, waiting for a batch
     double C64[VAL64 && sizeof(T) == 4 ? 12 : 1][32];   // FP64 values for the fix-up pass
     double W64[VAL64 && sizeof(T) == 4 ? 4 : 1][32];
 };
@@ -432,8 +432,8 @@ __device__ __forceinline__ bool tet_box(const BlockDesc* blocks, int nb, const f
 // one grid point of a row: classify against the tet's four numerator planes
 // (exact arithmetic when the filter cannot decide) and write the
 // interpolated density when it is inside
-template <typename T, bool VAL64>
-__device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64>& S, int j, int xi, int yi, int zi, float pyf,
+template <typename T, bool VAL64, bool FLAT, bool COMPACT>
+__device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, FLAT, COMPACT>& S, int j, int xi, int yi, int zi, float pyf,
                                              float pzf, const float4& A0, const float4& A1, const int4& I1,
                                              const T* cx, const T* RN, const T* Bk, const GridDesc& g,
                                              const int4* tv, const float4* pos, float* grid, int* owner,
@@ -506,10 +506,10 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
          int* fix_list, int* fix_count, Status* st)
 {
     typedef typename Vec4<T>::type T4;
-    __shared__ RasterSmem<T, VAL64> smem[NW];
+    __shared__ RasterSmem<T, VAL64, FLAT, COMPACT> smem[NW];
     constexpr bool F32 = sizeof(T) == 4;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    RasterSmem<T, VAL64>& S = smem[wid];
+    RasterSmem<T, VAL64, FLAT, COMPACT>& S = smem[wid];
     unsigned long long nexact = 0, nassigned = 0, nfix = 0, nrows = 0, ncand = 0;
     const int n = LIST ? *list_count : total;
     const int nchunks = (n + 31) / 32;
@@ -881,7 +881,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                                     Bk[k] = ck.w;
                                 }
                                 for (int xi = i0; xi <= i1; ++xi)
-                                    raster_point<T, VAL64>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv,
+                                    raster_point<T, VAL64, FLAT, COMPACT>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv,
                                                            pos, grid, owner, nexact, nassigned);
                             }
                         }
@@ -920,7 +920,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                             Bk[k] = ck.w;
                             RN[k] = S.RN[k][rs];
                         }
-                        raster_point<T, VAL64>(S, jj, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv, pos, grid,
+                        raster_point<T, VAL64, FLAT, COMPACT>(S, jj, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv, pos, grid,
                                                owner, nexact, nassigned);
                     }
                 }
