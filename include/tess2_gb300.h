@@ -96,6 +96,10 @@ typedef struct tessgpu_dense_params
     float mass;                 /* mass of one particle */
     float eps;                  /* floating point tolerance (the reference's drivers use 1e-4) */
     int   glo_num_idx[3];       /* global grid points per axis */
+    int   use_data_bounds;      /* 1: data_mins/maxs below are the data bounds (DataBounds'
+                                   all-reduce over every rank's blocks); 0: the union of the
+                                   given blocks' bounds, as DataBounds computes on one rank */
+    float data_mins[3], data_maxs[3];
 } tessgpu_dense_params;
 
 /* Outputs of dense() besides the grid (src/dense.cpp:37-43, 1294-1300). */
@@ -143,6 +147,13 @@ tessgpu_status tessgpu_fill_vert_to_tet(tessgpu_ctx* ctx, int num_particles, con
    (src/tet.cpp:37-66): 3 floats per tet, bit-identical to the reference */
 tessgpu_status tessgpu_fill_circumcenters(tessgpu_ctx* ctx, const float* particles, int num_particles,
                                           const int* tets, int num_tets, float* circumcenters);
+
+/* replaces reorder_neighbors (src/tess-qhull.c:161-225), run after Qhull's
+   output is copied into tet_t records: reorders each tet's four neighbours in
+   place so that tets[i] lies opposite verts[i] (-1 on the hull). */
+tessgpu_status tessgpu_reorder_neighbors(tessgpu_ctx* ctx, int* tets, int num_tets);
+/* the same on tet_t records already in device memory */
+tessgpu_status tessgpu_reorder_neighbors_device(tessgpu_ctx* ctx, int* d_tets, int num_tets);
 
 /* replaces complete (src/tet.cpp:337-378) for vertices [0, n): 1 finite
    Voronoi cell, 0 cell on the hull, -1 where vert_to_tet is -1 */

@@ -188,6 +188,11 @@ class Restated(Oracle):
                                       _ptr(out))
         return out
 
+    def reorder_neighbors(self, tets):
+        out = np.array(tets, dtype=np.int32, copy=True, order="C")
+        self._l.f("reorder_neighbors")(_ptr(out), ctypes.c_int(out.shape[0]))
+        return out
+
     def fill_circumcenters_f64(self, particles, tets):
         out = np.empty((tets.shape[0], 3), np.float64)
         self._l.f("fill_circumcenters_f64")(_ptr(particles), _ptr(tets), ctypes.c_int(tets.shape[0]), _ptr(out))

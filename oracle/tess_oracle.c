@@ -979,6 +979,40 @@ long orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float
     return lost;
 }
 
+/* src/tess-qhull.c:161-225: for vertex v in order, the first neighbour not yet
+   taken that does not hold verts[v]; -1 when none does */
+void orc_reorder_neighbors(orc_tet* tets, int num_tets)
+{
+    for (int t = 0; t < num_tets; ++t)
+    {
+        int nb[4], out[4];
+        for (int n = 0; n < 4; ++n)
+            nb[n] = tets[t].tets[n];
+        for (int v = 0; v < 4; ++v)
+        {
+            out[v] = -1;
+            for (int n = 0; n < 4; ++n)
+            {
+                int c = nb[n];
+                if (c < 0)
+                    continue;
+                int has = 0;
+                for (int k = 0; k < 4; ++k)
+                    if (tets[c].verts[k] == tets[t].verts[v])
+                        has = 1;
+                if (!has)
+                {
+                    out[v] = c;
+                    nb[n] = -2;
+                    break;
+                }
+            }
+        }
+        for (int n = 0; n < 4; ++n)
+            tets[t].tets[n] = out[n];
+    }
+}
+
 /* ------------------------------------------------------------------ */
 /* part 2: FP64 judges                                                */
 /* ------------------------------------------------------------------ */

@@ -91,6 +91,9 @@ long  orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const floa
                        float* global_grid, float* grid_out6, float* data_out6, double* stats3,
                        int* cell_counts);
 
+/* src/tess-qhull.c:161-225, in place */
+void  orc_reorder_neighbors(orc_tet* tets, int num_tets);
+
 /* ---- part 2: FP64 judges ---- */
 void  orc_fill_circumcenters_f64(const float* particles, const orc_tet* tets, int num_tets, double* out);
 void  orc_volumes_f64(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,

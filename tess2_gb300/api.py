@@ -44,7 +44,9 @@ class DenseParams(ctypes.Structure):
     """tessgpu_dense_params"""
     _fields_ = [("alg", ctypes.c_int), ("mode", ctypes.c_int), ("num_given_bounds", ctypes.c_int),
                 ("given_mins", ctypes.c_float * 3), ("given_maxs", ctypes.c_float * 3),
-                ("mass", ctypes.c_float), ("eps", ctypes.c_float), ("glo_num_idx", ctypes.c_int * 3)]
+                ("mass", ctypes.c_float), ("eps", ctypes.c_float), ("glo_num_idx", ctypes.c_int * 3),
+                ("use_data_bounds", ctypes.c_int), ("data_mins", ctypes.c_float * 3),
+                ("data_maxs", ctypes.c_float * 3)]
 
 
 class DenseInfo(ctypes.Structure):
@@ -107,6 +109,8 @@ def lib():
             "tessgpu_batch_keep_debug": (_I, [_VP, _I]),
             "tessgpu_batch_debug_outputs": (_I, [_VP, _VP, _VP, _VP, _VP]),
             "tessgpu_set_timing": (_I, [_VP, _I]),
+            "tessgpu_reorder_neighbors": (_I, [_VP, _VP, _I]),
+            "tessgpu_reorder_neighbors_device": (_I, [_VP, _VP, _I]),
             "tessgpu_stage_times": (_I, [_VP, _VP, _VP, _I]),
             "tessgpu_dtfe_densities_noalloc": (_I, [_VP, _I, _VP, _I, _VP, ctypes.c_float, _I, _VP, _VP]),
         }
@@ -149,8 +153,15 @@ def make_blocks(blocks):
     return arr, keep
 
 
-def make_params(alg, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None):
+def make_params(alg, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, data_bounds=None):
+    """data_bounds=(mins, maxs) fixes dense()'s data bounds (every rank's all-reduced
+    bounds when this process holds a share of the blocks)."""
     p = DenseParams()
+    if data_bounds is not None:
+        p.use_data_bounds = 1
+        for d in range(3):
+            p.data_mins[d] = data_bounds[0][d]
+            p.data_maxs[d] = data_bounds[1][d]
     p.alg = int(alg)
     p.mode = int(mode)
     if given is not None:
@@ -213,6 +224,16 @@ class Context:
         self._check(lib().tessgpu_fill_vert_to_tet(self._h, num_particles, _p(tets), tets.shape[0], _p(out)))
         return out
 
+    def reorder_neighbors(self, tets):
+        """reorder_neighbors (src/tess-qhull.c:161-225) on a copy of (T, 8) tet_t records."""
+        out = np.array(tets, dtype=np.int32, copy=True, order="C")
+        self._check(lib().tessgpu_reorder_neighbors(self._h, _p(out), out.shape[0]))
+        return out
+
+    def reorder_neighbors_device(self, d_tets, num_tets):
+        """in place on tet_t records in device memory (address d_tets)"""
+        self._check(lib().tessgpu_reorder_neighbors_device(self._h, ctypes.c_void_p(d_tets), num_tets))
+
     def fill_circumcenters(self, tets, particles):
         tets = np.ascontiguousarray(tets, np.int32)
         particles = np.ascontiguousarray(particles, np.float32)
@@ -253,10 +274,10 @@ class Context:
         return out
 
     def dense(self, alg, blocks, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, block_arrays=False,
-              global_grid=True, out=None):
+              global_grid=True, out=None, data_bounds=None):
         """dense() over host blocks.  Returns dict(grid=(nz,ny,nx) float32, info=..., blocks=[...])."""
         arr, keep = make_blocks(blocks)
-        p = make_params(alg, glo_num_idx, mass, eps, mode, given)
+        p = make_params(alg, glo_num_idx, mass, eps, mode, given, data_bounds)
         grid = None
         if global_grid:
             grid = out if out is not None else np.empty((glo_num_idx[2], glo_num_idx[1], glo_num_idx[0]), np.float32)
@@ -306,9 +327,10 @@ class Batch:
     def keep_debug(self, on=True):
         self.ctx._check(lib().tessgpu_batch_keep_debug(self._h, 1 if on else 0))
 
-    def dense(self, alg, glo_num_idx, d_grid, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, want_info=True):
+    def dense(self, alg, glo_num_idx, d_grid, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, want_info=True,
+              data_bounds=None):
         """dense() into the device grid at address d_grid (an int, e.g. torch tensor.data_ptr())."""
-        p = make_params(alg, glo_num_idx, mass, eps, mode, given)
+        p = make_params(alg, glo_num_idx, mass, eps, mode, given, data_bounds)
         info = DenseInfo() if want_info else None
         self.ctx._check(lib().tessgpu_batch_dense(self.ctx.handle, self._h, ctypes.byref(p), ctypes.c_void_p(d_grid),
                                                   ctypes.byref(info) if info is not None else None))

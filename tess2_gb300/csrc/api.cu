@@ -169,9 +169,15 @@ extern "C" tessgpu_status tessgpu_sync(tessgpu_ctx* ctx)
 // ---------------------------------------------------------------------------
 // dense() grid parameters on the host, in the reference's FP32 order
 // ---------------------------------------------------------------------------
-// DataBounds (src/dense.cpp:1221-1275)
-static void data_bounds(int nb, const tessgpu_block* b, float* mn, float* mx)
+// DataBounds (src/dense.cpp:1221-1275): the union of the blocks' bounds, or
+// the caller's all-reduced bounds when it processes a share of the blocks
+static void data_bounds(int nb, const tessgpu_block* b, const tessgpu_dense_params* p, float* mn, float* mx)
 {
+    if (p->use_data_bounds)
+    {
+        for (int d = 0; d < 3; ++d) { mn[d] = p->data_mins[d]; mx[d] = p->data_maxs[d]; }
+        return;
+    }
     for (int i = 0; i < nb; ++i)
         for (int d = 0; d < 3; ++d)
         {
@@ -253,7 +259,7 @@ extern "C" long long tessgpu_block_grid_points(int nblocks, const tessgpu_block*
 {
     if (nblocks <= 0 || !blocks || b < 0 || b >= nblocks || !valid_params(p)) return -1;
     float dmin[3], dmax[3], gmin[3], gmax[3], step[3];
-    data_bounds(nblocks, blocks, dmin, dmax);
+    data_bounds(nblocks, blocks, p, dmin, dmax);
     grid_step_params(p, dmin, dmax, gmin, gmax, step);
     int mn[3], mx[3], num[3];
     block_grid_params(blocks[b], gmin, step, p->eps, dmin, dmax, p->glo_num_idx, mn, mx, num);
@@ -535,7 +541,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     cudaStream_t s = ctx->stream;
     const int nb = bt->nb;
     float dmin[3], dmax[3], gmin[3], gmax[3], step[3];
-    data_bounds(nb, bt->blocks.data(), dmin, dmax);
+    data_bounds(nb, bt->blocks.data(), p, dmin, dmax);
     grid_step_params(p, dmin, dmax, gmin, gmax, step);
     GridDesc g;
     for (int i = 0; i < 3; ++i)
@@ -949,4 +955,33 @@ extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tes
         s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     tessgpu_batch_free(bt);
     return s;
+}
+
+// ---------------------------------------------------------------------------
+// reorder_neighbors
+// ---------------------------------------------------------------------------
+extern "C" tessgpu_status tessgpu_reorder_neighbors_device(tessgpu_ctx* ctx, int* d_tets, int num_tets)
+{
+    if (!ctx || num_tets < 0 || (num_tets && !d_tets)) return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    if (!num_tets) return TESSGPU_OK;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), ctx->stream));
+    launch_reorder_neighbors(d_tets, num_tets, ctx->d_status, ctx->stream);
+    ctx->launches++;
+    return finish_status(ctx);
+}
+
+extern "C" tessgpu_status tessgpu_reorder_neighbors(tessgpu_ctx* ctx, int* tets, int num_tets)
+{
+    if (!ctx || num_tets < 0 || (num_tets && !tets)) return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    if (!num_tets) return TESSGPU_OK;
+    CK(cudaSetDevice(ctx->device));
+    cudaError_t e;
+    int* d = (int*)pool_get(ctx, SLOT_STAGE, sizeof(int) * 8 * (size_t)num_tets, &e);
+    CK(e);
+    CK(cudaMemcpyAsync(d, tets, sizeof(int) * 8 * (size_t)num_tets, cudaMemcpyHostToDevice, ctx->stream));
+    tessgpu_status s = tessgpu_reorder_neighbors_device(ctx, d, num_tets);
+    if (s != TESSGPU_OK) return s;
+    CK(cudaMemcpy(tets, d, sizeof(int) * 8 * (size_t)num_tets, cudaMemcpyDeviceToHost));
+    return TESSGPU_OK;
 }

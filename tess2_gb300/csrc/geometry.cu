@@ -824,6 +824,49 @@ __global__ void k_cic(const BlockDesc* blocks, const int* c_off, int nb, int tot
     }
 }
 
+// reorder_neighbors (src/tess-qhull.c:161-225): for vertex v = 0..3 in turn,
+// the first still-unused neighbour (in the given order) that does not hold
+// verts[v] becomes tets[v]; -1 when none does (a hull face).  Each tet only
+// reads the other tets' vertices, which never change, so tets are independent.
+__global__ void k_reorder_neighbors(int* tets, int total, Status* st)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+    {
+        int* r = tets + 8 * (size_t)t;
+        int v[4], nb[4], out[4];
+        for (int i = 0; i < 4; ++i)
+        {
+            v[i] = r[i];
+            nb[i] = r[4 + i];
+            if (nb[i] >= total || nb[i] < -1)
+            {
+                fail(st, TESSGPU_ERR_BAD_MESH, t);
+                nb[i] = -1;
+            }
+        }
+        for (int i = 0; i < 4; ++i)
+        {
+            out[i] = -1;
+            for (int n = 0; n < 4; ++n)
+            {
+                const int c = nb[n];
+                if (c < 0)   // -1 (hull) or -2 (taken)
+                    continue;
+                const int4 cv = make_int4(tets[8 * (size_t)c], tets[8 * (size_t)c + 1], tets[8 * (size_t)c + 2],
+                                          tets[8 * (size_t)c + 3]);
+                if (cv.x != v[i] && cv.y != v[i] && cv.z != v[i] && cv.w != v[i])
+                {
+                    out[i] = c;
+                    nb[n] = -2;
+                    break;
+                }
+            }
+        }
+        for (int i = 0; i < 4; ++i)
+            r[4 + i] = out[i];
+    }
+}
+
 __global__ void k_grid_max(const float* grid, long long n, float* out)
 {
     float m = 0.0f;
@@ -910,6 +953,12 @@ void launch_cic(const BlockDesc* d_blocks, const int* d_c_off, int nb, int total
 {
     if (total <= 0) return;
     k_cic<<<grid1d(total, 256), 256, 0, s>>>(d_blocks, d_c_off, nb, total, pos, g, grid, st);
+}
+
+void launch_reorder_neighbors(int* d_tets, int total, Status* st, cudaStream_t s)
+{
+    if (total <= 0) return;
+    k_reorder_neighbors<<<grid1d(total, 256), 256, 0, s>>>(d_tets, total, st);
 }
 
 void launch_grid_max(const float* grid, long long n, float* d_max, cudaStream_t s)

@@ -144,3 +144,23 @@ def tessellate(blocks, processes=None):
         b["tets"] = t
         b["vert_to_tet"] = vert_to_tet_host(b["particles"].shape[0], t)
     return blocks
+
+
+def shard_blocks(blocks, rank, world):
+    """The blocks rank `rank` of `world` processes (round robin by position).
+
+    Blocks are independent units of the density path: each writes only the
+    grid points of its own BlockGridParams box, so ranks need no exchange on
+    the data path; the data bounds all ranks must agree on are those of the
+    whole decomposition (data_bounds_of(blocks)).
+    """
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad rank/world")
+    return blocks[rank::world]
+
+
+def data_bounds_of(blocks):
+    """DataBounds over all blocks (src/dense.cpp:1221-1275): min/max of block bounds."""
+    mn = np.min([b["bounds_min"] for b in blocks], axis=0).astype(np.float32)
+    mx = np.max([b["bounds_max"] for b in blocks], axis=0).astype(np.float32)
+    return mn, mx

@@ -150,3 +150,33 @@ def test_dtfe_multiblock(gpu_ctx, oracle, mode, tol):
     ref, grid, owner, info = _dtfe_case(oracle, gpu_ctx, blocks, gni, mode)
     assert np.array_equal(owner, ref["owner"])
     assert rel_l2(grid, ref["grid"]) < tol
+
+
+def test_dtfe_sharded_blocks_sum_to_whole(gpu_ctx):
+    """Blocks split over two shares (as ranks would hold them), each run with
+    the whole decomposition's data bounds: the grids add up to the one-batch
+    grid bit for bit, since every grid point has one owner."""
+    import torch
+    from tess2_gb300 import host
+    from tess2_gb300.api import DENSE_DTFE
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    gni = [int(x) for x in d["glo_num_idx"]]
+    whole = torch.zeros(gni[2], gni[1], gni[0], dtype=torch.float32, device="cuda")
+    gpu_ctx.upload(blocks).dense(DENSE_DTFE, gni, whole.data_ptr())
+    bounds = host.data_bounds_of(blocks)
+    total = torch.zeros_like(whole)
+    for r in range(2):
+        part = torch.zeros_like(whole)
+        gpu_ctx.upload(host.shard_blocks(blocks, r, 2)).dense(DENSE_DTFE, gni, part.data_ptr(), data_bounds=bounds)
+        total += part
+    assert torch.equal(total, whole)
+
+
+@pytest.mark.parametrize("name", SINGLE)
+def test_reorder_neighbors_bitexact(gpu_ctx, oracle, name):
+    from test_oracle_golden import shuffled_neighbors
+    d = load_single(name)
+    shuf = shuffled_neighbors(d["tets"], 2)
+    got = gpu_ctx.reorder_neighbors(shuf)
+    assert np.array_equal(got, oracle.reorder_neighbors(shuf))
+    assert np.array_equal(got, d["tets"])

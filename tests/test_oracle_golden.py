@@ -87,3 +87,19 @@ def test_empty_and_tiny_blocks(oracle):
     assert r["grid"].sum() == 0
     r = oracle.dense(1, [four], [8, 8, 8])
     assert r["check_mass"] == 4
+
+
+def shuffled_neighbors(tets, seed):
+    """tet_t records with each tet's neighbour list permuted (Qhull's order)."""
+    rng = np.random.default_rng(seed)
+    t = tets.copy()
+    perm = np.argsort(rng.random((t.shape[0], 4)), axis=1)
+    t[:, 4:] = np.take_along_axis(t[:, 4:], perm, axis=1)
+    return t
+
+
+@pytest.mark.parametrize("name", SINGLE)
+def test_reorder_neighbors(oracle, name):
+    d = load_single(name)
+    got = oracle.reorder_neighbors(shuffled_neighbors(d["tets"], 1))
+    assert np.array_equal(got, d["tets"])
