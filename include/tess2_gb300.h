@@ -43,7 +43,8 @@ typedef enum tessgpu_status
     TESSGPU_ERR_FACE_OVERFLOW  = 5,   /* a Voronoi cell exceeded TESSGPU_MAX_FACES faces */
     TESSGPU_ERR_LINK_OVERFLOW  = 6,   /* an edge ring exceeded TESSGPU_MAX_LINK tets */
     TESSGPU_ERR_BAD_MESH       = 7,   /* an index out of range or a broken adjacency */
-    TESSGPU_ERR_UNSUPPORTED    = 8
+    TESSGPU_ERR_UNSUPPORTED    = 8,
+    TESSGPU_ERR_IO             = 9    /* a file could not be opened or written */
 } tessgpu_status;
 
 /* bounds of the device loops; larger inputs report the overflow codes */
@@ -100,6 +101,10 @@ typedef struct tessgpu_dense_params
                                    all-reduce over every rank's blocks); 0: the union of the
                                    given blocks' bounds, as DataBounds computes on one rank */
     float data_mins[3], data_maxs[3];
+    int   project;              /* 1: project onto the x-y plane (dense()'s project with
+                                   proj_plane (0,0,1), the one plane the reference's
+                                   index() supports, src/dense.cpp:1077): densities are
+                                   mass per area, summed over z (see tessgpu_project_grid) */
 } tessgpu_dense_params;
 
 /* Outputs of dense() besides the grid (src/dense.cpp:37-43, 1294-1300). */
@@ -117,6 +122,8 @@ typedef struct tessgpu_dense_info
     long long points_tested;    /* DTFE: grid points the rasteriser classified */
     int       raster_variant;   /* DTFE: launch configuration the autotuner chose for this batch */
     float     raster_variant_ms[8]; /* DTFE: the autotuner's best time of each configuration (0 if not run) */
+    int       grid_layers;      /* project: z layers of the device grid; 0 for a 3-D grid */
+    long long grid_floats;      /* floats of the device grid tessgpu_batch_dense wrote */
 } tessgpu_dense_info;
 
 /* ---- context ---------------------------------------------------------- */
@@ -176,17 +183,21 @@ tessgpu_status tessgpu_volumes_f64(tessgpu_ctx* ctx, const float* particles, int
 
 /* replaces dense (src/dense.cpp:30-103) over nblocks blocks.  global_grid
    (may be NULL) receives the whole grid, glo_num_idx[0]*[1]*[2] floats, x
-   fastest (what WriteGrid writes).  block_density (may be NULL) is an array of
+   fastest (what WriteGrid writes); with params->project it receives the
+   projected glo_num_idx[0]*[1] floats after ProjectGrid's sum over z, which
+   is what WriteGrid writes then.  block_density (may be NULL) is an array of
    nblocks host pointers; block b's array must hold
    tessgpu_block_grid_points(...) floats and receives that block's density as
-   init_dense/est_dense/recvd_pts leave it.  info may be NULL. */
+   init_dense/est_dense/recvd_pts leave it (projected: the block's own z range
+   only, before ProjectGrid).  info may be NULL. */
 tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tessgpu_block* blocks,
                              const tessgpu_dense_params* params, float* global_grid,
                              float** block_density, tessgpu_dense_info* info);
 
 /* BlockGridParams (src/dense.cpp:575-648) of block b for the grid that
    dense() derives from params; writes min_idx[3], max_idx[3], num_idx[3] to
-   out9 and returns the block's number of grid points. */
+   out9 and returns the block's number of grid points (num_idx[0]*num_idx[1]
+   when projecting, as init_dense allocates, src/dense.cpp:118-121). */
 long long      tessgpu_block_grid_points(int nblocks, const tessgpu_block* blocks, int b,
                                          const tessgpu_dense_params* params, int* out9);
 
@@ -202,10 +213,39 @@ tessgpu_status tessgpu_batch_wrap_device(tessgpu_ctx* ctx, int nblocks, const te
 void           tessgpu_batch_free(tessgpu_batch* batch);
 
 /* dense() on a device batch into a device grid (d_grid: glo_num_idx product
-   floats, x fastest).  Nothing is copied to or from the host except info. */
+   floats, x fastest).  Nothing is copied to or from the host except info.
+   With params->project, d_grid holds L layers of glo_num_idx[0]*[1] floats,
+   one per distinct z range of the blocks' BlockGridParams boxes (layer 0 the
+   lowest): layer l holds what the blocks of that z range hold after dense()
+   and before ProjectGrid; tessgpu_project_grid sums them. */
 tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* batch,
                                    const tessgpu_dense_params* params, float* d_grid,
                                    tessgpu_dense_info* info);
+
+/* floats d_grid of tessgpu_batch_dense needs for these blocks and params, and
+   (layers, may be NULL) its number of z layers: 0 for a 3-D grid */
+long long      tessgpu_dense_grid_floats(int nblocks, const tessgpu_block* blocks,
+                                         const tessgpu_dense_params* params, int* layers);
+
+/* ---- output: ProjectGrid and WriteGrid -------------------------------- */
+
+/* ProjectGrid (src/dense.cpp:881-1023) on device memory: d_out[i] is the sum
+   over l = 0 .. num_layers-1, in that order, of d_layers[l * layer_floats + i]
+   (the z=0 block of each column adds the blocks above it in block order). */
+tessgpu_status tessgpu_project_grid(tessgpu_ctx* ctx, const float* d_layers, int num_layers,
+                                    long long layer_floats, float* d_out);
+
+/* WriteGrid's file (src/dense.cpp:751-870): num_floats floats of device
+   memory written to path as raw native float32 in the given order (x
+   fastest for a grid), the file truncated first.  The data goes device ->
+   pinned staging buffers -> file; the copy of one chunk overlaps the write
+   of the previous one.  Fails with TESSGPU_ERR_IO. */
+tessgpu_status tessgpu_write_grid(tessgpu_ctx* ctx, const float* d_grid, long long num_floats,
+                                  const char* path);
+
+/* WriteGrid as tess2 calls it after dense(): writes the global grid of this
+   context's last tessgpu_dense call, projected when that call projected. */
+tessgpu_status tessgpu_write_last_grid(tessgpu_ctx* ctx, const char* path);
 
 /* Validation outputs of the last tessgpu_batch_dense call, copied to host:
    cell_counts (DENSE_TESS: per original particle of every block in order,

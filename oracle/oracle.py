@@ -121,12 +121,15 @@ class Oracle:
             raise ValueError("neighbor_edges overflow")
         return pairs[:2 * n].reshape(n, 2).copy(), bool(fin.value)
 
-    def dense(self, alg, blocks, glo_num_idx, mass=1.0, eps=1e-4, given=None, cell_counts=False, data6=None):
+    def dense(self, alg, blocks, glo_num_idx, mass=1.0, eps=1e-4, given=None, cell_counts=False, data6=None,
+              project=False, block_arrays=False):
         """dense() into a global grid (z, y, x order, x fastest).  data6 (restated
-        oracle only) fixes the data bounds, as DataBounds' all-reduce would."""
+        oracle only) fixes the data bounds, as DataBounds' all-reduce would.
+        project (restated oracle only): x-y projection; grid is then (y, x) after
+        ProjectGrid and block_arrays returns each block's array before it."""
         arr, keep = make_blocks(blocks)
         gni = np.ascontiguousarray(glo_num_idx, dtype=np.int32)
-        grid = np.zeros((gni[2], gni[1], gni[0]), np.float32)
+        grid = np.zeros((gni[1], gni[0]) if project else (gni[2], gni[1], gni[0]), np.float32)
         g6 = np.zeros(6, np.float32)
         d6 = np.zeros(6, np.float32)
         st = np.zeros(3, np.float64)
@@ -140,13 +143,18 @@ class Oracle:
         if self.which == "oracle":
             total = sum(int(b["num_orig"]) for b in blocks)
             cc = np.zeros(max(total, 1), np.int32) if cell_counts else None
-            fn = self._l.f("dense_bounds")
+            fn = self._l.f("dense_ex")
             fn.restype = ctypes.c_long
             db = None if data6 is None else np.ascontiguousarray(data6, np.float32)
-            lost = fn(ctypes.c_int(alg), ctypes.c_int(len(blocks)), arr, _ptr(db), ctypes.c_int(ngiven), _ptr(gmin),
-                      _ptr(gmax), ctypes.c_float(mass), ctypes.c_float(eps), _ptr(gni), _ptr(grid),
-                      _ptr(g6), _ptr(d6), _ptr(st), _ptr(cc))
+            # per-block array sizes bound: a block array never exceeds the global grid
+            bo = np.zeros(len(blocks) * int(np.prod(gni)) // (int(gni[2]) if project else 1), np.float32) \
+                if block_arrays else None
+            lost = fn(ctypes.c_int(alg), ctypes.c_int(len(blocks)), arr, _ptr(db), ctypes.c_int(1 if project else 0),
+                      ctypes.c_int(ngiven), _ptr(gmin), _ptr(gmax), ctypes.c_float(mass), ctypes.c_float(eps),
+                      _ptr(gni), _ptr(grid), _ptr(bo), _ptr(g6), _ptr(d6), _ptr(st), _ptr(cc))
             res["lost"] = int(lost)
+            if block_arrays:
+                res["block_concat"] = bo
             if cell_counts:
                 res["cell_counts"] = cc[:total]
         else:
@@ -157,6 +165,34 @@ class Oracle:
                    data_max=d6[3:].copy(), max_dense=st[0], tot_mass=st[1], check_mass=st[2])
         del keep
         return res
+
+    def dense_write(self, alg, blocks, glo_num_idx, path, project=False, mass=1.0, eps=1e-4, given=None):
+        """The reference build only: dense() then WriteGrid(outfile=path), as
+        examples/dense/main.cpp calls them.  Returns the blocks' arrays as dense()
+        leaves them and the dense_stats values; the file is at path."""
+        assert self.which == "ref"
+        arr, keep = make_blocks(blocks)
+        gni = np.ascontiguousarray(glo_num_idx, dtype=np.int32)
+        nb = len(blocks)
+        bo = np.zeros(nb * int(np.prod(gni)), np.float32)
+        sizes = np.zeros(nb, np.int32)
+        st = np.zeros(3, np.float64)
+        ngiven = 0
+        gmin = gmax = None
+        if given is not None:
+            ngiven = 3
+            gmin = np.ascontiguousarray(given[0], dtype=np.float32)
+            gmax = np.ascontiguousarray(given[1], dtype=np.float32)
+        self._l.f("dense_write")(ctypes.c_int(alg), ctypes.c_int(nb), arr, ctypes.c_int(ngiven), _ptr(gmin),
+                                 _ptr(gmax), ctypes.c_float(mass), ctypes.c_float(eps), _ptr(gni),
+                                 ctypes.c_int(1 if project else 0), os.fsencode(path), _ptr(bo), _ptr(sizes),
+                                 _ptr(st))
+        del keep
+        out, off = [], 0
+        for n in sizes:
+            out.append(bo[off:off + n].copy())
+            off += n
+        return dict(blocks=out, max_dense=st[0], tot_mass=st[1], check_mass=st[2])
 
     def cell_grid_pts(self, block, cell, data_min, data_max, grid_min, grid_step, mass=1.0, eps=1e-4,
                       cap=1 << 16):
@@ -214,6 +250,35 @@ class Restated(Oracle):
         tet = np.ascontiguousarray(tet, np.int32)
         p = np.ascontiguousarray(p, np.float32)
         return bool(self._l.f("tet_contains")(_ptr(particles), _ptr(tet), _ptr(p)))
+
+    @staticmethod
+    def z_layers(block_zmin, nz):
+        """Layer of each z index of a projected grid: one layer per distinct
+        first z index of the blocks' BlockGridParams boxes, ascending."""
+        starts = sorted(set(int(min(max(z, 0), nz - 1)) for z in block_zmin))
+        zl = np.zeros(nz, np.int32)
+        for l, z0 in enumerate(starts):
+            zl[z0:] = l
+        return zl, max(len(starts), 1)
+
+    @staticmethod
+    def project_layers(grid3, zl, dz):
+        """z-projection of a (z, y, x) float32 grid into layers: layer l
+        accumulates grid * dz over its z indices in ascending z, in float32."""
+        nl = int(zl.max()) + 1
+        out = np.zeros((nl,) + grid3.shape[1:], np.float32)
+        dz = np.float32(dz)
+        for z in range(grid3.shape[0]):
+            out[zl[z]] = out[zl[z]] + grid3[z] * dz
+        return out
+
+    @staticmethod
+    def sum_layers(layers):
+        """ProjectGrid's column sum: layer 0 plus layers 1.. in order, in float32."""
+        acc = layers[0].copy()
+        for l in range(1, layers.shape[0]):
+            acc = acc + layers[l]
+        return acc
 
     def dtfe(self, blocks, glo_num_idx, mass=1.0, eps=1e-4, given=None, want_owner=True, want_rho=True,
              data6=None, raster_stride=1):

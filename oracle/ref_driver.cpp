@@ -156,13 +156,8 @@ int ref_cell_grid_pts(const ref_block* rb, int cell, const float* data_mins, con
 // grid_out6 receives grid_phys_mins[3], grid_step_size[3]; data_out6 the data
 // bounds; stats3 the values dense_stats() reduces: max_dense, tot_mass,
 // check_mass (accumulated over all calls in this process, as in the reference).
-void ref_dense(int alg_type, int nblocks, const ref_block* blocks,
-               int num_given_bounds, const float* given_mins, const float* given_maxs,
-               float mass, float eps, const int* glo_num_idx,
-               float* global_grid, float* grid_out6, float* data_out6, double* stats3)
+static void add_blocks(diy::Master& master, std::vector<DBlock*>& dbs, int nblocks, const ref_block* blocks)
 {
-    diy::Master master;
-    std::vector<DBlock*> dbs;
     for (int i = 0; i < nblocks; ++i)
     {
         DBlock* b = make_dblock(blocks[i]);
@@ -179,6 +174,16 @@ void ref_dense(int alg_type, int nblocks, const ref_block* blocks,
         master.add(blocks[i].gid, b, l);
         dbs.push_back(b);
     }
+}
+
+void ref_dense(int alg_type, int nblocks, const ref_block* blocks,
+               int num_given_bounds, const float* given_mins, const float* given_maxs,
+               float mass, float eps, const int* glo_num_idx,
+               float* global_grid, float* grid_out6, float* data_out6, double* stats3)
+{
+    diy::Master master;
+    std::vector<DBlock*> dbs;
+    add_blocks(master, dbs, nblocks, blocks);
 
     float gmins[3] = {0, 0, 0}, gmaxs[3] = {0, 0, 0};
     if (given_mins) for (int i = 0; i < 3; ++i) gmins[i] = given_mins[i];
@@ -216,6 +221,54 @@ void ref_dense(int alg_type, int nblocks, const ref_block* blocks,
     dense_stats(times, master, grid_step_size, grid_phys_mins, gni);
     for (int i = 0; i < 3; ++i)
         stats3[i] = tess_shim_reduce_record.value[i];
+
+    for (DBlock* b : dbs)
+        free_dblock(b);
+}
+
+// dense() followed by WriteGrid (src/dense.cpp:751-870, which runs
+// ProjectGrid, :881-1023, when projecting) to outfile, in the order
+// examples/dense/main.cpp:170-181 calls them, on the x-y plane.  block_out
+// (may be NULL) receives every block's density array as dense() leaves it
+// (before ProjectGrid), concatenated in block order; its length is the sum of
+// the blocks' b->num_grid_pts, which block_sizes (may be NULL) receives per
+// block.  stats3 as ref_dense.  Block gids must be 0..nblocks-1 (ProjectGrid
+// indexes its geometry table by gid).
+void ref_dense_write(int alg_type, int nblocks, const ref_block* blocks,
+                     int num_given_bounds, const float* given_mins, const float* given_maxs,
+                     float mass, float eps, const int* glo_num_idx, int project, const char* outfile,
+                     float* block_out, int* block_sizes, double* stats3)
+{
+    diy::Master master;
+    std::vector<DBlock*> dbs;
+    add_blocks(master, dbs, nblocks, blocks);
+    diy::RoundRobinAssigner assigner(1, nblocks);
+
+    float gmins[3] = {0, 0, 0}, gmaxs[3] = {0, 0, 0};
+    if (given_mins) for (int i = 0; i < 3; ++i) gmins[i] = given_mins[i];
+    if (given_maxs) for (int i = 0; i < 3; ++i) gmaxs[i] = given_maxs[i];
+    float proj_plane[3] = {0, 0, 1};
+    float data_mins[3], data_maxs[3], grid_phys_mins[3], grid_phys_maxs[3], grid_step_size[3];
+    int gni[3] = { glo_num_idx[0], glo_num_idx[1], glo_num_idx[2] };
+
+    dense((alg)alg_type, num_given_bounds, gmins, gmaxs, project != 0, proj_plane, mass,
+          data_mins, data_maxs, grid_phys_mins, grid_phys_maxs, grid_step_size, eps, gni, master);
+
+    size_t off = 0;
+    for (int i = 0; i < nblocks; ++i)
+    {
+        if (block_sizes) block_sizes[i] = dbs[i]->num_grid_pts;
+        if (block_out) std::memcpy(block_out + off, dbs[i]->density, sizeof(float) * dbs[i]->num_grid_pts);
+        off += dbs[i]->num_grid_pts;
+    }
+    tess_shim_reduce_record.n = 0;
+    double times[DENSE_MAX_TIMES] = {0};
+    dense_stats(times, master, grid_step_size, grid_phys_mins, gni);
+    for (int i = 0; i < 3; ++i)
+        stats3[i] = tess_shim_reduce_record.value[i];
+
+    WriteGrid(nblocks, nblocks, (char*)outfile, project != 0, gni, eps, data_mins, data_maxs,
+              num_given_bounds, gmins, gmaxs, master, assigner);
 
     for (DBlock* b : dbs)
         free_dblock(b);

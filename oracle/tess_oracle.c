@@ -797,8 +797,10 @@ static int inside_bounds(const float* p, const float* mn, const float* mx)
            p[2] >= mn[2] && p[2] <= mx[2];
 }
 
-/* local array slot of a global grid index, -1 past the block array */
-static long local_index(const block_grid* g, const int* gi)
+/* local array slot of a global grid index (Global2LocalIdx + index,
+   src/dense.cpp:1047-1090, 1210-1218), -1 past the block array; projected
+   onto the x-y plane every z maps to the block's 2-D array */
+static long local_index(const block_grid* g, const int* gi, int project)
 {
     int l[3];
     for (int d = 0; d < 3; ++d)
@@ -807,6 +809,8 @@ static long local_index(const block_grid* g, const int* gi)
         if (l[d] < 0 || l[d] >= g->num_idx[d])
             return -1;
     }
+    if (project)
+        return (long)l[1] * g->num_idx[0] + l[0];
     return ((long)l[2] * g->num_idx[1] + l[1]) * g->num_idx[0] + l[0];
 }
 
@@ -826,6 +830,16 @@ long orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float
                       float* global_grid, float* grid_out6, float* data_out6, double* stats3,
                       int* cell_counts)
 {
+    return orc_dense_ex(alg, nblocks, blocks, data6, 0, num_given_bounds, given_mins, given_maxs, mass, eps,
+                        glo_num_idx, global_grid, NULL, grid_out6, data_out6, stats3, cell_counts);
+}
+
+long orc_dense_ex(int alg, int nblocks, const orc_block* blocks, const float* data6, int project,
+                  int num_given_bounds, const float* given_mins, const float* given_maxs,
+                  float mass, float eps, const int* glo_num_idx,
+                  float* global_grid, float* block_out, float* grid_out6, float* data_out6, double* stats3,
+                  int* cell_counts)
+{
     float data_mins[3], data_maxs[3], gmin[3], gmax[3], step[3];
     orc_data_bounds(nblocks, blocks, data_mins, data_maxs);
     if (data6)
@@ -841,10 +855,12 @@ long orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float
     {
         orc_block_grid_params(&blocks[i], gmin, step, eps, data_mins, data_maxs, glo_num_idx,
                               bg[i].min_idx, bg[i].max_idx, bg[i].num_idx);
-        long npts = (long)bg[i].num_idx[0] * bg[i].num_idx[1] * bg[i].num_idx[2];
+        /* init_dense, src/dense.cpp:117-121 */
+        long npts = (long)bg[i].num_idx[0] * bg[i].num_idx[1] * (project ? 1 : bg[i].num_idx[2]);
         bg[i].density = (float*)calloc((size_t)(npts > 0 ? npts : 1), sizeof(float));
     }
-    float div = step[0] * step[1] * step[2];
+    /* src/dense.cpp:241-242 */
+    float div = project ? step[0] * step[1] : step[0] * step[1] * step[2];
 
     /* queues[dest * nblocks + src] */
     svec* queues = (svec*)calloc((size_t)nblocks * nblocks, sizeof(svec));
@@ -890,7 +906,7 @@ long orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float
                 idx2phys(gi, gp, step, gmin);
                 if (inside_bounds(gp, b->bounds_min, b->bounds_max))
                 {
-                    long li = local_index(&bg[bi], gi);
+                    long li = local_index(&bg[bi], gi, project);
                     if (li < 0) { lost++; continue; }
                     float* d = &bg[bi].density[li];
                     if (alg == 0)
@@ -937,7 +953,7 @@ long orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float
             svec* q = &queues[(size_t)bi * nblocks + order[k]];
             for (long j = 0; j < q->n; ++j)
             {
-                long li = local_index(&bg[bi], q->a[j].idx);
+                long li = local_index(&bg[bi], q->a[j].idx, project);
                 if (li < 0) { lost++; continue; }
                 float* d = &bg[bi].density[li];
                 *d = (float)((double)*d + q->a[j].mass / div);
@@ -949,8 +965,56 @@ long orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const float
     }
 
     size_t nx = glo_num_idx[0], ny = glo_num_idx[1];
-    memset(global_grid, 0, sizeof(float) * nx * ny * (size_t)glo_num_idx[2]);
-    for (int i = 0; i < nblocks; ++i)
+    if (block_out)
+    {
+        size_t off = 0;
+        for (int i = 0; i < nblocks; ++i)
+        {
+            size_t n = (size_t)bg[i].num_idx[0] * bg[i].num_idx[1] * (project ? 1 : bg[i].num_idx[2]);
+            memcpy(block_out + off, bg[i].density, sizeof(float) * n);
+            off += n;
+        }
+    }
+    if (project)
+    {
+        /* ProjectGrid (src/dense.cpp:881-1023) with every block in this
+           process: the root of a column is the block with the same x-y grid
+           origin and min_idx[2] == 0 (the last such block by gid order); the
+           other blocks, in block order, add their first num_idx[0]*num_idx[1]
+           values into it */
+        for (int i = 0; i < nblocks; ++i)
+        {
+            if (!bg[i].min_idx[2])
+                continue;
+            int root = -1;
+            for (int j = 0; j < nblocks; ++j)
+                if (bg[j].min_idx[0] == bg[i].min_idx[0] && bg[j].min_idx[1] == bg[i].min_idx[1] &&
+                    !bg[j].min_idx[2] && (root < 0 || blocks[j].gid > blocks[root].gid))
+                    root = j;
+            if (root < 0)
+                continue;
+            long n = (long)bg[i].num_idx[0] * bg[i].num_idx[1];
+            for (long k = 0; k < n; ++k)
+                bg[root].density[k] += bg[i].density[k];
+        }
+        /* WriteGrid (src/dense.cpp:812-828): root blocks write their 2-D
+           arrays at (min_idx[1], min_idx[0]) of the glo_num_idx[1] x [0] array */
+        memset(global_grid, 0, sizeof(float) * nx * ny);
+        for (int i = 0; i < nblocks; ++i)
+        {
+            if (bg[i].min_idx[2])
+                continue;
+            for (int y = 0; y < bg[i].num_idx[1]; ++y)
+                for (int x = 0; x < bg[i].num_idx[0]; ++x)
+                    global_grid[(size_t)(bg[i].min_idx[1] + y) * nx + (bg[i].min_idx[0] + x)] =
+                        bg[i].density[(size_t)y * bg[i].num_idx[0] + x];
+        }
+        for (int i = 0; i < nblocks; ++i)
+            free(bg[i].density);
+    }
+    else
+        memset(global_grid, 0, sizeof(float) * nx * ny * (size_t)glo_num_idx[2]);
+    for (int i = 0; i < nblocks && !project; ++i)
     {
         for (int z = 0; z < bg[i].num_idx[2]; ++z)
             for (int y = 0; y < bg[i].num_idx[1]; ++y)

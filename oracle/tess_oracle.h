@@ -91,6 +91,17 @@ long  orc_dense_bounds(int alg, int nblocks, const orc_block* blocks, const floa
                        float* global_grid, float* grid_out6, float* data_out6, double* stats3,
                        int* cell_counts);
 
+/* orc_dense_bounds with dense()'s project flag (x-y plane): block arrays of
+   num_idx[0]*num_idx[1] floats holding mass per area summed over the block's
+   z range; global_grid then receives ProjectGrid's column sums as WriteGrid
+   writes them (glo_num_idx[1] x [0] floats), block_out (optional) every
+   block's array as dense() leaves it, concatenated in block order. */
+long  orc_dense_ex(int alg, int nblocks, const orc_block* blocks, const float* data6, int project,
+                   int num_given_bounds, const float* given_mins, const float* given_maxs,
+                   float mass, float eps, const int* glo_num_idx,
+                   float* global_grid, float* block_out, float* grid_out6, float* data_out6, double* stats3,
+                   int* cell_counts);
+
 /* src/tess-qhull.c:161-225, in place */
 void  orc_reorder_neighbors(orc_tet* tets, int num_tets);
 

@@ -21,7 +21,7 @@ DENSE_TESS, DENSE_CIC, DENSE_DTFE = 0, 1, 2
 MODE_MIXED, MODE_FP64 = 0, 1
 
 _STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no CUDA device", 4: "star overflow",
-           5: "face overflow", 6: "edge ring overflow", 7: "malformed mesh", 8: "unsupported"}
+           5: "face overflow", 6: "edge ring overflow", 7: "malformed mesh", 8: "unsupported", 9: "I/O error"}
 
 
 class TessGpuError(RuntimeError):
@@ -46,7 +46,7 @@ class DenseParams(ctypes.Structure):
                 ("given_mins", ctypes.c_float * 3), ("given_maxs", ctypes.c_float * 3),
                 ("mass", ctypes.c_float), ("eps", ctypes.c_float), ("glo_num_idx", ctypes.c_int * 3),
                 ("use_data_bounds", ctypes.c_int), ("data_mins", ctypes.c_float * 3),
-                ("data_maxs", ctypes.c_float * 3)]
+                ("data_maxs", ctypes.c_float * 3), ("project", ctypes.c_int)]
 
 
 class DenseInfo(ctypes.Structure):
@@ -58,7 +58,8 @@ class DenseInfo(ctypes.Structure):
                 ("grid_pts_assigned", ctypes.c_longlong), ("fp64_tets", ctypes.c_longlong),
                 ("exact_tests", ctypes.c_longlong), ("rows_visited", ctypes.c_longlong),
                 ("points_tested", ctypes.c_longlong), ("raster_variant", ctypes.c_int),
-                ("raster_variant_ms", ctypes.c_float * 8)]
+                ("raster_variant_ms", ctypes.c_float * 8), ("grid_layers", ctypes.c_int),
+                ("grid_floats", ctypes.c_longlong)]
 
     def as_dict(self):
         return dict(data_mins=np.array(self.data_mins[:], np.float32), data_maxs=np.array(self.data_maxs[:], np.float32),
@@ -69,7 +70,8 @@ class DenseInfo(ctypes.Structure):
                     grid_pts_assigned=self.grid_pts_assigned, fp64_tets=self.fp64_tets,
                     exact_tests=self.exact_tests, rows_visited=self.rows_visited,
                     points_tested=self.points_tested, raster_variant=self.raster_variant,
-                    raster_variant_ms=list(self.raster_variant_ms))
+                    raster_variant_ms=list(self.raster_variant_ms), grid_layers=self.grid_layers,
+                    grid_floats=self.grid_floats)
 
 
 _LIB = None
@@ -113,6 +115,10 @@ def lib():
             "tessgpu_reorder_neighbors_device": (_I, [_VP, _VP, _I]),
             "tessgpu_stage_times": (_I, [_VP, _VP, _VP, _I]),
             "tessgpu_dtfe_densities_noalloc": (_I, [_VP, _I, _VP, _I, _VP, ctypes.c_float, _I, _VP, _VP]),
+            "tessgpu_dense_grid_floats": (ctypes.c_longlong, [_I, _VP, _VP, _VP]),
+            "tessgpu_project_grid": (_I, [_VP, _VP, _I, ctypes.c_longlong, _VP]),
+            "tessgpu_write_grid": (_I, [_VP, _VP, ctypes.c_longlong, ctypes.c_char_p]),
+            "tessgpu_write_last_grid": (_I, [_VP, ctypes.c_char_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -153,10 +159,13 @@ def make_blocks(blocks):
     return arr, keep
 
 
-def make_params(alg, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, data_bounds=None):
+def make_params(alg, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, data_bounds=None,
+                project=False):
     """data_bounds=(mins, maxs) fixes dense()'s data bounds (every rank's all-reduced
-    bounds when this process holds a share of the blocks)."""
+    bounds when this process holds a share of the blocks); project projects onto
+    the x-y plane (dense()'s project flag)."""
     p = DenseParams()
+    p.project = 1 if project else 0
     if data_bounds is not None:
         p.use_data_bounds = 1
         for d in range(3):
@@ -274,13 +283,15 @@ class Context:
         return out
 
     def dense(self, alg, blocks, glo_num_idx, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, block_arrays=False,
-              global_grid=True, out=None, data_bounds=None):
-        """dense() over host blocks.  Returns dict(grid=(nz,ny,nx) float32, info=..., blocks=[...])."""
+              global_grid=True, out=None, data_bounds=None, project=False):
+        """dense() over host blocks.  Returns dict(grid=(nz,ny,nx) float32 -- (ny,nx)
+        when projecting, after ProjectGrid -- info=..., blocks=[...])."""
         arr, keep = make_blocks(blocks)
-        p = make_params(alg, glo_num_idx, mass, eps, mode, given, data_bounds)
+        p = make_params(alg, glo_num_idx, mass, eps, mode, given, data_bounds, project)
         grid = None
         if global_grid:
-            grid = out if out is not None else np.empty((glo_num_idx[2], glo_num_idx[1], glo_num_idx[0]), np.float32)
+            shape = (glo_num_idx[1], glo_num_idx[0]) if project else (glo_num_idx[2], glo_num_idx[1], glo_num_idx[0])
+            grid = out if out is not None else np.empty(shape, np.float32)
         bd = None
         barrays = None
         if block_arrays:
@@ -299,6 +310,30 @@ class Context:
 
     def upload(self, blocks):
         return Batch(self, blocks, device=False)
+
+    # --- ProjectGrid / WriteGrid -----------------------------------------
+    def project_grid(self, d_layers, num_layers, layer_floats, d_out):
+        """ProjectGrid (src/dense.cpp:881-1023): d_out = sum of the layers, in order (device addresses)."""
+        self._check(lib().tessgpu_project_grid(self._h, ctypes.c_void_p(d_layers), int(num_layers), int(layer_floats),
+                                               ctypes.c_void_p(d_out)))
+
+    def write_grid(self, d_grid, num_floats, path):
+        """WriteGrid's raw float32 file (src/dense.cpp:751-870) from device memory at d_grid."""
+        self._check(lib().tessgpu_write_grid(self._h, ctypes.c_void_p(d_grid), int(num_floats), os.fsencode(path)))
+
+    def write_last_grid(self, path):
+        """WriteGrid after dense(): the last Context.dense call's global grid."""
+        self._check(lib().tessgpu_write_last_grid(self._h, os.fsencode(path)))
+
+
+def grid_floats(blocks, alg, glo_num_idx, project=False, **kw):
+    """(floats, layers) of the device grid Batch.dense writes for these blocks."""
+    arr, keep = make_blocks(blocks)
+    p = make_params(alg, glo_num_idx, project=project, **kw)
+    layers = ctypes.c_int()
+    n = lib().tessgpu_dense_grid_floats(len(blocks), arr, ctypes.byref(p), ctypes.byref(layers))
+    del keep
+    return int(n), int(layers.value)
 
 
 class Batch:
@@ -328,9 +363,10 @@ class Batch:
         self.ctx._check(lib().tessgpu_batch_keep_debug(self._h, 1 if on else 0))
 
     def dense(self, alg, glo_num_idx, d_grid, mass=1.0, eps=1e-4, mode=MODE_MIXED, given=None, want_info=True,
-              data_bounds=None):
-        """dense() into the device grid at address d_grid (an int, e.g. torch tensor.data_ptr())."""
-        p = make_params(alg, glo_num_idx, mass, eps, mode, given, data_bounds)
+              data_bounds=None, project=False):
+        """dense() into the device grid at address d_grid (an int, e.g. torch tensor.data_ptr());
+        projected: the grid holds info['grid_layers'] x-y layers (grid_floats() floats)."""
+        p = make_params(alg, glo_num_idx, mass, eps, mode, given, data_bounds, project)
         info = DenseInfo() if want_info else None
         self.ctx._check(lib().tessgpu_batch_dense(self.ctx.handle, self._h, ctypes.byref(p), ctypes.c_void_p(d_grid),
                                                   ctypes.byref(info) if info is not None else None))

@@ -39,6 +39,11 @@ struct tessgpu_ctx
     std::vector<cudaEvent_t> events;
     std::vector<const char*> marks;
     int                      nmarks = 0;
+    // WriteGrid: pinned staging buffers, and the global grid of the last tessgpu_dense call
+    float*                   h_stage[2] = { nullptr, nullptr };
+    cudaEvent_t              stage_ev[2] = { nullptr, nullptr };
+    const float*             last_grid = nullptr;
+    long long                last_grid_floats = 0;
 };
 
 static void mark(tessgpu_ctx* c, const char* name)
@@ -105,6 +110,7 @@ static void* pool_get(tessgpu_ctx* c, int slot, size_t bytes, cudaError_t* e)
     *e = cudaSuccess;
     if (p.second < bytes)
     {
+        if (c->last_grid == p.first) { c->last_grid = nullptr; c->last_grid_floats = 0; }
         if (p.first) cudaFree(p.first);
         p.first = nullptr;
         p.second = 0;
@@ -153,6 +159,11 @@ extern "C" void tessgpu_destroy(tessgpu_ctx* ctx)
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_max) cudaFree(ctx->d_max);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    for (int i = 0; i < 2; ++i)
+    {
+        if (ctx->h_stage[i]) cudaFreeHost(ctx->h_stage[i]);
+        if (ctx->stage_ev[i]) cudaEventDestroy(ctx->stage_ev[i]);
+    }
     delete ctx;
 }
 
@@ -248,6 +259,7 @@ static bool valid_params(const tessgpu_dense_params* p)
     if (!p) return false;
     if (p->alg < 0 || p->alg > 2 || p->mode < 0 || p->mode > 1) return false;
     if (p->num_given_bounds < 0 || p->num_given_bounds > 3) return false;
+    if (p->project != 0 && p->project != 1) return false;
     for (int i = 0; i < 3; ++i)
         if (p->glo_num_idx[i] < 2) return false;
     long long g = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
@@ -265,7 +277,56 @@ extern "C" long long tessgpu_block_grid_points(int nblocks, const tessgpu_block*
     block_grid_params(blocks[b], gmin, step, p->eps, dmin, dmax, p->glo_num_idx, mn, mx, num);
     if (out9)
         for (int i = 0; i < 3; ++i) { out9[i] = mn[i]; out9[3 + i] = mx[i]; out9[6 + i] = num[i]; }
-    return (long long)num[0] * num[1] * num[2];
+    return (long long)num[0] * num[1] * (p->project ? 1 : num[2]);
+}
+
+// Layers of a projected grid: one per distinct first z index of the blocks'
+// BlockGridParams boxes (clamped into the grid), ascending; zl[z] is the layer
+// that holds grid index z.  In a regular decomposition a layer is one
+// z-slab of blocks, and layer l at (x, y) is what the block of that slab
+// covering (x, y) holds after dense(), before ProjectGrid.
+static int z_layers(const std::vector<int>& block_zmin, int nz, std::vector<int>& zl)
+{
+    std::vector<int> starts;
+    for (int z0 : block_zmin)
+        starts.push_back(std::min(std::max(z0, 0), nz - 1));
+    std::sort(starts.begin(), starts.end());
+    starts.erase(std::unique(starts.begin(), starts.end()), starts.end());
+    zl.assign(nz, 0);
+    int l = 0;
+    for (int z = 0; z < nz; ++z)
+    {
+        while (l + 1 < (int)starts.size() && starts[l + 1] <= z) ++l;
+        zl[z] = l;
+    }
+    return starts.empty() ? 1 : (int)starts.size();
+}
+
+static int layer_of(const std::vector<int>& zl, int z0)
+{
+    return zl[std::min(std::max(z0, 0), (int)zl.size() - 1)];
+}
+
+extern "C" long long tessgpu_dense_grid_floats(int nblocks, const tessgpu_block* blocks,
+                                               const tessgpu_dense_params* p, int* layers)
+{
+    if (nblocks <= 0 || !blocks || !valid_params(p)) return -1;
+    const long long area = (long long)p->glo_num_idx[0] * p->glo_num_idx[1];
+    if (!p->project)
+    {
+        if (layers) *layers = 0;
+        return area * p->glo_num_idx[2];
+    }
+    std::vector<int> zmin(nblocks), zl;
+    for (int b = 0; b < nblocks; ++b)
+    {
+        int out9[9];
+        tessgpu_block_grid_points(nblocks, blocks, b, p, out9);
+        zmin[b] = out9[2];
+    }
+    const int L = z_layers(zmin, p->glo_num_idx[2], zl);
+    if (layers) *layers = L;
+    return area * L;
 }
 
 // ---------------------------------------------------------------------------
@@ -309,7 +370,7 @@ enum PoolSlot
 {
     SLOT_BLOCKS, SLOT_COFF, SLOT_POS, SLOT_TV, SLOT_TN, SLOT_V2T, SLOT_CC, SLOT_CC64, SLOT_W, SLOT_RHO32,
     SLOT_RHO64, SLOT_FIX, SLOT_FIXN, SLOT_STAGE, SLOT_RAWPTR, SLOT_RAWV2T, SLOT_GRID, SLOT_CELLS, SLOT_OUT,
-    SLOT_OUT2, SLOT_COUNT
+    SLOT_OUT2, SLOT_COUNT, SLOT_ZLAYER, SLOT_GRID3, SLOT_PROJ
 };
 
 static cudaError_t balloc(tessgpu_batch* bt, int slot, size_t bytes, void** out)
@@ -551,9 +612,11 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     }
     g.eps = p->eps;
     g.mass = p->mass;
-    g.div = step[0] * step[1] * step[2];   // src/dense.cpp:241-242
+    // src/dense.cpp:241-242: volume, or area when projecting
+    g.div = p->project ? step[0] * step[1] : step[0] * step[1] * step[2];
     for (int i = 0; i < 3; ++i)
         g.inv_step[i] = 1.0f / step[i];
+    g.zlayer = nullptr;
     for (int i = 0; i < nb; ++i)
     {
         BlockDesc& d = bt->hb[i];
@@ -568,10 +631,36 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     }
     CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
-    const long long G = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
+    const long long area = (long long)p->glo_num_idx[0] * p->glo_num_idx[1];
+    const long long G = area * p->glo_num_idx[2];
+    // projected: d_grid holds L layers of the x-y plane; DENSE_TESS / DENSE_CIC
+    // deposit into them directly, DTFE rasterises a 3-D scratch grid first
+    int L = 0;
+    int* d_zl = nullptr;
+    float* target = d_grid;
+    if (p->project)
+    {
+        std::vector<int> zmin(nb), zl;
+        for (int i = 0; i < nb; ++i)
+            zmin[i] = bt->hb[i].gmin_idx[2];
+        L = z_layers(zmin, p->glo_num_idx[2], zl);
+        cudaError_t e;
+        d_zl = (int*)pool_get(ctx, SLOT_ZLAYER, sizeof(int) * zl.size(), &e);
+        CK(e);
+        CK(cudaMemcpyAsync(d_zl, zl.data(), sizeof(int) * zl.size(), cudaMemcpyHostToDevice, s));
+        if (p->alg == TESSGPU_DENSE_DTFE)
+        {
+            target = (float*)pool_get(ctx, SLOT_GRID3, sizeof(float) * G, &e);
+            CK(e);
+        }
+        else
+            g.zlayer = d_zl;
+    }
+    const long long Gout = p->project ? area * L : G;
+    const long long Gtarget = target == d_grid ? Gout : G;
     ctx->nmarks = 0;
     mark(ctx, "start");
-    CK(cudaMemsetAsync(d_grid, 0, sizeof(float) * G, s));
+    CK(cudaMemsetAsync(target, 0, sizeof(float) * Gtarget, s));
     mark(ctx, "grid_zero");
     bt->last_alg = p->alg;
 
@@ -594,13 +683,13 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             counts = bt->d_cell_counts;
         }
         launch_cells(CELL_DENSE_TESS, bt->d_blocks, bt->d_c_off, nb, (int)bt->C, bt->pos, bt->tv, bt->tn, bt->v2t,
-                     bt->cc, nullptr, g, d_grid, nullptr, nullptr, nullptr, nullptr, counts, ctx->d_status, s);
+                     bt->cc, nullptr, g, target, nullptr, nullptr, nullptr, nullptr, counts, ctx->d_status, s);
         ctx->launches += bt->C ? 1 : 0;
         mark(ctx, "cells_dense_tess");
     }
     else if (p->alg == TESSGPU_DENSE_CIC)
     {
-        launch_cic(bt->d_blocks, bt->d_c_off, nb, (int)bt->C, bt->pos, g, d_grid, ctx->d_status, s);
+        launch_cic(bt->d_blocks, bt->d_c_off, nb, (int)bt->C, bt->pos, g, target, ctx->d_status, s);
         ctx->launches += bt->C ? 1 : 0;
         mark(ctx, "cic");
     }
@@ -665,7 +754,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
                     CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
                     cudaEventRecord(e0, s);
                     launch_raster(p->mode, v, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g,
-                                  kTau, d_grid, owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
+                                  kTau, target, owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
                     cudaEventRecord(e1, s);
                     ctx->launches++;
                     CK(cudaEventSynchronize(e1));
@@ -681,25 +770,33 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             ctx->raster_variant[p->mode] = var;
             CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
             CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
-            CK(cudaMemsetAsync(d_grid, 0, sizeof(float) * G, s));
+            CK(cudaMemsetAsync(target, 0, sizeof(float) * G, s));
             if (owner) CK(cudaMemsetAsync(owner, 0xff, sizeof(int) * G, s));
         }
         launch_raster(p->mode, var, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, kTau,
-                      d_grid, owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
+                      target, owner, bt->fix_list, bt->fix_count, ctx->d_status, s);
         mark(ctx, "raster");
         if (p->mode != TESSGPU_MODE_FP64)
         {
-            launch_raster_fix(bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, d_grid, owner,
+            launch_raster_fix(bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, target, owner,
                               bt->fix_list, bt->fix_count, ctx->d_status, s);
             mark(ctx, "raster_fp64_fixup");
         }
         ctx->launches += (bt->T ? (p->mode == TESSGPU_MODE_FP64 ? 2 : 3) : 0) + (bt->N ? 1 : 0);
+        if (p->project)
+        {
+            // surface density: the column integral of rho over each layer's z range
+            launch_project_layers(target, p->glo_num_idx[0], p->glo_num_idx[1], p->glo_num_idx[2], d_zl, step[2],
+                                  d_grid, s);
+            ctx->launches++;
+            mark(ctx, "project_layers");
+        }
     }
     double max_dense = 0.0;
     if (info || p->alg != TESSGPU_DENSE_DTFE)
     {
         CK(cudaMemsetAsync(ctx->d_max, 0, sizeof(float), s));
-        launch_grid_max(d_grid, G, ctx->d_max, s);
+        launch_grid_max(d_grid, Gout, ctx->d_max, s);
         ctx->launches++;
         mark(ctx, "grid_max");
     }
@@ -726,6 +823,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         info->raster_variant = bt->raster_variant[p->mode];
         for (int v = 0; v < 8; ++v)
             info->raster_variant_ms[v] = ctx->tune_ms[p->mode][v];
+        info->grid_layers = L;
+        info->grid_floats = Gout;
     }
     return st;
 }
@@ -909,17 +1008,44 @@ extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tes
 {
     if (!ctx || nblocks <= 0 || !blocks || !valid_params(p))
         return set_err(ctx, TESSGPU_ERR_INVALID, "bad dense arguments");
+    ctx->last_grid = nullptr;
+    ctx->last_grid_floats = 0;
     tessgpu_batch* bt = nullptr;
     tessgpu_status s = batch_build(ctx, nblocks, blocks, false, true, &bt);
     if (s != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
-    const long long G = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
+    const long long area = (long long)p->glo_num_idx[0] * p->glo_num_idx[1];
+    int L = 0;
+    const long long Gout = tessgpu_dense_grid_floats(nblocks, blocks, p, &L);
     cudaError_t e;
-    float* d_grid = (float*)pool_get(ctx, SLOT_GRID, sizeof(float) * G, &e);
+    float* d_grid = (float*)pool_get(ctx, SLOT_GRID, sizeof(float) * Gout, &e);
     if ((s = cuda_check(ctx, e, "cudaMalloc")) != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
     s = tessgpu_batch_dense(ctx, bt, p, d_grid, info);
+    // the global grid WriteGrid writes: 3-D, or the layers summed (ProjectGrid)
+    const float* d_global = d_grid;
+    long long Gglobal = Gout;
+    if (s == TESSGPU_OK && p->project)
+    {
+        float* d_proj = (float*)pool_get(ctx, SLOT_PROJ, sizeof(float) * area, &e);
+        if ((s = cuda_check(ctx, e, "cudaMalloc")) == TESSGPU_OK)
+            s = tessgpu_project_grid(ctx, d_grid, L, area, d_proj);
+        d_global = d_proj;
+        Gglobal = area;
+    }
     if (s == TESSGPU_OK && global_grid)
-        s = cuda_check(ctx, cudaMemcpyAsync(global_grid, d_grid, sizeof(float) * G, cudaMemcpyDeviceToHost, ctx->stream),
-                       "cudaMemcpy");
+        s = cuda_check(ctx, cudaMemcpyAsync(global_grid, d_global, sizeof(float) * Gglobal, cudaMemcpyDeviceToHost,
+                                            ctx->stream), "cudaMemcpy");
+    std::vector<int> zl;
+    if (s == TESSGPU_OK && block_density && p->project)
+    {
+        std::vector<int> zmin(nblocks);
+        for (int i = 0; i < nblocks; ++i)
+        {
+            int out9[9];
+            tessgpu_block_grid_points(nblocks, blocks, i, p, out9);
+            zmin[i] = out9[2];
+        }
+        z_layers(zmin, p->glo_num_idx[2], zl);
+    }
     if (s == TESSGPU_OK && block_density)
     {
         for (int i = 0; i < nblocks && s == TESSGPU_OK; ++i)
@@ -941,6 +1067,12 @@ extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tes
             float* d_tmp = (float*)pool_get(ctx, SLOT_OUT2, sizeof(float) * n, &e);
             if ((s = cuda_check(ctx, e, "cudaMalloc")) != TESSGPU_OK) break;
             int box[6] = { out9[0], out9[1], out9[2], out9[6], out9[7], out9[8] };
+            if (p->project)
+            {
+                // the block's 2-D array is its layer's rectangle
+                box[2] = layer_of(zl, out9[2]);
+                box[5] = 1;
+            }
             CK(cudaMemcpyAsync(d_box, box, sizeof(box), cudaMemcpyHostToDevice, ctx->stream));
             k_extract_box<<<grid_small(n), 256, 0, ctx->stream>>>(d_grid, p->glo_num_idx[0], p->glo_num_idx[1], d_box,
                                                                   d_box + 3, d_tmp);
@@ -953,8 +1085,78 @@ extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tes
     }
     if (s == TESSGPU_OK)
         s = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    if (s == TESSGPU_OK)
+    {
+        ctx->last_grid = d_global;
+        ctx->last_grid_floats = Gglobal;
+    }
     tessgpu_batch_free(bt);
     return s;
+}
+
+// ---------------------------------------------------------------------------
+// ProjectGrid and WriteGrid
+// ---------------------------------------------------------------------------
+extern "C" tessgpu_status tessgpu_project_grid(tessgpu_ctx* ctx, const float* d_layers, int num_layers,
+                                               long long layer_floats, float* d_out)
+{
+    if (!ctx || num_layers < 1 || layer_floats < 0 || (layer_floats && (!d_layers || !d_out)))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    if (!layer_floats) return TESSGPU_OK;
+    CK(cudaSetDevice(ctx->device));
+    launch_sum_layers(d_layers, num_layers, layer_floats, d_out, ctx->stream);
+    ctx->launches++;
+    mark(ctx, "project_grid");
+    CK(cudaGetLastError());
+    return TESSGPU_OK;
+}
+
+static const size_t kStageBytes = 32u << 20;   // one pinned staging chunk
+
+extern "C" tessgpu_status tessgpu_write_grid(tessgpu_ctx* ctx, const float* d_grid, long long num_floats,
+                                             const char* path)
+{
+    if (!ctx || !path || num_floats < 0 || (num_floats && !d_grid))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    for (int i = 0; i < 2; ++i)
+    {
+        if (!ctx->h_stage[i]) CK(cudaMallocHost(&ctx->h_stage[i], kStageBytes));
+        if (!ctx->stage_ev[i]) CK(cudaEventCreateWithFlags(&ctx->stage_ev[i], cudaEventDisableTiming));
+    }
+    FILE* f = std::fopen(path, "wb");   // truncates, as WriteGrid's MPI_File_set_size(fd, 0)
+    if (!f) return set_err(ctx, TESSGPU_ERR_IO, std::string("cannot open ") + path);
+    const size_t total = sizeof(float) * (size_t)num_floats;
+    const size_t nchunks = (total + kStageBytes - 1) / kStageBytes;
+    auto issue = [&](size_t c) -> cudaError_t {
+        const size_t off = c * kStageBytes, n = std::min(kStageBytes, total - off);
+        cudaError_t e = cudaMemcpyAsync(ctx->h_stage[c & 1], (const char*)d_grid + off, n, cudaMemcpyDeviceToHost,
+                                        ctx->stream);
+        return e != cudaSuccess ? e : cudaEventRecord(ctx->stage_ev[c & 1], ctx->stream);
+    };
+    tessgpu_status s = TESSGPU_OK;
+    if (nchunks) s = cuda_check(ctx, issue(0), "cudaMemcpyAsync");
+    for (size_t c = 0; c < nchunks && s == TESSGPU_OK; ++c)
+    {
+        // the next chunk's copy runs while this one is written
+        if (c + 1 < nchunks && (s = cuda_check(ctx, issue(c + 1), "cudaMemcpyAsync")) != TESSGPU_OK) break;
+        if ((s = cuda_check(ctx, cudaEventSynchronize(ctx->stage_ev[c & 1]), "cudaEventSynchronize")) != TESSGPU_OK)
+            break;
+        const size_t n = std::min(kStageBytes, total - c * kStageBytes);
+        if (std::fwrite(ctx->h_stage[c & 1], 1, n, f) != n)
+            s = set_err(ctx, TESSGPU_ERR_IO, std::string("short write to ") + path);
+    }
+    if (s != TESSGPU_OK) cudaStreamSynchronize(ctx->stream);   // no copy may land in a reused buffer later
+    if (std::fclose(f) != 0 && s == TESSGPU_OK)
+        s = set_err(ctx, TESSGPU_ERR_IO, std::string("cannot close ") + path);
+    return s;
+}
+
+extern "C" tessgpu_status tessgpu_write_last_grid(tessgpu_ctx* ctx, const char* path)
+{
+    if (!ctx) return TESSGPU_ERR_INVALID;
+    if (!ctx->last_grid) return set_err(ctx, TESSGPU_ERR_INVALID, "no tessgpu_dense call has finished on this context");
+    return tessgpu_write_grid(ctx, ctx->last_grid, ctx->last_grid_floats, path);
 }
 
 // ---------------------------------------------------------------------------

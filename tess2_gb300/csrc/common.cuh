@@ -30,6 +30,7 @@ struct GridDesc
     int   n[3];                  // glo_num_idx
     float eps, mass, div;        // eps, particle mass, step0*step1*step2
     float inv_step[3];           // 1 / step (index estimates only; exact checks follow)
+    const int* zlayer;           // projected grid: layer of each z index (nullptr: 3-D grid)
 };
 
 // first failure wins; detail records the offending item

@@ -286,7 +286,10 @@ __device__ __forceinline__ bool deposit(const int* gi, float inc, const GridDesc
     if (p[0] < g.dmin[0] || p[0] > g.dmax[0] || p[1] < g.dmin[1] || p[1] > g.dmax[1] ||
         p[2] < g.dmin[2] || p[2] > g.dmax[2])
         return false;
-    atomicAdd(&grid[((size_t)gi[2] * g.n[1] + gi[1]) * g.n[0] + gi[0]], inc);
+    // projected (src/dense.cpp:1047-1090 with the x-y plane): every z of a
+    // block lands in that block's 2-D array, one layer per z range of blocks
+    const size_t z = g.zlayer ? (size_t)g.zlayer[gi[2]] : (size_t)gi[2];
+    atomicAdd(&grid[(z * g.n[1] + gi[1]) * g.n[0] + gi[0]], inc);
     return true;
 }
 
@@ -867,6 +870,48 @@ __global__ void k_reorder_neighbors(int* tets, int total, Status* st)
     }
 }
 
+// z-projection of a 3-D grid into layers: layer l at (x, y) accumulates
+// value * dz over the z indices of layer l in ascending z (one thread per
+// column; consecutive threads read consecutive x, so every z step is coalesced)
+__global__ void k_project_layers(const float* grid, int nx, int ny, int nz, const int* zlayer, float dz,
+                                 float* layers)
+{
+    const long long area = (long long)nx * ny;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < area;
+         c += (long long)gridDim.x * blockDim.x)
+    {
+        int l = zlayer[0];
+        float acc = 0.0f;
+#pragma unroll 8
+        for (int z = 0; z < nz; ++z)
+        {
+            const int lz = zlayer[z];
+            if (lz != l)
+            {
+                layers[l * area + c] = acc;
+                acc = 0.0f;
+                l = lz;
+            }
+            acc += __ldcs(&grid[z * area + c]) * dz;
+        }
+        layers[l * area + c] = acc;
+    }
+}
+
+// ProjectGrid (src/dense.cpp:881-1023): the z=0 block of each column adds the
+// other blocks of the column in block order; here layer 0 adds layers 1.. in order
+__global__ void k_sum_layers(const float* layers, int num_layers, long long area, float* out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < area;
+         i += (long long)gridDim.x * blockDim.x)
+    {
+        float acc = layers[i];
+        for (int l = 1; l < num_layers; ++l)
+            acc += layers[l * area + i];
+        out[i] = acc;
+    }
+}
+
 __global__ void k_grid_max(const float* grid, long long n, float* out)
 {
     float m = 0.0f;
@@ -953,6 +998,20 @@ void launch_cic(const BlockDesc* d_blocks, const int* d_c_off, int nb, int total
 {
     if (total <= 0) return;
     k_cic<<<grid1d(total, 256), 256, 0, s>>>(d_blocks, d_c_off, nb, total, pos, g, grid, st);
+}
+
+void launch_project_layers(const float* grid, int nx, int ny, int nz, const int* zlayer, float dz, float* layers,
+                           cudaStream_t s)
+{
+    const long long area = (long long)nx * ny;
+    if (area <= 0 || nz <= 0) return;
+    k_project_layers<<<grid1d(area, 256), 256, 0, s>>>(grid, nx, ny, nz, zlayer, dz, layers);
+}
+
+void launch_sum_layers(const float* layers, int num_layers, long long area, float* out, cudaStream_t s)
+{
+    if (area <= 0 || num_layers <= 0) return;
+    k_sum_layers<<<grid1d(area, 256), 256, 0, s>>>(layers, num_layers, area, out);
 }
 
 void launch_reorder_neighbors(int* d_tets, int total, Status* st, cudaStream_t s)

@@ -24,6 +24,9 @@ void launch_cic(const BlockDesc* d_blocks, const int* d_cell_off, int nb, int to
                 const GridDesc& g, float* grid, Status* st, cudaStream_t s);
 void launch_grid_max(const float* grid, long long n, float* d_max, cudaStream_t s);
 void launch_reorder_neighbors(int* d_tets, int total_tets, Status* st, cudaStream_t s);
+void launch_project_layers(const float* grid, int nx, int ny, int nz, const int* zlayer, float dz, float* layers,
+                           cudaStream_t s);
+void launch_sum_layers(const float* layers, int num_layers, long long area, float* out, cudaStream_t s);
 
 // dtfe.cu  (built with -fmad=false; FMAs only where written)
 void launch_star_volumes(int mode, int total_tets, const float4* pos, const int4* tv, unsigned long long* W,

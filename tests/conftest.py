@@ -61,3 +61,21 @@ def gpu_ctx():
     build.build()
     from tess2_gb300.api import Context
     return Context(0)
+
+
+WRITEGRID_CASES = ["c1_uniform4096_seed1", "mix2048_seed7", "blocks8_mix8192_seed3"]
+
+
+def load_case_blocks(name):
+    """(fixture dict, blocks, glo_num_idx) of a single-block or multi-block golden case."""
+    if name.startswith("blocks"):
+        d, blocks = load_blocks(name)
+    else:
+        d = load_single(name)
+        blocks = single_block(d)
+    return d, blocks, [int(x) for x in d["glo_num_idx"]]
+
+
+def load_writegrid():
+    z = np.load(os.path.join(GOLDEN, "writegrid.npz"))
+    return {k: z[k] for k in z.files}

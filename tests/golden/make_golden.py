@@ -8,7 +8,8 @@ the stand-in for tess2's host Qhull engine, and are stored with the outputs
 so that no machine has to reproduce Qhull's numbering.
 
 Run from the repository root where the reference sources exist:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py             (everything)
+    python tests/golden/make_golden.py writegrid   (only writegrid.npz, from the stored inputs)
 Each dense() call runs in a fresh process: the reference keeps its
 max_dense / tot_mass / check_mass statistics in process-global variables
 (src/dense.cpp:25-27).
@@ -36,6 +37,26 @@ def dense_fresh(alg, blocks, gni):
     ctx = mp.get_context("spawn")
     with ctx.Pool(1) as pool:
         return pool.map(_dense_in_child, [(alg, blocks, gni)])[0]
+
+
+def _write_in_child(args):
+    alg, blocks, gni, project, path = args
+    from oracle.oracle import Oracle
+    return Oracle("ref").dense_write(alg, blocks, gni, path, project=project)
+
+
+def dense_write_fresh(alg, blocks, gni, project):
+    """dense() + WriteGrid of the reference in a fresh process; returns (result, file contents)."""
+    import tempfile
+    fd, path = tempfile.mkstemp(suffix=".raw")
+    os.close(fd)
+    try:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(1) as pool:
+            r = pool.map(_write_in_child, [(alg, blocks, gni, project, path)])[0]
+        return r, np.fromfile(path, np.float32)
+    finally:
+        os.remove(path)
 
 
 def flags():
@@ -87,7 +108,41 @@ def case_blocks(name, pts, dims, ghost, gni):
     return dict(name=name, blocks=len(blocks), dims=list(dims), ghost=ghost, grid=list(gni))
 
 
+def case_writegrid():
+    """WriteGrid files (src/dense.cpp:751-870) written by the reference's own
+    WriteGrid through oracle/ref_shim's MPI-IO, for the stored inputs above:
+    projected (ProjectGrid) for every case, and a check that the 3-D file is
+    the stored global grid.  Inputs are read back from the fixtures, not
+    re-tessellated."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from conftest import load_blocks, load_single, single_block
+    out = {}
+    cases = []
+    for name in ("c1_uniform4096_seed1", "mix2048_seed7"):
+        d = load_single(name)
+        cases.append((name, single_block(d), [int(x) for x in d["glo_num_idx"]], d))
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    cases.append(("blocks8_mix8192_seed3", blocks, [int(x) for x in d["glo_num_idx"]], d))
+    for name, blocks, gni, d in cases:
+        for alg, tag in ((0, "tess"), (1, "cic")):
+            r3, f3 = dense_write_fresh(alg, blocks, gni, False)
+            assert np.array_equal(f3.view(np.uint32), d[f"{tag}_grid"].ravel().view(np.uint32)), name
+            r, f = dense_write_fresh(alg, blocks, gni, True)
+            out[f"{name}_{tag}_proj_file"] = f
+            out[f"{name}_{tag}_proj_blocks"] = np.concatenate(r["blocks"])
+            out[f"{name}_{tag}_proj_block_sizes"] = np.array([len(b) for b in r["blocks"]], np.int32)
+            out[f"{name}_{tag}_proj_stats"] = np.array([r["max_dense"], r["tot_mass"], r["check_mass"]])
+    np.savez_compressed(os.path.join(OUT, "writegrid.npz"), **out)
+    return dict(name="writegrid", files=sorted(k for k in out if k.endswith("_file")))
+
+
 def main():
+    if sys.argv[1:] == ["writegrid"]:
+        meta = json.load(open(os.path.join(OUT, "golden.json")))
+        meta["cases"] = [c for c in meta["cases"] if c["name"] != "writegrid"] + [case_writegrid()]
+        with open(os.path.join(OUT, "golden.json"), "w") as f:
+            json.dump(meta, f, indent=1)
+        return
     from tess2_gb300 import host
     meta = dict(reference_build=flags(), delaunay="scipy.spatial.Delaunay(qhull_options='Qt')",
                 mass=1.0, eps=1e-4, cases=[])
@@ -99,6 +154,8 @@ def main():
     # 2x2x2 blocks with ghosts: cross-block deposits through the exchange
     meta["cases"].append(case_blocks("blocks8_mix8192_seed3", host.mixture_particles(8192, 3), (2, 2, 2), 0.1,
                                      [40, 40, 40]))
+    # WriteGrid / ProjectGrid output of the cases above
+    meta["cases"].append(case_writegrid())
     with open(os.path.join(OUT, "golden.json"), "w") as f:
         json.dump(meta, f, indent=1)
     print(json.dumps(meta, indent=1))

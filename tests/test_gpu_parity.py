@@ -180,3 +180,117 @@ def test_reorder_neighbors_bitexact(gpu_ctx, oracle, name):
     got = gpu_ctx.reorder_neighbors(shuf)
     assert np.array_equal(got, oracle.reorder_neighbors(shuf))
     assert np.array_equal(got, d["tets"])
+
+
+# ---------------------------------------------------------------------------
+# dense(project) + ProjectGrid + WriteGrid
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("name", ["c1_uniform4096_seed1", "mix2048_seed7", "blocks8_mix8192_seed3"])
+@pytest.mark.parametrize("alg,tag", [(0, "tess"), (1, "cic")])
+def test_dense_projected_vs_reference_writegrid(gpu_ctx, tmp_path, name, alg, tag):
+    """Projected densities against the file the reference's WriteGrid wrote
+    (after its ProjectGrid) and each block's array as dense() left it.  Column
+    sums gather a deposit per z, so the atomic adds' order shows at the
+    level of a few ulps of the sum: rtol 2e-5 (one grid point's share of a
+    column is >1e-3 of it)."""
+    from conftest import load_case_blocks, load_writegrid
+    d, blocks, gni = load_case_blocks(name)
+    w = load_writegrid()
+    r = gpu_ctx.dense(alg, blocks, gni, project=True, block_arrays=True)
+    f = w[f"{name}_{tag}_proj_file"].reshape(gni[1], gni[0])
+    assert r["grid"].shape == f.shape
+    np.testing.assert_allclose(r["grid"], f, rtol=2e-5, atol=0)
+    assert np.array_equal(r["grid"] == 0, f == 0)
+    got = np.concatenate(r["blocks"])
+    ref = w[f"{name}_{tag}_proj_blocks"]
+    assert got.size == ref.size
+    np.testing.assert_allclose(got, ref, rtol=2e-5, atol=0)
+    st = w[f"{name}_{tag}_proj_stats"]
+    assert r["info"]["check_mass"] == st[2]
+    assert np.isclose(r["info"]["tot_mass"], st[1], rtol=1e-12)
+    assert np.isclose(r["info"]["max_dense"], st[0], rtol=2e-5)
+    # WriteGrid after dense(): the file is the projected grid, byte for byte
+    out = tmp_path / "proj.raw"
+    gpu_ctx.write_last_grid(str(out))
+    assert np.array_equal(np.fromfile(out, np.float32), r["grid"].ravel())
+
+
+def test_write_grid_exact_bytes(gpu_ctx, tmp_path):
+    """The writer's file is the device buffer byte for byte, over several
+    staging chunks and a ragged last chunk; a zero-length write truncates."""
+    import torch
+    from tess2_gb300.api import TessGpuError
+    n = 3 * (8 << 20) + 12345          # 3 x 32 MiB chunks of floats plus a tail
+    g = torch.randn(n, device="cuda:0")
+    torch.cuda.synchronize()
+    out = tmp_path / "g.raw"
+    out.write_bytes(b"x" * (4 * n + 100))   # longer old contents must go
+    gpu_ctx.write_grid(g.data_ptr(), n, str(out))
+    got = np.fromfile(out, np.float32)
+    assert got.size == n and np.array_equal(got, g.cpu().numpy())
+    gpu_ctx.write_grid(g.data_ptr(), 0, str(out))
+    assert out.stat().st_size == 0
+    with pytest.raises(TessGpuError) as e:
+        gpu_ctx.write_grid(g.data_ptr(), 16, str(tmp_path / "no_such_dir" / "g.raw"))
+    assert e.value.code == 9
+
+
+def test_write_last_grid_3d(gpu_ctx, tmp_path):
+    d = load_single("mix2048_seed7")
+    gni = [int(x) for x in d["glo_num_idx"]]
+    r = gpu_ctx.dense(0, single_block(d), gni)
+    out = tmp_path / "g3.raw"
+    gpu_ctx.write_last_grid(str(out))
+    assert np.array_equal(np.fromfile(out, np.float32), r["grid"].ravel())
+
+
+def test_project_grid_sums_layers_in_order(gpu_ctx, oracle):
+    import torch
+    gen = torch.Generator().manual_seed(5)
+    lay = (torch.rand((3, 41, 37), generator=gen) * 1e3).to(torch.float32)
+    d_l = lay.to("cuda:0")
+    d_o = torch.empty((41, 37), device="cuda:0")
+    gpu_ctx.project_grid(d_l.data_ptr(), 3, 41 * 37, d_o.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(d_o.cpu().numpy(), oracle.sum_layers(lay.numpy()))
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1), (2, 2, 2)])
+def test_dtfe_projected(gpu_ctx, oracle, dims):
+    """DTFE projected: each layer is the column integral (sum of rho * dz in
+    ascending z) of the 3-D DTFE grid over the layer's z range -- bit for bit
+    the projection of the GPU's own 3-D grid, and within 1e-6 relative L2 of
+    the projection of the FP64 oracle's grid."""
+    import ctypes
+    import torch
+    from tess2_gb300 import host
+    from tess2_gb300.api import DENSE_DTFE, grid_floats, lib, make_blocks, make_params
+    pts = host.mixture_particles(6000, 11, n_clumps=8, sigma=0.05)
+    blocks = host.tessellate(host.decompose(pts, dims, 0.15), processes=1)
+    gni = [36, 30, 33]
+    nfl, L = grid_floats(blocks, DENSE_DTFE, gni, project=True)
+    assert L == dims[2] and nfl == L * gni[0] * gni[1]
+    batch = gpu_ctx.upload(blocks)
+    g3 = torch.zeros(int(np.prod(gni)), device="cuda:0")
+    info3 = batch.dense(DENSE_DTFE, gni, g3.data_ptr())
+    gp = torch.zeros(nfl, device="cuda:0")
+    info = batch.dense(DENSE_DTFE, gni, gp.data_ptr(), project=True)
+    torch.cuda.synchronize()
+    assert info["grid_layers"] == L and info["grid_floats"] == nfl
+    grid3 = g3.cpu().numpy().reshape(gni[2], gni[1], gni[0])
+    layers = gp.cpu().numpy().reshape(L, gni[1], gni[0])
+    zmin = []
+    arr, keep = make_blocks(blocks)
+    prm = make_params(DENSE_DTFE, gni, project=True)
+    for i in range(len(blocks)):
+        o9 = np.zeros(9, np.int32)
+        lib().tessgpu_block_grid_points(len(blocks), arr, i, ctypes.byref(prm), o9.ctypes.data)
+        zmin.append(int(o9[2]))
+    zl, nl = oracle.z_layers(zmin, gni[2])
+    assert nl == L
+    dz = info3["grid_step_size"][2]
+    assert np.array_equal(layers, oracle.project_layers(grid3, zl, dz))
+    ref = oracle.dtfe(blocks, gni, want_owner=False, want_rho=False)["grid"]
+    assert rel_l2(layers, oracle.project_layers(ref, zl, dz)) < 1e-6
+    # max over the layers, as dense() reports it before ProjectGrid
+    assert np.isclose(info["max_dense"], layers.max(), rtol=0)

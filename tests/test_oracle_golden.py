@@ -103,3 +103,34 @@ def test_reorder_neighbors(oracle, name):
     d = load_single(name)
     got = oracle.reorder_neighbors(shuffled_neighbors(d["tets"], 1))
     assert np.array_equal(got, d["tets"])
+
+
+@pytest.mark.parametrize("name", ["c1_uniform4096_seed1", "mix2048_seed7", "blocks8_mix8192_seed3"])
+@pytest.mark.parametrize("alg,tag", [(0, "tess"), (1, "cic")])
+def test_projected_writegrid(oracle, name, alg, tag):
+    """dense(project) + ProjectGrid + WriteGrid: the restated oracle against
+    the file the reference's own WriteGrid wrote, and every block's array."""
+    from conftest import load_case_blocks, load_writegrid
+    d, blocks, gni = load_case_blocks(name)
+    w = load_writegrid()
+    r = oracle.dense(alg, blocks, gni, project=True, block_arrays=True)
+    f = w[f"{name}_{tag}_proj_file"]
+    assert f.size == gni[0] * gni[1]
+    assert np.array_equal(bits(r["grid"].ravel()), bits(f))
+    sizes = w[f"{name}_{tag}_proj_block_sizes"]
+    ref_blocks = w[f"{name}_{tag}_proj_blocks"]
+    assert np.array_equal(bits(r["block_concat"][:sizes.sum()]), bits(ref_blocks))
+    st = w[f"{name}_{tag}_proj_stats"]
+    assert (r["max_dense"], r["tot_mass"], r["check_mass"]) == (st[0], st[1], st[2])
+
+
+def test_project_helpers(oracle):
+    """z layers from block starts, and the float32 z-projection order."""
+    zl, n = oracle.z_layers([0, 20, 20, 0], 40)
+    assert n == 2 and zl[19] == 0 and zl[20] == 1 and zl[-1] == 1
+    zl1, n1 = oracle.z_layers([5], 8)
+    assert n1 == 1 and not zl1.any()
+    g = np.arange(2 * 3 * 4, dtype=np.float32).reshape(2, 3, 4)
+    lay = oracle.project_layers(g, np.array([0, 1], np.int32), 0.5)
+    assert np.array_equal(lay[0], g[0] * np.float32(0.5)) and np.array_equal(lay[1], g[1] * np.float32(0.5))
+    assert np.array_equal(oracle.sum_layers(lay), lay[0] + lay[1])
