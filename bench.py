@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64-mode and DENSE_TESS comparison runs")
+    ap.add_argument("--no-rows", action="store_true",
+                    help="skip the timings of the stages around the path (reorder_neighbors, incomplete_cells, "
+                         "projection, WriteGrid)")
     return ap.parse_args()
 
 
@@ -226,6 +229,118 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------------------
+# the stages either side of the density path, on the same blocks
+# ---------------------------------------------------------------------------
+def _event_ms(fn, reps):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def time_rows(ctx, batch, blocks, gni, hbm, local):
+    """Device times of reorder_neighbors, incomplete_cells, the projected DTFE
+    step and ProjectGrid, and WriteGrid's file bandwidth, each with its
+    algorithmic bytes against the HBM peak."""
+    import tempfile
+    import torch
+    from tess2_gb300.api import DENSE_DTFE, grid_floats
+    dev = f"cuda:{local}"
+    rows = {}
+    T = sum(int(b["tets"].shape[0]) for b in blocks)
+    # reorder_neighbors over every block's tets (block-local numbering), neighbours shuffled per tet
+    rng = np.random.default_rng(1)
+    shuffled = []
+    for b in blocks:
+        t = b["tets"].copy()
+        perm = np.argsort(rng.random((t.shape[0], 4)), axis=1)
+        t[:, 4:] = np.take_along_axis(t[:, 4:], perm, axis=1)
+        shuffled.append(t)
+    src = [torch.from_numpy(t).to(dev) for t in shuffled]
+    work = [x.clone() for x in src]
+
+    t_ro = []
+    ctx.set_timing(True)
+    for _ in range(5):
+        for w, x in zip(work, src):
+            w.copy_(x)
+        torch.cuda.synchronize()
+        tot = 0.0
+        for w in work:
+            ctx.reorder_neighbors_device(w.data_ptr(), w.shape[0])
+            tot += sum(m for _, m in ctx.stage_times())
+        t_ro.append(tot)
+    ctx.set_timing(False)
+    ms = statistics.median(t_ro)
+    ok = all(np.array_equal(w.cpu().numpy(), b["tets"]) for w, b in zip(work, blocks))
+    # bytes: the tet record read and its neighbours written (48 B) + 4 neighbour vertex rows (64 B)
+    rb = 112.0 * T
+    rows["reorder_neighbors"] = dict(ms=ms, tets=T, tets_per_s=T / (ms * 1e-3), restores_qhull_order=ok,
+                                     algorithmic_bytes=rb, achieved_gbs=rb / (ms * 1e-3) / 1e9,
+                                     frac=rb / (ms * 1e-3) / 1e9 / hbm)
+    # incomplete_cells for every block against the other blocks' boxes
+    links = [np.array([np.concatenate([o["bounds_min"], o["bounds_max"]]) for k, o in enumerate(blocks) if k != i],
+                      np.float32) for i in range(len(blocks))]
+    C = sum(int(b["num_orig"]) for b in blocks)
+    dm = torch.zeros(C, dtype=torch.int64, device=dev)
+    ctx.set_timing(True)
+    t_ic = []
+    for _ in range(5):
+        enq = batch.incomplete_cells(links, dm.data_ptr())
+        t_ic.append(sum(ms for name, ms in ctx.stage_times()))
+    ctx.set_timing(False)
+    ms = statistics.median(t_ic)
+    # bytes: 32 B of tet record + 48 B of vertex positions per tet, 8 B per mask
+    ib = 80.0 * T + 8.0 * C
+    rows["incomplete_cells"] = dict(ms=ms, tets=T, tets_per_s=T / (ms * 1e-3), enqueued=int(enq.sum()),
+                                    algorithmic_bytes=ib, achieved_gbs=ib / (ms * 1e-3) / 1e9,
+                                    frac=ib / (ms * 1e-3) / 1e9 / hbm)
+    # projected DTFE (x-y plane) and ProjectGrid
+    nfl, L = grid_floats(blocks, DENSE_DTFE, gni, project=True)
+    gp = torch.empty(nfl, device=dev)
+    for _ in range(2):
+        batch.dense(DENSE_DTFE, gni, gp.data_ptr(), project=True, want_info=False)
+    ctx.set_timing(True)
+    batch.dense(DENSE_DTFE, gni, gp.data_ptr(), project=True, want_info=False)
+    st = dict(ctx.stage_times())
+    ctx.set_timing(False)
+    step = _event_ms(lambda: batch.dense(DENSE_DTFE, gni, gp.data_ptr(), project=True, want_info=False), 3)
+    G = float(np.prod(gni))
+    pl = st.get("project_layers", float("nan"))
+    out2 = torch.empty(gni[0] * gni[1], device=dev)
+    ps = _event_ms(lambda: ctx.project_grid(gp.data_ptr(), L, gni[0] * gni[1], out2.data_ptr()), 10)
+    rows["dtfe_projected"] = dict(ms_per_step=step, layers=L, grid_pts_per_s=G / (step * 1e-3),
+                                  project_layers_ms=pl, project_layers_gbs=(4.0 * G + 4.0 * nfl) / (pl * 1e-3) / 1e9,
+                                  project_grid_ms=ps)
+    # WriteGrid of the 3-D grid: device -> pinned -> file (local disk of the host)
+    g3 = torch.empty(int(G), device=dev).uniform_()
+    torch.cuda.synchronize()
+    d = tempfile.mkdtemp()
+    path = os.path.join(d, "grid.raw")
+    ctx.write_grid(g3.data_ptr(), int(G), path)
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        ctx.write_grid(g3.data_ptr(), int(G), path)
+    tw = (time.perf_counter() - t0) / reps
+    ok = os.path.getsize(path) == 4 * int(G)
+    os.remove(path)
+    os.rmdir(d)
+    h = torch.empty(int(G), dtype=torch.float32, pin_memory=True)
+    td = _event_ms(lambda: h.copy_(g3, non_blocking=True), 3)
+    rows["write_grid"] = dict(bytes=4 * int(G), s=tw, gbs=4 * G / tw / 1e9, size_ok=ok,
+                              d2h_pinned_gbs=4 * G / (td * 1e-3) / 1e9, dir=tempfile.gettempdir())
+    return rows
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_gpu(args):
@@ -389,6 +504,11 @@ def run_gpu(args):
         h2d = sum(b["particles"].nbytes + b["tets"].nbytes + b["vert_to_tet"].nbytes for b in blocks)
         e2e = dict(value=G / te, unit=UNIT, ms_per_step=te * 1e3, h2d_bytes_per_step=int(h2d),
                    d2h_bytes_per_step=int(4 * G), api="tessgpu_dense (host buffers)")
+
+    rows = None
+    if not args.no_rows:
+        rows = time_rows(ctx, batch, blocks, gni, hbm, local)
+        extra["rows"] = rows
 
     cpu = None
     if rank == 0 and not args.no_cpu:

@@ -162,6 +162,29 @@ tessgpu_status tessgpu_reorder_neighbors(tessgpu_ctx* ctx, int* tets, int num_te
 /* the same on tet_t records already in device memory */
 tessgpu_status tessgpu_reorder_neighbors_device(tessgpu_ctx* ctx, int* d_tets, int num_tets);
 
+/* One neighbour link of a block (an RCLink entry, include/tess/tess.hpp):
+   the neighbour's core bounds and its wrap direction (-1, 0 or 1 per axis;
+   all 0 without periodic boundaries), applied as DIY's wrap_bounds does:
+   bounds += wrap * (data_max - data_min) of the block's data bounds. */
+typedef struct tessgpu_link
+{
+    float bounds_min[3], bounds_max[3];
+    int   wrap[3];
+} tessgpu_link;
+
+/* replaces incomplete_cells (src/tess.cpp:492-628), the per-tet step that
+   picks the particles a block sends to its neighbours in tess2's ghost
+   exchange rounds, for one block with num_links <= 64 links, testing links
+   [last_neighbor, num_links).  send_mask[p] for each original particle p:
+   bit i set when the reference's to_send[p] holds link i.  enqueued (may be
+   NULL) receives the number of (particle, link) pairs, its return value.  A
+   block without tets sends every original particle to every tested link, as
+   the reference's release builds do (its debug builds assert that each such
+   particle lies in a tet). */
+tessgpu_status tessgpu_incomplete_cells(tessgpu_ctx* ctx, const tessgpu_block* block, int num_links,
+                                        const tessgpu_link* links, int last_neighbor,
+                                        unsigned long long* send_mask, long long* enqueued);
+
 /* replaces complete (src/tet.cpp:337-378) for vertices [0, n): 1 finite
    Voronoi cell, 0 cell on the hull, -1 where vert_to_tet is -1 */
 tessgpu_status tessgpu_complete_all(tessgpu_ctx* ctx, const float* particles, int num_particles,
@@ -221,6 +244,15 @@ void           tessgpu_batch_free(tessgpu_batch* batch);
 tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* batch,
                                    const tessgpu_dense_params* params, float* d_grid,
                                    tessgpu_dense_info* info);
+
+/* incomplete_cells for every block of a device batch: block b's links are
+   links[link_offsets[b] .. link_offsets[b+1]) (host arrays, at most 64 per
+   block), tested from last_neighbor[b] (NULL: all from 0); d_send_mask
+   (device) receives one mask per original particle of the batch, blocks in
+   order; enqueued (host, may be NULL) one count per block. */
+tessgpu_status tessgpu_batch_incomplete_cells(tessgpu_ctx* ctx, tessgpu_batch* batch, const int* link_offsets,
+                                              const tessgpu_link* links, const int* last_neighbor,
+                                              unsigned long long* d_send_mask, long long* enqueued);
 
 /* floats d_grid of tessgpu_batch_dense needs for these blocks and params, and
    (layers, may be NULL) its number of z layers: 0 for a 3-D grid */

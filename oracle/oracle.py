@@ -194,6 +194,21 @@ class Oracle:
             off += n
         return dict(blocks=out, max_dense=st[0], tot_mass=st[1], check_mass=st[2])
 
+    def side_of_plane(self, box6, tet, particles, j):
+        """side_of_plane (src/tet.cpp:70-119)."""
+        box6 = np.ascontiguousarray(box6, np.float32)
+        tet = np.ascontiguousarray(tet, np.int32)
+        particles = np.ascontiguousarray(particles, np.float32)
+        return int(self._l.f("side_of_plane")(_ptr(box6), _ptr(tet), _ptr(particles), ctypes.c_int(j)))
+
+    def distance(self, u, v):
+        """distance (src/tet.cpp:146-153)."""
+        fn = self._l.f("distance")
+        fn.restype = ctypes.c_float
+        u = np.ascontiguousarray(u, np.float32)
+        v = np.ascontiguousarray(v, np.float32)
+        return np.float32(fn(_ptr(u), _ptr(v)))
+
     def cell_grid_pts(self, block, cell, data_min, data_max, grid_min, grid_step, mass=1.0, eps=1e-4,
                       cap=1 << 16):
         arr, keep = make_blocks([block])
@@ -250,6 +265,26 @@ class Restated(Oracle):
         tet = np.ascontiguousarray(tet, np.int32)
         p = np.ascontiguousarray(p, np.float32)
         return bool(self._l.f("tet_contains")(_ptr(particles), _ptr(tet), _ptr(p)))
+
+    def incomplete_cells(self, block, links6, wrap3=None, last_neighbor=0):
+        """incomplete_cells (src/tess.cpp:492-628) for one block: (masks, enqueued),
+        masks a uint64 per original particle, bit i = send to link i."""
+        arr, keep = make_blocks([block])
+        l6 = np.ascontiguousarray(links6, np.float32).reshape(-1, 6)
+        w3 = None if wrap3 is None else np.ascontiguousarray(wrap3, np.int32).reshape(-1, 3)
+        masks = np.zeros(max(int(block["num_orig"]), 1), np.uint64)
+        fn = self._l.f("incomplete_cells")
+        fn.restype = ctypes.c_long
+        n = fn(arr, ctypes.c_int(l6.shape[0]), _ptr(l6), _ptr(w3), ctypes.c_int(last_neighbor), _ptr(masks))
+        del keep
+        return masks[:int(block["num_orig"])], int(n)
+
+    def box_distance(self, box6, c):
+        fn = self._l.f("box_distance")
+        fn.restype = ctypes.c_float
+        box6 = np.ascontiguousarray(box6, np.float32)
+        c = np.ascontiguousarray(c, np.float32)
+        return np.float32(fn(_ptr(box6), _ptr(c)))
 
     @staticmethod
     def z_layers(block_zmin, nz):

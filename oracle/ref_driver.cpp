@@ -274,6 +274,20 @@ void ref_dense_write(int alg_type, int nblocks, const ref_block* blocks,
         free_dblock(b);
 }
 
+// side_of_plane (src/tet.cpp:70-119) on a box given as min xyz, max xyz
+int ref_side_of_plane(const float* box6, const int* tet, const float* particles, int j)
+{
+    diy::ContinuousBounds box(3);
+    for (int i = 0; i < 3; ++i) { box.min[i] = box6[i]; box.max[i] = box6[3 + i]; }
+    return side_of_plane(box, (tet_t*)tet, (float*)particles, j);
+}
+
+// distance (src/tet.cpp:146-153)
+float ref_distance(const float* u, const float* v)
+{
+    return distance((float*)u, (float*)v);
+}
+
 // BlockGridParams (src/dense.cpp:575-648) for one block
 void ref_block_grid_params(const ref_block* rb, const float* grid_phys_mins, const float* grid_step_size,
                            float eps, const float* data_mins, const float* data_maxs, const int* glo_num_idx,

@@ -1043,6 +1043,146 @@ long orc_dense_ex(int alg, int nblocks, const orc_block* blocks, const float* da
     return lost;
 }
 
+/* ------------------------------------------------------------------ */
+/* part 1: incomplete_cells (src/tess.cpp:492-628)                    */
+/* ------------------------------------------------------------------ */
+/* src/tet.cpp:70-119; dot, src/tet.cpp:22-28 */
+int orc_side_of_plane(const float* box6, const orc_tet* tet, const float* particles, int j)
+{
+    int idx[4] = { 0, 1, 2, 3 };
+    int tmp = idx[j]; idx[j] = idx[3]; idx[3] = tmp;
+    const float* x = &particles[3 * tet->verts[idx[0]]];
+    const float* y = &particles[3 * tet->verts[idx[1]]];
+    const float* z = &particles[3 * tet->verts[idx[2]]];
+    const float* p = &particles[3 * tet->verts[idx[3]]];
+    float u[3], v[3], n[3];
+    for (int i = 0; i < 3; ++i)
+    {
+        u[i] = y[i] - x[i];
+        v[i] = z[i] - x[i];
+    }
+    cross3(n, u, v);
+    float res = 0;
+    for (int i = 0; i < 3; ++i)
+        res += n[i] * (p[i] - x[i]);
+    int sign = res > 0 ? 1 : (res < 0 ? -1 : 0);
+    if (sign == 0)
+        return 1;
+    res = 0;
+    for (int i = 0; i < 3; ++i)
+    {
+        if ((sign > 0) != (n[i] < 0))
+            res += n[i] * (box6[i] - x[i]);
+        else
+            res += n[i] * (box6[3 + i] - x[i]);
+    }
+    return (sign > 0) != (res > 0);
+}
+
+float orc_distance(const float* u, const float* v) { return dist3(u, v); }
+
+/* DIY's distance(bounds, point) (github.com/diatomic/diy, not vendored by
+   the reference): per axis the excess of the point beyond the box, squared
+   and summed in float; the square root of the sum */
+float orc_box_distance(const float* box6, const float* c)
+{
+    float res = 0;
+    for (int i = 0; i < 3; ++i)
+    {
+        float diff = 0, d;
+        d = box6[i] - c[i];
+        if (d > diff) diff = d;
+        d = c[i] - box6[3 + i];
+        if (d > diff) diff = d;
+        res += diff * diff;
+    }
+    return (float)sqrt((double)res);
+}
+
+long orc_incomplete_cells(const orc_block* b, int num_links, const float* links6, const int* wrap3,
+                          int last_neighbor, unsigned long long* masks)
+{
+    int norig = b->num_orig_particles;
+    for (int p = 0; p < norig; ++p)
+        masks[p] = 0;
+    /* wrap_bounds (DIY): bounds += wrap * (data max - data min) */
+    float* nb6 = (float*)malloc(sizeof(float) * 6 * (size_t)(num_links > 0 ? num_links : 1));
+    for (int i = 0; i < num_links; ++i)
+        for (int d = 0; d < 3; ++d)
+        {
+            float ext = b->data_max[d] - b->data_min[d];
+            int w = wrap3 ? wrap3[3 * i + d] : 0;
+            nb6[6 * i + d] = links6[6 * i + d] + w * ext;
+            nb6[6 * i + 3 + d] = links6[6 * i + 3 + d] + w * ext;
+        }
+    for (int t = 0; t < b->num_tets; ++t)
+    {
+        const orc_tet* tt = &b->tets[t];
+        int j;
+        for (j = 0; j < 4; ++j)
+            if (tt->verts[j] < norig)
+                break;
+        if (j == 4)
+            continue;
+        float center[3];
+        orc_circumcenter(center, tt, b->particles);
+        float rad = dist3(center, &b->particles[3 * tt->verts[0]]);
+        for (j = 0; j < 4; ++j)
+        {
+            if (tt->tets[j] != -1)
+                continue;
+            int k;
+            for (k = 0; k < 4; ++k)
+            {
+                if (k == j) continue;
+                if (tt->verts[k] < norig) break;
+            }
+            if (k == 4)
+                continue;
+            for (int i = last_neighbor; i < num_links; ++i)
+            {
+                if (!orc_side_of_plane(&nb6[6 * i], tt, b->particles, j))
+                    continue;
+                for (int v = 0; v < 4; ++v)
+                {
+                    if (v == j) continue;
+                    int p = tt->verts[v];
+                    if (p >= norig) continue;
+                    masks[p] |= 1ull << i;
+                }
+            }
+        }
+        for (j = 0; j < 3; ++j)
+        {
+            if (center[j] - b->bounds_min[j] <= rad) break;
+            if (b->bounds_max[j] - center[j] <= rad) break;
+        }
+        if (j == 3)
+            continue;
+        for (int i = last_neighbor; i < num_links; ++i)
+        {
+            if (orc_box_distance(&nb6[6 * i], center) <= rad)
+                for (int v = 0; v < 4; ++v)
+                {
+                    int p = tt->verts[v];
+                    if (p >= norig) continue;
+                    masks[p] |= 1ull << i;
+                }
+        }
+    }
+    /* src/tess.cpp:587-603 (release build: no assert) */
+    if (b->num_tets == 0)
+        for (int p = 0; p < norig; ++p)
+            for (int i = last_neighbor; i < num_links; ++i)
+                masks[p] |= 1ull << i;
+    long enqueued = 0;
+    for (int p = 0; p < norig; ++p)
+        for (int i = 0; i < 64; ++i)
+            enqueued += (long)((masks[p] >> i) & 1ull);
+    free(nb6);
+    return enqueued;
+}
+
 /* src/tess-qhull.c:161-225: for vertex v in order, the first neighbour not yet
    taken that does not hold verts[v]; -1 when none does */
 void orc_reorder_neighbors(orc_tet* tets, int num_tets)

@@ -102,6 +102,20 @@ long  orc_dense_ex(int alg, int nblocks, const orc_block* blocks, const float* d
                    float* global_grid, float* block_out, float* grid_out6, float* data_out6, double* stats3,
                    int* cell_counts);
 
+/* incomplete_cells (src/tess.cpp:492-628) for one block: links6 holds the
+   num_links (<= 64) neighbour core boxes (min xyz, max xyz), wrap3 (may be
+   NULL) their wrap directions; masks[p] for each original particle gets bit i
+   when the reference's to_send[p] holds link i.  Returns the number of
+   (particle, link) pairs (the reference's return value). */
+long  orc_incomplete_cells(const orc_block* b, int num_links, const float* links6, const int* wrap3,
+                           int last_neighbor, unsigned long long* masks);
+/* side_of_plane (src/tet.cpp:70-119) */
+int   orc_side_of_plane(const float* box6, const orc_tet* tet, const float* particles, int j);
+/* distance (src/tet.cpp:146-153) */
+float orc_distance(const float* u, const float* v);
+/* DIY's distance(bounds, point) */
+float orc_box_distance(const float* box6, const float* c);
+
 /* src/tess-qhull.c:161-225, in place */
 void  orc_reorder_neighbors(orc_tet* tets, int num_tets);
 

@@ -40,6 +40,23 @@ class Block(ctypes.Structure):
                 ("tets", ctypes.c_void_p), ("vert_to_tet", ctypes.c_void_p)]
 
 
+class Link(ctypes.Structure):
+    """tessgpu_link: a neighbour's core bounds and wrap direction"""
+    _fields_ = [("bounds_min", ctypes.c_float * 3), ("bounds_max", ctypes.c_float * 3), ("wrap", ctypes.c_int * 3)]
+
+
+def make_links(links6, wrap3=None):
+    """ctypes array of Link from (L, 6) boxes (min xyz, max xyz) and optional (L, 3) wraps."""
+    l6 = np.asarray(links6, np.float32).reshape(-1, 6)
+    arr = (Link * max(len(l6), 1))()
+    for i, row in enumerate(l6):
+        for d in range(3):
+            arr[i].bounds_min[d] = row[d]
+            arr[i].bounds_max[d] = row[3 + d]
+            arr[i].wrap[d] = 0 if wrap3 is None else int(np.asarray(wrap3).reshape(-1, 3)[i][d])
+    return arr
+
+
 class DenseParams(ctypes.Structure):
     """tessgpu_dense_params"""
     _fields_ = [("alg", ctypes.c_int), ("mode", ctypes.c_int), ("num_given_bounds", ctypes.c_int),
@@ -119,6 +136,8 @@ def lib():
             "tessgpu_project_grid": (_I, [_VP, _VP, _I, ctypes.c_longlong, _VP]),
             "tessgpu_write_grid": (_I, [_VP, _VP, ctypes.c_longlong, ctypes.c_char_p]),
             "tessgpu_write_last_grid": (_I, [_VP, ctypes.c_char_p]),
+            "tessgpu_incomplete_cells": (_I, [_VP, _VP, _I, _VP, _I, _VP, _VP]),
+            "tessgpu_batch_incomplete_cells": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -242,6 +261,19 @@ class Context:
     def reorder_neighbors_device(self, d_tets, num_tets):
         """in place on tet_t records in device memory (address d_tets)"""
         self._check(lib().tessgpu_reorder_neighbors_device(self._h, ctypes.c_void_p(d_tets), num_tets))
+
+    def incomplete_cells(self, block, links6, wrap3=None, last_neighbor=0):
+        """incomplete_cells (src/tess.cpp:492-628) for one host block: (masks, enqueued),
+        masks a uint64 per original particle with bit i set to send it to link i."""
+        arr, keep = make_blocks([block])
+        links = make_links(links6, wrap3)
+        nl = int(np.asarray(links6).size // 6)
+        masks = np.zeros(max(arr[0].num_orig_particles, 1), np.uint64)
+        enq = ctypes.c_longlong()
+        self._check(lib().tessgpu_incomplete_cells(self._h, arr, nl, links, int(last_neighbor), _p(masks),
+                                                   ctypes.byref(enq)))
+        del keep
+        return masks[:arr[0].num_orig_particles], int(enq.value)
 
     def fill_circumcenters(self, tets, particles):
         tets = np.ascontiguousarray(tets, np.int32)
@@ -371,6 +403,26 @@ class Batch:
         self.ctx._check(lib().tessgpu_batch_dense(self.ctx.handle, self._h, ctypes.byref(p), ctypes.c_void_p(d_grid),
                                                   ctypes.byref(info) if info is not None else None))
         return info.as_dict() if info is not None else None
+
+    def incomplete_cells(self, links6_per_block, d_masks, wrap3_per_block=None, last_neighbor=None):
+        """incomplete_cells for every block; masks (one uint64 per original particle of
+        the batch, blocks in order) go to device memory at d_masks.  Returns enqueued per block."""
+        nb = len(links6_per_block)
+        off = np.zeros(nb + 1, np.int32)
+        rows, wraps = [], []
+        for b, l6 in enumerate(links6_per_block):
+            l6 = np.asarray(l6, np.float32).reshape(-1, 6)
+            off[b + 1] = off[b] + len(l6)
+            rows.append(l6)
+            w = None if wrap3_per_block is None else wrap3_per_block[b]
+            wraps.append(np.zeros((len(l6), 3), np.int32) if w is None else np.asarray(w, np.int32).reshape(-1, 3))
+        links = make_links(np.concatenate(rows) if rows else np.zeros((0, 6), np.float32),
+                           np.concatenate(wraps) if wraps else None)
+        last = None if last_neighbor is None else np.ascontiguousarray(last_neighbor, np.int32)
+        enq = np.zeros(nb, np.int64)
+        self.ctx._check(lib().tessgpu_batch_incomplete_cells(self.ctx.handle, self._h, _p(off), links, _p(last),
+                                                             ctypes.c_void_p(d_masks), _p(enq)))
+        return enq
 
     def debug_outputs(self, cells=None, grid_points=None, particles=None):
         cc = np.empty(cells, np.int32) if cells else None

@@ -370,7 +370,8 @@ enum PoolSlot
 {
     SLOT_BLOCKS, SLOT_COFF, SLOT_POS, SLOT_TV, SLOT_TN, SLOT_V2T, SLOT_CC, SLOT_CC64, SLOT_W, SLOT_RHO32,
     SLOT_RHO64, SLOT_FIX, SLOT_FIXN, SLOT_STAGE, SLOT_RAWPTR, SLOT_RAWV2T, SLOT_GRID, SLOT_CELLS, SLOT_OUT,
-    SLOT_OUT2, SLOT_COUNT, SLOT_ZLAYER, SLOT_GRID3, SLOT_PROJ
+    SLOT_OUT2, SLOT_COUNT, SLOT_ZLAYER, SLOT_GRID3, SLOT_PROJ, SLOT_LINKS, SLOT_LINKOFF, SLOT_MASK,
+    SLOT_SENDS
 };
 
 static cudaError_t balloc(tessgpu_batch* bt, int slot, size_t bytes, void** out)
@@ -1160,6 +1161,106 @@ extern "C" tessgpu_status tessgpu_write_last_grid(tessgpu_ctx* ctx, const char* 
 }
 
 // ---------------------------------------------------------------------------
+// incomplete_cells
+// ---------------------------------------------------------------------------
+extern "C" tessgpu_status tessgpu_batch_incomplete_cells(tessgpu_ctx* ctx, tessgpu_batch* bt, const int* link_offsets,
+                                                         const tessgpu_link* links, const int* last_neighbor,
+                                                         unsigned long long* d_send_mask, long long* enqueued)
+{
+    if (!ctx || !bt || !link_offsets || (!links && link_offsets[bt->nb]) || (bt->C && !d_send_mask))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    const int nb = bt->nb;
+    if (link_offsets[0] != 0) return set_err(ctx, TESSGPU_ERR_INVALID, "link_offsets[0] must be 0");
+    for (int b = 0; b < nb; ++b)
+    {
+        const int n = link_offsets[b + 1] - link_offsets[b];
+        const int f = last_neighbor ? last_neighbor[b] : 0;
+        if (n < 0 || n > 64 || f < 0)
+            return set_err(ctx, n > 64 ? TESSGPU_ERR_UNSUPPORTED : TESSGPU_ERR_INVALID,
+                           "block " + std::to_string(b) + ": links must number 0..64 and last_neighbor be >= 0");
+    }
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int nl = link_offsets[nb];
+    // wrap_bounds: a link across a periodic boundary sees its box shifted by
+    // the wrap direction times the data extent (DBlock::data_bounds)
+    std::vector<float> l6(6 * (size_t)std::max(nl, 1), 0.0f);
+    std::vector<int> meta(2 * nb + 1);
+    std::vector<unsigned long long> fill(nb, 0ull);
+    for (int b = 0; b < nb; ++b)
+    {
+        const tessgpu_block& B = bt->blocks[b];
+        for (int i = link_offsets[b]; i < link_offsets[b + 1]; ++i)
+            for (int d = 0; d < 3; ++d)
+            {
+                const float ext = B.data_max[d] - B.data_min[d];
+                l6[6 * i + d] = links[i].bounds_min[d] + links[i].wrap[d] * ext;
+                l6[6 * i + 3 + d] = links[i].bounds_max[d] + links[i].wrap[d] * ext;
+            }
+        const int f = last_neighbor ? last_neighbor[b] : 0;
+        for (int i = f; i < link_offsets[b + 1] - link_offsets[b]; ++i)
+            fill[b] |= 1ull << i;
+    }
+    for (int b = 0; b <= nb; ++b) meta[b] = link_offsets[b];
+    for (int b = 0; b < nb; ++b) meta[nb + 1 + b] = last_neighbor ? last_neighbor[b] : 0;
+    cudaError_t e;
+    float* d_l6 = (float*)pool_get(ctx, SLOT_LINKS, sizeof(float) * l6.size(), &e);
+    CK(e);
+    int* d_meta = (int*)pool_get(ctx, SLOT_LINKOFF, sizeof(int) * meta.size(), &e);
+    CK(e);
+    unsigned long long* d_aux =
+        (unsigned long long*)pool_get(ctx, SLOT_SENDS, sizeof(unsigned long long) * 2 * nb, &e);
+    CK(e);
+    CK(cudaMemcpyAsync(d_l6, l6.data(), sizeof(float) * l6.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_aux, fill.data(), sizeof(unsigned long long) * nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(d_aux + nb, 0, sizeof(unsigned long long) * nb, s));
+    if (bt->C) CK(cudaMemsetAsync(d_send_mask, 0, sizeof(unsigned long long) * bt->C, s));
+    ctx->nmarks = 0;
+    mark(ctx, "start");
+    launch_incomplete_cells(bt->d_blocks, bt->d_c_off, nb, (int)bt->T, (int)bt->C, bt->pos, bt->tv, bt->tn, d_l6,
+                            d_meta, d_meta + nb + 1, d_aux, d_send_mask, d_aux + nb, s);
+    ctx->launches += (bt->C ? 2 : 0) + (bt->T ? 1 : 0);
+    mark(ctx, "incomplete_cells");
+    CK(cudaGetLastError());
+    if (enqueued)
+    {
+        std::vector<unsigned long long> cnt(nb);
+        CK(cudaMemcpyAsync(cnt.data(), d_aux + nb, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (int b = 0; b < nb; ++b) enqueued[b] = (long long)cnt[b];
+    }
+    return TESSGPU_OK;
+}
+
+extern "C" tessgpu_status tessgpu_incomplete_cells(tessgpu_ctx* ctx, const tessgpu_block* block, int num_links,
+                                                   const tessgpu_link* links, int last_neighbor,
+                                                   unsigned long long* send_mask, long long* enqueued)
+{
+    if (!ctx || !block || num_links < 0 || (num_links && !links) || last_neighbor < 0 ||
+        (block->num_orig_particles && !send_mask))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad arguments");
+    tessgpu_batch* bt = nullptr;
+    tessgpu_status s = batch_build(ctx, 1, block, false, true, &bt);
+    if (s != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }
+    cudaError_t e;
+    unsigned long long* d_mask =
+        (unsigned long long*)pool_get(ctx, SLOT_MASK, sizeof(unsigned long long) * std::max<long long>(bt->C, 1), &e);
+    if ((s = cuda_check(ctx, e, "cudaMalloc")) == TESSGPU_OK)
+    {
+        const int off[2] = { 0, num_links };
+        long long enq = 0;
+        s = tessgpu_batch_incomplete_cells(ctx, bt, off, links, &last_neighbor, d_mask, &enq);
+        if (s == TESSGPU_OK && bt->C)
+            s = cuda_check(ctx, cudaMemcpy(send_mask, d_mask, sizeof(unsigned long long) * bt->C,
+                                           cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (s == TESSGPU_OK && enqueued) *enqueued = enq;
+    }
+    tessgpu_batch_free(bt);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
 // reorder_neighbors
 // ---------------------------------------------------------------------------
 extern "C" tessgpu_status tessgpu_reorder_neighbors_device(tessgpu_ctx* ctx, int* d_tets, int num_tets)
@@ -1168,7 +1269,10 @@ extern "C" tessgpu_status tessgpu_reorder_neighbors_device(tessgpu_ctx* ctx, int
     if (!num_tets) return TESSGPU_OK;
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), ctx->stream));
+    ctx->nmarks = 0;
+    mark(ctx, "start");
     launch_reorder_neighbors(d_tets, num_tets, ctx->d_status, ctx->stream);
+    mark(ctx, "reorder_neighbors");
     ctx->launches++;
     return finish_status(ctx);
 }

@@ -870,6 +870,166 @@ __global__ void k_reorder_neighbors(int* tets, int total, Status* st)
     }
 }
 
+// ---------------------------------------------------------------------------
+// incomplete_cells (src/tess.cpp:492-628)
+// ---------------------------------------------------------------------------
+// side_of_plane (src/tet.cpp:70-119): whether the box reaches the far side of
+// the plane of the face opposite vertex j, as seen from vertex j; a degenerate
+// face counts as reaching it.  dot (src/tet.cpp:22) and cross (:131) in the
+// reference's order.
+__device__ __forceinline__ bool side_of_plane_ref(const float* box, const float3* P, int j)
+{
+    int idx[4] = { 0, 1, 2, 3 };
+    idx[j] = 3;
+    idx[3] = j;
+    const float3 x = P[idx[0]], y = P[idx[1]], z = P[idx[2]], p = P[idx[3]];
+    const float u[3] = { y.x - x.x, y.y - x.y, y.z - x.z };
+    const float v[3] = { z.x - x.x, z.y - x.y, z.z - x.z };
+    const float n[3] = { u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0] };
+    const float xx[3] = { x.x, x.y, x.z };
+    const float pp[3] = { p.x, p.y, p.z };
+    float res = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        res += n[i] * (pp[i] - xx[i]);
+    const int sign = res > 0.0f ? 1 : (res < 0.0f ? -1 : 0);
+    if (sign == 0)
+        return true;
+    res = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        if ((sign > 0) != (n[i] < 0.0f))
+            res += n[i] * (box[i] - xx[i]);
+        else
+            res += n[i] * (box[3 + i] - xx[i]);
+    }
+    return (sign > 0) != (res > 0.0f);
+}
+
+// Euclidean distance from a point to a box (0 inside), as DIY's
+// distance(bounds, point) computes it: per axis the excess beyond the box,
+// squared and summed in float, then the square root
+__device__ __forceinline__ float box_distance(const float* box, const float* c)
+{
+    float res = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        float diff = 0.0f, d;
+        d = box[i] - c[i];
+        if (d > diff) diff = d;
+        d = c[i] - box[3 + i];
+        if (d > diff) diff = d;
+        res += diff * diff;
+    }
+    return sqrtf(res);
+}
+
+// One thread per tet.  Bit i of masks[c_off + p] is set when original particle
+// p must go to link i of its block (the reference's to_send[p] sets):
+//  - for a hull face opposite vertex j with a local vertex, every link whose
+//    (wrapped) box reaches past the face gets the face's local vertices;
+//  - unless the circumsphere lies deeper in the block than its radius on
+//    every axis, every link whose box is within the radius of the
+//    circumcenter gets the tet's local vertices.
+// links6: wrapped link boxes (min xyz, max xyz), block b's at link_off[b]..link_off[b+1)
+__global__ void k_incomplete_cells(const BlockDesc* blocks, int nb, int total, const float4* pos, const int4* tv,
+                                   const int4* tn, const float* links6, const int* link_off, const int* first_link,
+                                   unsigned long long* masks)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+    {
+        const int b = find_block_t(blocks, nb, t);
+        const BlockDesc& B = blocks[b];
+        const int4 v4 = __ldg(&tv[t]);
+        const int4 n4 = __ldg(&tn[t]);
+        const int vl[4] = { v4.x - B.p_off, v4.y - B.p_off, v4.z - B.p_off, v4.w - B.p_off };
+        const int nbr[4] = { n4.x, n4.y, n4.z, n4.w };
+        bool local[4];
+        bool any = false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+        {
+            local[k] = vl[k] >= 0 && vl[k] < B.norig;
+            any |= local[k];
+        }
+        if (!any)
+            continue;
+        const float3 P[4] = { ld3(pos, v4.x), ld3(pos, v4.y), ld3(pos, v4.z), ld3(pos, v4.w) };
+        float c[3];
+        circumcenter_ref(P[0], P[1], P[2], P[3], c);
+        // distance (src/tet.cpp:146-153) from the circumcenter to vertex 0
+        const float p0[3] = { P[0].x, P[0].y, P[0].z };
+        float n2 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            n2 += (c[i] - p0[i]) * (c[i] - p0[i]);
+        const float rad = sqrtf(n2);
+
+        const int l0 = link_off[b] + first_link[b], l1 = link_off[b + 1];
+        unsigned long long m[4] = { 0ull, 0ull, 0ull, 0ull };
+        for (int j = 0; j < 4; ++j)
+        {
+            if (nbr[j] != -1)
+                continue;
+            bool face_local = false;
+            for (int k = 0; k < 4; ++k)
+                if (k != j && local[k]) face_local = true;
+            if (!face_local)
+                continue;
+            for (int i = l0; i < l1; ++i)
+                if (side_of_plane_ref(&links6[6 * i], P, j))
+                {
+                    const unsigned long long bit = 1ull << (i - link_off[b]);
+                    for (int k = 0; k < 4; ++k)
+                        if (k != j) m[k] |= bit;
+                }
+        }
+        int j;
+        for (j = 0; j < 3; ++j)
+        {
+            if (c[j] - B.bmin[j] <= rad) break;
+            if (B.bmax[j] - c[j] <= rad) break;
+        }
+        if (j < 3)
+            for (int i = l0; i < l1; ++i)
+                if (box_distance(&links6[6 * i], c) <= rad)
+                {
+                    const unsigned long long bit = 1ull << (i - link_off[b]);
+                    for (int k = 0; k < 4; ++k) m[k] |= bit;
+                }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (local[k] && m[k])
+                atomicOr(&masks[B.c_off + vl[k]], m[k]);
+    }
+}
+
+// blocks without tets send every original particle to every link
+// (src/tess.cpp:587-603); fill: per block, the mask of its links from first_link
+__global__ void k_fill_masks(const BlockDesc* blocks, const int* c_off, int nb, int total_cells,
+                             const unsigned long long* fill, unsigned long long* masks)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total_cells; c += gridDim.x * blockDim.x)
+    {
+        const int b = find_block_c(c_off, nb, c);
+        if (blocks[b].nt == 0)
+            masks[c] = fill[b];
+    }
+}
+
+// enqueued (the reference's return value) per block: set bits of its masks
+__global__ void k_count_sends(const int* c_off, int nb, int total_cells, const unsigned long long* masks,
+                              unsigned long long* counts)
+{
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total_cells; c += gridDim.x * blockDim.x)
+    {
+        const int n = __popcll(masks[c]);
+        if (n) atomicAdd(&counts[find_block_c(c_off, nb, c)], (unsigned long long)n);
+    }
+}
+
 // z-projection of a 3-D grid into layers: layer l at (x, y) accumulates
 // value * dz over the z indices of layer l in ascending z (one thread per
 // column; consecutive threads read consecutive x, so every z step is coalesced)
@@ -1012,6 +1172,20 @@ void launch_sum_layers(const float* layers, int num_layers, long long area, floa
 {
     if (area <= 0 || num_layers <= 0) return;
     k_sum_layers<<<grid1d(area, 256), 256, 0, s>>>(layers, num_layers, area, out);
+}
+
+void launch_incomplete_cells(const BlockDesc* blocks, const int* c_off, int nb, int total_tets, int total_cells,
+                             const float4* pos, const int4* tv, const int4* tn, const float* links6,
+                             const int* link_off, const int* first_link, const unsigned long long* fill,
+                             unsigned long long* masks, unsigned long long* counts, cudaStream_t s)
+{
+    if (total_cells > 0)
+        k_fill_masks<<<grid1d(total_cells, 256), 256, 0, s>>>(blocks, c_off, nb, total_cells, fill, masks);
+    if (total_tets > 0)
+        k_incomplete_cells<<<grid1d(total_tets, 256), 256, 0, s>>>(blocks, nb, total_tets, pos, tv, tn, links6,
+                                                                   link_off, first_link, masks);
+    if (total_cells > 0)
+        k_count_sends<<<grid1d(total_cells, 256), 256, 0, s>>>(c_off, nb, total_cells, masks, counts);
 }
 
 void launch_reorder_neighbors(int* d_tets, int total, Status* st, cudaStream_t s)

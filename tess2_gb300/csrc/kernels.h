@@ -24,6 +24,10 @@ void launch_cic(const BlockDesc* d_blocks, const int* d_cell_off, int nb, int to
                 const GridDesc& g, float* grid, Status* st, cudaStream_t s);
 void launch_grid_max(const float* grid, long long n, float* d_max, cudaStream_t s);
 void launch_reorder_neighbors(int* d_tets, int total_tets, Status* st, cudaStream_t s);
+void launch_incomplete_cells(const BlockDesc* blocks, const int* c_off, int nb, int total_tets, int total_cells,
+                             const float4* pos, const int4* tv, const int4* tn, const float* links6,
+                             const int* link_off, const int* first_link, const unsigned long long* fill,
+                             unsigned long long* masks, unsigned long long* counts, cudaStream_t s);
 void launch_project_layers(const float* grid, int nx, int ny, int nz, const int* zlayer, float dz, float* layers,
                            cudaStream_t s);
 void launch_sum_layers(const float* layers, int num_layers, long long area, float* out, cudaStream_t s);

@@ -294,3 +294,55 @@ def test_dtfe_projected(gpu_ctx, oracle, dims):
     assert rel_l2(layers, oracle.project_layers(ref, zl, dz)) < 1e-6
     # max over the layers, as dense() reports it before ProjectGrid
     assert np.isclose(info["max_dense"], layers.max(), rtol=0)
+
+
+# ---------------------------------------------------------------------------
+# incomplete_cells
+# ---------------------------------------------------------------------------
+def _links_of(blocks, bi):
+    return np.array([np.concatenate([o["bounds_min"], o["bounds_max"]]) for k, o in enumerate(blocks) if k != bi],
+                    np.float32)
+
+
+def test_incomplete_cells_batch_bitexact(gpu_ctx, oracle):
+    """Every block of the 2x2x2 golden decomposition, all links from 0: the
+    send masks bit for bit, and the per-block counts."""
+    import torch
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    batch = gpu_ctx.upload(blocks)
+    C = sum(int(b["num_orig"]) for b in blocks)
+    dm = torch.zeros(C, dtype=torch.int64, device="cuda:0")
+    enq = batch.incomplete_cells([_links_of(blocks, i) for i in range(len(blocks))], dm.data_ptr())
+    torch.cuda.synchronize()
+    got = dm.cpu().numpy().view(np.uint64)
+    off = 0
+    for i, b in enumerate(blocks):
+        m, n = oracle.incomplete_cells(b, _links_of(blocks, i))
+        assert np.array_equal(got[off:off + b["num_orig"]], m), i
+        assert enq[i] == n
+        off += b["num_orig"]
+
+
+@pytest.mark.parametrize("last", [0, 3])
+def test_incomplete_cells_periodic_bitexact(gpu_ctx, oracle, last):
+    from tess2_gb300 import host
+    pts = host.mixture_particles(20000, 9, n_clumps=32, sigma=0.02)
+    blocks = host.tessellate(host.decompose(pts, (3, 2, 2), 0.06), processes=1)
+    b = blocks[4]
+    l6 = _links_of(blocks, 4)
+    w3 = np.zeros((len(l6), 3), np.int32)
+    w3[::3, 0] = 1
+    w3[1::4, 1] = -1
+    m, n = gpu_ctx.incomplete_cells(b, l6, w3, last_neighbor=last)
+    mo, no = oracle.incomplete_cells(b, l6, w3, last_neighbor=last)
+    assert np.array_equal(m, mo) and n == no and n > 0
+
+
+def test_incomplete_cells_without_tets_gpu(gpu_ctx, oracle):
+    p = np.random.default_rng(1).random((4, 3), dtype=np.float32)
+    b = dict(particles=p, tets=np.zeros((0, 8), np.int32), vert_to_tet=np.full(4, -1, np.int32), num_orig=3,
+             bounds_min=np.zeros(3, np.float32), bounds_max=np.ones(3, np.float32),
+             data_min=np.zeros(3, np.float32), data_max=np.ones(3, np.float32))
+    l6 = np.tile(np.array([0, 0, 0, 1, 1, 1], np.float32), (5, 1))
+    m, n = gpu_ctx.incomplete_cells(b, l6, last_neighbor=2)
+    assert list(m) == [0b11100] * 3 and n == 9

@@ -134,3 +134,97 @@ def test_project_helpers(oracle):
     lay = oracle.project_layers(g, np.array([0, 1], np.int32), 0.5)
     assert np.array_equal(lay[0], g[0] * np.float32(0.5)) and np.array_equal(lay[1], g[1] * np.float32(0.5))
     assert np.array_equal(oracle.sum_layers(lay), lay[0] + lay[1])
+
+
+def test_side_of_plane_and_distance_pinned():
+    """side_of_plane and distance of the restated oracle against the
+    reference's own src/tet.cpp (oracle/_ref), on random and coplanar tets."""
+    import os
+    from oracle.oracle import REF_SO, Oracle, Restated
+    if not os.path.exists(REF_SO):
+        pytest.skip("reference build not present")
+    R, O = Oracle("ref"), Restated()
+    rng = np.random.default_rng(3)
+    tet = np.array([0, 1, 2, 3, -1, -1, -1, -1], np.int32)
+    for it in range(2000):
+        P = rng.random((4, 3), dtype=np.float32)
+        if it % 5 == 0:   # vertex 3 on the plane of 0, 1, 2 (up to rounding)
+            w = rng.random(2).astype(np.float32)
+            P[3] = P[0] + w[0] * (P[1] - P[0]) + w[1] * (P[2] - P[0])
+        lo = (rng.random(3, dtype=np.float32) * 2 - 0.5).astype(np.float32)
+        box = np.concatenate([lo, lo + rng.random(3, dtype=np.float32)]).astype(np.float32)
+        for j in range(4):
+            assert R.side_of_plane(box, tet, P, j) == O.side_of_plane(box, tet, P, j)
+        assert R.distance(P[0], P[1]).view(np.uint32) == O.distance(P[0], P[1]).view(np.uint32)
+
+
+def _incomplete_cells_loops(O, b, links6, wrap3, last):
+    """incomplete_cells (src/tess.cpp:492-628) once more, in Python loops over
+    the oracle's pinned primitives, as an independent check of the C oracle's
+    control flow."""
+    f32 = np.float32
+    norig = int(b["num_orig"])
+    P, T = b["particles"], b["tets"]
+    ext = (b["data_max"] - b["data_min"]).astype(f32)
+    boxes = []
+    for i, l6 in enumerate(links6):
+        w = wrap3[i] if wrap3 is not None else np.zeros(3, np.int32)
+        sh = np.array([f32(w[d]) * ext[d] for d in range(3)], f32)
+        boxes.append(np.concatenate([(l6[:3] + sh).astype(f32), (l6[3:] + sh).astype(f32)]))
+    cc = O.fill_circumcenters(P, T)
+    masks = [0] * norig
+    for t in range(len(T)):
+        verts, nbrs = T[t, :4], T[t, 4:]
+        if not any(v < norig for v in verts):
+            continue
+        c = cc[t]
+        rad = O.distance(c, P[verts[0]])
+        for j in range(4):
+            if nbrs[j] != -1 or not any(verts[k] < norig for k in range(4) if k != j):
+                continue
+            for i in range(last, len(boxes)):
+                if O.side_of_plane(boxes[i], T[t], P, j):
+                    for k in range(4):
+                        if k != j and verts[k] < norig:
+                            masks[verts[k]] |= 1 << i
+        deep = all(c[d] - b["bounds_min"][d] > rad and b["bounds_max"][d] - c[d] > rad for d in range(3))
+        if deep:
+            continue
+        for i in range(last, len(boxes)):
+            if O.box_distance(boxes[i], c) <= rad:
+                for v in verts:
+                    if v < norig:
+                        masks[v] |= 1 << i
+    return np.array(masks, np.uint64)
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_incomplete_cells_restated_twice(oracle, periodic):
+    from tess2_gb300 import host
+    pts = host.mixture_particles(1200, 5, n_clumps=4, sigma=0.05)
+    blocks = host.tessellate(host.decompose(pts, (2, 2, 2), 0.08), processes=1)
+    b = blocks[5]
+    links6 = np.array([np.concatenate([o["bounds_min"], o["bounds_max"]]) for k, o in enumerate(blocks) if k != 5],
+                      np.float32)
+    wrap3 = None
+    if periodic:
+        wrap3 = np.zeros((len(links6), 3), np.int32)
+        wrap3[::2, 0] = 1
+        wrap3[1::3, 2] = -1
+    m, enq = oracle.incomplete_cells(b, links6, wrap3, last_neighbor=1)
+    ref = _incomplete_cells_loops(oracle, b, links6, wrap3, 1)
+    assert np.array_equal(m, ref)
+    assert enq == sum(bin(int(x)).count("1") for x in m)
+    assert enq > 0 and not (m & np.uint64(1)).any()   # link 0 is below last_neighbor
+
+
+def test_incomplete_cells_without_tets(oracle):
+    """A block with fewer than five particles has no tets: every original
+    particle goes to every tested link."""
+    p = np.random.default_rng(1).random((4, 3), dtype=np.float32)
+    b = dict(particles=p, tets=np.zeros((0, 8), np.int32), vert_to_tet=np.full(4, -1, np.int32), num_orig=3,
+             bounds_min=np.zeros(3, np.float32), bounds_max=np.ones(3, np.float32),
+             data_min=np.zeros(3, np.float32), data_max=np.ones(3, np.float32))
+    links6 = np.tile(np.array([0, 0, 0, 1, 1, 1], np.float32), (5, 1))
+    m, enq = oracle.incomplete_cells(b, links6, last_neighbor=2)
+    assert list(m) == [0b11100] * 3 and enq == 9
