@@ -1019,16 +1019,115 @@ int raster_variants() { return N_RASTER_VARIANTS; }
 
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
-                   int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s)
+                   int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s, const int* order,
+                   const int* order_count)
 {
     if (total <= 0) return;
     const long long work = (long long)((total + 31) / 32) * 32 * 32;
+    if (order)
+    {
+        if (mode == TESSGPU_MODE_FP64)
+            raster_variant<double, true, true>(variant, work, s, d_blocks, nb, total, order, order_count, pos, tv,
+                                               rho32, rho64, g, tau, grid, owner, nullptr, nullptr, st);
+        else
+            raster_variant<float, false, true>(variant, work, s, d_blocks, nb, total, order, order_count, pos, tv,
+                                               rho32, rho64, g, tau, grid, owner, fix_list, fix_count, st);
+        return;
+    }
     if (mode == TESSGPU_MODE_FP64)
         raster_variant<double, true, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
                                             rho64, g, tau, grid, owner, nullptr, nullptr, st);
     else
         raster_variant<float, false, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
                                             rho64, g, tau, grid, owner, fix_list, fix_count, st);
+}
+
+// ---------------------------------------------------------------------------
+// spatial processing order of the tets
+// ---------------------------------------------------------------------------
+// The rasteriser writes each grid point once, 4 bytes at a time; tets in
+// Qhull's order scatter those writes over the grid, so a 32-byte sector is
+// written back to HBM several times (partial sectors cost a read-modify-write
+// too).  Processing the tets brick by brick (8x8x8 grid points, bricks in
+// x-fastest order, by the brick of the tet's centroid) keeps the sectors
+// being written in L2.  A counting sort: key and histogram, one exclusive
+// scan, scatter.  The order within a brick follows the atomics; the grid does
+// not depend on it (every grid point has exactly one owner tet).
+__global__ void k_order_keys(const float4* pos, const int4* tv, int total, GridDesc g, int nbx, int nby, int nbz,
+                             int* key, int* hist)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+    {
+        const int4 v = __ldg(&tv[t]);
+        const float4 a = __ldg(&pos[v.x]), b = __ldg(&pos[v.y]), c = __ldg(&pos[v.z]), d = __ldg(&pos[v.w]);
+        const float cen[3] = { 0.25f * ((a.x + b.x) + (c.x + d.x)), 0.25f * ((a.y + b.y) + (c.y + d.y)),
+                               0.25f * ((a.z + b.z) + (c.z + d.z)) };
+        const int nbk[3] = { nbx, nby, nbz };
+        int br[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+        {
+            const float f = (cen[i] - g.gmin[i]) * g.inv_step[i];
+            int gi = f > 0.0f ? (int)fminf(f, (float)(g.n[i] - 1)) : 0;
+            br[i] = min(gi >> 3, nbk[i] - 1);
+        }
+        const int k = (br[2] * nby + br[1]) * nbx + br[0];
+        key[t] = k;
+        atomicAdd(&hist[k], 1);
+    }
+}
+
+// exclusive prefix sum of n counts in place, one block of 1024 threads
+__global__ void __launch_bounds__(1024) k_scan_counts(int* a, int n)
+{
+    __shared__ long long part[1024];
+    const int per = (n + 1023) / 1024;
+    const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
+    long long s = 0;
+    for (int i = lo; i < hi; ++i)
+        s += a[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1)
+    {
+        const long long v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    long long run = part[threadIdx.x] - s;
+    for (int i = lo; i < hi; ++i)
+    {
+        const int c = a[i];
+        a[i] = (int)run;
+        run += c;
+    }
+}
+
+__global__ void k_order_scatter(const int* key, int total, int* cursor, int* order)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
+        order[atomicAdd(&cursor[key[t]], 1)] = t;
+}
+
+void order_bricks(const GridDesc& g, int* nbx, int* nby, int* nbz)
+{
+    *nbx = (g.n[0] + 7) >> 3;
+    *nby = (g.n[1] + 7) >> 3;
+    *nbz = (g.n[2] + 7) >> 3;
+}
+
+void launch_tet_order(const float4* pos, const int4* tv, int total, const GridDesc& g, int* key, int* hist,
+                      int* order, cudaStream_t s)
+{
+    if (total <= 0) return;
+    int nbx, nby, nbz;
+    order_bricks(g, &nbx, &nby, &nbz);
+    const int nk = nbx * nby * nbz;
+    cudaMemsetAsync(hist, 0, sizeof(int) * nk, s);
+    k_order_keys<<<grid_for(total, 256, 8), 256, 0, s>>>(pos, tv, total, g, nbx, nby, nbz, key, hist);
+    k_scan_counts<<<1, 1024, 0, s>>>(hist, nk);
+    k_order_scatter<<<grid_for(total, 256, 8), 256, 0, s>>>(key, total, hist, order);
 }
 
 // the tets the mixed pass listed, with FP64 values; sized for the longest
