@@ -44,6 +44,9 @@ struct tessgpu_ctx
     cudaEvent_t              stage_ev[2] = { nullptr, nullptr };
     const float*             last_grid = nullptr;
     long long                last_grid_floats = 0;
+    // the pipelined host-buffer DTFE call: copy streams and events
+    cudaStream_t             h2d = nullptr, d2h = nullptr;
+    std::vector<cudaEvent_t> pipe_ev;
 };
 
 static void mark(tessgpu_ctx* c, const char* name)
@@ -164,6 +167,10 @@ extern "C" void tessgpu_destroy(tessgpu_ctx* ctx)
         if (ctx->h_stage[i]) cudaFreeHost(ctx->h_stage[i]);
         if (ctx->stage_ev[i]) cudaEventDestroy(ctx->stage_ev[i]);
     }
+    for (cudaEvent_t e : ctx->pipe_ev)
+        cudaEventDestroy(e);
+    if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
+    if (ctx->d2h) cudaStreamDestroy(ctx->d2h);
     delete ctx;
 }
 
@@ -783,7 +790,10 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             // fastest; the grid is rewritten by every run, the fix list is reset
             const char* env = getenv("TESSGPU_RASTER_VARIANT");
             if (env && *env)
+            {
                 var = std::min(std::max(atoi(env), 0), raster_variants() - 1);
+                ctx->raster_variant[p->mode] = var;
+            }
         }
         if (var < 0)
         {
@@ -1047,6 +1057,253 @@ __global__ void k_extract_box(const float* grid, int nx, int ny, const int* mn, 
     }
 }
 
+// ---------------------------------------------------------------------------
+// DTFE through host buffers, pipelined per block
+// ---------------------------------------------------------------------------
+// one block's particles: xyz -> float4
+__global__ void k_pack_block(const float* raw, int np, float4* pos)
+{
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x)
+        pos[p] = make_float4(raw[3 * (size_t)p], raw[3 * (size_t)p + 1], raw[3 * (size_t)p + 2], 0.0f);
+}
+
+// one block's tet_t vertices -> batch-wide particle indices, checked
+__global__ void k_ingest_verts(const int4* raw, int nt, int np, int p_off, int4* tv, Status* st)
+{
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x)
+    {
+        int4 v = raw[2 * (size_t)t];   // verts; raw[2t + 1] holds the neighbours
+        if ((unsigned)v.x >= (unsigned)np || (unsigned)v.y >= (unsigned)np || (unsigned)v.z >= (unsigned)np ||
+            (unsigned)v.w >= (unsigned)np)
+        {
+            fail(st, TESSGPU_ERR_BAD_MESH, t);
+            v = make_int4(0, 0, 0, 0);
+        }
+        tv[t] = make_int4(v.x + p_off, v.y + p_off, v.z + p_off, v.w + p_off);
+    }
+}
+
+// The host-buffer DTFE call with its copies overlapped: block b's particles
+// and tets go up on one copy stream while the compute stream works on the
+// blocks before it (ingest, star volumes, densities, rasteriser and its FP64
+// fix-up, block by block), and each z-slab of the grid goes down on another
+// copy stream as soon as the last block that writes into it is done.  Same
+// kernels and results as the batch path; it needs the rasteriser's launch
+// variant chosen already.
+static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessgpu_block* blocks,
+                                           const tessgpu_dense_params* p, int variant, float* host_grid,
+                                           tessgpu_dense_info* info, float** d_grid_out)
+{
+    CK(cudaSetDevice(ctx->device));
+    for (int i = 0; i < nb; ++i)
+        if (blocks[i].num_particles < 0 || blocks[i].num_tets < 0 || blocks[i].num_orig_particles < 0 ||
+            blocks[i].num_orig_particles > blocks[i].num_particles ||
+            (blocks[i].num_particles && !blocks[i].particles) || (blocks[i].num_tets && !blocks[i].tets))
+            return set_err(ctx, TESSGPU_ERR_INVALID, "block " + std::to_string(i) + " is malformed");
+    if (!ctx->h2d) CK(cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
+    if (!ctx->d2h) CK(cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
+    while ((int)ctx->pipe_ev.size() < 2 * nb + 1)
+    {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->pipe_ev.push_back(e);
+    }
+    cudaStream_t s = ctx->stream;
+    // descriptors and grid
+    float dmin[3], dmax[3], gmin[3], gmax[3], step[3];
+    data_bounds(nb, blocks, p, dmin, dmax);
+    grid_step_params(p, dmin, dmax, gmin, gmax, step);
+    GridDesc g;
+    std::memset(&g, 0, sizeof(g));
+    for (int i = 0; i < 3; ++i)
+    {
+        g.gmin[i] = gmin[i]; g.step[i] = step[i]; g.dmin[i] = dmin[i]; g.dmax[i] = dmax[i];
+        g.n[i] = p->glo_num_idx[i];
+        g.inv_step[i] = 1.0f / step[i];
+    }
+    g.eps = p->eps;
+    g.mass = p->mass;
+    g.div = step[0] * step[1] * step[2];
+    std::vector<BlockDesc> hb(nb);
+    long long N = 0, T = 0, C = 0;
+    for (int i = 0; i < nb; ++i)
+    {
+        BlockDesc& d = hb[i];
+        std::memset(&d, 0, sizeof(d));
+        d.gid = blocks[i].gid;
+        for (int k = 0; k < 3; ++k) { d.bmin[k] = blocks[i].bounds_min[k]; d.bmax[k] = blocks[i].bounds_max[k]; }
+        d.p_off = (int)N; d.np = blocks[i].num_particles; d.norig = blocks[i].num_orig_particles;
+        d.t_off = (int)T; d.nt = blocks[i].num_tets; d.c_off = (int)C;
+        N += d.np; T += d.nt; C += d.norig;
+        block_grid_params(blocks[i], gmin, step, p->eps, dmin, dmax, p->glo_num_idx, d.gmin_idx, d.gmax_idx,
+                          d.gnum_idx);
+        for (int k = 0; k < 3; ++k)
+        {
+            d.gmin_idx[k] = std::max(d.gmin_idx[k], 0);
+            d.gmax_idx[k] = std::min(d.gmax_idx[k], p->glo_num_idx[k] - 1);
+        }
+    }
+    if (N >= (1LL << 31) || T >= (1LL << 31))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "batch larger than 2^31 particles or tets");
+    const long long area = (long long)p->glo_num_idx[0] * p->glo_num_idx[1];
+    const long long G = area * p->glo_num_idx[2];
+    cudaError_t e = cudaSuccess;
+    auto get = [&](int slot, size_t bytes) { cudaError_t ee; void* q = pool_get(ctx, slot, bytes, &ee);
+                                             if (ee != cudaSuccess) e = ee; return q; };
+    BlockDesc* d_blocks = (BlockDesc*)get(SLOT_BLOCKS, sizeof(BlockDesc) * nb);
+    float4* pos = (float4*)get(SLOT_POS, sizeof(float4) * std::max(N, 1LL));
+    int4* tv = (int4*)get(SLOT_TV, sizeof(int4) * std::max(T, 1LL));
+    char* stage = (char*)get(SLOT_STAGE, 32 * (size_t)T + 12 * (size_t)N + 16);
+    unsigned long long* W = (unsigned long long*)get(SLOT_W, sizeof(double) * std::max(N, 1LL));
+    float* rho32 = (float*)get(SLOT_RHO32, sizeof(float) * std::max(N, 1LL));
+    double* rho64 = (double*)get(SLOT_RHO64, sizeof(double) * std::max(N, 1LL));
+    int* fix = (int*)get(SLOT_FIX, sizeof(int) * std::max(T, 1LL));
+    int* fixn = (int*)get(SLOT_FIXN, sizeof(int));
+    float* grid = (float*)get(SLOT_GRID, sizeof(float) * G);
+    CK(e);
+    *d_grid_out = grid;
+    int4* stage_tets = (int4*)stage;                     // 32 B per tet, first: 16-byte aligned
+    float* stage_xyz = (float*)(stage + 32 * (size_t)T);
+
+    // processing order: by first z index of the block's grid box; slab l of
+    // the grid (between consecutive distinct first z indices) goes down after
+    // the last block whose box reaches into it
+    std::vector<int> order(nb);
+    for (int i = 0; i < nb; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return hb[a].gmin_idx[2] < hb[b].gmin_idx[2]; });
+    std::vector<int> zmin(nb), zl;
+    for (int i = 0; i < nb; ++i) zmin[i] = hb[i].gmin_idx[2];
+    const int L = z_layers(zmin, p->glo_num_idx[2], zl);
+    std::vector<int> slab_lo(L, -1), slab_hi(L, -1), slab_ready(L, -1);
+    for (int z = 0; z < p->glo_num_idx[2]; ++z)
+    {
+        if (slab_lo[zl[z]] < 0) slab_lo[zl[z]] = z;
+        slab_hi[zl[z]] = z;
+    }
+    for (int k = 0; k < nb; ++k)
+    {
+        const BlockDesc& d = hb[order[k]];
+        for (int l = 0; l < L; ++l)
+            if (d.gmax_idx[2] >= slab_lo[l] && d.gmin_idx[2] <= slab_hi[l])
+                slab_ready[l] = k;
+    }
+
+    double vbox = 48.0;
+    for (int i = 0; i < 3; ++i)
+        vbox *= std::max((double)dmax[i] - (double)dmin[i], 1e-30);
+    const int bits = 61 - (int)std::ceil(std::log2(vbox));
+    const double scale = std::ldexp(1.0, bits);
+
+    ctx->nmarks = 0;
+    mark(ctx, "start");
+    // the copy streams start after whatever the compute stream was doing with the pool
+    cudaEvent_t ev0 = ctx->pipe_ev[2 * nb];
+    CK(cudaEventRecord(ev0, s));
+    CK(cudaStreamWaitEvent(ctx->h2d, ev0, 0));
+    CK(cudaStreamWaitEvent(ctx->d2h, ev0, 0));
+    for (int k = 0; k < nb; ++k)
+    {
+        const int b = order[k];
+        const BlockDesc& d = hb[b];
+        if (d.nt)
+            CK(cudaMemcpyAsync(stage_tets + 2 * (size_t)d.t_off, blocks[b].tets, 32 * (size_t)d.nt,
+                               cudaMemcpyHostToDevice, ctx->h2d));
+        if (d.np)
+            CK(cudaMemcpyAsync(stage_xyz + 3 * (size_t)d.p_off, blocks[b].particles, 12 * (size_t)d.np,
+                               cudaMemcpyHostToDevice, ctx->h2d));
+        CK(cudaEventRecord(ctx->pipe_ev[k], ctx->h2d));
+    }
+    CK(cudaMemcpyAsync(d_blocks, hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
+    CK(cudaMemsetAsync(grid, 0, sizeof(float) * G, s));
+    const bool mixed = p->mode != TESSGPU_MODE_FP64;
+    for (int k = 0; k < nb; ++k)
+    {
+        const int b = order[k];
+        const BlockDesc& d = hb[b];
+        CK(cudaStreamWaitEvent(s, ctx->pipe_ev[k], 0));
+        if (d.np)
+        {
+            k_pack_block<<<grid_small(d.np), 256, 0, s>>>(stage_xyz + 3 * (size_t)d.p_off, d.np, pos + d.p_off);
+            CK(cudaMemsetAsync(W + d.p_off, 0, sizeof(unsigned long long) * d.np, s));
+            ctx->launches++;
+        }
+        if (d.nt)
+        {
+            k_ingest_verts<<<grid_small(d.nt), 256, 0, s>>>(stage_tets + 2 * (size_t)d.t_off, d.nt, d.np, d.p_off,
+                                                             tv + d.t_off, ctx->d_status);
+            launch_star_volumes(p->mode, d.nt, pos, tv + d.t_off, W, scale, kTau, ctx->d_status, s);
+            ctx->launches += 2;
+        }
+        if (d.np)
+        {
+            launch_densities(W + d.p_off, d.np, p->mass, 1.0 / scale, rho32 + d.p_off, rho64 + d.p_off,
+                             ctx->d_status, s);
+            ctx->launches++;
+        }
+        if (d.nt)
+        {
+            CK(cudaMemsetAsync(fixn, 0, sizeof(int), s));
+            launch_raster(p->mode, variant, d_blocks, nb, d.nt, pos, tv, rho32, rho64, g, kTau, grid, nullptr,
+                          fix, fixn, ctx->d_status, s, nullptr, nullptr, d.t_off);
+            ctx->launches++;
+            if (mixed)
+            {
+                launch_raster_fix(d_blocks, nb, d.nt, pos, tv, rho32, rho64, g, grid, nullptr, fix, fixn,
+                                  ctx->d_status, s);
+                ctx->launches++;
+            }
+        }
+        CK(cudaEventRecord(ctx->pipe_ev[nb + k], s));
+        for (int l = 0; l < L; ++l)
+            if (slab_ready[l] == k && host_grid)
+            {
+                CK(cudaStreamWaitEvent(ctx->d2h, ctx->pipe_ev[nb + k], 0));
+                const size_t off = (size_t)slab_lo[l] * area, n = (size_t)(slab_hi[l] - slab_lo[l] + 1) * area;
+                CK(cudaMemcpyAsync(host_grid + off, grid + off, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                                   ctx->d2h));
+            }
+    }
+    mark(ctx, "compute");
+    if (info)
+    {
+        CK(cudaMemsetAsync(ctx->d_max, 0, sizeof(float), s));
+        launch_grid_max(grid, G, ctx->d_max, s);
+        ctx->launches++;
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(ctx->d2h));
+    CK(cudaStreamSynchronize(s));
+    const Status& st = *ctx->h_status;
+    if (st.code)
+        return set_err(ctx, (tessgpu_status)st.code, "DTFE failed at item " + std::to_string(st.detail));
+    if (info)
+    {
+        float mx = 0.0f;
+        CK(cudaMemcpy(&mx, ctx->d_max, sizeof(float), cudaMemcpyDeviceToHost));
+        std::memset(info, 0, sizeof(*info));
+        for (int i = 0; i < 3; ++i)
+        {
+            info->data_mins[i] = dmin[i]; info->data_maxs[i] = dmax[i];
+            info->grid_phys_mins[i] = gmin[i]; info->grid_phys_maxs[i] = gmax[i]; info->grid_step_size[i] = step[i];
+        }
+        info->max_dense = mx;
+        info->grid_pts_assigned = (long long)st.assigned;
+        info->fp64_tets = (long long)st.fp64_tets;
+        info->exact_tests = (long long)st.exact_tests;
+        info->rows_visited = (long long)st.rows;
+        info->points_tested = (long long)st.candidates;
+        info->raster_variant = variant;
+        for (int v = 0; v < 8; ++v)
+            info->raster_variant_ms[v] = ctx->tune_ms[p->mode][v];
+        info->grid_layers = 0;
+        info->grid_floats = G;
+    }
+    return TESSGPU_OK;
+}
+
 extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tessgpu_block* blocks,
                                         const tessgpu_dense_params* p, float* global_grid, float** block_density,
                                         tessgpu_dense_info* info)
@@ -1055,6 +1312,23 @@ extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tes
         return set_err(ctx, TESSGPU_ERR_INVALID, "bad dense arguments");
     ctx->last_grid = nullptr;
     ctx->last_grid_floats = 0;
+    if (p->alg == TESSGPU_DENSE_DTFE && !p->project && !block_density && ctx->raster_variant[p->mode] >= 0)
+    {
+        const char* oenv = getenv("TESSGPU_RASTER_ORDER");
+        const char* penv = getenv("TESSGPU_PIPELINE");
+        if (!(oenv && atoi(oenv) == 1) && !(penv && *penv && atoi(penv) == 0))
+        {
+            float* d_grid = nullptr;
+            tessgpu_status s = dense_dtfe_pipelined(ctx, nblocks, blocks, p, ctx->raster_variant[p->mode],
+                                                    global_grid, info, &d_grid);
+            if (s == TESSGPU_OK)
+            {
+                ctx->last_grid = d_grid;
+                ctx->last_grid_floats = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
+            }
+            return s;
+        }
+    }
     tessgpu_batch* bt = nullptr;
     tessgpu_status s = batch_build(ctx, nblocks, blocks, false, true, &bt);
     if (s != TESSGPU_OK) { tessgpu_batch_free(bt); return s; }

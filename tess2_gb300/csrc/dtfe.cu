@@ -503,7 +503,7 @@ template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, boo
 __global__ void __launch_bounds__(NW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
-         int* fix_list, int* fix_count, Status* st)
+         int* fix_list, int* fix_count, Status* st, int t0)
 {
     typedef typename Vec4<T>::type T4;
     __shared__ RasterSmem<T, VAL64, FLAT, COMPACT> smem[NW];
@@ -525,7 +525,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
             int t = -1;
             if (it < n)
             {
-                t = LIST ? list[it] : it;
+                t = LIST ? list[it] : t0 + it;
                 int b, vid[4], ilo[3], ihi[3];
                 float a[4][3], lo[3], hi[3];
                 keep = !tet_box(blocks, nb, pos, tv, g, t, b, vid, a, lo, hi, ilo, ihi);
@@ -556,7 +556,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
             else
             {
                 const int it = chunk * 32 + lane;
-                tq = it < n ? (LIST ? list[it] : it) : -1;
+                tq = it < n ? (LIST ? list[it] : t0 + it) : -1;
                 qn = 0;
             }
             int rows = 0;
@@ -993,7 +993,7 @@ template <typename T, bool VAL64, bool LIST>
 static void raster_variant(int variant, long long work, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
                            const int* list, const int* list_count, const float4* pos, const int4* tv,
                            const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
-                           int* owner, int* fix_list, int* fix_count, Status* st)
+                           int* owner, int* fix_list, int* fix_count, Status* st, int t0 = 0)
 {
     // the double-precision tables need more shared memory: 3 warps per block
     constexpr int NW = (sizeof(T) == 4 && !VAL64) ? 4 : 3;
@@ -1001,7 +1001,7 @@ static void raster_variant(int variant, long long work, cudaStream_t s, const Bl
 #define TG_RASTER(MB, C, F)                                                                                        \
     k_raster<T, VAL64, LIST, MB, NW, C, F><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, \
                                                                       rho32, rho64, g, tau, grid, owner, fix_list,  \
-                                                                      fix_count, st)
+                                                                      fix_count, st, t0)
     switch (variant)
     {
     case 1: TG_RASTER(5, false, false); break;
@@ -1020,7 +1020,7 @@ int raster_variants() { return N_RASTER_VARIANTS; }
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                    int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s, const int* order,
-                   const int* order_count)
+                   const int* order_count, int t0)
 {
     if (total <= 0) return;
     const long long work = (long long)((total + 31) / 32) * 32 * 32;
@@ -1036,10 +1036,10 @@ void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int
     }
     if (mode == TESSGPU_MODE_FP64)
         raster_variant<double, true, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                            rho64, g, tau, grid, owner, nullptr, nullptr, st);
+                                            rho64, g, tau, grid, owner, nullptr, nullptr, st, t0);
     else
         raster_variant<float, false, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                            rho64, g, tau, grid, owner, fix_list, fix_count, st);
+                                            rho64, g, tau, grid, owner, fix_list, fix_count, st, t0);
 }
 
 // ---------------------------------------------------------------------------

@@ -40,7 +40,7 @@ void launch_densities(const unsigned long long* W, int total_particles, float ma
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                    int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s,
-                   const int* order = nullptr, const int* order_count = nullptr);
+                   const int* order = nullptr, const int* order_count = nullptr, int t0 = 0);
 int  raster_variants();
 void order_bricks(const GridDesc& g, int* nbx, int* nby, int* nbz);
 void launch_tet_order(const float4* pos, const int4* tv, int total, const GridDesc& g, int* key, int* hist,

@@ -346,3 +346,60 @@ def test_incomplete_cells_without_tets_gpu(gpu_ctx, oracle):
     l6 = np.tile(np.array([0, 0, 0, 1, 1, 1], np.float32), (5, 1))
     m, n = gpu_ctx.incomplete_cells(b, l6, last_neighbor=2)
     assert list(m) == [0b11100] * 3 and n == 9
+
+
+@pytest.mark.parametrize("dims", [(2, 2, 2), (1, 2, 3)])
+def test_dtfe_host_pipeline_matches_batch(gpu_ctx, dims):
+    """The host-buffer DTFE call (copies overlapped with the per-block
+    kernels, grid slabs copied back as they complete) against the
+    device-resident batch path: the same grid bit for bit, and the same counts;
+    TESSGPU_PIPELINE=0 takes the unpipelined host path."""
+    import os
+    import torch
+    from tess2_gb300 import host
+    from tess2_gb300.api import DENSE_DTFE, MODE_FP64, MODE_MIXED
+    pts = host.mixture_particles(30000, 21, n_clumps=16, sigma=0.02)
+    blocks = host.tessellate(host.decompose(pts, dims, 0.08), processes=1)
+    gni = [48, 44, 52]
+    for mode in (MODE_MIXED, MODE_FP64):
+        batch = gpu_ctx.upload(blocks)
+        g = torch.zeros(int(np.prod(gni)), device="cuda:0")
+        ib = batch.dense(DENSE_DTFE, gni, g.data_ptr(), mode=mode)   # chooses the launch variant if not yet chosen
+        torch.cuda.synchronize()
+        ref = g.cpu().numpy().reshape(gni[2], gni[1], gni[0])
+        batch.free()
+        r1 = gpu_ctx.dense(DENSE_DTFE, blocks, gni, mode=mode)
+        assert np.array_equal(r1["grid"], ref)
+        for k in ("grid_pts_assigned", "fp64_tets", "exact_tests"):
+            assert r1["info"][k] == ib[k], k
+        assert r1["info"]["max_dense"] == ib["max_dense"]
+        os.environ["TESSGPU_PIPELINE"] = "0"
+        try:
+            r0 = gpu_ctx.dense(DENSE_DTFE, blocks, gni, mode=mode)
+        finally:
+            del os.environ["TESSGPU_PIPELINE"]
+        assert np.array_equal(r0["grid"], ref)
+
+
+def test_dtfe_brick_order_same_grid(gpu_ctx):
+    """TESSGPU_RASTER_ORDER=1 (tets rasterised brick by brick) writes the
+    same grid bit for bit: every grid point has exactly one owner tet."""
+    import os
+    import torch
+    from tess2_gb300.api import DENSE_DTFE
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    gni = [56, 60, 52]
+    out = []
+    for env in (None, "1"):
+        if env:
+            os.environ["TESSGPU_RASTER_ORDER"] = env
+        try:
+            batch = gpu_ctx.upload(blocks)
+            g = torch.zeros(int(np.prod(gni)), device="cuda:0")
+            info = batch.dense(DENSE_DTFE, gni, g.data_ptr())
+            torch.cuda.synchronize()
+            out.append((g.cpu().numpy(), info["grid_pts_assigned"]))
+            batch.free()
+        finally:
+            os.environ.pop("TESSGPU_RASTER_ORDER", None)
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
