@@ -660,10 +660,17 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         for (int i = 0; i < nb; ++i)
             zmin[i] = bt->hb[i].gmin_idx[2];
         L = z_layers(zmin, p->glo_num_idx[2], zl);
+        // zl (layer of each z), then the layers' z bounds zs[0..L]
+        std::vector<int> tbl(zl);
+        for (int l = 0, z = 0; l <= L; ++l)
+        {
+            while (z < (int)zl.size() && zl[z] < l) ++z;
+            tbl.push_back(z);
+        }
         cudaError_t e;
-        d_zl = (int*)pool_get(ctx, SLOT_ZLAYER, sizeof(int) * zl.size(), &e);
+        d_zl = (int*)pool_get(ctx, SLOT_ZLAYER, sizeof(int) * tbl.size(), &e);
         CK(e);
-        CK(cudaMemcpyAsync(d_zl, zl.data(), sizeof(int) * zl.size(), cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(d_zl, tbl.data(), sizeof(int) * tbl.size(), cudaMemcpyHostToDevice, s));
         if (p->alg == TESSGPU_DENSE_DTFE)
         {
             target = (float*)pool_get(ctx, SLOT_GRID3, sizeof(float) * G, &e);
@@ -841,7 +848,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         if (p->project)
         {
             // surface density: the column integral of rho over each layer's z range
-            launch_project_layers(target, p->glo_num_idx[0], p->glo_num_idx[1], p->glo_num_idx[2], d_zl, step[2],
+            launch_project_layers(target, p->glo_num_idx[0], p->glo_num_idx[1], d_zl + p->glo_num_idx[2], L, step[2],
                                   d_grid, s);
             ctx->launches++;
             mark(ctx, "project_layers");
@@ -1188,6 +1195,29 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             if (d.gmax_idx[2] >= slab_lo[l] && d.gmin_idx[2] <= slab_hi[l])
                 slab_ready[l] = k;
     }
+    // when the blocks' grid boxes tile the grid (the usual case), each box
+    // goes down as soon as its block is done, so only the last box trails
+    bool tiles = true;
+    long long covered = 0;
+    for (int i = 0; i < nb && tiles; ++i)
+    {
+        long long v = 1;
+        for (int k = 0; k < 3; ++k)
+        {
+            const int n = hb[i].gmax_idx[k] - hb[i].gmin_idx[k] + 1;
+            if (n <= 0) tiles = false;
+            v *= n;
+        }
+        covered += v;
+        for (int j = 0; j < i && tiles; ++j)
+        {
+            bool meet = true;
+            for (int k = 0; k < 3; ++k)
+                if (hb[i].gmax_idx[k] < hb[j].gmin_idx[k] || hb[j].gmax_idx[k] < hb[i].gmin_idx[k]) meet = false;
+            if (meet) tiles = false;
+        }
+    }
+    tiles = tiles && covered == G;
 
     double vbox = 48.0;
     for (int i = 0; i < 3; ++i)
@@ -1256,7 +1286,22 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             }
         }
         CK(cudaEventRecord(ctx->pipe_ev[nb + k], s));
-        for (int l = 0; l < L; ++l)
+        if (tiles && host_grid)
+        {
+            CK(cudaStreamWaitEvent(ctx->d2h, ctx->pipe_ev[nb + k], 0));
+            cudaMemcpy3DParms prm;
+            std::memset(&prm, 0, sizeof(prm));
+            const int nx = p->glo_num_idx[0], ny = p->glo_num_idx[1];
+            prm.srcPtr = make_cudaPitchedPtr(grid, sizeof(float) * nx, nx, ny);
+            prm.dstPtr = make_cudaPitchedPtr(host_grid, sizeof(float) * nx, nx, ny);
+            prm.srcPos = make_cudaPos(sizeof(float) * d.gmin_idx[0], d.gmin_idx[1], d.gmin_idx[2]);
+            prm.dstPos = prm.srcPos;
+            prm.extent = make_cudaExtent(sizeof(float) * (d.gmax_idx[0] - d.gmin_idx[0] + 1),
+                                         d.gmax_idx[1] - d.gmin_idx[1] + 1, d.gmax_idx[2] - d.gmin_idx[2] + 1);
+            prm.kind = cudaMemcpyDeviceToHost;
+            CK(cudaMemcpy3DAsync(&prm, ctx->d2h));
+        }
+        for (int l = 0; l < L && !tiles; ++l)
             if (slab_ready[l] == k && host_grid)
             {
                 CK(cudaStreamWaitEvent(ctx->d2h, ctx->pipe_ev[nb + k], 0));

@@ -836,37 +836,39 @@ __global__ void k_reorder_neighbors(int* tets, int total, Status* st)
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
     {
         int* r = tets + 8 * (size_t)t;
-        int v[4], nb[4], out[4];
+        const int4 rv = reinterpret_cast<const int4*>(r)[0], rn = reinterpret_cast<const int4*>(r)[1];
+        int v[4] = { rv.x, rv.y, rv.z, rv.w }, nb[4] = { rn.x, rn.y, rn.z, rn.w }, out[4];
         for (int i = 0; i < 4; ++i)
         {
-            v[i] = r[i];
-            nb[i] = r[4 + i];
             if (nb[i] >= total || nb[i] < -1)
             {
                 fail(st, TESSGPU_ERR_BAD_MESH, t);
                 nb[i] = -1;
             }
         }
+        // the neighbours' vertices (never written here), all four loads in flight at once
+        int4 cv[4];
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+            cv[n] = nb[n] >= 0 ? __ldg(reinterpret_cast<const int4*>(tets + 8 * (size_t)nb[n]))
+                               : make_int4(-1, -1, -1, -1);
+#pragma unroll
         for (int i = 0; i < 4; ++i)
         {
             out[i] = -1;
+#pragma unroll
             for (int n = 0; n < 4; ++n)
             {
-                const int c = nb[n];
-                if (c < 0)   // -1 (hull) or -2 (taken)
+                if (out[i] >= 0 || nb[n] < 0)   // found already; -1 (hull) or -2 (taken)
                     continue;
-                const int4 cv = make_int4(tets[8 * (size_t)c], tets[8 * (size_t)c + 1], tets[8 * (size_t)c + 2],
-                                          tets[8 * (size_t)c + 3]);
-                if (cv.x != v[i] && cv.y != v[i] && cv.z != v[i] && cv.w != v[i])
+                if (cv[n].x != v[i] && cv[n].y != v[i] && cv[n].z != v[i] && cv[n].w != v[i])
                 {
-                    out[i] = c;
+                    out[i] = nb[n];
                     nb[n] = -2;
-                    break;
                 }
             }
         }
-        for (int i = 0; i < 4; ++i)
-            r[4 + i] = out[i];
+        reinterpret_cast<int4*>(r)[1] = make_int4(out[0], out[1], out[2], out[3]);
     }
 }
 
@@ -1031,31 +1033,46 @@ __global__ void k_count_sends(const int* c_off, int nb, int total_cells, const u
 }
 
 // z-projection of a 3-D grid into layers: layer l at (x, y) accumulates
-// value * dz over the z indices of layer l in ascending z (one thread per
-// column; consecutive threads read consecutive x, so every z step is coalesced)
-__global__ void k_project_layers(const float* grid, int nx, int ny, int nz, const int* zlayer, float dz,
-                                 float* layers)
+// value * dz over its z indices [zs[l], zs[l+1]) in ascending z.  One thread
+// per column (scalar) or per four columns (x extent a multiple of 4: 16-byte
+// loads); consecutive threads read consecutive x, so every z step is
+// coalesced, and the inner loop has no store, so its loads overlap.
+__global__ void k_project_layers(const float* __restrict__ grid, long long area, const int* __restrict__ zs,
+                                 int num_layers, float dz, float* __restrict__ layers)
 {
-    const long long area = (long long)nx * ny;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < area;
          c += (long long)gridDim.x * blockDim.x)
-    {
-        int l = zlayer[0];
-        float acc = 0.0f;
-#pragma unroll 8
-        for (int z = 0; z < nz; ++z)
+        for (int l = 0; l < num_layers; ++l)
         {
-            const int lz = zlayer[z];
-            if (lz != l)
-            {
-                layers[l * area + c] = acc;
-                acc = 0.0f;
-                l = lz;
-            }
-            acc += __ldcs(&grid[z * area + c]) * dz;
+            float acc = 0.0f;
+            const int z1 = zs[l + 1];
+#pragma unroll 16
+            for (int z = zs[l]; z < z1; ++z)
+                acc += __ldcs(&grid[z * area + c]) * dz;
+            layers[l * area + c] = acc;
         }
-        layers[l * area + c] = acc;
-    }
+}
+
+__global__ void k_project_layers4(const float4* __restrict__ grid, long long area4, const int* __restrict__ zs,
+                                  int num_layers, float dz, float4* __restrict__ layers)
+{
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < area4;
+         c += (long long)gridDim.x * blockDim.x)
+        for (int l = 0; l < num_layers; ++l)
+        {
+            float4 acc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const int z1 = zs[l + 1];
+#pragma unroll 8
+            for (int z = zs[l]; z < z1; ++z)
+            {
+                const float4 v = __ldcs(&grid[z * area4 + c]);
+                acc.x += v.x * dz;
+                acc.y += v.y * dz;
+                acc.z += v.z * dz;
+                acc.w += v.w * dz;
+            }
+            layers[l * area4 + c] = acc;
+        }
 }
 
 // ProjectGrid (src/dense.cpp:881-1023): the z=0 block of each column adds the
@@ -1160,12 +1177,16 @@ void launch_cic(const BlockDesc* d_blocks, const int* d_c_off, int nb, int total
     k_cic<<<grid1d(total, 256), 256, 0, s>>>(d_blocks, d_c_off, nb, total, pos, g, grid, st);
 }
 
-void launch_project_layers(const float* grid, int nx, int ny, int nz, const int* zlayer, float dz, float* layers,
-                           cudaStream_t s)
+void launch_project_layers(const float* grid, int nx, int ny, const int* zs, int num_layers, float dz,
+                           float* layers, cudaStream_t s)
 {
     const long long area = (long long)nx * ny;
-    if (area <= 0 || nz <= 0) return;
-    k_project_layers<<<grid1d(area, 256), 256, 0, s>>>(grid, nx, ny, nz, zlayer, dz, layers);
+    if (area <= 0 || num_layers <= 0) return;
+    if (nx % 4 == 0 && ((uintptr_t)grid & 15) == 0 && ((uintptr_t)layers & 15) == 0)
+        k_project_layers4<<<grid1d(area / 4, 256, 16), 256, 0, s>>>((const float4*)grid, area / 4, zs, num_layers,
+                                                                    dz, (float4*)layers);
+    else
+        k_project_layers<<<grid1d(area, 256, 16), 256, 0, s>>>(grid, area, zs, num_layers, dz, layers);
 }
 
 void launch_sum_layers(const float* layers, int num_layers, long long area, float* out, cudaStream_t s)
@@ -1191,7 +1212,7 @@ void launch_incomplete_cells(const BlockDesc* blocks, const int* c_off, int nb, 
 void launch_reorder_neighbors(int* d_tets, int total, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
-    k_reorder_neighbors<<<grid1d(total, 256), 256, 0, s>>>(d_tets, total, st);
+    k_reorder_neighbors<<<grid1d(total, 256, 32), 256, 0, s>>>(d_tets, total, st);
 }
 
 void launch_grid_max(const float* grid, long long n, float* d_max, cudaStream_t s)

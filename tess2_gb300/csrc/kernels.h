@@ -28,8 +28,8 @@ void launch_incomplete_cells(const BlockDesc* blocks, const int* c_off, int nb, 
                              const float4* pos, const int4* tv, const int4* tn, const float* links6,
                              const int* link_off, const int* first_link, const unsigned long long* fill,
                              unsigned long long* masks, unsigned long long* counts, cudaStream_t s);
-void launch_project_layers(const float* grid, int nx, int ny, int nz, const int* zlayer, float dz, float* layers,
-                           cudaStream_t s);
+void launch_project_layers(const float* grid, int nx, int ny, const int* zs, int num_layers, float dz,
+                           float* layers, cudaStream_t s);
 void launch_sum_layers(const float* layers, int num_layers, long long area, float* out, cudaStream_t s);
 
 // dtfe.cu  (built with -fmad=false; FMAs only where written)

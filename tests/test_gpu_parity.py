@@ -348,18 +348,23 @@ def test_incomplete_cells_without_tets_gpu(gpu_ctx, oracle):
     assert list(m) == [0b11100] * 3 and n == 9
 
 
-@pytest.mark.parametrize("dims", [(2, 2, 2), (1, 2, 3)])
+@pytest.mark.parametrize("dims", [(2, 2, 2), (1, 2, 3), "gap"])
 def test_dtfe_host_pipeline_matches_batch(gpu_ctx, dims):
     """The host-buffer DTFE call (copies overlapped with the per-block
-    kernels, grid slabs copied back as they complete) against the
-    device-resident batch path: the same grid bit for bit, and the same counts;
-    TESSGPU_PIPELINE=0 takes the unpipelined host path."""
+    kernels, each block's grid box -- or, when the boxes leave a gap, each
+    z-slab -- copied back as it completes) against the device-resident batch
+    path: the same grid bit for bit, and the same counts; TESSGPU_PIPELINE=0
+    takes the unpipelined host path."""
     import os
     import torch
     from tess2_gb300 import host
     from tess2_gb300.api import DENSE_DTFE, MODE_FP64, MODE_MIXED
     pts = host.mixture_particles(30000, 21, n_clumps=16, sigma=0.02)
-    blocks = host.tessellate(host.decompose(pts, dims, 0.08), processes=1)
+    if dims == "gap":
+        blocks = host.tessellate(host.decompose(pts, (1, 1, 2), 0.08), processes=1)
+        blocks[1]["bounds_min"] = np.array([0.0, 0.0, 0.6], np.float32)   # z in (0.5, 0.6): no block's box
+    else:
+        blocks = host.tessellate(host.decompose(pts, dims, 0.08), processes=1)
     gni = [48, 44, 52]
     for mode in (MODE_MIXED, MODE_FP64):
         batch = gpu_ctx.upload(blocks)
