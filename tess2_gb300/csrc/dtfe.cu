@@ -444,8 +444,7 @@ __device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, FLAT, CO
     const float pxf = xi * g.step[0] + g.gmin[0];
     const T px = pxf;
     const int s = I1.y;
-    const T sf = (T)s;
-    T N[4];
+    T N[4];   // s N_k: the tables hold s c_k (see the setup)
     N[0] = Real<T>::fma_(cx[0], px - (T)A1.x, RN[0]);
     const T qx = px - (T)A0.x;
     N[1] = Real<T>::fma_(cx[1], qx, RN[1]);
@@ -456,7 +455,7 @@ __device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, FLAT, CO
 #pragma unroll
     for (int k = 0; k < 4; ++k)
     {
-        const T sn = sf * N[k];
+        const T sn = N[k];
         const bool ik = sn > Bk[k];
         in = in && ik;
         out = out || (sn < -Bk[k]);
@@ -612,9 +611,13 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         for (int k = 0; k < 4; ++k)
                         {
                             T4 ck;
-                            ck.x = c[k][0]; ck.y = c[k][1]; ck.z = c[k][2]; ck.w = Bk[k];
+                            // the orientation folded in (exact: s = +-1): a point is inside
+                            // when every s N_k > B_k, and s N_k times s rho_k / 6V is the
+                            // same product, so the points need no sign multiply
+                            const T sg = (T)s;
+                            ck.x = sg * c[k][0]; ck.y = sg * c[k][1]; ck.z = sg * c[k][2]; ck.w = Bk[k];
                             S.C[k][lane] = ck;
-                            const T wk = F32 ? (T)(__ldg(&rho32[vid[k]]) * r6) : (T)__ldg(&rho64[vid[k]]) / v6;
+                            const T wk = sg * (F32 ? (T)(__ldg(&rho32[vid[k]]) * r6) : (T)__ldg(&rho64[vid[k]]) / v6);
                             if (k == 0) w4.x = wk;
                             else if (k == 1) w4.y = wk;
                             else if (k == 2) w4.z = wk;
