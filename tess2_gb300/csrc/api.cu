@@ -45,7 +45,7 @@ struct tessgpu_ctx
     const float*             last_grid = nullptr;
     long long                last_grid_floats = 0;
     // the pipelined host-buffer DTFE call: copy streams and events
-    cudaStream_t             h2d = nullptr, d2h = nullptr;
+    cudaStream_t             h2d = nullptr, d2h = nullptr, cs2 = nullptr;
     std::vector<cudaEvent_t> pipe_ev;
 };
 
@@ -171,6 +171,7 @@ extern "C" void tessgpu_destroy(tessgpu_ctx* ctx)
         cudaEventDestroy(e);
     if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
     if (ctx->d2h) cudaStreamDestroy(ctx->d2h);
+    if (ctx->cs2) cudaStreamDestroy(ctx->cs2);
     delete ctx;
 }
 
@@ -1109,7 +1110,8 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             return set_err(ctx, TESSGPU_ERR_INVALID, "block " + std::to_string(i) + " is malformed");
     if (!ctx->h2d) CK(cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
     if (!ctx->d2h) CK(cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
-    while ((int)ctx->pipe_ev.size() < 2 * nb + 1)
+    if (!ctx->cs2) CK(cudaStreamCreateWithFlags(&ctx->cs2, cudaStreamNonBlocking));
+    while ((int)ctx->pipe_ev.size() < 2 * nb + 2)
     {
         cudaEvent_t e;
         CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1165,7 +1167,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     float* rho32 = (float*)get(SLOT_RHO32, sizeof(float) * std::max(N, 1LL));
     double* rho64 = (double*)get(SLOT_RHO64, sizeof(double) * std::max(N, 1LL));
     int* fix = (int*)get(SLOT_FIX, sizeof(int) * std::max(T, 1LL));
-    int* fixn = (int*)get(SLOT_FIXN, sizeof(int));
+    int* fixn = (int*)get(SLOT_FIXN, sizeof(int) * nb);   // one fix-list length per block
     float* grid = (float*)get(SLOT_GRID, sizeof(float) * G);
     CK(e);
     *d_grid_out = grid;
@@ -1247,11 +1249,20 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     CK(cudaMemcpyAsync(d_blocks, hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
     CK(cudaMemsetAsync(grid, 0, sizeof(float) * G, s));
+    CK(cudaMemsetAsync(fixn, 0, sizeof(int) * nb, s));
+    // blocks alternate between two compute streams, so one block's launches
+    // fill the SMs the previous block's last waves leave idle; they share
+    // nothing but read-only descriptors, the status word (atomics) and the grid,
+    // where each writes only its own box
+    cudaEvent_t ev_setup = ctx->pipe_ev[2 * nb + 1];
+    CK(cudaEventRecord(ev_setup, s));
+    CK(cudaStreamWaitEvent(ctx->cs2, ev_setup, 0));
     const bool mixed = p->mode != TESSGPU_MODE_FP64;
     for (int k = 0; k < nb; ++k)
     {
         const int b = order[k];
         const BlockDesc& d = hb[b];
+        cudaStream_t s = (k & 1) ? ctx->cs2 : ctx->stream;
         CK(cudaStreamWaitEvent(s, ctx->pipe_ev[k], 0));
         if (d.np)
         {
@@ -1274,14 +1285,14 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         }
         if (d.nt)
         {
-            CK(cudaMemsetAsync(fixn, 0, sizeof(int), s));
+            // the block's FP64 fix-up list: its own segment of the list buffer
             launch_raster(p->mode, variant, d_blocks, nb, d.nt, pos, tv, rho32, rho64, g, kTau, grid, nullptr,
-                          fix, fixn, ctx->d_status, s, nullptr, nullptr, d.t_off);
+                          fix + d.t_off, fixn + k, ctx->d_status, s, nullptr, nullptr, d.t_off);
             ctx->launches++;
             if (mixed)
             {
-                launch_raster_fix(d_blocks, nb, d.nt, pos, tv, rho32, rho64, g, grid, nullptr, fix, fixn,
-                                  ctx->d_status, s);
+                launch_raster_fix(d_blocks, nb, d.nt, pos, tv, rho32, rho64, g, grid, nullptr, fix + d.t_off,
+                                  fixn + k, ctx->d_status, s);
                 ctx->launches++;
             }
         }
@@ -1304,12 +1315,20 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         for (int l = 0; l < L && !tiles; ++l)
             if (slab_ready[l] == k && host_grid)
             {
-                CK(cudaStreamWaitEvent(ctx->d2h, ctx->pipe_ev[nb + k], 0));
+                for (int kk = std::max(0, k - 1); kk <= k; ++kk)   // this block and the one on the other stream
+                    CK(cudaStreamWaitEvent(ctx->d2h, ctx->pipe_ev[nb + kk], 0));
                 const size_t off = (size_t)slab_lo[l] * area, n = (size_t)(slab_hi[l] - slab_lo[l] + 1) * area;
                 CK(cudaMemcpyAsync(host_grid + off, grid + off, sizeof(float) * n, cudaMemcpyDeviceToHost,
                                    ctx->d2h));
             }
     }
+    // the second compute stream's last block, before the statistics
+    for (int k = nb - 1; k >= 0; --k)
+        if (k & 1)
+        {
+            CK(cudaStreamWaitEvent(s, ctx->pipe_ev[nb + k], 0));
+            break;
+        }
     mark(ctx, "compute");
     if (info)
     {
