@@ -39,6 +39,11 @@ struct tessgpu_ctx
     std::vector<cudaEvent_t> events;
     std::vector<const char*> marks;
     int                      nmarks = 0;
+    // stages that run on several streams: events recorded on the stage's own
+    // stream, and (name, first event, last event) spans summed per name
+    std::vector<cudaEvent_t> sevents;
+    int                      nsev = 0;
+    std::vector<std::pair<const char*, std::pair<int, int>>> spans;
     // WriteGrid: pinned staging buffers, and the global grid of the last tessgpu_dense call
     float*                   h_stage[2] = { nullptr, nullptr };
     cudaEvent_t              stage_ev[2] = { nullptr, nullptr };
@@ -48,6 +53,25 @@ struct tessgpu_ctx
     cudaStream_t             h2d = nullptr, d2h = nullptr, cs2 = nullptr;
     std::vector<cudaEvent_t> pipe_ev;
 };
+
+// an event on stream s for a span (timing on), its index; -1 otherwise
+static int smark(tessgpu_ctx* c, cudaStream_t s)
+{
+    if (!c->timing) return -1;
+    if (c->nsev >= (int)c->sevents.size())
+    {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        c->sevents.push_back(e);
+    }
+    cudaEventRecord(c->sevents[c->nsev], s);
+    return c->nsev++;
+}
+
+static void span(tessgpu_ctx* c, const char* name, int e0, int e1)
+{
+    if (e0 >= 0 && e1 >= 0) c->spans.push_back({ name, { e0, e1 } });
+}
 
 static void mark(tessgpu_ctx* c, const char* name)
 {
@@ -82,6 +106,30 @@ extern "C" int tessgpu_stage_times(tessgpu_ctx* ctx, const char** names, float* 
         cudaEventElapsedTime(&t, ctx->events[i - 1], ctx->events[i]);
         if (names) names[n] = ctx->marks[i];
         if (ms) ms[n] = t;
+    }
+    // spans: per name, the sum of its launches' durations on their own streams
+    std::vector<const char*> seen;
+    for (size_t i = 0; i < ctx->spans.size(); ++i)
+    {
+        const char* nm = ctx->spans[i].first;
+        if (std::find(seen.begin(), seen.end(), nm) != seen.end()) continue;
+        seen.push_back(nm);
+        float tot = 0.0f;
+        for (size_t j = i; j < ctx->spans.size(); ++j)
+            if (ctx->spans[j].first == nm)
+            {
+                float t = 0.0f;
+                cudaEventSynchronize(ctx->sevents[ctx->spans[j].second.second]);
+                cudaEventElapsedTime(&t, ctx->sevents[ctx->spans[j].second.first],
+                                     ctx->sevents[ctx->spans[j].second.second]);
+                tot += t;
+            }
+        if (n < cap)
+        {
+            if (names) names[n] = nm;
+            if (ms) ms[n] = tot;
+            ++n;
+        }
     }
     return n;
 }
@@ -158,6 +206,8 @@ extern "C" void tessgpu_destroy(tessgpu_ctx* ctx)
     for (auto& p : ctx->pool)
         if (p.first) cudaFree(p.first);
     for (cudaEvent_t e : ctx->events)
+        cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->sevents)
         cudaEventDestroy(e);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_max) cudaFree(ctx->d_max);
@@ -683,6 +733,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     const long long Gout = p->project ? area * L : G;
     const long long Gtarget = target == d_grid ? Gout : G;
     ctx->nmarks = 0;
+    ctx->nsev = 0;
+    ctx->spans.clear();
     mark(ctx, "start");
     CK(cudaMemsetAsync(target, 0, sizeof(float) * Gtarget, s));
     mark(ctx, "grid_zero");
@@ -725,7 +777,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
             BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
             BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
-            BALLOC(SLOT_FIXN, sizeof(int), bt->fix_count);
+            BALLOC(SLOT_FIXN, sizeof(int) * (nb + 1), bt->fix_count);
         }
         int* owner = nullptr;
         if (bt->keep_debug)
@@ -737,7 +789,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             owner = bt->d_owner;
         }
         CK(cudaMemsetAsync(bt->W, 0, sizeof(unsigned long long) * bt->N, s));
-        CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
+        CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int) * (nb + 1), s));
         // fixed-point scale of the star-volume sums: any star volume is below
         // the volume of the particles' bounding box; allow 8x the data box
         double vbox = 48.0;   // 6V sums of up to 8x the data box
@@ -745,6 +797,69 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             vbox *= std::max((double)dmax[i] - (double)dmin[i], 1e-30);
         const int bits = 61 - (int)std::ceil(std::log2(vbox));
         const double scale = std::ldexp(1.0, bits);
+        // once the launch variant is known, blocks run their stages on two
+        // streams in turn (as the host pipeline does), so one block's star
+        // volumes overlap another's rasteriser
+        {
+            const char* ov = getenv("TESSGPU_BATCH_OVERLAP");
+            const char* oenv = getenv("TESSGPU_RASTER_ORDER");
+            int known = bt->raster_variant[p->mode] >= 0 ? bt->raster_variant[p->mode] : ctx->raster_variant[p->mode];
+            if (!(ov && *ov && atoi(ov) == 0) && known >= 0 && !(oenv && atoi(oenv) == 1) && !p->project)
+            {
+                bt->raster_variant[p->mode] = known;
+                if (!ctx->cs2) CK(cudaStreamCreateWithFlags(&ctx->cs2, cudaStreamNonBlocking));
+                while ((int)ctx->pipe_ev.size() < 2 * nb + 2)
+                {
+                    cudaEvent_t e;
+                    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                    ctx->pipe_ev.push_back(e);
+                }
+                CK(cudaEventRecord(ctx->pipe_ev[2 * nb + 1], s));
+                CK(cudaStreamWaitEvent(ctx->cs2, ctx->pipe_ev[2 * nb + 1], 0));
+                for (int k = 0; k < nb; ++k)
+                {
+                    const BlockDesc& d = bt->hb[k];
+                    cudaStream_t sk = (k & 1) ? ctx->cs2 : s;
+                    const int t0 = smark(ctx, sk);
+                    if (d.nt)
+                        launch_star_volumes(p->mode, d.nt, bt->pos, bt->tv + d.t_off, (unsigned long long*)bt->W, scale,
+                                            kTau, ctx->d_status, sk);
+                    const int t1 = smark(ctx, sk);
+                    if (d.np)
+                        launch_densities((const unsigned long long*)bt->W + d.p_off, d.np, p->mass, 1.0 / scale,
+                                         bt->rho32 + d.p_off, bt->rho64 + d.p_off, ctx->d_status, sk);
+                    const int t2 = smark(ctx, sk);
+                    int t3 = -1, t4 = -1;
+                    if (d.nt)
+                    {
+                        launch_raster(p->mode, known, bt->d_blocks, nb, d.nt, bt->pos, bt->tv, bt->rho32, bt->rho64,
+                                      g, kTau, target, owner, bt->fix_list + d.t_off, bt->fix_count + k,
+                                      ctx->d_status, sk, nullptr, nullptr, d.t_off);
+                        t3 = smark(ctx, sk);
+                        if (p->mode != TESSGPU_MODE_FP64)
+                        {
+                            launch_raster_fix(bt->d_blocks, nb, d.nt, bt->pos, bt->tv, bt->rho32, bt->rho64, g, target,
+                                              owner, bt->fix_list + d.t_off, bt->fix_count + k, ctx->d_status, sk);
+                            t4 = smark(ctx, sk);
+                        }
+                    }
+                    span(ctx, "star_volumes", t0, t1);
+                    span(ctx, "densities", t1, t2);
+                    span(ctx, "raster", t2, t3);
+                    span(ctx, "raster_fp64_fixup", t3, t4);
+                    ctx->launches += (d.nt ? (p->mode == TESSGPU_MODE_FP64 ? 2 : 3) : 0) + (d.np ? 1 : 0);
+                    CK(cudaEventRecord(ctx->pipe_ev[nb + k], sk));
+                }
+                for (int k = nb - 1; k >= 0; --k)
+                    if (k & 1)
+                    {
+                        CK(cudaStreamWaitEvent(s, ctx->pipe_ev[nb + k], 0));
+                        break;
+                    }
+                mark(ctx, "dtfe_blocks");
+                goto dtfe_done;
+            }
+        }
         launch_star_volumes(p->mode, (int)bt->T, bt->pos, bt->tv, (unsigned long long*)bt->W, scale, kTau,
                             ctx->d_status, s);
         mark(ctx, "star_volumes");
@@ -855,6 +970,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             mark(ctx, "project_layers");
         }
     }
+dtfe_done:
     double max_dense = 0.0;
     if (info || p->alg != TESSGPU_DENSE_DTFE)
     {
@@ -1228,6 +1344,8 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     const double scale = std::ldexp(1.0, bits);
 
     ctx->nmarks = 0;
+    ctx->nsev = 0;
+    ctx->spans.clear();
     mark(ctx, "start");
     // the copy streams start after whatever the compute stream was doing with the pool
     cudaEvent_t ev0 = ctx->pipe_ev[2 * nb];
@@ -1599,6 +1717,8 @@ extern "C" tessgpu_status tessgpu_batch_incomplete_cells(tessgpu_ctx* ctx, tessg
     CK(cudaMemsetAsync(d_aux + nb, 0, sizeof(unsigned long long) * nb, s));
     if (bt->C) CK(cudaMemsetAsync(d_send_mask, 0, sizeof(unsigned long long) * bt->C, s));
     ctx->nmarks = 0;
+    ctx->nsev = 0;
+    ctx->spans.clear();
     mark(ctx, "start");
     launch_incomplete_cells(bt->d_blocks, bt->d_c_off, nb, (int)bt->T, (int)bt->C, bt->pos, bt->tv, bt->tn, d_l6,
                             d_meta, d_meta + nb + 1, d_aux, d_send_mask, d_aux + nb, s);
@@ -1652,6 +1772,8 @@ extern "C" tessgpu_status tessgpu_reorder_neighbors_device(tessgpu_ctx* ctx, int
     CK(cudaSetDevice(ctx->device));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), ctx->stream));
     ctx->nmarks = 0;
+    ctx->nsev = 0;
+    ctx->spans.clear();
     mark(ctx, "start");
     launch_reorder_neighbors(d_tets, num_tets, ctx->d_status, ctx->stream);
     mark(ctx, "reorder_neighbors");

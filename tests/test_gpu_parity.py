@@ -408,3 +408,32 @@ def test_dtfe_brick_order_same_grid(gpu_ctx):
         finally:
             os.environ.pop("TESSGPU_RASTER_ORDER", None)
     assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+
+
+def test_dtfe_batch_overlap_same_grid(gpu_ctx):
+    """The batch path with blocks on two streams (the default once the launch
+    variant is known) and TESSGPU_BATCH_OVERLAP=0 (stages one after the other
+    over all blocks): the same grid bit for bit and the same counts."""
+    import os
+    import torch
+    from tess2_gb300.api import DENSE_DTFE, MODE_FP64, MODE_MIXED
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    gni = [50, 46, 54]
+    for mode in (MODE_MIXED, MODE_FP64):
+        out = []
+        for env in ("0", None):
+            if env:
+                os.environ["TESSGPU_BATCH_OVERLAP"] = env
+            try:
+                batch = gpu_ctx.upload(blocks)
+                g = torch.zeros(int(np.prod(gni)), device="cuda:0")
+                batch.dense(DENSE_DTFE, gni, g.data_ptr(), mode=mode)     # chooses the variant if needed
+                info = batch.dense(DENSE_DTFE, gni, g.data_ptr(), mode=mode)
+                torch.cuda.synchronize()
+                out.append((g.cpu().numpy(), info))
+                batch.free()
+            finally:
+                os.environ.pop("TESSGPU_BATCH_OVERLAP", None)
+        assert np.array_equal(out[0][0], out[1][0])
+        for k in ("grid_pts_assigned", "fp64_tets", "exact_tests", "max_dense"):
+            assert out[0][1][k] == out[1][1][k], k
