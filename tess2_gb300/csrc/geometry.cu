@@ -323,6 +323,65 @@ __device__ void distribute_cic(const float* pt, float scalar, int* idx, float* w
         w[i] = (weights[i] / tot_weight) * scalar;
 }
 
+// PtInCell at up to four points at once: lane group q = lane / 8 takes point q
+// (coordinate `axis` = cmin_pos[axis] + (start + (k0 + q) d) step[axis], the
+// other two fixed), each lane every 8th face.  The same per-face arithmetic as
+// warp_pt_in_cell, so each answer is the one a single probe gives.  Bit q of
+// the result is the answer at point q (q < npts).
+__device__ __forceinline__ unsigned warp_pt_in_cell4(int axis, float fixed_a, float fixed_b, int start, int d, int k0,
+                                                     int npts, const float* cmin_pos, const GridDesc& g,
+                                                     const WarpSmem& S, int nf, float eps, int lane)
+{
+    const int q = lane >> 3, sub = lane & 7;
+    bool pos = false, neg = false;
+    if (q < npts)
+    {
+        const int idx = start + (k0 + q) * d;
+        const float c = cmin_pos[axis] + idx * g.step[axis];
+        const float px = axis == 0 ? c : fixed_a;
+        const float py = axis == 0 ? fixed_a : c;
+        const float pz = fixed_b;
+        for (int k = sub; k < nf; k += 8)
+        {
+            const float* n = &S.fa[3 * k];
+            const float* v = &S.fb[3 * k];
+            float dist = n[0] * (px - v[0]) + n[1] * (py - v[1]) + n[2] * (pz - v[2]);
+            if (fabsf(dist) > eps)
+            {
+                if (dist >= 0.0f) pos = true; else neg = true;
+            }
+        }
+    }
+    const unsigned bp = __ballot_sync(FULL, pos), bn = __ballot_sync(FULL, neg);
+    unsigned res = 0;
+#pragma unroll
+    for (int h = 0; h < 4; ++h)
+    {
+        const unsigned m = 0xffu << (8 * h);
+        if (h < npts && !((bp & m) && (bn & m)))
+            res |= 1u << h;
+    }
+    return res;
+}
+
+// The scanline's walks: the first k in [k0, kmax) whose PtInCell answer at
+// position start + k d differs from c (kmax if none), probing four positions
+// per round.  The walk itself is the reference's; only its probes run ahead.
+__device__ __forceinline__ int warp_walk(int axis, float fixed_a, float fixed_b, int start, int d, bool c, int k0,
+                                         int kmax, const float* cmin_pos, const GridDesc& g, const WarpSmem& S,
+                                         int nf, float eps, int lane)
+{
+    for (int k = k0; k < kmax; k += 4)
+    {
+        const int n = min(4, kmax - k);
+        const unsigned r = warp_pt_in_cell4(axis, fixed_a, fixed_b, start, d, k, n, cmin_pos, g, S, nf, eps, lane);
+        const unsigned differ = (c ? ~r : r) & ((1u << n) - 1u);
+        if (differ)
+            return k + __ffs(differ) - 1;
+    }
+    return kmax;
+}
+
 // CellInteriorGridPts (src/dense.cpp:1475-1701).  All lanes run the same
 // state machine; PtInCell is evaluated cooperatively.  With rec == true the
 // nonempty rows go to S.rows (overflow is flagged); with rec == false every
@@ -348,36 +407,50 @@ __device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cm
             bool x_in_left = warp_pt_in_cell(gp[0], gp[1], gp[2], S, nf, eps, lane);
             bool x_in_right = x_in_left;
             int min_xi = cgp[0] - 1, max_xi = 0;
-            for (int xi = x_left; xi >= 0 && xi < cgp[0];)
+            // left walk: from x_left, leftwards while inside (x_in_left) or
+            // rightwards while outside; x_left moves to the first point that
+            // answers otherwise.  Position 0 is x_left, already probed.
             {
-                gp[0] = cmin_pos[0] + xi * g.step[0];
-                if (warp_pt_in_cell(gp[0], gp[1], gp[2], S, nf, eps, lane))
+                const bool c = x_in_left;
+                const int d = c ? -1 : 1;
+                const int kmax = d < 0 ? x_left + 1 : cgp[0] - x_left;
+                const int ks = warp_walk(0, gp[1], gp[2], x_left, d, c, 1, kmax, cmin_pos, g, S, nf, eps, lane);
+                if (c && ks > 0)
                 {
-                    if (xi < min_xi) min_xi = xi;
-                    if (xi > max_xi) max_xi = xi;
-                    if (x_in_left) xi--;
-                    else { x_left = xi; break; }
+                    min_xi = min(min_xi, x_left - (ks - 1));
+                    max_xi = max(max_xi, x_left);
                 }
-                else
+                if (ks < kmax)
                 {
-                    if (!x_in_left) xi++;
-                    else { x_left = xi; break; }
+                    const int xs = x_left + ks * d;
+                    if (!c)
+                    {
+                        min_xi = min(min_xi, xs);
+                        max_xi = max(max_xi, xs);
+                    }
+                    x_left = xs;
                 }
             }
-            for (int xi = x_right; xi >= 0 && xi < cgp[0];)
+            // right walk, mirrored, from x_right
             {
-                gp[0] = cmin_pos[0] + xi * g.step[0];
-                if (warp_pt_in_cell(gp[0], gp[1], gp[2], S, nf, eps, lane))
+                const bool c = x_in_right;
+                const int d = c ? 1 : -1;
+                const int kmax = d > 0 ? cgp[0] - x_right : x_right + 1;
+                const int ks = warp_walk(0, gp[1], gp[2], x_right, d, c, 0, kmax, cmin_pos, g, S, nf, eps, lane);
+                if (c && ks > 0)
                 {
-                    if (xi < min_xi) min_xi = xi;
-                    if (xi > max_xi) max_xi = xi;
-                    if (x_in_right) xi++;
-                    else { x_right = xi; break; }
+                    min_xi = min(min_xi, x_right);
+                    max_xi = max(max_xi, x_right + (ks - 1));
                 }
-                else
+                if (ks < kmax)
                 {
-                    if (!x_in_right) xi--;
-                    else { x_right = xi; break; }
+                    const int xs = x_right + ks * d;
+                    if (!c)
+                    {
+                        min_xi = min(min_xi, xs);
+                        max_xi = max(max_xi, xs);
+                    }
+                    x_right = xs;
                 }
             }
             if (min_xi <= max_xi)
@@ -417,14 +490,10 @@ __device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cm
             {
                 gp[2] = cmin_pos[2] + (zi + 1) * g.step[2];
                 gp[0] = cmin_pos[0] + first_x * g.step[0];
-                int yj;
-                for (yj = first_y; yj > 0; yj--)
-                {
-                    gp[1] = cmin_pos[1] + yj * g.step[1];
-                    if (!warp_pt_in_cell(gp[0], gp[1], gp[2], S, nf, eps, lane))
-                        break;
-                }
-                y_start = yj;
+                // from first_y down while inside, never below 1: y_start is the first
+                // row that answers outside, or 0
+                y_start = first_y - warp_walk(1, gp[0], gp[2], first_y, -1, true, 0, first_y, cmin_pos, g, S, nf, eps,
+                                              lane);
             }
             if (z_step_done)
                 break;

@@ -437,3 +437,31 @@ def test_dtfe_batch_overlap_same_grid(gpu_ctx):
         assert np.array_equal(out[0][0], out[1][0])
         for k in ("grid_pts_assigned", "fp64_tets", "exact_tests", "max_dense"):
             assert out[0][1][k] == out[1][1][k], k
+
+
+# ---------------------------------------------------------------------------
+# error statuses (the kernels check their indices and report; nothing faults)
+# ---------------------------------------------------------------------------
+def test_error_statuses(gpu_ctx):
+    from tess2_gb300.api import DENSE_DTFE, TessGpuError
+    d = load_single("mix2048_seed7")
+    bad = d["tets"].copy()
+    bad[7, 5] = bad.shape[0] + 3          # a neighbour index past the tets
+    with pytest.raises(TessGpuError) as e:
+        gpu_ctx.reorder_neighbors(bad)
+    assert e.value.code == 7
+    b = single_block(d)[0]
+    l6 = np.tile(np.array([0, 0, 0, 1, 1, 1], np.float32), (65, 1))
+    with pytest.raises(TessGpuError) as e:
+        gpu_ctx.incomplete_cells(b, l6)
+    assert e.value.code == 8
+    gni = [int(x) for x in d["glo_num_idx"]]
+    badv = dict(b, tets=d["tets"].copy())
+    badv["tets"][11, 2] = len(d["particles"]) + 5   # a vertex index past the particles
+    for _ in range(2):   # twice: the first call may choose the launch variant, the second is pipelined
+        with pytest.raises(TessGpuError) as e:
+            gpu_ctx.dense(DENSE_DTFE, [badv], gni)
+        assert e.value.code == 7
+    # the context stays usable
+    r = gpu_ctx.dense(DENSE_DTFE, [b], gni)
+    assert r["info"]["grid_pts_assigned"] > 0
