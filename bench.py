@@ -372,6 +372,12 @@ def run_gpu(args):
     cfg = workload_config(args, blocks)
     T, N = cfg["tets"], cfg["particles_with_ghosts"]
 
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
     ctx = Context(local)
     batch = ctx.upload(blocks)
     grid = torch.empty(G, dtype=torch.float32, device=f"cuda:{local}")
@@ -467,19 +473,26 @@ def run_gpu(args):
         e1.record()
         torch.cuda.synchronize()
         mst = e0.elapsed_time(e1) / kt
-        extra["dense_tess_gpu"] = dict(value=G / (mst * 1e-3), unit=UNIT, ms_per_step=mst)
+        it = batch.dense(DENSE_TESS, gni, gptr, want_info=True)
+        # its roofline: 12 B/particle + 32 B/tet + 4 B/grid point of HBM, and
+        # 8 FP32 operations per face-plane test (probes x faces); no measured
+        # FP32 peak exists, so the nominal 152 SMs x 128 lanes x 2 x 2.07 GHz
+        tb = 12.0 * N + 32.0 * T + 4.0 * G
+        tf = 8.0 * it["face_tests"]
+        fp32_nominal = 152 * 128 * 2 * 2.07e9
+        extra["dense_tess_gpu"] = dict(value=G / (mst * 1e-3), unit=UNIT, ms_per_step=mst,
+                                       cells_deposited=it["check_mass"], cell_probes=it["cell_probes"],
+                                       face_tests=it["face_tests"], algorithmic_bytes=tb,
+                                       achieved_gbs=tb / (mst * 1e-3) / 1e9, hbm_frac=tb / (mst * 1e-3) / 1e9 / hbm,
+                                       achieved_gflops=tf / (mst * 1e-3) / 1e9,
+                                       fp32_frac_of_nominal=tf / (mst * 1e-3) / fp32_nominal)
 
     # roofline of the dominant kernel: the mixed rasteriser
     # algorithmic bytes per launch: tet vertices 16 B/tet, particle positions
     # 16 B and densities 4 B per particle (each read once), 4 B per grid point written
     assigned = info["grid_pts_assigned"]
     raster_bytes = 16.0 * T + 20.0 * N + 4.0 * assigned
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
+
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     r_ms = stage_ms.get("raster", float("nan"))
     achieved = raster_bytes / (r_ms * 1e-3) / 1e9

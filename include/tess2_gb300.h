@@ -124,6 +124,8 @@ typedef struct tessgpu_dense_info
     float     raster_variant_ms[8]; /* DTFE: the autotuner's best time of each configuration (0 if not run) */
     int       grid_layers;      /* project: z layers of the device grid; 0 for a 3-D grid */
     long long grid_floats;      /* floats of the device grid tessgpu_batch_dense wrote */
+    long long cell_probes;      /* DENSE_TESS: PtInCell calls of the scanline (src/dense.cpp:1475-1701) */
+    long long face_tests;       /* DENSE_TESS: face-plane tests of those calls (probes x faces) */
 } tessgpu_dense_info;
 
 /* ---- context ---------------------------------------------------------- */

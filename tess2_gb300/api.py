@@ -76,7 +76,8 @@ class DenseInfo(ctypes.Structure):
                 ("exact_tests", ctypes.c_longlong), ("rows_visited", ctypes.c_longlong),
                 ("points_tested", ctypes.c_longlong), ("raster_variant", ctypes.c_int),
                 ("raster_variant_ms", ctypes.c_float * 8), ("grid_layers", ctypes.c_int),
-                ("grid_floats", ctypes.c_longlong)]
+                ("grid_floats", ctypes.c_longlong), ("cell_probes", ctypes.c_longlong),
+                ("face_tests", ctypes.c_longlong)]
 
     def as_dict(self):
         return dict(data_mins=np.array(self.data_mins[:], np.float32), data_maxs=np.array(self.data_maxs[:], np.float32),
@@ -88,7 +89,7 @@ class DenseInfo(ctypes.Structure):
                     exact_tests=self.exact_tests, rows_visited=self.rows_visited,
                     points_tested=self.points_tested, raster_variant=self.raster_variant,
                     raster_variant_ms=list(self.raster_variant_ms), grid_layers=self.grid_layers,
-                    grid_floats=self.grid_floats)
+                    grid_floats=self.grid_floats, cell_probes=self.cell_probes, face_tests=self.face_tests)
 
 
 _LIB = None

@@ -1004,6 +1004,8 @@ dtfe_done:
             info->raster_variant_ms[v] = ctx->tune_ms[p->mode][v];
         info->grid_layers = L;
         info->grid_floats = Gout;
+        info->cell_probes = (long long)ctx->h_status->probes;
+        info->face_tests = (long long)ctx->h_status->face_tests;
     }
     return st;
 }

@@ -45,6 +45,8 @@ struct Status
     unsigned long long check_mass;
     unsigned long long rows;        // DTFE: grid rows visited
     unsigned long long candidates;  // DTFE: grid points tested
+    unsigned long long probes;      // DENSE_TESS: PtInCell calls of the scanline
+    unsigned long long face_tests;  // DENSE_TESS: probes x faces of the cell
 };
 
 __device__ __forceinline__ void fail(Status* st, int code, int detail)

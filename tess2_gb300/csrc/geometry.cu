@@ -386,12 +386,14 @@ __device__ __forceinline__ int warp_walk(int axis, float fixed_a, float fixed_b,
 // state machine; PtInCell is evaluated cooperatively.  With rec == true the
 // nonempty rows go to S.rows (overflow is flagged); with rec == false every
 // row is deposited at once with per-point increment inc.
-struct ScanOut { int tot; int nrows; bool overflow; int deposited; };
+// probes: the PtInCell calls the reference's scanline makes (its walks, one
+// call per position, the first position of the left walk probed twice)
+struct ScanOut { int tot; int nrows; bool overflow; int deposited; int probes; };
 
 __device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cmin_pos, WarpSmem& S, int nf,
                             const GridDesc& g, int lane, bool rec, float inc, float* grid)
 {
-    ScanOut o = { 0, 0, false, 0 };
+    ScanOut o = { 0, 0, false, 0, 0 };
     float gp[3];
     int x_left = cgp[0] / 2, x_right = cgp[0] / 2, y_start = 0, first_x = 0;
     const float eps = g.eps;
@@ -415,6 +417,7 @@ __device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cm
                 const int d = c ? -1 : 1;
                 const int kmax = d < 0 ? x_left + 1 : cgp[0] - x_left;
                 const int ks = warp_walk(0, gp[1], gp[2], x_left, d, c, 1, kmax, cmin_pos, g, S, nf, eps, lane);
+                o.probes += 1 + (ks < kmax ? ks + 1 : ks);
                 if (c && ks > 0)
                 {
                     min_xi = min(min_xi, x_left - (ks - 1));
@@ -437,6 +440,7 @@ __device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cm
                 const int d = c ? 1 : -1;
                 const int kmax = d > 0 ? cgp[0] - x_right : x_right + 1;
                 const int ks = warp_walk(0, gp[1], gp[2], x_right, d, c, 0, kmax, cmin_pos, g, S, nf, eps, lane);
+                o.probes += ks < kmax ? ks + 1 : ks;
                 if (c && ks > 0)
                 {
                     min_xi = min(min_xi, x_right);
@@ -492,8 +496,9 @@ __device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cm
                 gp[0] = cmin_pos[0] + first_x * g.step[0];
                 // from first_y down while inside, never below 1: y_start is the first
                 // row that answers outside, or 0
-                y_start = first_y - warp_walk(1, gp[0], gp[2], first_y, -1, true, 0, first_y, cmin_pos, g, S, nf, eps,
-                                              lane);
+                const int ks = warp_walk(1, gp[0], gp[2], first_y, -1, true, 0, first_y, cmin_pos, g, S, nf, eps, lane);
+                o.probes += ks < first_y ? ks + 1 : ks;
+                y_start = first_y - ks;
             }
             if (z_step_done)
                 break;
@@ -504,7 +509,7 @@ __device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cm
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(CELL_WARPS * 32)
+__global__ void __launch_bounds__(CELL_WARPS * 32, 7)   // 7 blocks per SM: shared memory allows 7 as well
 k_cells(const BlockDesc* blocks, const int* c_off, int nb, int total_cells, const float4* pos,
         const int4* tv, const int4* tn, const int* v2t, const float4* cc, const double* cc64, GridDesc g,
         float* grid, int* out_i, float* out_f, float* out_area, double* out_d, int* cell_counts, Status* st)
@@ -513,7 +518,7 @@ k_cells(const BlockDesc* blocks, const int* c_off, int nb, int total_cells, cons
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     WarpSmem& S = smem[w];
     double acc_mass = 0.0;
-    unsigned long long acc_cells = 0;
+    unsigned long long acc_cells = 0, acc_probes = 0, acc_faces = 0;
 
     for (int c = blockIdx.x * CELL_WARPS + w; c < total_cells; c += gridDim.x * CELL_WARPS)
     {
@@ -793,6 +798,8 @@ k_cells(const BlockDesc* blocks, const int* c_off, int nb, int total_cells, cons
             cgp[d] = cmax_idx[d] - cmin_idx[d] + 1;
 
         ScanOut so = scanline(cgp, cmin_idx, cmin_pos, S, nf, g, lane, true, 0.0f, grid);
+        acc_probes += (unsigned)so.probes;
+        acc_faces += (unsigned long long)so.probes * nf;
         int ndep = 0, npts;
         double cell_mass = 0.0;
         if (so.tot > 0)
@@ -852,6 +859,8 @@ k_cells(const BlockDesc* blocks, const int* c_off, int nb, int total_cells, cons
     {
         atomicAdd(&st->tot_mass, acc_mass);
         atomicAdd(&st->check_mass, acc_cells);
+        atomicAdd(&st->probes, acc_probes);
+        atomicAdd(&st->face_tests, acc_faces);
     }
 }
 
