@@ -371,24 +371,20 @@ template <typename T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; };
 template <> struct Vec4<double> { typedef double4 type; };
 
-template <typename T, bool VAL64, bool FLAT, bool COMPACT>
+template <typename T, bool VAL64, bool COMPACT>
 struct __align__(16) RasterSmem
 {
     typedef typename Vec4<T>::type T4;
     // per tet of the current batch (lane = tet slot)
-    float4 A0[32], A1[32];                   // vertices 0, 1; A0.w = bbox x lo, A1.w = bbox x hi
+    float4 A0[32], A1[32];                   // vertices 0, 1 (row-axis order); .w = bbox lo, hi along the row axis
     int    TG[32];                           // global tet index (the exact path reloads vertices 2, 3)
     T4     C[4][32];                         // c_k.x, c_k.y, c_k.z, B_k
     T4     W[32];                            // rho_k / 6V
     float4 XA[32], XB[32], XG[32];           // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
     int4   I0[32];                           // ix0, ix1, iy0, ny
-    int4   I1[32];                           // iz0, s, local tet index, face masks | sliced flag
+    int4   I1[32];                           // iz0, s, local tet index, face masks | sliced flag | row axis
     int    SLC[SLICES][32];                  // per z slice: first row dy << 16 | rows
     int    pre[33];                          // prefix of the tets' row counts
-    // per row of the current round (lane = row slot)
-    T      RN[4][FLAT ? 32 : 1];             // R_k(y, z) of the row
-    int    RJ[FLAT ? 32 : 1], RI0[FLAT ? 32 : 1], RY[FLAT ? 32 : 1], RZ[FLAT ? 32 : 1];  // tet slot, first x, y, z
-    int    pp[33];                           // prefix of the rows' point counts
     int    Q[COMPACT ? 64 : 1];              // tets whose box holds grid points, waiting for a batch
     double C64[VAL64 && sizeof(T) == 4 ? 12 : 1][32];   // FP64 values for the fix-up pass
     double W64[VAL64 && sizeof(T) == 4 ? 4 : 1][32];
@@ -429,19 +425,41 @@ __device__ __forceinline__ bool tet_box(const BlockDesc* blocks, int nb, const f
     return empty;
 }
 
+// Each tet's rows run along the axis of its smallest projected area (fewest
+// rows).  Row axis ra: the tet's coordinates are taken in the order
+// (ra, b, c) = (0,1,2), (1,0,2) or (2,0,1); "x" below is the row axis, "y"
+// the axis of the rows within a z slice, "z" the slice axis.  The arithmetic
+// and its error bounds are the same in any order.
+template <typename V>
+__device__ __forceinline__ void perm3(int ra, V o0, V o1, V o2, V& n0, V& n1, V& n2)
+{
+    n0 = ra == 0 ? o0 : (ra == 1 ? o1 : o2);
+    n1 = ra == 0 ? o1 : o0;
+    n2 = ra == 2 ? o1 : o2;
+}
+template <typename V>
+__device__ __forceinline__ void unperm3(int ra, V n0, V n1, V n2, V& x, V& y, V& z)
+{
+    x = ra == 0 ? n0 : n1;
+    y = ra == 0 ? n1 : (ra == 1 ? n0 : n2);
+    z = ra == 2 ? n0 : n2;
+}
+
 // one grid point of a row: classify against the tet's four numerator planes
 // (exact arithmetic when the filter cannot decide) and write the
 // interpolated density when it is inside
-template <typename T, bool VAL64, bool FLAT, bool COMPACT>
-__device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, FLAT, COMPACT>& S, int j, int xi, int yi, int zi, float pyf,
+// xi, yi, zi and pyf, pzf are in the tet's row-axis order; hx, gx the row
+// axis' grid step and origin
+template <typename T, bool VAL64, bool COMPACT>
+__device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, COMPACT>& S, int j, int xi, int yi, int zi, float pyf,
                                              float pzf, const float4& A0, const float4& A1, const int4& I1,
-                                             const T* cx, const T* RN, const T* Bk, const GridDesc& g,
-                                             const int4* tv, const float4* pos, float* grid, int* owner,
-                                             unsigned long long& nexact, unsigned long long& nassigned)
+                                             const T* cx, const T* RN, const T* Bk, float hx, float gx, int ra,
+                                             const GridDesc& g, const int4* tv, const float4* pos, float* grid,
+                                             int* owner, unsigned long long& nexact, unsigned long long& nassigned)
 {
     typedef typename Vec4<T>::type T4;
     constexpr bool F32 = sizeof(T) == 4;
-    const float pxf = xi * g.step[0] + g.gmin[0];
+    const float pxf = xi * hx + gx;
     const T px = pxf;
     const int s = I1.y;
     T N[4];   // s N_k: the tables hold s c_k (see the setup)
@@ -468,8 +486,11 @@ __device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, FLAT, CO
         nexact++;
         const int4 vt = __ldg(&tv[S.TG[j]]);
         const float4 A2 = __ldg(&pos[vt.z]), A3 = __ldg(&pos[vt.w]);
-        if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf, pyf, pzf, s,
-                          open))
+        float a0x, a0y, a0z, a1x, a1y, a1z, qx_, qy_, qz_;
+        unperm3(ra, A0.x, A0.y, A0.z, a0x, a0y, a0z);
+        unperm3(ra, A1.x, A1.y, A1.z, a1x, a1y, a1z);
+        unperm3(ra, pxf, pyf, pzf, qx_, qy_, qz_);
+        if (!inside_exact(a0x, a0y, a0z, a1x, a1y, a1z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, qx_, qy_, qz_, s, open))
             return;
     }
     float f;
@@ -480,8 +501,13 @@ __device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, FLAT, CO
     }
     else
     {
-        const double q1[3] = { (double)pxf - A1.x, (double)pyf - A1.y, (double)pzf - A1.z };
-        const double q0[3] = { (double)pxf - A0.x, (double)pyf - A0.y, (double)pzf - A0.z };
+        // the FP64 tables are in x, y, z order
+        float a0x, a0y, a0z, a1x, a1y, a1z, qx_, qy_, qz_;
+        unperm3(ra, A0.x, A0.y, A0.z, a0x, a0y, a0z);
+        unperm3(ra, A1.x, A1.y, A1.z, a1x, a1y, a1z);
+        unperm3(ra, pxf, pyf, pzf, qx_, qy_, qz_);
+        const double q1[3] = { (double)qx_ - a1x, (double)qy_ - a1y, (double)qz_ - a1z };
+        const double q0[3] = { (double)qx_ - a0x, (double)qy_ - a0y, (double)qz_ - a0z };
         double acc = 0.0;
         for (int k = 0; k < 4; ++k)
         {
@@ -491,24 +517,26 @@ __device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, FLAT, CO
         }
         f = (float)acc;
     }
-    const size_t gi = ((size_t)zi * g.n[1] + yi) * g.n[0] + xi;
+    int gx_, gy_, gz_;
+    unperm3(ra, xi, yi, zi, gx_, gy_, gz_);
+    const size_t gi = ((size_t)gz_ * g.n[1] + gy_) * g.n[0] + gx_;
     grid[gi] = f;
     if (owner)
         owner[gi] = I1.z;
     nassigned++;
 }
 
-template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, bool FLAT>
+template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT>
 __global__ void __launch_bounds__(NW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
          int* fix_list, int* fix_count, Status* st, int t0)
 {
     typedef typename Vec4<T>::type T4;
-    __shared__ RasterSmem<T, VAL64, FLAT, COMPACT> smem[NW];
+    __shared__ RasterSmem<T, VAL64, COMPACT> smem[NW];
     constexpr bool F32 = sizeof(T) == 4;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    RasterSmem<T, VAL64, FLAT, COMPACT>& S = smem[wid];
+    RasterSmem<T, VAL64, COMPACT>& S = smem[wid];
     unsigned long long nexact = 0, nassigned = 0, nfix = 0, nrows = 0, ncand = 0;
     const int n = LIST ? *list_count : total;
     const int nchunks = (n + 31) / 32;
@@ -602,21 +630,13 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                     }
                     if (keep)
                     {
-                        S.A0[lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
-                        S.A1[lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
                         S.TG[lane] = t;
                         T4 w4;
                         const float r6 = F32 ? __frcp_rn((float)v6) : 0.0f;
 #pragma unroll
                         for (int k = 0; k < 4; ++k)
                         {
-                            T4 ck;
-                            // the orientation folded in (exact: s = +-1): a point is inside
-                            // when every s N_k > B_k, and s N_k times s rho_k / 6V is the
-                            // same product, so the points need no sign multiply
                             const T sg = (T)s;
-                            ck.x = sg * c[k][0]; ck.y = sg * c[k][1]; ck.z = sg * c[k][2]; ck.w = Bk[k];
-                            S.C[k][lane] = ck;
                             const T wk = sg * (F32 ? (T)(__ldg(&rho32[vid[k]]) * r6) : (T)__ldg(&rho64[vid[k]]) / v6);
                             if (k == 0) w4.x = wk;
                             else if (k == 1) w4.y = wk;
@@ -652,6 +672,46 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                                 S.W64[k][lane] = __ldg(&rho64[vid[k]]) / v6d;
                             }
                         }
+                        // the row axis: the one along which the tet's projection is smallest
+                        // (the projected area across axis d is half the sum of |c_k[d]|)
+                        int ra = 0;
+                        {
+                            float pr[3];
+#pragma unroll
+                            for (int d = 0; d < 3; ++d)
+                                pr[d] = fabsf((float)c[0][d]) + fabsf((float)c[1][d]) + fabsf((float)c[2][d]) +
+                                        fabsf((float)c[3][d]);
+                            if (pr[1] < pr[0] && pr[1] <= pr[2]) ra = 1;
+                            else if (pr[2] < pr[0] && pr[2] < pr[1]) ra = 2;
+                        }
+                        // everything below in (row axis, y, z) order
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            perm3(ra, a[k][0], a[k][1], a[k][2], a[k][0], a[k][1], a[k][2]);
+                            perm3(ra, c[k][0], c[k][1], c[k][2], c[k][0], c[k][1], c[k][2]);
+                        }
+                        perm3(ra, lo[0], lo[1], lo[2], lo[0], lo[1], lo[2]);
+                        perm3(ra, hi[0], hi[1], hi[2], hi[0], hi[1], hi[2]);
+                        perm3(ra, ilo[0], ilo[1], ilo[2], ilo[0], ilo[1], ilo[2]);
+                        perm3(ra, ihi[0], ihi[1], ihi[2], ihi[0], ihi[1], ihi[2]);
+                        float gst[3], gmn[3], ginv[3];
+                        perm3(ra, g.step[0], g.step[1], g.step[2], gst[0], gst[1], gst[2]);
+                        perm3(ra, g.gmin[0], g.gmin[1], g.gmin[2], gmn[0], gmn[1], gmn[2]);
+                        perm3(ra, g.inv_step[0], g.inv_step[1], g.inv_step[2], ginv[0], ginv[1], ginv[2]);
+                        S.A0[lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
+                        S.A1[lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            // the orientation folded in (exact: s = +-1): a point is inside
+                            // when every s N_k > B_k, and s N_k times s rho_k / 6V is the
+                            // same product, so the points need no sign multiply
+                            const T sg = (T)s;
+                            T4 ck;
+                            ck.x = sg * c[k][0]; ck.y = sg * c[k][1]; ck.z = sg * c[k][2]; ck.w = Bk[k];
+                            S.C[k][lane] = ck;
+                        }
                         // Row-wise x bounds.  Inside needs s*N_k >= -B_k, N_k = c_kx (x - bx)
                         // + R_k(y, z); along row (dy, dz) of the box this is x >= bnd_k
                         // (s c_kx > 0) or x <= bnd_k (s c_kx < 0) with
@@ -663,10 +723,10 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         const int nyb = ihi[1] - ilo[1] + 1, nzb = ihi[2] - ilo[2] + 1;
                         int masks = 0;
                         {
-                            const float h1 = g.step[1], h2 = g.step[2];
-                            const float py0 = ilo[1] * h1 + g.gmin[1], pz0 = ilo[2] * h2 + g.gmin[2];
-                            const float ymx = fmaxf(fabsf(py0), fabsf(ihi[1] * h1 + g.gmin[1]));
-                            const float zmx = fmaxf(fabsf(pz0), fabsf(ihi[2] * h2 + g.gmin[2]));
+                            const float h1 = gst[1], h2 = gst[2];
+                            const float py0 = ilo[1] * h1 + gmn[1], pz0 = ilo[2] * h2 + gmn[2];
+                            const float ymx = fmaxf(fabsf(py0), fabsf(ihi[1] * h1 + gmn[1]));
+                            const float zmx = fmaxf(fabsf(pz0), fabsf(ihi[2] * h2 + gmn[2]));
                             const float xmx = fmaxf(fabsf(lo[0]), fabsf(hi[0]));
                             float xa[4], xb[4], xg[4];
 #pragma unroll
@@ -719,7 +779,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                             }
                             for (int zo = 0; zo < nzb; ++zo)
                             {
-                                const float pz = (ilo[2] + zo) * g.step[2] + g.gmin[2];
+                                const float pz = (ilo[2] + zo) * gst[2] + gmn[2];
                                 float ylo = FLT_MAX, yhi = -FLT_MAX;
 #pragma unroll
                                 for (int e = 0; e < 6; ++e)
@@ -747,10 +807,10 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                                 if (ylo <= yhi)
                                 {
                                     const float my = 64.0f * EPS32 * (fmaxf(fabsf(ylo), fabsf(yhi)) + hi[1] - lo[1]);
-                                    const float f0 = (ylo - my - g.gmin[1]) * g.inv_step[1];
-                                    const float f1 = (yhi + my - g.gmin[1]) * g.inv_step[1];
+                                    const float f0 = (ylo - my - gmn[1]) * ginv[1];
+                                    const float f1 = (yhi + my - gmn[1]) * ginv[1];
                                     const float mm = 1e-3f + 8.0f * EPS32 *
-                                        ((fabsf(g.gmin[1]) + fmaxf(fabsf(ylo), fabsf(yhi))) * g.inv_step[1] +
+                                        ((fabsf(gmn[1]) + fmaxf(fabsf(ylo), fabsf(yhi))) * ginv[1] +
                                          fmaxf(fabsf(f0), fabsf(f1)));
                                     const int y0i = max(ilo[1], (int)ceilf(fmaxf(f0 - mm, (float)(ilo[1] - 1))));
                                     const int y1i = min(ihi[1], (int)floorf(fminf(f1 + mm, (float)(ihi[1] + 1))));
@@ -767,7 +827,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         }
                         else
                             rows = nyb * nzb;
-                        S.I1[lane] = make_int4(ilo[2], s, t - blocks[b].t_off, masks);
+                        S.I1[lane] = make_int4(ilo[2], s, t - blocks[b].t_off, masks | (ra << 9));
                     }
                 }
             }
@@ -836,21 +896,27 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                     nrows++;
                     if (xmin <= xmax)
                     {
+                        // the tet's axes: row axis ra, then y, z (see perm3)
+                        const int ra = (I1.w >> 9) & 3;
+                        float gst[3], gmn[3], ginv0;
+                        perm3(ra, g.step[0], g.step[1], g.step[2], gst[0], gst[1], gst[2]);
+                        perm3(ra, g.gmin[0], g.gmin[1], g.gmin[2], gmn[0], gmn[1], gmn[2]);
+                        ginv0 = ra == 0 ? g.inv_step[0] : (ra == 1 ? g.inv_step[1] : g.inv_step[2]);
                         // grid indices inside [xmin, xmax]: an index estimate widened by m
                         // grid steps, where m exceeds the rounding of the estimate and of the
                         // float grid positions (2 eps |pos| each), so no point in the range is
                         // dropped; an extra point at the edge is classified like any other
-                        const float f0 = (xmin - g.gmin[0]) * g.inv_step[0];
-                        const float f1 = (xmax - g.gmin[0]) * g.inv_step[0];
-                        const float mg = 1e-3f + 8.0f * EPS32 * ((fabsf(g.gmin[0]) + fmaxf(fabsf(xmin), fabsf(xmax))) *
-                                                                 g.inv_step[0] + fmaxf(fabsf(f0), fabsf(f1)));
+                        const float f0 = (xmin - gmn[0]) * ginv0;
+                        const float f1 = (xmax - gmn[0]) * ginv0;
+                        const float mg = 1e-3f + 8.0f * EPS32 * ((fabsf(gmn[0]) + fmaxf(fabsf(xmin), fabsf(xmax))) *
+                                                                 ginv0 + fmaxf(fabsf(f0), fabsf(f1)));
                         const int i0 = max(I0.x, (int)ceilf(fmaxf(f0 - mg, (float)(I0.x - 1))));
                         const int i1 = min(I0.y, (int)floorf(fminf(f1 + mg, (float)(I0.y + 1))));
                         if (i0 <= i1)
                         {
                             const int yi = I0.z + dy, zi = I1.x + zo;
-                            const float pyf = yi * g.step[1] + g.gmin[1];
-                            const float pzf = zi * g.step[2] + g.gmin[2];
+                            const float pyf = yi * gst[1] + gmn[1];
+                            const float pzf = zi * gst[2] + gmn[2];
                             T RN[4];
 #pragma unroll
                             for (int k = 0; k < 4; ++k)
@@ -861,70 +927,20 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                                 RN[k] = Real<T>::fma_(ck.y, qy, ck.z * qz);
                             }
                             ncand += i1 - i0 + 1;
-                            if (FLAT)
+                            // this lane's row, point by point
+                            T cx[4], Bk[4];
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
                             {
-#pragma unroll
-                                for (int k = 0; k < 4; ++k)
-                                    S.RN[k][lane] = RN[k];
-                                S.RJ[lane] = j;
-                                S.RI0[lane] = i0;
-                                S.RY[lane] = yi;
-                                S.RZ[lane] = zi;
-                                cnt = i1 - i0 + 1;
+                                const T4 ck = S.C[k][j];
+                                cx[k] = ck.x;
+                                Bk[k] = ck.w;
                             }
-                            else
-                            {
-                                // this lane's row, point by point
-                                T cx[4], Bk[4];
-#pragma unroll
-                                for (int k = 0; k < 4; ++k)
-                                {
-                                    const T4 ck = S.C[k][j];
-                                    cx[k] = ck.x;
-                                    Bk[k] = ck.w;
-                                }
-                                for (int xi = i0; xi <= i1; ++xi)
-                                    raster_point<T, VAL64, FLAT, COMPACT>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv,
-                                                           pos, grid, owner, nexact, nassigned);
-                            }
+                            for (int xi = i0; xi <= i1; ++xi)
+                                raster_point<T, VAL64, COMPACT>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk,
+                                                                gst[0], gmn[0], ra, g, tv, pos, grid, owner, nexact,
+                                                                nassigned);
                         }
-                    }
-                }
-                if (FLAT)
-                {
-                    // prefix of the rows' point counts, then the points spread over the lanes
-                    int pin = cnt;
-                    for (int o = 1; o < 32; o <<= 1)
-                    {
-                        const int v = __shfl_up_sync(FULL, pin, o);
-                        if (lane >= o) pin += v;
-                    }
-                    S.pp[lane + 1] = pin;
-                    if (lane == 0) S.pp[0] = 0;
-                    __syncwarp();
-                    const int P = S.pp[32];
-                    int rs = 0;
-                    for (int q = lane; q < P; q += 32)
-                    {
-                        while (S.pp[rs + 1] <= q) ++rs;
-                        const int jj = S.RJ[rs];
-                        const int xi = S.RI0[rs] + (q - S.pp[rs]);
-                        const int yi = S.RY[rs], zi = S.RZ[rs];
-                        const float pyf = yi * g.step[1] + g.gmin[1];
-                        const float pzf = zi * g.step[2] + g.gmin[2];
-                        const float4 A0 = S.A0[jj], A1 = S.A1[jj];
-                        const int4 I1 = S.I1[jj];
-                        T cx[4], Bk[4], RN[4];
-#pragma unroll
-                        for (int k = 0; k < 4; ++k)
-                        {
-                            const T4 ck = S.C[k][jj];
-                            cx[k] = ck.x;
-                            Bk[k] = ck.w;
-                            RN[k] = S.RN[k][rs];
-                        }
-                        raster_point<T, VAL64, FLAT, COMPACT>(S, jj, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, g, tv, pos, grid,
-                                               owner, nexact, nassigned);
                     }
                 }
                 __syncwarp();
@@ -980,17 +996,11 @@ void launch_densities(const unsigned long long* W, int n, float mass, double inv
     k_densities<<<grid_for(n, 256, 8), 256, 0, s>>>(W, n, mass, inv_scale, rho32, rho64, st);
 }
 
-// Block residency per SM trades registers against latency hiding; which
-// bound is fastest depends on the GPU and the mesh, so the caller picks it
-// (variant 0, 1, 2 = 4, 5, 6 resident blocks per SM).
 // Launch variants.  Block residency per SM trades registers against latency
-// hiding; COMPACT screens tets with empty boxes out before the setup; FLAT
-// spreads a round's points over the lanes (good when a point is expensive,
-// as in FP64, costly in shared-memory traffic when it is cheap).  The
+// hiding; COMPACT screens tets with empty boxes out before the setup.  The
 // fastest depends on the GPU, the mesh and the mode, so the caller times them.
-//   0..2: per-lane rows, 4/5/6 blocks per SM    3: compact, 5 blocks
-//   4..5: compact + flat, 4/5 blocks per SM
-constexpr int N_RASTER_VARIANTS = 6;
+//   0..2: 4/5/6 blocks per SM    3: compact, 5 blocks per SM
+constexpr int N_RASTER_VARIANTS = 4;
 
 template <typename T, bool VAL64, bool LIST>
 static void raster_variant(int variant, long long work, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
@@ -1001,18 +1011,16 @@ static void raster_variant(int variant, long long work, cudaStream_t s, const Bl
     // the double-precision tables need more shared memory: 3 warps per block
     constexpr int NW = (sizeof(T) == 4 && !VAL64) ? 4 : 3;
     const int nblk = grid_for(work, NW * 32, 16);
-#define TG_RASTER(MB, C, F)                                                                                        \
-    k_raster<T, VAL64, LIST, MB, NW, C, F><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, \
+#define TG_RASTER(MB, C)                                                                                           \
+    k_raster<T, VAL64, LIST, MB, NW, C><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, \
                                                                       rho32, rho64, g, tau, grid, owner, fix_list,  \
                                                                       fix_count, st, t0)
     switch (variant)
     {
-    case 1: TG_RASTER(5, false, false); break;
-    case 2: TG_RASTER(6, false, false); break;
-    case 3: TG_RASTER(5, true, false); break;
-    case 4: TG_RASTER(4, true, true); break;
-    case 5: TG_RASTER(5, true, true); break;
-    default: TG_RASTER(4, false, false); break;
+    case 1: TG_RASTER(5, false); break;
+    case 2: TG_RASTER(6, false); break;
+    case 3: TG_RASTER(5, true); break;
+    default: TG_RASTER(4, false); break;
     }
 #undef TG_RASTER
 }
