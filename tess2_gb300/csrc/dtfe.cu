@@ -356,7 +356,8 @@ __device__ __noinline__ bool inside_exact(float a00, float a01, float a02, float
 // spread over the lanes instead of serialising one.  A row finds the x range
 // its four planes allow, tests those points with the filter (exact
 // arithmetic when it cannot decide) and writes the interpolated density of
-// every point inside.
+// every point inside.  "x" is the tet's row axis (perm3): the axis across
+// which it projects smallest, so it has the fewest rows.
 //
 // Instances:
 //   T=float,  VAL64=false, LIST=false  mixed main pass: FP32 classification and
