@@ -146,7 +146,8 @@ long long      tessgpu_launch_count(const tessgpu_ctx* ctx);
    rasteriser's launch variant is chosen; TESSGPU_BATCH_OVERLAP=0 runs the
    stages one after the other over all blocks instead), the per-stage entries
    are sums over the blocks of spans timed on each block's stream, which
-   overlap one another. */
+   overlap one another; the pipelined host-buffer DTFE call reports its
+   upload, compute and download spans the same way. */
 tessgpu_status tessgpu_set_timing(tessgpu_ctx* ctx, int on);
 int            tessgpu_stage_times(tessgpu_ctx* ctx, const char** names, float* ms, int cap);
 

@@ -52,6 +52,7 @@ struct tessgpu_ctx
     // the pipelined host-buffer DTFE call: copy streams and events
     cudaStream_t             h2d = nullptr, d2h = nullptr, cs2 = nullptr;
     std::vector<cudaEvent_t> pipe_ev;
+    cudaEvent_t              first_ev[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
 };
 
 // an event on stream s for a span (timing on), its index; -1 otherwise
@@ -219,6 +220,8 @@ extern "C" void tessgpu_destroy(tessgpu_ctx* ctx)
     }
     for (cudaEvent_t e : ctx->pipe_ev)
         cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->first_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
     if (ctx->d2h) cudaStreamDestroy(ctx->d2h);
     if (ctx->cs2) cudaStreamDestroy(ctx->cs2);
@@ -1354,10 +1357,35 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     CK(cudaEventRecord(ev0, s));
     CK(cudaStreamWaitEvent(ctx->h2d, ev0, 0));
     CK(cudaStreamWaitEvent(ctx->d2h, ev0, 0));
+    // the first block goes up in quarters (particles first), so its ingest and
+    // star volumes start after a quarter of its upload rather than all of it
+    constexpr int kFirstParts = 4;
+    for (int i = 0; i < 1 + kFirstParts; ++i)
+        if (!ctx->first_ev[i]) CK(cudaEventCreateWithFlags(&ctx->first_ev[i], cudaEventDisableTiming));
+    auto part = [&](const BlockDesc& d, int i) { return (long long)d.nt * i / kFirstParts; };
     for (int k = 0; k < nb; ++k)
     {
         const int b = order[k];
         const BlockDesc& d = hb[b];
+        const int eu0 = smark(ctx, ctx->h2d);
+        if (k == 0)
+        {
+            if (d.np)
+                CK(cudaMemcpyAsync(stage_xyz + 3 * (size_t)d.p_off, blocks[b].particles, 12 * (size_t)d.np,
+                                   cudaMemcpyHostToDevice, ctx->h2d));
+            CK(cudaEventRecord(ctx->first_ev[0], ctx->h2d));
+            for (int i = 0; i < kFirstParts; ++i)
+            {
+                const long long t0 = part(d, i), t1 = part(d, i + 1);
+                if (t1 > t0)
+                    CK(cudaMemcpyAsync(stage_tets + 2 * ((size_t)d.t_off + t0), blocks[b].tets + 8 * t0,
+                                       32 * (size_t)(t1 - t0), cudaMemcpyHostToDevice, ctx->h2d));
+                CK(cudaEventRecord(ctx->first_ev[1 + i], ctx->h2d));
+            }
+            CK(cudaEventRecord(ctx->pipe_ev[k], ctx->h2d));
+            span(ctx, "upload", eu0, smark(ctx, ctx->h2d));
+            continue;
+        }
         if (d.nt)
             CK(cudaMemcpyAsync(stage_tets + 2 * (size_t)d.t_off, blocks[b].tets, 32 * (size_t)d.nt,
                                cudaMemcpyHostToDevice, ctx->h2d));
@@ -1365,6 +1393,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             CK(cudaMemcpyAsync(stage_xyz + 3 * (size_t)d.p_off, blocks[b].particles, 12 * (size_t)d.np,
                                cudaMemcpyHostToDevice, ctx->h2d));
         CK(cudaEventRecord(ctx->pipe_ev[k], ctx->h2d));
+        span(ctx, "upload", eu0, smark(ctx, ctx->h2d));
     }
     CK(cudaMemcpyAsync(d_blocks, hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
@@ -1383,18 +1412,24 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         const int b = order[k];
         const BlockDesc& d = hb[b];
         cudaStream_t s = (k & 1) ? ctx->cs2 : ctx->stream;
-        CK(cudaStreamWaitEvent(s, ctx->pipe_ev[k], 0));
+        CK(cudaStreamWaitEvent(s, k == 0 ? ctx->first_ev[0] : ctx->pipe_ev[k], 0));
+        const int ec0 = smark(ctx, s);
         if (d.np)
         {
             k_pack_block<<<grid_small(d.np), 256, 0, s>>>(stage_xyz + 3 * (size_t)d.p_off, d.np, pos + d.p_off);
             CK(cudaMemsetAsync(W + d.p_off, 0, sizeof(unsigned long long) * d.np, s));
             ctx->launches++;
         }
-        if (d.nt)
+        for (int i = 0; i < (k == 0 ? kFirstParts : 1); ++i)
         {
-            k_ingest_verts<<<grid_small(d.nt), 256, 0, s>>>(stage_tets + 2 * (size_t)d.t_off, d.nt, d.np, d.p_off,
-                                                             tv + d.t_off, ctx->d_status);
-            launch_star_volumes(p->mode, d.nt, pos, tv + d.t_off, W, scale, kTau, ctx->d_status, s);
+            // the tets in the parts they came up in (one part after the first block)
+            const long long t0 = k == 0 ? part(d, i) : 0, t1 = k == 0 ? part(d, i + 1) : d.nt;
+            if (k == 0)
+                CK(cudaStreamWaitEvent(s, ctx->first_ev[1 + i], 0));
+            if (t1 <= t0) continue;
+            k_ingest_verts<<<grid_small(t1 - t0), 256, 0, s>>>(stage_tets + 2 * ((size_t)d.t_off + t0), (int)(t1 - t0),
+                                                                d.np, d.p_off, tv + d.t_off + t0, ctx->d_status);
+            launch_star_volumes(p->mode, (int)(t1 - t0), pos, tv + d.t_off + t0, W, scale, kTau, ctx->d_status, s);
             ctx->launches += 2;
         }
         if (d.np)
@@ -1417,6 +1452,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             }
         }
         CK(cudaEventRecord(ctx->pipe_ev[nb + k], s));
+        span(ctx, "compute", ec0, smark(ctx, s));
         if (tiles && host_grid)
         {
             CK(cudaStreamWaitEvent(ctx->d2h, ctx->pipe_ev[nb + k], 0));
@@ -1430,7 +1466,9 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             prm.extent = make_cudaExtent(sizeof(float) * (d.gmax_idx[0] - d.gmin_idx[0] + 1),
                                          d.gmax_idx[1] - d.gmin_idx[1] + 1, d.gmax_idx[2] - d.gmin_idx[2] + 1);
             prm.kind = cudaMemcpyDeviceToHost;
+            const int e0 = smark(ctx, ctx->d2h);
             CK(cudaMemcpy3DAsync(&prm, ctx->d2h));
+            span(ctx, "download", e0, smark(ctx, ctx->d2h));
         }
         for (int l = 0; l < L && !tiles; ++l)
             if (slab_ready[l] == k && host_grid)
@@ -1449,7 +1487,14 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             CK(cudaStreamWaitEvent(s, ctx->pipe_ev[nb + k], 0));
             break;
         }
-    mark(ctx, "compute");
+    mark(ctx, "blocks_done");
+    if (host_grid)
+    {
+        // the last download, on the context's stream's timeline
+        CK(cudaEventRecord(ctx->pipe_ev[2 * nb], ctx->d2h));
+        CK(cudaStreamWaitEvent(s, ctx->pipe_ev[2 * nb], 0));
+        mark(ctx, "downloads_done");
+    }
     if (info)
     {
         CK(cudaMemsetAsync(ctx->d_max, 0, sizeof(float), s));
