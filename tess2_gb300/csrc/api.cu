@@ -381,7 +381,7 @@ extern "C" long long tessgpu_dense_grid_floats(int nblocks, const tessgpu_block*
     std::vector<int> zmin(nblocks), zl;
     for (int b = 0; b < nblocks; ++b)
     {
-        int out9[9];
+        int out9[9] = { 0 };
         tessgpu_block_grid_points(nblocks, blocks, b, p, out9);
         zmin[b] = out9[2];
     }

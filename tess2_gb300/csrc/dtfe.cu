@@ -370,10 +370,10 @@ constexpr int SLICES = 16;  // tets with at most this many z slices visit only t
 
 template <typename T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; };
-template <> struct Vec4<double> { typedef double4 type; };
+template <> struct Vec4<double> { typedef double4_32a type; };
 
 template <typename T, bool VAL64, bool COMPACT>
-struct __align__(16) RasterSmem
+struct __align__(32) RasterSmem
 {
     typedef typename Vec4<T>::type T4;
     // per tet of the current batch (lane = tet slot)
@@ -850,7 +850,6 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
             for (int rbase = 0; rbase < R; rbase += 32)
             {
                 const int r = rbase + lane;
-                int cnt = 0;
                 if (r < R)
                 {
                     while (S.pre[j + 1] <= r) ++j;
