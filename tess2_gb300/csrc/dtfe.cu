@@ -372,7 +372,7 @@ template <typename T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; };
 template <> struct Vec4<double> { typedef double4_32a type; };
 
-template <typename T, bool VAL64, bool COMPACT>
+template <typename T, bool VAL64, bool COMPACT, bool FLAT = false>
 struct __align__(32) RasterSmem
 {
     typedef typename Vec4<T>::type T4;
@@ -386,6 +386,10 @@ struct __align__(32) RasterSmem
     int4   I1[32];                           // iz0, s, local tet index, face masks | sliced flag | row axis
     int    SLC[SLICES][32];                  // per z slice: first row dy << 16 | rows
     int    pre[33];                          // prefix of the tets' row counts
+    // FLAT: a round's points spread over the lanes (per row of the round)
+    T      RN[4][FLAT ? 32 : 1];             // the row's R_k
+    int    RJ[FLAT ? 32 : 1], RI0[FLAT ? 32 : 1], RY[FLAT ? 32 : 1], RZ[FLAT ? 32 : 1];   // tet slot, first x, y, z
+    int    pp[FLAT ? 33 : 1];                // prefix of the rows' point counts
     int    Q[COMPACT ? 64 : 1];              // tets whose box holds grid points, waiting for a batch
     double C64[VAL64 && sizeof(T) == 4 ? 12 : 1][32];   // FP64 values for the fix-up pass
     double W64[VAL64 && sizeof(T) == 4 ? 4 : 1][32];
@@ -451,8 +455,8 @@ __device__ __forceinline__ void unperm3(int ra, V n0, V n1, V n2, V& x, V& y, V&
 // interpolated density when it is inside
 // xi, yi, zi and pyf, pzf are in the tet's row-axis order; hx, gx the row
 // axis' grid step and origin
-template <typename T, bool VAL64, bool COMPACT>
-__device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, COMPACT>& S, int j, int xi, int yi, int zi, float pyf,
+template <typename T, bool VAL64, typename SM>
+__device__ __forceinline__ void raster_point(const SM& S, int j, int xi, int yi, int zi, float pyf,
                                              float pzf, const float4& A0, const float4& A1, const int4& I1,
                                              const T* cx, const T* RN, const T* Bk, float hx, float gx, int ra,
                                              const GridDesc& g, const int4* tv, const float4* pos, float* grid,
@@ -527,17 +531,17 @@ __device__ __forceinline__ void raster_point(const RasterSmem<T, VAL64, COMPACT>
     nassigned++;
 }
 
-template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT>
+template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, bool FLAT>
 __global__ void __launch_bounds__(NW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
          int* fix_list, int* fix_count, Status* st, int t0)
 {
     typedef typename Vec4<T>::type T4;
-    __shared__ RasterSmem<T, VAL64, COMPACT> smem[NW];
+    __shared__ RasterSmem<T, VAL64, COMPACT, FLAT> smem[NW];
     constexpr bool F32 = sizeof(T) == 4;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    RasterSmem<T, VAL64, COMPACT>& S = smem[wid];
+    RasterSmem<T, VAL64, COMPACT, FLAT>& S = smem[wid];
     unsigned long long nexact = 0, nassigned = 0, nfix = 0, nrows = 0, ncand = 0;
     const int n = LIST ? *list_count : total;
     const int nchunks = (n + 31) / 32;
@@ -850,6 +854,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
             for (int rbase = 0; rbase < R; rbase += 32)
             {
                 const int r = rbase + lane;
+                int cnt = 0;   // FLAT: this lane's row's points
                 if (r < R)
                 {
                     while (S.pre[j + 1] <= r) ++j;
@@ -936,11 +941,63 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                                 cx[k] = ck.x;
                                 Bk[k] = ck.w;
                             }
-                            for (int xi = i0; xi <= i1; ++xi)
-                                raster_point<T, VAL64, COMPACT>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk,
-                                                                gst[0], gmn[0], ra, g, tv, pos, grid, owner, nexact,
-                                                                nassigned);
+                            if (FLAT)
+                            {
+#pragma unroll
+                                for (int k = 0; k < 4; ++k)
+                                    S.RN[k][lane] = RN[k];
+                                S.RJ[lane] = j;
+                                S.RI0[lane] = i0;
+                                S.RY[lane] = yi;
+                                S.RZ[lane] = zi;
+                                cnt = i1 - i0 + 1;
+                            }
+                            else
+                                for (int xi = i0; xi <= i1; ++xi)
+                                    raster_point<T, VAL64>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0],
+                                                           gmn[0], ra, g, tv, pos, grid, owner, nexact, nassigned);
                         }
+                    }
+                }
+                if (FLAT)
+                {
+                    // prefix of the rows' point counts, then the points spread over the lanes
+                    int pin = cnt;
+                    for (int o = 1; o < 32; o <<= 1)
+                    {
+                        const int v = __shfl_up_sync(FULL, pin, o);
+                        if (lane >= o) pin += v;
+                    }
+                    S.pp[lane + 1] = pin;
+                    if (lane == 0) S.pp[0] = 0;
+                    __syncwarp();
+                    const int P = S.pp[32];
+                    int rs = 0;
+                    for (int q = lane; q < P; q += 32)
+                    {
+                        while (S.pp[rs + 1] <= q) ++rs;
+                        const int jj = S.RJ[rs];
+                        const int xi = S.RI0[rs] + (q - S.pp[rs]);
+                        const int yi = S.RY[rs], zi = S.RZ[rs];
+                        const float4 A0 = S.A0[jj], A1 = S.A1[jj];
+                        const int4 I1 = S.I1[jj];
+                        const int ra = (I1.w >> 9) & 3;
+                        float gst[3], gmn[3];
+                        perm3(ra, g.step[0], g.step[1], g.step[2], gst[0], gst[1], gst[2]);
+                        perm3(ra, g.gmin[0], g.gmin[1], g.gmin[2], gmn[0], gmn[1], gmn[2]);
+                        const float pyf = yi * gst[1] + gmn[1];
+                        const float pzf = zi * gst[2] + gmn[2];
+                        T cx[4], Bk[4], RN[4];
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            const T4 ck = S.C[k][jj];
+                            cx[k] = ck.x;
+                            Bk[k] = ck.w;
+                            RN[k] = S.RN[k][rs];
+                        }
+                        raster_point<T, VAL64>(S, jj, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0], gmn[0], ra,
+                                               g, tv, pos, grid, owner, nexact, nassigned);
                     }
                 }
                 __syncwarp();
@@ -997,10 +1054,14 @@ void launch_densities(const unsigned long long* W, int n, float mass, double inv
 }
 
 // Launch variants.  Block residency per SM trades registers against latency
-// hiding; COMPACT screens tets with empty boxes out before the setup.  The
-// fastest depends on the GPU, the mesh and the mode, so the caller times them.
-//   0..2: 4/5/6 blocks per SM    3: compact, 5 blocks per SM
-constexpr int N_RASTER_VARIANTS = 4;
+// hiding; COMPACT screens tets with empty boxes out before the setup; FLAT
+// spreads a round's points over the lanes (it pays when a point is expensive,
+// as in FP64 mode, and costs more shared-memory traffic than it saves when a
+// point is cheap).  The fastest depends on the GPU, the mesh and the mode, so
+// the caller times them.
+//   0..2: per-lane rows, 4/5/6 blocks per SM    3: compact, 5 blocks
+//   4..5: compact + flat, 4/5 blocks per SM
+constexpr int N_RASTER_VARIANTS = 6;
 
 template <typename T, bool VAL64, bool LIST>
 static void raster_variant(int variant, long long work, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
@@ -1011,16 +1072,18 @@ static void raster_variant(int variant, long long work, cudaStream_t s, const Bl
     // the double-precision tables need more shared memory: 3 warps per block
     constexpr int NW = (sizeof(T) == 4 && !VAL64) ? 4 : 3;
     const int nblk = grid_for(work, NW * 32, 16);
-#define TG_RASTER(MB, C)                                                                                           \
-    k_raster<T, VAL64, LIST, MB, NW, C><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, \
+#define TG_RASTER(MB, C, F)                                                                                        \
+    k_raster<T, VAL64, LIST, MB, NW, C, F><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, \
                                                                       rho32, rho64, g, tau, grid, owner, fix_list,  \
                                                                       fix_count, st, t0)
     switch (variant)
     {
-    case 1: TG_RASTER(5, false); break;
-    case 2: TG_RASTER(6, false); break;
-    case 3: TG_RASTER(5, true); break;
-    default: TG_RASTER(4, false); break;
+    case 1: TG_RASTER(5, false, false); break;
+    case 2: TG_RASTER(6, false, false); break;
+    case 3: TG_RASTER(5, true, false); break;
+    case 4: TG_RASTER(4, true, true); break;
+    case 5: TG_RASTER(5, true, true); break;
+    default: TG_RASTER(4, false, false); break;
     }
 #undef TG_RASTER
 }
