@@ -228,3 +228,41 @@ def test_incomplete_cells_without_tets(oracle):
     links6 = np.tile(np.array([0, 0, 0, 1, 1, 1], np.float32), (5, 1))
     m, enq = oracle.incomplete_cells(b, links6, last_neighbor=2)
     assert list(m) == [0b11100] * 3 and enq == 9
+
+
+def _shifted_blocks(given):
+    """2x1x2 blocks over an anisotropic, offset domain, for the given-bounds path."""
+    from tess2_gb300 import host
+    p = host.mixture_particles(3000, 17, n_clumps=6, sigma=0.05)
+    scale = np.array([8.0, 1.0, 2.0], np.float32)
+    off = np.array([-3.0, 10.0, 0.0], np.float32)
+    pts = (p * scale + off).astype(np.float32)
+    blocks = host.tessellate(host.decompose(pts, (2, 1, 2), 0.4, domain_min=off, domain_max=off + scale),
+                             processes=1)
+    # grid sizes and given bounds are chosen so that no grid point lies on the
+    # blocks' shared faces (x = 1, z = 1): there the reference's inclusive
+    # bounds test and its trimmed block boxes disagree (src/dense.cpp:279-284
+    # against :615-626) and its deposit lands outside the block's array
+    g = (off - np.array([0.3, 0.1, 0.35], np.float32), off + scale + np.array([0.5, 0.05, 0.2], np.float32)) \
+        if given else None
+    return blocks, g
+
+
+@pytest.mark.parametrize("given", [False, True])
+@pytest.mark.parametrize("alg", [0, 1])
+def test_offset_domain_matches_reference(oracle, given, alg):
+    """GridStepParams' cube-ified bounds (anisotropic, offset domain) and the
+    given-bounds override: the restated oracle against the reference build."""
+    import os
+    from oracle.oracle import REF_SO, Oracle
+    if not os.path.exists(REF_SO):
+        pytest.skip("reference build not present")
+    blocks, g = _shifted_blocks(given)
+    gni = [36, 23, 28]
+    r = oracle.dense(alg, blocks, gni, given=g)
+    ref = Oracle("ref").dense(alg, blocks, gni, given=g)
+    # deposits at grid points outside every block's bounds are dropped by both
+    # (the cube-ified grid reaches past the data in y)
+    assert np.array_equal(bits(r["grid"]), bits(ref["grid"]))
+    assert np.array_equal(r["grid_step"], ref["grid_step"]) and np.array_equal(r["grid_min"], ref["grid_min"])
+    assert r["grid"].sum() > 0
