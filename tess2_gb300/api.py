@@ -5,7 +5,11 @@
   fill_circumcenters src/volume.cpp:6-11      (circumcenter, src/tet.cpp:37-66)
   complete           src/tet.cpp:337-378      (all vertices at once)
   volume             src/volume.cpp:13-54     (all vertices at once)
-  dense              src/dense.cpp:30-103     (DENSE_TESS, DENSE_CIC, plus DENSE_DTFE)
+  dense              src/dense.cpp:30-103     (DENSE_TESS, DENSE_CIC, plus DENSE_DTFE; project)
+  ProjectGrid        src/dense.cpp:881-1023   (project_grid)
+  WriteGrid          src/dense.cpp:751-870    (write_grid, write_last_grid)
+  reorder_neighbors  src/tess-qhull.c:161-225
+  incomplete_cells   src/tess.cpp:492-628
 
 Everything runs in libtess2_gb300.so on the GPU; there is no CPU fallback.
 If the library is missing the calls raise.
