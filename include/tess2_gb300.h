@@ -325,6 +325,34 @@ tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particles, int num_
                                               int num_tets, const float* bounds6, float mass, int mode,
                                               float* d_rho, void* stream);
 
+/* ---- the DTFE surrogate's kernels ------------------------------------ */
+/* A 3-D convolutional network that maps a cloud-in-cell density grid to the
+   DTFE grid.  Device pointers; activations bf16, channels last (voxel
+   (z * Y + y) * X + x, channel fastest); weights bf16 [27 taps][c_out][c_in],
+   tap = (dz * 3 + dy) * 3 + dx for offsets -1..1, zero outside the grid.
+   stream may be NULL.  Nothing is synchronised. */
+
+/* y = act(conv3x3x3(x, w) + bias): act = relu when relu != 0; bias may be
+   NULL; y_bf16 and/or y_f32 receive it.  X a multiple of 16, c_in of 16,
+   c_out of 8 and at most 64.  Tensor cores (bf16 in, f32 accumulation).  The
+   data gradient is the same call on the output gradient with the weights
+   tessgpu_conv3d_prepare_weights flips. */
+tessgpu_status tessgpu_conv3d_fwd(const void* x, int X, int Y, int Z, int c_in, int c_out, const void* w,
+                                  const float* bias, int relu, void* y_bf16, float* y_f32, void* stream);
+/* dw[tap][co][ci] += sum_v dy[v][co] x[v + tap][ci] and db[co] += sum_v dy[v][co]
+   (FP32; db may be NULL); c_in * c_out <= 4096 */
+tessgpu_status tessgpu_conv3d_wgrad(const void* x, const void* dy, int X, int Y, int Z, int c_in, int c_out,
+                                    float* dw, float* db, void* stream);
+/* bf16 weights for the forward pass and, flipped and transposed
+   ([26 - tap][ci][co]), for the data gradient, from FP32 weights */
+tessgpu_status tessgpu_conv3d_prepare_weights(const float* w, int c_out, int c_in, void* w_bf16, void* wt_bf16,
+                                              void* stream);
+/* out = g * (y > 0), bf16 (n values) */
+tessgpu_status tessgpu_relu_grad(const float* g, const void* y, long long n, void* out, void* stream);
+/* one Adam step (bias-corrected; step counts from 1) on FP32 weights */
+tessgpu_status tessgpu_adam(float* w, const float* g, float* m, float* v, int n, float lr, float beta1, float beta2,
+                            float eps, int step, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

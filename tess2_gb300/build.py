@@ -25,6 +25,7 @@ UNITS = {
     "dtfe.cu": ["-fmad=false"],
     "api.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
+    "surrogate.cu": [],
 }
 
 

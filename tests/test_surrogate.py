@@ -1,0 +1,99 @@
+"""The surrogate's kernels against the FP64 CPU oracle (oracle/surrogate_oracle.py),
+and a short training run on fields the plain DTFE path makes."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+
+def _bf16(a):
+    """float32 values exactly representable in bf16 (round to nearest even)."""
+    a = np.ascontiguousarray(a, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
+def test_oracle_gradients_finite_differences():
+    """The oracle's data and weight gradients against finite differences."""
+    from oracle.surrogate_oracle import conv3d, conv3d_dgrad, conv3d_wgrad
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((3, 4, 5, 2))
+    w = rng.standard_normal((27, 3, 2))
+    b = rng.standard_normal(3)
+    dy = rng.standard_normal((3, 4, 5, 3))
+    f = lambda xx, ww, bb: float((dy * conv3d(xx, ww, bb)).sum())
+    dx = conv3d_dgrad(dy, w)
+    dw, db = conv3d_wgrad(x, dy)
+    h = 1e-6
+    for idx in [(0, 0, 0, 0), (1, 2, 3, 1), (2, 3, 4, 0)]:
+        e = np.zeros_like(x); e[idx] = h
+        assert abs((f(x + e, w, b) - f(x - e, w, b)) / (2 * h) - dx[idx]) < 1e-6
+    for idx in [(0, 0, 0), (13, 2, 1), (26, 1, 0)]:
+        e = np.zeros_like(w); e[idx] = h
+        assert abs((f(x, w + e, b) - f(x, w - e, b)) / (2 * h) - dw[idx]) < 1e-6
+    e = np.zeros_like(b); e[1] = h
+    assert abs((f(x, w, b + e) - f(x, w, b - e)) / (2 * h) - db[1]) < 1e-6
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 16), (32, 32)])
+def test_conv3d_kernels_vs_oracle(gpu_ctx, cin, cout):
+    import torch
+    from oracle.surrogate_oracle import conv3d, conv3d_dgrad, conv3d_wgrad
+    from tess2_gb300 import surrogate as S
+    rng = np.random.default_rng(cin * 100 + cout)
+    Z, Y, X = 5, 6, 32
+    x = _bf16(rng.standard_normal((Z, Y, X, cin)).astype(np.float32))
+    w = (rng.standard_normal((27, cout, cin)) * 0.2).astype(np.float32)
+    wq = _bf16(w)
+    b = rng.standard_normal(cout).astype(np.float32)
+    dy = _bf16(rng.standard_normal((Z, Y, X, cout)).astype(np.float32))
+    dev = "cuda:0"
+    tx = torch.from_numpy(x).to(dev).to(torch.bfloat16).reshape(-1, cin)
+    tw = torch.from_numpy(w).to(dev)
+    wb = torch.empty((27, cout, cin), dtype=torch.bfloat16, device=dev)
+    wt = torch.empty((27, cin, cout), dtype=torch.bfloat16, device=dev)
+    S.prepare_weights(tw, cout, cin, wb, wt)
+    tb = torch.from_numpy(b).to(dev)
+    y32 = torch.empty((Z * Y * X, cout), device=dev)
+    S.conv3d_fwd(tx, (Z, Y, X), cin, cout, wb, tb, relu=False, y_f32=y32)
+    ref = conv3d(x, wq, b)
+    torch.cuda.synchronize()
+    assert rel_l2(y32.cpu().numpy(), ref.reshape(-1, cout)) < 1e-5
+    # relu and bf16 output
+    yb = torch.empty((Z * Y * X, cout), dtype=torch.bfloat16, device=dev)
+    S.conv3d_fwd(tx, (Z, Y, X), cin, cout, wb, tb, relu=True, y_bf16=yb)
+    assert rel_l2(yb.float().cpu().numpy(), np.maximum(ref, 0).reshape(-1, cout)) < 1e-2
+    # data gradient through the flipped weights
+    tdy = torch.from_numpy(dy).to(dev).to(torch.bfloat16).reshape(-1, cout)
+    dx = torch.empty((Z * Y * X, cin), device=dev)
+    S.conv3d_fwd(tdy, (Z, Y, X), cout, cin, wt, None, relu=False, y_f32=dx)
+    assert rel_l2(dx.cpu().numpy(), conv3d_dgrad(dy, wq).reshape(-1, cin)) < 1e-5
+    # weight and bias gradient
+    dw = torch.zeros((27, cout, cin), device=dev)
+    db = torch.zeros(cout, device=dev)
+    S.conv3d_wgrad(tx, tdy, (Z, Y, X), cin, cout, dw, db)
+    rdw, rdb = conv3d_wgrad(x, dy)
+    torch.cuda.synchronize()
+    assert rel_l2(dw.cpu().numpy(), rdw) < 1e-5
+    assert rel_l2(db.cpu().numpy(), rdb) < 1e-5
+
+
+@pytest.mark.gpu
+def test_surrogate_learns(gpu_ctx):
+    """A few Adam steps on a handful of small fields lower the loss, and the
+    trained network beats its own input (the CIC grid) against DTFE on the
+    training fields."""
+    import torch
+    from tess2_gb300 import surrogate as S
+    fields = S.make_fields(gpu_ctx, range(5), 20000, 32, processes=1)
+    net = S.Surrogate((32, 32, 32), seed=1)
+    t = [(torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()) for x, y in fields]
+    first = np.mean([net.train_step(x, y, lr=3e-3) for x, y in t])
+    for _ in range(30):
+        last = np.mean([net.train_step(x, y, lr=3e-3) for x, y in t])
+    assert last < 0.7 * first
+    err = np.mean([S.rel_l2(net.forward(x).cpu().numpy(), y.cpu().numpy()) for x, y in t])
+    base = np.mean([S.rel_l2(x.cpu().numpy(), y.cpu().numpy()) for x, y in t])
+    assert err < base
