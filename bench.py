@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64-mode and DENSE_TESS comparison runs")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="skip training and timing the DTFE surrogate network")
+    ap.add_argument("--surrogate-fields", type=int, default=24, help="training fields for the surrogate")
+    ap.add_argument("--surrogate-epochs", type=int, default=10)
     ap.add_argument("--no-rows", action="store_true",
                     help="skip the timings of the stages around the path (reorder_neighbors, incomplete_cells, "
                          "projection, WriteGrid)")
@@ -344,6 +348,54 @@ def time_rows(ctx, batch, blocks, gni, hbm, local):
 
 
 # ---------------------------------------------------------------------------
+# the surrogate network against the plain path
+# ---------------------------------------------------------------------------
+def time_surrogate(args, peaks, local):
+    """Trains the surrogate on fields the plain path makes (131,072 particles ->
+    64^3), then compares fields/s: the network (forward, CIC grid resident)
+    against the plain DTFE path on the GPU (star volumes + rasteriser, tets
+    resident) and against the plain path with its host Delaunay."""
+    import torch
+    from tess2_gb300 import host
+    from tess2_gb300 import surrogate as S
+    from tess2_gb300.api import DENSE_DTFE, Context
+    npart, side = 131072, 64
+    r = S.train_and_evaluate(n_train=args.surrogate_fields, n_val=4, n_particles=npart, side=side,
+                             epochs=args.surrogate_epochs, lr=2e-3)
+    r.pop("net")
+    # the plain path on one such field: host Qhull, then the GPU DTFE pass
+    pts = host.mixture_particles(npart, 424242, frac_uniform=0.5, n_clumps=64, sigma=0.02)
+    t0 = time.time()
+    blk = host.tessellate([host.decompose(pts)[0]], processes=1)
+    t_qhull = time.time() - t0
+    ctx = Context(local)
+    batch = ctx.upload(blk)
+    g = torch.empty(side ** 3, device=f"cuda:{local}")
+    gni = [side] * 3
+    for _ in range(3):
+        batch.dense(DENSE_DTFE, gni, g.data_ptr(), want_info=False)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(10):
+        batch.dense(DENSE_DTFE, gni, g.data_ptr(), want_info=False)
+    e1.record()
+    torch.cuda.synchronize()
+    dtfe_ms = e0.elapsed_time(e1) / 10
+    bf16 = float(peaks.get("bf16_tflops", 1900.0))
+    r.update(plain_gpu_ms=dtfe_ms, plain_host_delaunay_s=t_qhull,
+             fields_per_s=1e3 / r["forward_ms"], plain_gpu_fields_per_s=1e3 / dtfe_ms,
+             plain_with_delaunay_fields_per_s=1.0 / (t_qhull + dtfe_ms * 1e-3),
+             speedup_vs_plain_gpu=dtfe_ms / r["forward_ms"],
+             speedup_vs_plain_with_delaunay=(t_qhull + dtfe_ms * 1e-3) / (r["forward_ms"] * 1e-3),
+             tensor_frac_of_bf16_peak=r["forward_tflops"] / bf16,
+             bf16_peak_source="measured MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
+             kernels="mma.sync m16n8k16 bf16 implicit GEMM (forward, data gradient); FP32 weight gradient")
+    return r
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_gpu(args):
@@ -544,6 +596,8 @@ def run_gpu(args):
     if not args.no_rows:
         rows = time_rows(ctx, batch, blocks, gni, hbm, local)
         extra["rows"] = rows
+    if not args.no_surrogate:
+        extra["surrogate"] = time_surrogate(args, peaks, local)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
