@@ -44,7 +44,8 @@ typedef enum tessgpu_status
     TESSGPU_ERR_LINK_OVERFLOW  = 6,   /* an edge ring exceeded TESSGPU_MAX_LINK tets */
     TESSGPU_ERR_BAD_MESH       = 7,   /* an index out of range or a broken adjacency */
     TESSGPU_ERR_UNSUPPORTED    = 8,
-    TESSGPU_ERR_IO             = 9    /* a file could not be opened or written */
+    TESSGPU_ERR_IO             = 9,   /* a file could not be opened or written */
+    TESSGPU_ERR_TIMEOUT        = 10   /* a bounded wait inside a kernel ran out */
 } tessgpu_status;
 
 /* bounds of the device loops; larger inputs report the overflow codes */
@@ -334,9 +335,10 @@ tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particles, int num_
 
 /* y = act(conv3x3x3(x, w) + bias): act = relu when relu != 0; bias may be
    NULL; y_bf16 and/or y_f32 receive it.  X a multiple of 16, c_in of 16,
-   c_out of 8 and at most 64.  Tensor cores (bf16 in, f32 accumulation).  The
-   data gradient is the same call on the output gradient with the weights
-   tessgpu_conv3d_prepare_weights flips. */
+   c_out of 8 and at most 64.  Tensor cores (bf16 in, f32 accumulation):
+   tcgen05 with tensor-memory accumulators when c_in and c_out are 16 or 32,
+   mma.sync otherwise.  The data gradient is the same call on the output
+   gradient with the weights tessgpu_conv3d_prepare_weights flips. */
 tessgpu_status tessgpu_conv3d_fwd(const void* x, int X, int Y, int Z, int c_in, int c_out, const void* w,
                                   const float* bias, int relu, void* y_bf16, float* y_f32, void* stream);
 /* dw[tap][co][ci] += sum_v dy[v][co] x[v + tap][ci] and db[co] += sum_v dy[v][co]
@@ -347,6 +349,12 @@ tessgpu_status tessgpu_conv3d_wgrad(const void* x, const void* dy, int X, int Y,
    ([26 - tap][ci][co]), for the data gradient, from FP32 weights */
 tessgpu_status tessgpu_conv3d_prepare_weights(const float* w, int c_out, int c_in, void* w_bf16, void* wt_bf16,
                                               void* stream);
+/* engine 0 (the default): tcgen05 where the channel counts allow; 1: the
+   mma.sync kernel for every shape.  Process-wide. */
+tessgpu_status tessgpu_conv3d_set_engine(int engine);
+/* Synchronises stream; TESSGPU_ERR_TIMEOUT (and the flag cleared) when a
+   tcgen05 convolution gave up on a bounded wait since the last check. */
+tessgpu_status tessgpu_conv3d_check(void* stream);
 /* out = g * (y > 0), bf16 (n values) */
 tessgpu_status tessgpu_relu_grad(const float* g, const void* y, long long n, void* out, void* stream);
 /* one Adam step (bias-corrected; step counts from 1) on FP32 weights */

@@ -25,7 +25,8 @@ DENSE_TESS, DENSE_CIC, DENSE_DTFE = 0, 1, 2
 MODE_MIXED, MODE_FP64 = 0, 1
 
 _STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no CUDA device", 4: "star overflow",
-           5: "face overflow", 6: "edge ring overflow", 7: "malformed mesh", 8: "unsupported", 9: "I/O error"}
+           5: "face overflow", 6: "edge ring overflow", 7: "malformed mesh", 8: "unsupported", 9: "I/O error",
+           10: "a bounded wait inside a kernel ran out"}
 
 
 class TessGpuError(RuntimeError):

@@ -113,6 +113,283 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
     }
 }
 
+// ---------------------------------------------------------------------------
+// the same forward pass on the 5th-generation tensor cores (tcgen05)
+// ---------------------------------------------------------------------------
+// Rows of the GEMM are positions u = r * (X + 2) + x + 1 of the x-padded row
+// space (r = z * Y + y the x row, x in -1..X, the two halo positions zero), so
+// that a shift by dx is a shift by dx positions.  A persistent CTA of 128
+// threads keeps all 27 taps' weights in shared memory (K-major core-matrix
+// layout: 8 rows x 16 bytes per core matrix) and takes tiles of 128 positions
+// (the M of one MMA) x c_out (its N).  Per (dz, dy) it gathers one slab: the
+// 130 positions u0 - 1 .. u0 + 128 of the x row shifted by (dy, dz), stored
+// as c_in / 8 planes of 16-byte rows; the three taps dx = -1, 0, 1 then read
+// that slab at row offsets 0, 1, 2 — start addresses 16 bytes apart in the
+// shared-memory descriptor — so each input row is gathered 9 times per output
+// tile, not 27.  Slabs are gathered with cp.async (zero-filled outside the
+// grid) into a ring of STAGES buffers, STAGES - 2 slabs ahead of the one the
+// MMAs read; one thread issues the tcgen05.mma (kind::f16: bf16 x bf16 ->
+// f32, accumulating in tensor memory) and commits them to the buffer's
+// mbarrier, which says when the buffer may be refilled.  The epilogue reads
+// row tid of the accumulator with tcgen05.ld, adds the bias, applies ReLU and
+// stores the interior positions.  Every wait is bounded: on a timeout the
+// kernel raises *err, drains its copies, waits a bounded time for its MMAs,
+// frees its tensor memory and returns.
+constexpr int TC_M = 128;      // GEMM rows per tile
+constexpr int TC_SLAB = 136;   // rows per slab plane (>= 130, a multiple of 8)
+constexpr int TC_PLANE = TC_SLAB * 16;
+
+template <int COUT, int CIN>
+struct TcLayout
+{
+    static constexpr int TAPB = COUT * CIN * 2;    // one tap's weights
+    static constexpr int WBYTES = 27 * TAPB;
+    static constexpr int SBYTES = (CIN / 8) * TC_PLANE;
+    static constexpr int STAGES = CIN == 32 ? 5 : 6;
+    static constexpr int AHEAD = STAGES - 2;   // slabs in flight ahead of the MMAs
+    static constexpr int BAR = WBYTES + STAGES * SBYTES;   // STAGES mbarriers, then the tensor-memory address
+    static constexpr int TOTAL = BAR + 8 * STAGES + 16;
+    static constexpr int TCOLS = COUT < 32 ? 32 : COUT;   // a power of two >= 32
+};
+
+__device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;   // stride between core matrices along K
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;   // stride between 8-row groups
+    d |= (uint64_t)1 << 46;                       // descriptor version; base offset 0; no swizzle
+    return d;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+{
+    for (int it = 0; it < (1 << 22); ++it)
+    {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done)
+                     : "r"(mbar), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// the slab entries one thread gathers for one tile: j = tid and, for tid < 2, j = 128 + tid
+struct SlabRows
+{
+    int x[2], y[2], z[2];
+    bool valid[2];
+};
+
+__device__ __forceinline__ void slab_rows(SlabRows& s, unsigned u0, int tid, int X, int Y, unsigned XP, unsigned U)
+{
+#pragma unroll
+    for (int e = 0; e < 2; ++e)
+    {
+        const long long u = (long long)u0 - 1 + tid + e * 128;
+        const unsigned uu = u < 0 ? 0u : (unsigned)u;
+        const unsigned r = uu / XP;
+        s.x[e] = (int)(uu - r * XP) - 1;
+        s.y[e] = (int)(r % (unsigned)Y);
+        s.z[e] = (int)(r / (unsigned)Y);
+        s.valid[e] = u >= 0 && uu < U && s.x[e] >= 0 && s.x[e] < X && (e == 0 || tid < 2);
+    }
+}
+
+template <int COUT, int CIN>
+__global__ void __launch_bounds__(128) k_conv3d_fwd_tc(const __nv_bfloat16* __restrict__ x, int X, int Y, int Z,
+                                                       const __nv_bfloat16* __restrict__ w,
+                                                       const float* __restrict__ bias, int relu,
+                                                       __nv_bfloat16* y_bf16, float* y_f32, int* err)
+{
+    using L = TcLayout<COUT, CIN>;
+    constexpr int CH = CIN / 8;   // 16-byte chunks per row
+    constexpr int S = L::STAGES;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ float sbias[COUT];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const unsigned XP = (unsigned)X + 2;
+    const unsigned U = (unsigned)Y * (unsigned)Z * XP;   // < 2^31, checked by the launcher
+    const int tiles = (int)((U + TC_M - 1) / TC_M);
+    const int ntl = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int N = 9 * ntl;   // slabs this CTA fills
+
+    // all taps' weights -> shared memory: row co of tap t, chunk c at
+    // t * TAPB + (co / 8) * (CH * 128) + c * 128 + (co % 8) * 16
+    const uint4* wg = reinterpret_cast<const uint4*>(w);
+    for (int i = tid; i < 27 * COUT * CH; i += 128)
+    {
+        const int t = i / (COUT * CH), rem = i % (COUT * CH), r = rem / CH, c = rem % CH;
+        *reinterpret_cast<uint4*>(smem + t * L::TAPB + (r / 8) * (CH * 128) + c * 128 + (r % 8) * 16) = wg[i];
+    }
+    if (tid < COUT) sbias[tid] = bias ? bias[tid] : 0.0f;
+    const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t slab_a = s_base + L::WBYTES;   // buffer b at slab_a + b * SBYTES
+    const uint32_t mb0 = s_base + L::BAR;         // buffer b's mbarrier at mb0 + 8 b
+    if (tid == 0)
+    {
+        for (int b = 0; b < S; ++b)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb0 + 8 * b));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 0)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(mb0 + 8 * S),
+                     "r"(L::TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tbase = *reinterpret_cast<const uint32_t*>(smem + L::BAR + 8 * S);
+    // instruction descriptor: D f32, A and B bf16, both K-major, N = COUT, M = 128
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) |
+                           ((uint32_t)(TC_M >> 4) << 24);
+
+    SlabRows pr;   // the producer's tile
+    auto gather = [&](int m) {
+        const int g = m % 9;
+        if (g == 0) slab_rows(pr, (unsigned)(blockIdx.x + (m / 9) * gridDim.x) * TC_M, tid, X, Y, XP, U);
+        const int dz = g / 3 - 1, dy = g % 3 - 1;
+        const uint32_t buf = slab_a + (m % S) * L::SBYTES;
+#pragma unroll
+        for (int e = 0; e < 2; ++e)
+        {
+            if (e == 1 && tid >= 2) break;
+            const int sy = pr.y[e] + dy, sz = pr.z[e] + dz;
+            const bool in = pr.valid[e] && sy >= 0 && sy < Y && sz >= 0 && sz < Z;
+            const long long sv = in ? ((long long)sz * Y + sy) * X + pr.x[e] : 0;
+            const __nv_bfloat16* src = x + sv * CIN;
+            const uint32_t dst = buf + (tid + e * 128) * 16;
+            const uint32_t bytes = in ? 16u : 0u;   // 0: zero fill, nothing read
+#pragma unroll
+            for (int c = 0; c < CH; ++c)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst + c * TC_PLANE),
+                             "l"(src + c * 8), "r"(bytes)
+                             : "memory");
+        }
+    };
+
+#pragma unroll 1
+    for (int m = 0; m < L::AHEAD; ++m)
+    {
+        if (m < N) gather(m);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    bool ok = true;
+    int committed = -1;   // the last slab whose MMAs were committed
+#pragma unroll 1
+    for (int n = 0; n < N; ++n)
+    {
+        const int m = n + L::AHEAD;
+        bool mine = true;
+        if (m < N)
+        {
+            // buffer m % S last held slab m - S: its MMAs must be done
+            if (m >= S) mine = mbar_wait(mb0 + 8 * (m % S), (uint32_t)(((m - S) / S) & 1));
+            if (mine) gather(m);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group %0;" ::"n"(L::AHEAD) : "memory");   // slab n has landed
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        ok = __syncthreads_and(mine);
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const int g = n % 9;
+        if (tid == 0)
+        {
+            const uint32_t a0 = slab_a + (n % S) * L::SBYTES;
+#pragma unroll
+            for (int sh = 0; sh < 3; ++sh)
+#pragma unroll
+                for (int ks = 0; ks < CIN / 16; ++ks)
+                {
+                    const int tap = g * 3 + sh;
+                    const uint64_t da = umma_sdesc(a0 + sh * 16 + ks * 2 * TC_PLANE, TC_PLANE, 128);
+                    const uint64_t db = umma_sdesc(s_base + tap * L::TAPB + ks * 256, 128, CH * 128);
+                    const uint32_t acc = (g > 0 || sh > 0 || ks > 0) ? 1u : 0u;
+                    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tbase),
+                                 "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             mb0 + 8 * (n % S))
+                         : "memory");
+        }
+        committed = n;
+        if (g != 8) continue;
+        // epilogue of tile n / 9: the slab's commit covers every MMA before it
+        ok = __syncthreads_and(mbar_wait(mb0 + 8 * (n % S), (uint32_t)((n / S) & 1)));
+        if (!ok) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        uint32_t acc[COUT];
+        const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16);
+#pragma unroll
+        for (int c = 0; c < COUT; c += 16)
+            tmem_ld16(taddr + c, acc + c);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        const unsigned u = (unsigned)(blockIdx.x + (n / 9) * gridDim.x) * TC_M + tid;
+        const unsigned r = u / XP;
+        const int ox = (int)(u - r * XP) - 1;
+        if (u < U && ox >= 0 && ox < X)
+        {
+            const long long vox = (long long)r * X + ox;
+            float f[COUT];
+#pragma unroll
+            for (int c = 0; c < COUT; ++c)
+            {
+                f[c] = __uint_as_float(acc[c]) + sbias[c];
+                if (relu) f[c] = fmaxf(f[c], 0.0f);
+            }
+            if (y_bf16)
+#pragma unroll
+                for (int c = 0; c < COUT; c += 8)
+                    *reinterpret_cast<uint4*>(y_bf16 + vox * COUT + c) =
+                        make_uint4(pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
+                                   pack_bf16(f[c + 4], f[c + 5]), pack_bf16(f[c + 6], f[c + 7]));
+            if (y_f32)
+#pragma unroll
+                for (int c = 0; c < COUT; c += 4)
+                    *reinterpret_cast<float4*>(y_f32 + vox * COUT + c) = make_float4(f[c], f[c + 1], f[c + 2], f[c + 3]);
+        }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (!ok)
+    {
+        if (tid == 0)
+        {
+            atomicExch(err, 1);
+            // a bounded wait for the MMAs still in flight before the memory goes
+            if (committed >= 0) mbar_wait(mb0 + 8 * (committed % S), (uint32_t)((committed / S) & 1));
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
+}
+
 // dw[tap][co][ci] += sum_v dy[v][co] x[v + tap][ci]; db[co] += sum_v dy[v][co]
 // (FP32 accumulation).  Block: one tap, VB voxels of one x row band; thread
 // (co, ci) pairs.
@@ -205,7 +482,62 @@ int blocks_for(long long n, int t)
     return (int)(b < 1 ? 1 : (b > 65535LL * 8 ? 65535LL * 8 : b));
 }
 
+__device__ int g_conv_err;   // raised by a tcgen05 kernel whose bounded wait ran out
+int g_conv_engine = 0;       // 0: tcgen05 where the channel counts allow, 1: mma.sync only
+
+template <int COUT, int CIN>
+tessgpu_status launch_fwd_tc(const __nv_bfloat16* x, int X, int Y, int Z, const __nv_bfloat16* w, const float* bias,
+                             int relu, __nv_bfloat16* yb, float* yf, cudaStream_t s)
+{
+    using L = TcLayout<COUT, CIN>;
+    static int resident[64];   // CTAs resident on the whole device, per device ordinal
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
+    if (!resident[dev])
+    {
+        if (cudaFuncSetAttribute(k_conv3d_fwd_tc<COUT, CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL) !=
+            cudaSuccess)
+            return TESSGPU_ERR_CUDA;
+        int per_sm = 0, sms = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_fwd_tc<COUT, CIN>, 128, L::TOTAL);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        // tensor memory: 512 columns per SM
+        per_sm = per_sm < 1 ? 1 : (per_sm > 512 / L::TCOLS ? 512 / L::TCOLS : per_sm);
+        resident[dev] = per_sm * (sms > 0 ? sms : 1);
+    }
+    int* err = nullptr;
+    if (cudaGetSymbolAddress((void**)&err, g_conv_err) != cudaSuccess) return TESSGPU_ERR_CUDA;
+    const long long U = (long long)Y * Z * (X + 2);
+    if (U + TC_M >= (1LL << 31)) return TESSGPU_ERR_UNSUPPORTED;
+    const long long tiles = (U + TC_M - 1) / TC_M;
+    const int grid = (int)(tiles < resident[dev] ? tiles : resident[dev]);
+    k_conv3d_fwd_tc<COUT, CIN><<<grid, 128, L::TOTAL, s>>>(x, X, Y, Z, w, bias, relu, yb, yf, err);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
 }  // namespace
+
+extern "C" tessgpu_status tessgpu_conv3d_set_engine(int engine)
+{
+    if (engine != 0 && engine != 1) return TESSGPU_ERR_INVALID;
+    g_conv_engine = engine;
+    return TESSGPU_OK;
+}
+
+extern "C" tessgpu_status tessgpu_conv3d_check(void* stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    int h = 0;
+    const int zero = 0;
+    if (cudaMemcpyFromSymbolAsync(&h, g_conv_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return TESSGPU_ERR_CUDA;
+    if (!h) return TESSGPU_OK;
+    if (cudaMemcpyToSymbolAsync(g_conv_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return TESSGPU_ERR_CUDA;
+    return TESSGPU_ERR_TIMEOUT;
+}
 
 extern "C" tessgpu_status tessgpu_conv3d_fwd(const void* x, int X, int Y, int Z, int cin, int cout, const void* w,
                                              const float* bias, int relu, void* y_bf16, float* y_f32, void* stream)
@@ -219,6 +551,15 @@ extern "C" tessgpu_status tessgpu_conv3d_fwd(const void* x, int X, int Y, int Z,
     const __nv_bfloat16* xx = (const __nv_bfloat16*)x;
     const __nv_bfloat16* ww = (const __nv_bfloat16*)w;
     __nv_bfloat16* yb = (__nv_bfloat16*)y_bf16;
+    if (g_conv_engine == 0)
+    {
+        if ((long long)Y * Z * (X + 2) + TC_M >= (1LL << 31))
+            ;   // positions past 32 bits: the mma.sync kernel below
+        else if (cin == 16 && cout == 16) return launch_fwd_tc<16, 16>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        if (cin == 16 && cout == 32) return launch_fwd_tc<32, 16>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        if (cin == 32 && cout == 16) return launch_fwd_tc<16, 32>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        if (cin == 32 && cout == 32) return launch_fwd_tc<32, 32>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+    }
     switch (cout / 8)
     {
     case 1: k_conv3d_fwd<1><<<nb, 128, 0, s>>>(xx, X, Y, Z, cin, ww, bias, relu, yb, y_f32); break;

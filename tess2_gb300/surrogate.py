@@ -34,6 +34,8 @@ def _lib():
         "tessgpu_relu_grad": (i, [vp, vp, ctypes.c_longlong, vp, vp]),
         "tessgpu_adam": (i, [vp, vp, vp, vp, i, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, i,
                              vp]),
+        "tessgpu_conv3d_set_engine": (i, [i]),
+        "tessgpu_conv3d_check": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -55,6 +57,21 @@ def conv3d_fwd(x, shape, cin, cout, w_bf16, bias=None, relu=False, y_bf16=None, 
     Z, Y, X = shape
     _ok(_lib().tessgpu_conv3d_fwd(_p(x), X, Y, Z, cin, cout, _p(w_bf16), _p(bias), 1 if relu else 0, _p(y_bf16),
                                   _p(y_f32), stream), "tessgpu_conv3d_fwd")
+
+
+ENGINE_TCGEN05, ENGINE_MMA_SYNC = 0, 1
+
+
+def set_engine(engine):
+    """ENGINE_TCGEN05 (the default: tcgen05 with tensor-memory accumulators
+    where c_in and c_out are 16 or 32) or ENGINE_MMA_SYNC (mma.sync for every
+    shape); process-wide."""
+    _ok(_lib().tessgpu_conv3d_set_engine(engine), "tessgpu_conv3d_set_engine")
+
+
+def check(stream=None):
+    """Synchronises; raises if a tcgen05 convolution gave up on a bounded wait."""
+    _ok(_lib().tessgpu_conv3d_check(stream), "tessgpu_conv3d_check")
 
 
 def conv3d_wgrad(x, dy, shape, cin, cout, dw, db=None, stream=None):
@@ -202,6 +219,39 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
+def forward_ms(net, x, engine=ENGINE_TCGEN05, reps=10):
+    """Mean forward time (ms, CUDA events) of net on the resident input x with
+    the given convolution engine; the engine is reset to tcgen05 after."""
+    import torch
+    set_engine(engine)
+    try:
+        for _ in range(3):
+            net.forward(x)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            net.forward(x)
+        e1.record()
+        torch.cuda.synchronize()
+        check()
+    finally:
+        set_engine(ENGINE_TCGEN05)
+    return e0.elapsed_time(e1) / reps
+
+
+def forward_throughput(side, engine=ENGINE_TCGEN05, reps=5, seed=3):
+    """(ms, TFLOP/s) of one forward pass of a randomly initialised network on
+    a side^3 grid of random log densities."""
+    import torch
+    net = Surrogate((side, side, side), seed=seed)
+    g = torch.Generator(device=net.dev).manual_seed(seed)
+    x = torch.rand(side ** 3, device=net.dev, generator=g)
+    ms = forward_ms(net, x, engine=engine, reps=reps)
+    return ms, forward_flops(net.shape) / (ms * 1e-3) / 1e12
+
+
 def train_and_evaluate(n_train=32, n_val=8, n_particles=262144, side=64, epochs=8, lr=2e-3, seed=7, log=None):
     """Trains on fields the plain path makes and reports validation error, the
     CIC input's own error (the method without the network), and throughputs."""
@@ -251,7 +301,8 @@ def train_and_evaluate(n_train=32, n_val=8, n_particles=262144, side=64, epochs=
     torch.cuda.synchronize()
     fwd_ms = e0.elapsed_time(e1) / reps
     flops = forward_flops(net.shape)
-    return dict(n_train=n_train, n_val=n_val, particles=n_particles, grid=side, epochs=epochs, steps=steps,
+    fwd_mma_ms = forward_ms(net, x, engine=ENGINE_MMA_SYNC)
+    return dict(forward_mma_sync_ms=fwd_mma_ms, n_train=n_train, n_val=n_val, particles=n_particles, grid=side, epochs=epochs, steps=steps,
                 train_mse=losses, val_rel_l2=float(np.mean(errs)), val_rel_l2_max=float(np.max(errs)),
                 cic_rel_l2=float(np.mean(base)), fields_s=t_fields, train_s=t_train,
                 train_step_ms=1e3 * t_train / max(steps, 1), forward_ms=fwd_ms, forward_gflop=flops / 1e9,

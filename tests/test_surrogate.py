@@ -36,14 +36,30 @@ def test_oracle_gradients_finite_differences():
     assert abs((f(x, w, b + e) - f(x, w, b - e)) / (2 * h) - db[1]) < 1e-6
 
 
+@pytest.fixture
+def engine(request):
+    from tess2_gb300 import surrogate as S
+    S.set_engine(request.param)
+    yield request.param
+    S.check()
+    S.set_engine(S.ENGINE_TCGEN05)
+
+
+# shapes: tiles of 128 x-padded positions that cross x rows; a ragged last
+# tile; a grid smaller than one tile
+SHAPES = [(5, 6, 32), (3, 7, 48), (1, 2, 16)]
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("engine", [0, 1], ids=["tcgen05", "mma_sync"], indirect=True)
+@pytest.mark.parametrize("shape", SHAPES, ids=["5x6x32", "3x7x48", "1x2x16"])
 @pytest.mark.parametrize("cin,cout", [(16, 16), (16, 32), (32, 16), (32, 32)])
-def test_conv3d_kernels_vs_oracle(gpu_ctx, cin, cout):
+def test_conv3d_kernels_vs_oracle(gpu_ctx, engine, shape, cin, cout):
     import torch
     from oracle.surrogate_oracle import conv3d, conv3d_dgrad, conv3d_wgrad
     from tess2_gb300 import surrogate as S
     rng = np.random.default_rng(cin * 100 + cout)
-    Z, Y, X = 5, 6, 32
+    Z, Y, X = shape
     x = _bf16(rng.standard_normal((Z, Y, X, cin)).astype(np.float32))
     w = (rng.standard_normal((27, cout, cin)) * 0.2).astype(np.float32)
     wq = _bf16(w)
@@ -78,6 +94,34 @@ def test_conv3d_kernels_vs_oracle(gpu_ctx, cin, cout):
     torch.cuda.synchronize()
     assert rel_l2(dw.cpu().numpy(), rdw) < 1e-5
     assert rel_l2(db.cpu().numpy(), rdb) < 1e-5
+    S.check()
+
+
+@pytest.mark.gpu
+def test_conv3d_engines_agree_large(gpu_ctx):
+    """tcgen05 and mma.sync on a 64 x 48 x 80 grid, 32 -> 32 channels: the same
+    bf16 products, FP32 sums in another order."""
+    import torch
+    from tess2_gb300 import surrogate as S
+    Z, Y, X, c = 64, 48, 80, 32
+    g = torch.Generator(device="cuda:0").manual_seed(7)
+    x = torch.randn((Z * Y * X, c), device="cuda:0", generator=g).to(torch.bfloat16)
+    w = torch.randn((27, c, c), device="cuda:0", generator=g) * 0.1
+    wb = torch.empty((27, c, c), dtype=torch.bfloat16, device="cuda:0")
+    wt = torch.empty_like(wb)
+    S.prepare_weights(w, c, c, wb, wt)
+    b = torch.randn(c, device="cuda:0", generator=g)
+    out = {}
+    for e in (S.ENGINE_TCGEN05, S.ENGINE_MMA_SYNC):
+        S.set_engine(e)
+        y = torch.full((Z * Y * X, c), float("nan"), device="cuda:0")
+        S.conv3d_fwd(x, (Z, Y, X), c, c, wb, b, relu=True, y_f32=y)
+        out[e] = y
+    S.set_engine(S.ENGINE_TCGEN05)
+    S.check()
+    a, m = out[S.ENGINE_TCGEN05], out[S.ENGINE_MMA_SYNC]
+    assert torch.isfinite(a).all()
+    assert float((a - m).abs().max()) < 1e-4 * float(m.abs().max())
 
 
 @pytest.mark.gpu
