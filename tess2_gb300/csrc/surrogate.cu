@@ -118,26 +118,40 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 // ---------------------------------------------------------------------------
 // Rows of the GEMM are positions u = r * (X + 2) + x + 1 of the x-padded row
 // space (r = z * Y + y the x row, x in -1..X, the two halo positions zero), so
-// that a shift by dx is a shift by dx positions.  A persistent CTA of 128
-// threads keeps all 27 taps' weights in shared memory (K-major core-matrix
-// layout: 8 rows x 16 bytes per core matrix) and takes tiles of 128 positions
-// (the M of one MMA) x c_out (its N).  Per (dz, dy) it gathers one slab: the
-// 130 positions u0 - 1 .. u0 + 128 of the x row shifted by (dy, dz), stored
-// as c_in / 8 planes of 16-byte rows; the three taps dx = -1, 0, 1 then read
-// that slab at row offsets 0, 1, 2 — start addresses 16 bytes apart in the
-// shared-memory descriptor — so each input row is gathered 9 times per output
-// tile, not 27.  Slabs are gathered with cp.async (zero-filled outside the
-// grid) into a ring of STAGES buffers, STAGES - 2 slabs ahead of the one the
-// MMAs read; one thread issues the tcgen05.mma (kind::f16: bf16 x bf16 ->
-// f32, accumulating in tensor memory) and commits them to the buffer's
-// mbarrier, which says when the buffer may be refilled.  The epilogue reads
-// row tid of the accumulator with tcgen05.ld, adds the bias, applies ReLU and
-// stores the interior positions.  Every wait is bounded: on a timeout the
-// kernel raises *err, drains its copies, waits a bounded time for its MMAs,
-// frees its tensor memory and returns.
+// that a shift by dx is a shift by dx positions.  One persistent CTA per SM
+// keeps all 27 taps' weights in shared memory (K-major core-matrix layout: 8
+// rows x 16 bytes per core matrix) and takes tiles of 128 positions (the M of
+// one MMA) x c_out (its N).  Per (dz, dy) a tile needs one slab: the 130
+// positions u0 - 1 .. u0 + 128 of the x row shifted by (dy, dz), stored as
+// c_in / 8 planes of 16-byte rows; the three taps dx = -1, 0, 1 read that slab
+// at row offsets 0, 1, 2 (start addresses 16 bytes apart in the shared-memory
+// descriptor), so each input row is gathered 9 times per output tile, not 27.
+// Warp roles, all synchronised through mbarriers (no block-wide barrier in
+// the loop):
+//   warps 4-11 producers: gather slabs with cp.async (zero-filled outside the
+//              grid) into a ring of STAGES buffers; a buffer's "full" barrier
+//              completes when every producer's copies for it have landed
+//              (cp.async.mbarrier.arrive), so the whole ring can be in flight;
+//   warp 12    allocates tensor memory; one lane issues tcgen05.mma (kind::f16,
+//              bf16 x bf16 -> f32) for each slab and commits them to the
+//              buffer's "empty" barrier, and each finished tile to its
+//              accumulator's "full" barrier (two accumulators alternate);
+//   warps 0-3  epilogue: tcgen05.ld of row tid (warp w reads lanes 32w..),
+//              release the accumulator, bias, ReLU, store the interior rows.
+// Every wait is bounded; a timed-out wait raises an abort flag that ends every
+// role's loop, the kernel reports it in *err, drains its copies, waits a
+// bounded time for its MMAs and frees its tensor memory.
 constexpr int TC_M = 128;      // GEMM rows per tile
 constexpr int TC_SLAB = 136;   // rows per slab plane (>= 130, a multiple of 8)
 constexpr int TC_PLANE = TC_SLAB * 16;
+constexpr int TC_PRODUCERS = 256;      // 8 producer warps
+constexpr int TC_THREADS = 128 + TC_PRODUCERS + 32;   // 4 epilogue warps, the producers, 1 MMA warp
+constexpr int TC_MMA_WARP = (128 + TC_PRODUCERS) / 32;
+#ifndef TESSGPU_CONV_TILES
+#define TESSGPU_CONV_TILES 1
+#endif
+constexpr int TC_T = TESSGPU_CONV_TILES;   // tiles whose MMAs interleave (independent accumulators)
+constexpr int TC_SMEM = 227 * 1024;    // dynamic shared memory a CTA may opt into
 
 template <int COUT, int CIN>
 struct TcLayout
@@ -145,11 +159,19 @@ struct TcLayout
     static constexpr int TAPB = COUT * CIN * 2;    // one tap's weights
     static constexpr int WBYTES = 27 * TAPB;
     static constexpr int SBYTES = (CIN / 8) * TC_PLANE;
-    static constexpr int STAGES = CIN == 32 ? 5 : 6;
-    static constexpr int AHEAD = STAGES - 2;   // slabs in flight ahead of the MMAs
-    static constexpr int BAR = WBYTES + STAGES * SBYTES;   // STAGES mbarriers, then the tensor-memory address
-    static constexpr int TOTAL = BAR + 8 * STAGES + 16;
-    static constexpr int TCOLS = COUT < 32 ? 32 : COUT;   // a power of two >= 32
+    static constexpr int FIT = (TC_SMEM - WBYTES - 512) / SBYTES;
+    static constexpr int STAGES = FIT < 24 ? FIT : 24;
+    static constexpr int BAR = WBYTES + STAGES * SBYTES;   // mbarriers, tensor-memory address, abort flag
+    // full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], fin
+    static constexpr int OFF_FULL = BAR, OFF_EMPTY = BAR + 8 * STAGES, OFF_ACCF = BAR + 16 * STAGES,
+                         OFF_ACCE = OFF_ACCF + 16, OFF_FIN = OFF_ACCE + 16, OFF_TMEM = OFF_FIN + 8,
+                         OFF_ABORT = OFF_TMEM + 4, OFF_BIAS = OFF_ABORT + 4;
+    static constexpr int TOTAL = OFF_BIAS + 4 * COUT;
+    // two sets of TC_T accumulators of COUT columns; a power of two >= 32
+    static constexpr int TCOLS = 2 * TC_T * COUT <= 32 ? 32 : (2 * TC_T * COUT <= 64 ? 64 : (2 * TC_T * COUT <= 128 ? 128 : (2 * TC_T * COUT <= 256 ? 256 : 512)));
+    static_assert(2 * TC_T * COUT <= 512, "tensor memory");
+    static_assert(STAGES >= 3, "shared memory too small for the slab ring");
+    static_assert(TOTAL <= TC_SMEM, "shared memory");
 };
 
 __device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
@@ -161,19 +183,48 @@ __device__ __forceinline__ uint64_t umma_sdesc(uint32_t saddr, uint32_t lbo, uin
     return d;
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity)
+// the thread sleeps in try_wait until the phase completes or about 50 us pass
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity)
 {
-    for (int it = 0; it < (1 << 22); ++it)
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(mbar), "r"(parity), "n"(50000)
+                 : "memory");
+    return done != 0;
+}
+
+// bounded wait (about a second); gives up when another role raised the abort
+// flag, and raises it when the bound runs out
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t parity, volatile int* abort)
+{
+    for (int it = 0; it < 20000; ++it)
     {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done)
-                     : "r"(mbar), "r"(parity)
-                     : "memory");
-        if (done) return true;
+        if (mbar_try(mbar, parity)) return true;
+        if (*abort) return false;
     }
+    *abort = 1;
     return false;
+}
+
+// the same outcome on every lane of the warp
+__device__ __forceinline__ bool warp_wait(uint32_t mbar, uint32_t parity, volatile int* abort)
+{
+    return __all_sync(0xffffffffu, mbar_wait_or_abort(mbar, parity, abort));
+}
+
+// true on one lane of the (fully active) warp
+__device__ __forceinline__ bool elect_one()
+{
+    uint32_t e;
+    asm volatile("{\n\t.reg .pred P;\n\telect.sync _|P, 0xffffffff;\n\tselp.u32 %0, 1, 0, P;\n\t}" : "=r"(e));
+    return e != 0;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar)
+{
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r)
@@ -191,67 +242,96 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-// the slab entries one thread gathers for one tile: j = tid and, for tid < 2, j = 128 + tid
-struct SlabRows
+// A slab holds 130 entries x CH 16-byte chunks; producer thread q copies
+// chunks i = q + k * TC_PRODUCERS (entry i / CH, chunk i % CH), so that
+// consecutive threads read consecutive 16 bytes.  Per tile it keeps, for each
+// of its chunks, the source element of the unshifted entry and a 9-bit mask of
+// the (dz, dy) shifts that stay inside the grid.
+template <int CH>
+struct SlabItems
 {
-    int x[2], y[2], z[2];
-    bool valid[2];
+    static constexpr int K = (130 * CH + TC_PRODUCERS - 1) / TC_PRODUCERS;
+    long long src[K];   // element index of the chunk for dz = dy = 0
+    unsigned mask[K];   // bit g: shift (g / 3 - 1, g % 3 - 1) is inside the grid
 };
 
-__device__ __forceinline__ void slab_rows(SlabRows& s, unsigned u0, int tid, int X, int Y, unsigned XP, unsigned U)
+template <int CH>
+__device__ __forceinline__ void slab_items(SlabItems<CH>& s, unsigned u0, int q, int X, int Y, int Z, unsigned XP,
+                                           unsigned U)
 {
 #pragma unroll
-    for (int e = 0; e < 2; ++e)
+    for (int k = 0; k < SlabItems<CH>::K; ++k)
     {
-        const long long u = (long long)u0 - 1 + tid + e * 128;
+        const int i = q + k * TC_PRODUCERS;
+        const int j = i / CH, c = i % CH;
+        const long long u = (long long)u0 - 1 + j;
         const unsigned uu = u < 0 ? 0u : (unsigned)u;
         const unsigned r = uu / XP;
-        s.x[e] = (int)(uu - r * XP) - 1;
-        s.y[e] = (int)(r % (unsigned)Y);
-        s.z[e] = (int)(r / (unsigned)Y);
-        s.valid[e] = u >= 0 && uu < U && s.x[e] >= 0 && s.x[e] < X && (e == 0 || tid < 2);
+        const int x = (int)(uu - r * XP) - 1, y = (int)(r % (unsigned)Y), z = (int)(r / (unsigned)Y);
+        unsigned m = 0;
+        if (i < 130 * CH && u >= 0 && uu < U && x >= 0 && x < X)
+        {
+#pragma unroll
+            for (int g = 0; g < 9; ++g)
+            {
+                const int sy = y + g % 3 - 1, sz = z + g / 3 - 1;
+                if (sy >= 0 && sy < Y && sz >= 0 && sz < Z) m |= 1u << g;
+            }
+        }
+        s.mask[k] = m;
+        s.src[k] = m ? ((long long)(z * Y + y) * X + x) * (CH * 8) + c * 8 : 0;
     }
 }
 
 template <int COUT, int CIN>
-__global__ void __launch_bounds__(128) k_conv3d_fwd_tc(const __nv_bfloat16* __restrict__ x, int X, int Y, int Z,
-                                                       const __nv_bfloat16* __restrict__ w,
-                                                       const float* __restrict__ bias, int relu,
-                                                       __nv_bfloat16* y_bf16, float* y_f32, int* err)
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_conv3d_fwd_tc(const __nv_bfloat16* __restrict__ x, int X, int Y, int Z, const __nv_bfloat16* __restrict__ w,
+                    const float* __restrict__ bias, int relu, __nv_bfloat16* y_bf16, float* y_f32, int* err)
 {
     using L = TcLayout<COUT, CIN>;
     constexpr int CH = CIN / 8;   // 16-byte chunks per row
     constexpr int S = L::STAGES;
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ float sbias[COUT];
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const unsigned XP = (unsigned)X + 2;
     const unsigned U = (unsigned)Y * (unsigned)Z * XP;   // < 2^31, checked by the launcher
     const int tiles = (int)((U + TC_M - 1) / TC_M);
     const int ntl = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const int N = 9 * ntl;   // slabs this CTA fills
+    const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t slab_a = s_base + L::WBYTES;   // buffer b at slab_a + b * SBYTES
+    const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY;
+    const uint32_t accf0 = s_base + L::OFF_ACCF, acce0 = s_base + L::OFF_ACCE, fin = s_base + L::OFF_FIN;
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
+    float* sbias = reinterpret_cast<float*>(smem + L::OFF_BIAS);
 
     // all taps' weights -> shared memory: row co of tap t, chunk c at
     // t * TAPB + (co / 8) * (CH * 128) + c * 128 + (co % 8) * 16
     const uint4* wg = reinterpret_cast<const uint4*>(w);
-    for (int i = tid; i < 27 * COUT * CH; i += 128)
+    for (int i = tid; i < 27 * COUT * CH; i += TC_THREADS)
     {
         const int t = i / (COUT * CH), rem = i % (COUT * CH), r = rem / CH, c = rem % CH;
         *reinterpret_cast<uint4*>(smem + t * L::TAPB + (r / 8) * (CH * 128) + c * 128 + (r % 8) * 16) = wg[i];
     }
     if (tid < COUT) sbias[tid] = bias ? bias[tid] : 0.0f;
-    const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
-    const uint32_t slab_a = s_base + L::WBYTES;   // buffer b at slab_a + b * SBYTES
-    const uint32_t mb0 = s_base + L::BAR;         // buffer b's mbarrier at mb0 + 8 b
     if (tid == 0)
     {
         for (int b = 0; b < S; ++b)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb0 + 8 * b));
+        {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(full0 + 8 * b), "n"(TC_PRODUCERS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty0 + 8 * b));    // one commit
+        }
+        for (int a = 0; a < 2; ++a)
+        {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(accf0 + 8 * a));     // one commit
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(acce0 + 8 * a));   // 128 epilogue threads
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fin));
+        *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
-    if (warp == 0)
+    if (warp == TC_MMA_WARP)
     {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(mb0 + 8 * S),
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_base + L::OFF_TMEM),
                      "r"(L::TCOLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
@@ -259,134 +339,191 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd_tc(const __nv_bfloat16* __re
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t tbase = *reinterpret_cast<const uint32_t*>(smem + L::BAR + 8 * S);
-    // instruction descriptor: D f32, A and B bf16, both K-major, N = COUT, M = 128
-    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) |
-                           ((uint32_t)(TC_M >> 4) << 24);
+    const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
 
-    SlabRows pr;   // the producer's tile
-    auto gather = [&](int m) {
-        const int g = m % 9;
-        if (g == 0) slab_rows(pr, (unsigned)(blockIdx.x + (m / 9) * gridDim.x) * TC_M, tid, X, Y, XP, U);
-        const int dz = g / 3 - 1, dy = g % 3 - 1;
-        const uint32_t buf = slab_a + (m % S) * L::SBYTES;
-#pragma unroll
-        for (int e = 0; e < 2; ++e)
-        {
-            if (e == 1 && tid >= 2) break;
-            const int sy = pr.y[e] + dy, sz = pr.z[e] + dz;
-            const bool in = pr.valid[e] && sy >= 0 && sy < Y && sz >= 0 && sz < Z;
-            const long long sv = in ? ((long long)sz * Y + sy) * X + pr.x[e] : 0;
-            const __nv_bfloat16* src = x + sv * CIN;
-            const uint32_t dst = buf + (tid + e * 128) * 16;
-            const uint32_t bytes = in ? 16u : 0u;   // 0: zero fill, nothing read
-#pragma unroll
-            for (int c = 0; c < CH; ++c)
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst + c * TC_PLANE),
-                             "l"(src + c * 8), "r"(bytes)
-                             : "memory");
-        }
-    };
-
-#pragma unroll 1
-    for (int m = 0; m < L::AHEAD; ++m)
+    // Tiles go in groups of TC_T (the last group may be short).  Slabs run in
+    // the order (group, (dz, dy), tile of the group), one ring position each.
+    const int FG = ntl / TC_T, rem = ntl % TC_T, NG = FG + (rem ? 1 : 0);
+    if (warp >= 4 && warp < TC_MMA_WARP)
     {
-        if (m < N) gather(m);
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    }
-    bool ok = true;
-    int committed = -1;   // the last slab whose MMAs were committed
-#pragma unroll 1
-    for (int n = 0; n < N; ++n)
-    {
-        const int m = n + L::AHEAD;
-        bool mine = true;
-        if (m < N)
+        // ---- producers ----
+        const int q = tid - 128;
+        const long long plane_xy = (long long)X * Y;
+        int m = 0;   // slabs issued
+        bool stop = false;
+        for (int G = 0; G < NG && !stop; ++G)
         {
-            // buffer m % S last held slab m - S: its MMAs must be done
-            if (m >= S) mine = mbar_wait(mb0 + 8 * (m % S), (uint32_t)(((m - S) / S) & 1));
-            if (mine) gather(m);
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-        asm volatile("cp.async.wait_group %0;" ::"n"(L::AHEAD) : "memory");   // slab n has landed
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        ok = __syncthreads_and(mine);
-        if (!ok) break;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        const int g = n % 9;
-        if (tid == 0)
-        {
-            const uint32_t a0 = slab_a + (n % S) * L::SBYTES;
+            const int Tg = G < FG ? TC_T : rem;
+            SlabItems<CH> it[TC_T];
 #pragma unroll
-            for (int sh = 0; sh < 3; ++sh)
-#pragma unroll
-                for (int ks = 0; ks < CIN / 16; ++ks)
-                {
-                    const int tap = g * 3 + sh;
-                    const uint64_t da = umma_sdesc(a0 + sh * 16 + ks * 2 * TC_PLANE, TC_PLANE, 128);
-                    const uint64_t db = umma_sdesc(s_base + tap * L::TAPB + ks * 256, 128, CH * 128);
-                    const uint32_t acc = (g > 0 || sh > 0 || ks > 0) ? 1u : 0u;
-                    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tbase),
-                                 "l"(da), "l"(db), "r"(idesc), "r"(acc));
-                }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             mb0 + 8 * (n % S))
-                         : "memory");
-        }
-        committed = n;
-        if (g != 8) continue;
-        // epilogue of tile n / 9: the slab's commit covers every MMA before it
-        ok = __syncthreads_and(mbar_wait(mb0 + 8 * (n % S), (uint32_t)((n / S) & 1)));
-        if (!ok) break;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        uint32_t acc[COUT];
-        const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16);
-#pragma unroll
-        for (int c = 0; c < COUT; c += 16)
-            tmem_ld16(taddr + c, acc + c);
-        asm volatile("tcgen05.wait::ld.sync.aligned;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        const unsigned u = (unsigned)(blockIdx.x + (n / 9) * gridDim.x) * TC_M + tid;
-        const unsigned r = u / XP;
-        const int ox = (int)(u - r * XP) - 1;
-        if (u < U && ox >= 0 && ox < X)
-        {
-            const long long vox = (long long)r * X + ox;
-            float f[COUT];
-#pragma unroll
-            for (int c = 0; c < COUT; ++c)
+            for (int t = 0; t < TC_T; ++t)
+                if (t < Tg)
+                    slab_items(it[t], (unsigned)(blockIdx.x + (G * TC_T + t) * gridDim.x) * TC_M, q, X, Y, Z, XP, U);
+            for (int g = 0; g < 9 && !stop; ++g)
             {
-                f[c] = __uint_as_float(acc[c]) + sbias[c];
-                if (relu) f[c] = fmaxf(f[c], 0.0f);
+                // element offset of the (dz, dy) shift
+                const long long shift = ((long long)(g / 3 - 1) * plane_xy + (long long)(g % 3 - 1) * X) * CIN;
+#pragma unroll
+                for (int t = 0; t < TC_T; ++t)
+                {
+                    if (t >= Tg) break;
+                    const int b = m % S;
+                    if (m >= S && !mbar_wait_or_abort(empty0 + 8 * b, (uint32_t)((m / S - 1) & 1), abort))
+                    {
+                        stop = true;
+                        break;
+                    }
+                    const uint32_t buf = slab_a + b * L::SBYTES;
+#pragma unroll
+                    for (int k = 0; k < SlabItems<CH>::K; ++k)
+                    {
+                        const int i = q + k * TC_PRODUCERS;
+                        if (i >= 130 * CH) break;
+                        const bool in = (it[t].mask[k] >> g) & 1u;
+                        const __nv_bfloat16* src = x + (in ? it[t].src[k] + shift : 0);
+                        const uint32_t dst = buf + (i % CH) * TC_PLANE + (i / CH) * 16;
+                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
+                                     "r"(in ? 16u : 0u)   // 0: zero fill, nothing read
+                                     : "memory");
+                    }
+                    // the buffer's full barrier gets this thread's arrival once its copies have landed
+                    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(full0 + 8 * b)
+                                 : "memory");
+                    ++m;
+                }
             }
-            if (y_bf16)
-#pragma unroll
-                for (int c = 0; c < COUT; c += 8)
-                    *reinterpret_cast<uint4*>(y_bf16 + vox * COUT + c) =
-                        make_uint4(pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
-                                   pack_bf16(f[c + 4], f[c + 5]), pack_bf16(f[c + 6], f[c + 7]));
-            if (y_f32)
-#pragma unroll
-                for (int c = 0; c < COUT; c += 4)
-                    *reinterpret_cast<float4*>(y_f32 + vox * COUT + c) = make_float4(f[c], f[c + 1], f[c + 2], f[c + 3]);
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    if (!ok)
+    else if (warp == TC_MMA_WARP)
     {
-        if (tid == 0)
+        // ---- MMA issue: the whole warp runs the loop (descriptors stay warp-uniform), the elected
+        // lane issues every tcgen05.mma and tcgen05.commit ----
+        // D f32; A, B bf16, both K-major; N = COUT, M = 128
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) |
+                               ((uint32_t)(TC_M >> 4) << 24);
+        const bool leader = elect_one();
+        bool go = true;
+        int n = 0;   // slabs consumed
+        for (int G = 0; G < NG && go; ++G)
         {
-            atomicExch(err, 1);
-            // a bounded wait for the MMAs still in flight before the memory goes
-            if (committed >= 0) mbar_wait(mb0 + 8 * (committed % S), (uint32_t)((committed / S) & 1));
+            const int Tg = G < FG ? TC_T : rem, A = G & 1;
+            if (G >= 2 && !warp_wait(acce0 + 8 * A, (uint32_t)(((G - 2) >> 1) & 1), abort)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t dcol = tbase + (uint32_t)(A * TC_T * COUT);   // tile t at dcol + t COUT
+            for (int g = 0; g < 9 && go; ++g)
+            {
+                for (int t = 0; t < Tg && go; ++t)
+                    go = warp_wait(full0 + 8 * ((n + t) % S), (uint32_t)(((n + t) / S) & 1), abort);
+                if (!go) break;
+                // the copies landed through the generic proxy; the MMAs read through the async one
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                // consecutive MMAs go to different tiles' accumulators
+#pragma unroll
+                for (int sh = 0; sh < 3; ++sh)
+#pragma unroll
+                    for (int ks = 0; ks < CIN / 16; ++ks)
+                    {
+                        const int tap = g * 3 + sh;
+                        const uint64_t db = umma_sdesc(s_base + tap * L::TAPB + ks * 256, 128, CH * 128);
+                        const uint32_t acc = (g > 0 || sh > 0 || ks > 0) ? 1u : 0u;
+#pragma unroll
+                        for (int t = 0; t < TC_T; ++t)
+                        {
+                            if (t >= Tg) break;
+                            const uint32_t a0 = slab_a + ((n + t) % S) * L::SBYTES;
+                            const uint64_t da = umma_sdesc(a0 + sh * 16 + ks * 2 * TC_PLANE, TC_PLANE, 128);
+                            if (leader)
+                                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                                                 dcol + (uint32_t)(t * COUT)),
+                                             "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                        }
+                    }
+                if (leader)
+                    for (int t = 0; t < Tg; ++t)
+                        asm volatile(
+                            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                empty0 + 8 * ((n + t) % S))
+                            : "memory");
+                __syncwarp();
+                n += Tg;
+            }
+            if (!go) break;
+            if (leader)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 accf0 + 8 * A)
+                             : "memory");
+            __syncwarp();
+        }
+        // every MMA issued has completed once fin's first phase does
+        if (leader)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(fin)
+                         : "memory");
+        __syncwarp();
+        for (int it = 0; it < 20000 && !mbar_try(fin, 0u); ++it)
+            ;
+        __syncwarp();
+    }
+    else
+    {
+        // ---- epilogue (warps 0-3: tensor-memory lanes 32 warp .. 32 warp + 31) ----
+        for (int G = 0; G < NG; ++G)
+        {
+            const int Tg = G < FG ? TC_T : rem, A = G & 1;
+            bool ready = false;
+            if (lane == 0) ready = mbar_wait_or_abort(accf0 + 8 * A, (uint32_t)((G >> 1) & 1), abort);
+            if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int t = 0; t < Tg; ++t)
+            {
+                uint32_t acc[COUT];
+                const uint32_t taddr =
+                    tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)((A * TC_T + t) * COUT);
+#pragma unroll
+                for (int c = 0; c < COUT; c += 16)
+                    tmem_ld16(taddr + c, acc + c);
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (t == Tg - 1)
+                {
+                    // every accumulator of the group is read: hand them back to the MMA issuer
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    mbar_arrive(acce0 + 8 * A);
+                }
+                const unsigned u = (unsigned)(blockIdx.x + (G * TC_T + t) * gridDim.x) * TC_M + tid;
+                const unsigned r = u / XP;
+                const int ox = (int)(u - r * XP) - 1;
+                if (u < U && ox >= 0 && ox < X)
+                {
+                    const long long vox = (long long)r * X + ox;
+                    float f[COUT];
+#pragma unroll
+                    for (int c = 0; c < COUT; ++c)
+                    {
+                        f[c] = __uint_as_float(acc[c]) + sbias[c];
+                        if (relu) f[c] = fmaxf(f[c], 0.0f);
+                    }
+                    if (y_bf16)
+#pragma unroll
+                        for (int c = 0; c < COUT; c += 8)
+                            *reinterpret_cast<uint4*>(y_bf16 + vox * COUT + c) =
+                                make_uint4(pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
+                                           pack_bf16(f[c + 4], f[c + 5]), pack_bf16(f[c + 6], f[c + 7]));
+                    if (y_f32)
+#pragma unroll
+                        for (int c = 0; c < COUT; c += 4)
+                            *reinterpret_cast<float4*>(y_f32 + vox * COUT + c) =
+                                make_float4(f[c], f[c + 1], f[c + 2], f[c + 3]);
+                }
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
-    if (warp == 0)
+    if (tid == 0 && *abort) atomicExch(err, 1);
+    if (warp == TC_MMA_WARP)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
 }
 
@@ -490,28 +627,28 @@ tessgpu_status launch_fwd_tc(const __nv_bfloat16* x, int X, int Y, int Z, const 
                              int relu, __nv_bfloat16* yb, float* yf, cudaStream_t s)
 {
     using L = TcLayout<COUT, CIN>;
-    static int resident[64];   // CTAs resident on the whole device, per device ordinal
+    static int sms_of[64];   // SMs per device ordinal, once the kernel is set up there
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
-    if (!resident[dev])
+    if (!sms_of[dev])
     {
+        int optin = 0, sms = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (optin < L::TOTAL || sms <= 0) return TESSGPU_ERR_UNSUPPORTED;
         if (cudaFuncSetAttribute(k_conv3d_fwd_tc<COUT, CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, L::TOTAL) !=
             cudaSuccess)
             return TESSGPU_ERR_CUDA;
-        int per_sm = 0, sms = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3d_fwd_tc<COUT, CIN>, 128, L::TOTAL);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        // tensor memory: 512 columns per SM
-        per_sm = per_sm < 1 ? 1 : (per_sm > 512 / L::TCOLS ? 512 / L::TCOLS : per_sm);
-        resident[dev] = per_sm * (sms > 0 ? sms : 1);
+        sms_of[dev] = sms;
     }
     int* err = nullptr;
     if (cudaGetSymbolAddress((void**)&err, g_conv_err) != cudaSuccess) return TESSGPU_ERR_CUDA;
     const long long U = (long long)Y * Z * (X + 2);
     if (U + TC_M >= (1LL << 31)) return TESSGPU_ERR_UNSUPPORTED;
     const long long tiles = (U + TC_M - 1) / TC_M;
-    const int grid = (int)(tiles < resident[dev] ? tiles : resident[dev]);
-    k_conv3d_fwd_tc<COUT, CIN><<<grid, 128, L::TOTAL, s>>>(x, X, Y, Z, w, bias, relu, yb, yf, err);
+    // one persistent CTA per SM (the slab ring fills its shared memory)
+    const int grid = (int)(tiles < sms_of[dev] ? tiles : sms_of[dev]);
+    k_conv3d_fwd_tc<COUT, CIN><<<grid, TC_THREADS, L::TOTAL, s>>>(x, X, Y, Z, w, bias, relu, yb, yf, err);
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
