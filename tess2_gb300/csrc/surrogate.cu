@@ -15,6 +15,7 @@
 // outside the grid) and its B fragment from the weights.  The weight gradient
 // reduces over voxels on the CUDA cores (FP32), per tap, with the block's
 // voxel slice staged in shared memory.
+#include <cuda.h>   // CUtensorMap and its encoder's types (the encoder comes through the runtime)
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -116,37 +117,37 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 // ---------------------------------------------------------------------------
 // the same forward pass on the 5th-generation tensor cores (tcgen05)
 // ---------------------------------------------------------------------------
-// Rows of the GEMM are positions u = r * (X + 2) + x + 1 of the x-padded row
-// space (r = z * Y + y the x row, x in -1..X, the two halo positions zero), so
-// that a shift by dx is a shift by dx positions.  One persistent CTA per SM
-// keeps all 27 taps' weights in shared memory (K-major core-matrix layout: 8
-// rows x 16 bytes per core matrix) and takes tiles of 128 positions (the M of
-// one MMA) x c_out (its N).  Per (dz, dy) a tile needs one slab: the 130
-// positions u0 - 1 .. u0 + 128 of the x row shifted by (dy, dz), stored as
-// c_in / 8 planes of 16-byte rows; the three taps dx = -1, 0, 1 read that slab
-// at row offsets 0, 1, 2 (start addresses 16 bytes apart in the shared-memory
-// descriptor), so each input row is gathered 9 times per output tile, not 27.
-// Warp roles, all synchronised through mbarriers (no block-wide barrier in
-// the loop):
-//   warps 4-11 producers: gather slabs with cp.async (zero-filled outside the
-//              grid) into a ring of STAGES buffers; a buffer's "full" barrier
-//              completes when every producer's copies for it have landed
-//              (cp.async.mbarrier.arrive), so the whole ring can be in flight;
-//   warp 12    allocates tensor memory; one lane issues tcgen05.mma (kind::f16,
-//              bf16 x bf16 -> f32) for each slab and commits them to the
-//              buffer's "empty" barrier, and each finished tile to its
-//              accumulator's "full" barrier (two accumulators alternate);
+// A tile is 128 consecutive voxels x0 .. x0 + 127 of one x row (the M of one
+// MMA; positions past X are computed and dropped) x c_out (its N).  One
+// persistent CTA per SM keeps all 27 taps' weights in shared memory (K-major
+// core-matrix layout: 8 rows x 16 bytes per core matrix).  Per (dz, dy) a tile
+// needs one slab: positions x0 - 1 .. x0 + 128 of the x row shifted by
+// (dy, dz), stored as c_in / 8 planes of 16-byte rows; the three taps
+// dx = -1, 0, 1 read that slab at row offsets 0, 1, 2 (start addresses 16
+// bytes apart in the shared-memory descriptor), so each input row is fetched
+// 9 times per output tile, not 27.  Warp roles, synchronised through
+// mbarriers only (no block-wide barrier in the loop):
+//   warp 4     TMA: per slab one cp.async.bulk.tensor copy per plane (box 8
+//              channels x 130 positions of a 5-D view (8, c_in / 8, X, Y, Z)
+//              of the input); positions outside the grid (the x halo, rows
+//              past y or z) arrive as zeros without a memory read; the
+//              buffer's "full" barrier completes on the copies' bytes;
+//   warp 5     allocates tensor memory; the whole warp runs the loop (so the
+//              descriptors stay warp-uniform) and its elected lane issues
+//              tcgen05.mma (kind::f16, bf16 x bf16 -> f32) for each slab,
+//              commits them to the buffer's "empty" barrier and each finished
+//              tile to its accumulator's "full" barrier (two sets alternate);
 //   warps 0-3  epilogue: tcgen05.ld of row tid (warp w reads lanes 32w..),
-//              release the accumulator, bias, ReLU, store the interior rows.
+//              release the accumulators, bias, ReLU, store the rows inside X.
 // Every wait is bounded; a timed-out wait raises an abort flag that ends every
-// role's loop, the kernel reports it in *err, drains its copies, waits a
-// bounded time for its MMAs and frees its tensor memory.
+// role's loop, the kernel reports it in *err, waits a bounded time for its
+// MMAs and frees its tensor memory.
 constexpr int TC_M = 128;      // GEMM rows per tile
 constexpr int TC_SLAB = 136;   // rows per slab plane (>= 130, a multiple of 8)
 constexpr int TC_PLANE = TC_SLAB * 16;
-constexpr int TC_PRODUCERS = 256;      // 8 producer warps
-constexpr int TC_THREADS = 128 + TC_PRODUCERS + 32;   // 4 epilogue warps, the producers, 1 MMA warp
-constexpr int TC_MMA_WARP = (128 + TC_PRODUCERS) / 32;
+constexpr int TC_THREADS = 192;        // 4 epilogue warps, 1 TMA warp, 1 MMA warp
+constexpr int TC_TMA_WARP = 4, TC_MMA_WARP = 5;
+constexpr int TC_BOX = 130;            // positions per slab plane a TMA copy writes
 #ifndef TESSGPU_CONV_TILES
 #define TESSGPU_CONV_TILES 1
 #endif
@@ -242,60 +243,20 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
     return *reinterpret_cast<uint32_t*>(&h);
 }
 
-// A slab holds 130 entries x CH 16-byte chunks; producer thread q copies
-// chunks i = q + k * TC_PRODUCERS (entry i / CH, chunk i % CH), so that
-// consecutive threads read consecutive 16 bytes.  Per tile it keeps, for each
-// of its chunks, the source element of the unshifted entry and a 9-bit mask of
-// the (dz, dy) shifts that stay inside the grid.
-template <int CH>
-struct SlabItems
-{
-    static constexpr int K = (130 * CH + TC_PRODUCERS - 1) / TC_PRODUCERS;
-    long long src[K];   // element index of the chunk for dz = dy = 0
-    unsigned mask[K];   // bit g: shift (g / 3 - 1, g % 3 - 1) is inside the grid
-};
-
-template <int CH>
-__device__ __forceinline__ void slab_items(SlabItems<CH>& s, unsigned u0, int q, int X, int Y, int Z, unsigned XP,
-                                           unsigned U)
-{
-#pragma unroll
-    for (int k = 0; k < SlabItems<CH>::K; ++k)
-    {
-        const int i = q + k * TC_PRODUCERS;
-        const int j = i / CH, c = i % CH;
-        const long long u = (long long)u0 - 1 + j;
-        const unsigned uu = u < 0 ? 0u : (unsigned)u;
-        const unsigned r = uu / XP;
-        const int x = (int)(uu - r * XP) - 1, y = (int)(r % (unsigned)Y), z = (int)(r / (unsigned)Y);
-        unsigned m = 0;
-        if (i < 130 * CH && u >= 0 && uu < U && x >= 0 && x < X)
-        {
-#pragma unroll
-            for (int g = 0; g < 9; ++g)
-            {
-                const int sy = y + g % 3 - 1, sz = z + g / 3 - 1;
-                if (sy >= 0 && sy < Y && sz >= 0 && sz < Z) m |= 1u << g;
-            }
-        }
-        s.mask[k] = m;
-        s.src[k] = m ? ((long long)(z * Y + y) * X + x) * (CH * 8) + c * 8 : 0;
-    }
-}
-
 template <int COUT, int CIN>
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_conv3d_fwd_tc(const __nv_bfloat16* __restrict__ x, int X, int Y, int Z, const __nv_bfloat16* __restrict__ w,
-                    const float* __restrict__ bias, int relu, __nv_bfloat16* y_bf16, float* y_f32, int* err)
+    k_conv3d_fwd_tc(const __grid_constant__ CUtensorMap xmap, int X, int Y, int Z,
+                    const __nv_bfloat16* __restrict__ w, const float* __restrict__ bias, int relu,
+                    __nv_bfloat16* y_bf16, float* y_f32, int* err)
 {
     using L = TcLayout<COUT, CIN>;
     constexpr int CH = CIN / 8;   // 16-byte chunks per row
     constexpr int S = L::STAGES;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const unsigned XP = (unsigned)X + 2;
-    const unsigned U = (unsigned)Y * (unsigned)Z * XP;   // < 2^31, checked by the launcher
-    const int tiles = (int)((U + TC_M - 1) / TC_M);
+    // tile t: x row r = t / per_row (y = r % Y, z = r / Y), positions x0 = (t % per_row) * 128 ..
+    const int per_row = (X + TC_M - 1) / TC_M;
+    const int tiles = per_row * Y * Z;   // < 2^31, checked by the launcher
     const int ntl = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
     const uint32_t slab_a = s_base + L::WBYTES;   // buffer b at slab_a + b * SBYTES
@@ -317,7 +278,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     {
         for (int b = 0; b < S; ++b)
         {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(full0 + 8 * b), "n"(TC_PRODUCERS));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * b));   // expect_tx + copies
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty0 + 8 * b));    // one commit
         }
         for (int a = 0; a < 2; ++a)
@@ -344,56 +305,50 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // Tiles go in groups of TC_T (the last group may be short).  Slabs run in
     // the order (group, (dz, dy), tile of the group), one ring position each.
     const int FG = ntl / TC_T, rem = ntl % TC_T, NG = FG + (rem ? 1 : 0);
-    if (warp >= 4 && warp < TC_MMA_WARP)
+    if (warp == TC_TMA_WARP)
     {
-        // ---- producers ----
-        const int q = tid - 128;
-        const long long plane_xy = (long long)X * Y;
+        // ---- TMA: per slab, one copy per 8-channel plane; positions outside the grid arrive as zeros ----
+        const bool leader = elect_one();
+        const uint64_t map = reinterpret_cast<uint64_t>(&xmap);
+        if (leader) asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
         int m = 0;   // slabs issued
         bool stop = false;
         for (int G = 0; G < NG && !stop; ++G)
         {
             const int Tg = G < FG ? TC_T : rem;
-            SlabItems<CH> it[TC_T];
-#pragma unroll
-            for (int t = 0; t < TC_T; ++t)
-                if (t < Tg)
-                    slab_items(it[t], (unsigned)(blockIdx.x + (G * TC_T + t) * gridDim.x) * TC_M, q, X, Y, Z, XP, U);
             for (int g = 0; g < 9 && !stop; ++g)
             {
-                // element offset of the (dz, dy) shift
-                const long long shift = ((long long)(g / 3 - 1) * plane_xy + (long long)(g % 3 - 1) * X) * CIN;
-#pragma unroll
-                for (int t = 0; t < TC_T; ++t)
+                const int dz = g / 3 - 1, dy = g % 3 - 1;
+                for (int t = 0; t < Tg; ++t)
                 {
-                    if (t >= Tg) break;
                     const int b = m % S;
-                    if (m >= S && !mbar_wait_or_abort(empty0 + 8 * b, (uint32_t)((m / S - 1) & 1), abort))
+                    if (m >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((m / S - 1) & 1), abort))
                     {
                         stop = true;
                         break;
                     }
-                    const uint32_t buf = slab_a + b * L::SBYTES;
-#pragma unroll
-                    for (int k = 0; k < SlabItems<CH>::K; ++k)
+                    const int tile = (int)blockIdx.x + (G * TC_T + t) * (int)gridDim.x;
+                    const int r = tile / per_row, x0 = (tile - r * per_row) * TC_M;
+                    const int sy = r % Y + dy, sz = r / Y + dz;
+                    if (leader)
                     {
-                        const int i = q + k * TC_PRODUCERS;
-                        if (i >= 130 * CH) break;
-                        const bool in = (it[t].mask[k] >> g) & 1u;
-                        const __nv_bfloat16* src = x + (in ? it[t].src[k] + shift : 0);
-                        const uint32_t dst = buf + (i % CH) * TC_PLANE + (i / CH) * 16;
-                        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
-                                     "r"(in ? 16u : 0u)   // 0: zero fill, nothing read
+                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full0 + 8 * b),
+                                     "r"((uint32_t)(CH * TC_BOX * 16))
                                      : "memory");
+#pragma unroll
+                        for (int c = 0; c < CH; ++c)
+                            asm volatile(
+                                "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                                " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(slab_a + b * L::SBYTES +
+                                                                                  c * TC_PLANE),
+                                "l"(map), "r"(0), "r"(c), "r"(x0 - 1), "r"(sy), "r"(sz), "r"(full0 + 8 * b)
+                                : "memory");
                     }
-                    // the buffer's full barrier gets this thread's arrival once its copies have landed
-                    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(full0 + 8 * b)
-                                 : "memory");
+                    __syncwarp();
                     ++m;
                 }
             }
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
     }
     else if (warp == TC_MMA_WARP)
     {
@@ -416,8 +371,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int t = 0; t < Tg && go; ++t)
                     go = warp_wait(full0 + 8 * ((n + t) % S), (uint32_t)(((n + t) / S) & 1), abort);
                 if (!go) break;
-                // the copies landed through the generic proxy; the MMAs read through the async one
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 // consecutive MMAs go to different tiles' accumulators
 #pragma unroll
@@ -491,10 +444,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     asm volatile("tcgen05.fence::before_thread_sync;");
                     mbar_arrive(acce0 + 8 * A);
                 }
-                const unsigned u = (unsigned)(blockIdx.x + (G * TC_T + t) * gridDim.x) * TC_M + tid;
-                const unsigned r = u / XP;
-                const int ox = (int)(u - r * XP) - 1;
-                if (u < U && ox >= 0 && ox < X)
+                const int tile = (int)blockIdx.x + (G * TC_T + t) * (int)gridDim.x;
+                const int r = tile / per_row, ox = (tile - r * per_row) * TC_M + tid;
+                if (ox < X)
                 {
                     const long long vox = (long long)r * X + ox;
                     float f[COUT];
@@ -622,6 +574,27 @@ int blocks_for(long long n, int t)
 __device__ int g_conv_err;   // raised by a tcgen05 kernel whose bounded wait ran out
 int g_conv_engine = 0;       // 0: tcgen05 where the channel counts allow, 1: mma.sync only
 
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver, through the runtime (no link against libcuda)
+EncodeTiled tensor_map_encoder()
+{
+    static EncodeTiled fn = nullptr;
+    if (!fn)
+    {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiled)p;
+        cudaGetLastError();
+    }
+    return fn;
+}
+
 template <int COUT, int CIN>
 tessgpu_status launch_fwd_tc(const __nv_bfloat16* x, int X, int Y, int Z, const __nv_bfloat16* w, const float* bias,
                              int relu, __nv_bfloat16* yb, float* yf, cudaStream_t s)
@@ -643,12 +616,22 @@ tessgpu_status launch_fwd_tc(const __nv_bfloat16* x, int X, int Y, int Z, const 
     }
     int* err = nullptr;
     if (cudaGetSymbolAddress((void**)&err, g_conv_err) != cudaSuccess) return TESSGPU_ERR_CUDA;
-    const long long U = (long long)Y * Z * (X + 2);
-    if (U + TC_M >= (1LL << 31)) return TESSGPU_ERR_UNSUPPORTED;
-    const long long tiles = (U + TC_M - 1) / TC_M;
+    const long long tiles = (long long)((X + TC_M - 1) / TC_M) * Y * Z;
+    const EncodeTiled encode = tensor_map_encoder();
+    if (tiles >= (1LL << 31) || !encode || ((uintptr_t)x & 15)) return TESSGPU_ERR_UNSUPPORTED;
+    // the input as (8 channels, CIN / 8 chunks, X, Y, Z); a box is one chunk plane of TC_BOX positions
+    CUtensorMap xmap;
+    const cuuint64_t dims[5] = { 8, (cuuint64_t)(CIN / 8), (cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z };
+    const cuuint64_t strides[4] = { 16, (cuuint64_t)CIN * 2, (cuuint64_t)X * CIN * 2, (cuuint64_t)X * Y * CIN * 2 };
+    const cuuint32_t box[5] = { 8, 1, (cuuint32_t)TC_BOX, 1, 1 };
+    const cuuint32_t estride[5] = { 1, 1, 1, 1, 1 };
+    if (encode(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)x, dims, strides, box, estride,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return TESSGPU_ERR_UNSUPPORTED;
     // one persistent CTA per SM (the slab ring fills its shared memory)
     const int grid = (int)(tiles < sms_of[dev] ? tiles : sms_of[dev]);
-    k_conv3d_fwd_tc<COUT, CIN><<<grid, TC_THREADS, L::TOTAL, s>>>(x, X, Y, Z, w, bias, relu, yb, yf, err);
+    k_conv3d_fwd_tc<COUT, CIN><<<grid, TC_THREADS, L::TOTAL, s>>>(xmap, X, Y, Z, w, bias, relu, yb, yf, err);
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
@@ -690,12 +673,13 @@ extern "C" tessgpu_status tessgpu_conv3d_fwd(const void* x, int X, int Y, int Z,
     __nv_bfloat16* yb = (__nv_bfloat16*)y_bf16;
     if (g_conv_engine == 0)
     {
-        if ((long long)Y * Z * (X + 2) + TC_M >= (1LL << 31))
-            ;   // positions past 32 bits: the mma.sync kernel below
-        else if (cin == 16 && cout == 16) return launch_fwd_tc<16, 16>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
-        if (cin == 16 && cout == 32) return launch_fwd_tc<32, 16>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
-        if (cin == 32 && cout == 16) return launch_fwd_tc<16, 32>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
-        if (cin == 32 && cout == 32) return launch_fwd_tc<32, 32>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        // TESSGPU_ERR_UNSUPPORTED (more than 2^31 tiles, no tensor-map encoder): the mma.sync kernel below
+        tessgpu_status st = TESSGPU_ERR_UNSUPPORTED;
+        if (cin == 16 && cout == 16) st = launch_fwd_tc<16, 16>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        if (cin == 16 && cout == 32) st = launch_fwd_tc<32, 16>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        if (cin == 32 && cout == 16) st = launch_fwd_tc<16, 32>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        if (cin == 32 && cout == 32) st = launch_fwd_tc<32, 32>(xx, X, Y, Z, ww, bias, relu, yb, y_f32, s);
+        if (st != TESSGPU_ERR_UNSUPPORTED) return st;
     }
     switch (cout / 8)
     {
