@@ -127,16 +127,20 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 // bytes apart in the shared-memory descriptor), so each input row is fetched
 // 9 times per output tile, not 27.  Warp roles, synchronised through
 // mbarriers only (no block-wide barrier in the loop):
-//   warp 4     TMA: per slab one cp.async.bulk.tensor copy per plane (box 8
+//   warps 4-5  TMA (tiles alternate between them): per slab one
+//              cp.async.bulk.tensor copy per plane (box 8
 //              channels x 130 positions of a 5-D view (8, c_in / 8, X, Y, Z)
 //              of the input); positions outside the grid (the x halo, rows
 //              past y or z) arrive as zeros without a memory read; the
 //              buffer's "full" barrier completes on the copies' bytes;
-//   warp 5     allocates tensor memory; the whole warp runs the loop (so the
-//              descriptors stay warp-uniform) and its elected lane issues
-//              tcgen05.mma (kind::f16, bf16 x bf16 -> f32) for each slab,
-//              commits them to the buffer's "empty" barrier and each finished
-//              tile to its accumulator's "full" barrier (two sets alternate);
+//   warps 6-7  MMA (tiles alternate between them; warp 6 allocates tensor
+//              memory): the whole warp runs the loop (so the descriptors stay
+//              warp-uniform) and its elected lane issues tcgen05.mma
+//              (kind::f16, bf16 x bf16 -> f32) for each slab, commits them to
+//              the buffer's "empty" barrier and each finished tile to its
+//              accumulator's "full" barrier (TC_SETS sets in rotation).  With
+//              16-32 output channels an MMA is small and its issue cost,
+//              not the tensor pipe, sets the pace, hence two issuers;
 //   warps 0-3  epilogue: tcgen05.ld of row tid (warp w reads lanes 32w..),
 //              release the accumulators, bias, ReLU, store the rows inside X.
 // Every wait is bounded; a timed-out wait raises an abort flag that ends every
@@ -145,8 +149,11 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 constexpr int TC_M = 128;      // GEMM rows per tile
 constexpr int TC_SLAB = 136;   // rows per slab plane (>= 130, a multiple of 8)
 constexpr int TC_PLANE = TC_SLAB * 16;
-constexpr int TC_THREADS = 192;        // 4 epilogue warps, 1 TMA warp, 1 MMA warp
-constexpr int TC_TMA_WARP = 4, TC_MMA_WARP = 5;
+constexpr int TC_LOADERS = 2;          // TMA warps (alternate tiles)
+constexpr int TC_ISSUERS = 2;          // MMA-issuing warps (alternate tiles)
+constexpr int TC_SETS = 4;             // accumulator sets in tensor memory (a multiple of TC_ISSUERS)
+constexpr int TC_TMA_WARP = 4, TC_MMA_WARP = 4 + TC_LOADERS;
+constexpr int TC_THREADS = 32 * (4 + TC_LOADERS + TC_ISSUERS);   // epilogue, TMA, MMA warps
 constexpr int TC_BOX = 130;            // positions per slab plane a TMA copy writes
 #ifndef TESSGPU_CONV_TILES
 #define TESSGPU_CONV_TILES 1
@@ -163,14 +170,15 @@ struct TcLayout
     static constexpr int FIT = (TC_SMEM - WBYTES - 512) / SBYTES;
     static constexpr int STAGES = FIT < 24 ? FIT : 24;
     static constexpr int BAR = WBYTES + STAGES * SBYTES;   // mbarriers, tensor-memory address, abort flag
-    // full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], fin
+    // full[STAGES], empty[STAGES], acc_full[TC_SETS], acc_empty[TC_SETS], fin
     static constexpr int OFF_FULL = BAR, OFF_EMPTY = BAR + 8 * STAGES, OFF_ACCF = BAR + 16 * STAGES,
-                         OFF_ACCE = OFF_ACCF + 16, OFF_FIN = OFF_ACCE + 16, OFF_TMEM = OFF_FIN + 8,
+                         OFF_ACCE = OFF_ACCF + 8 * TC_SETS, OFF_FIN = OFF_ACCE + 8 * TC_SETS, OFF_TMEM = OFF_FIN + 8,
                          OFF_ABORT = OFF_TMEM + 4, OFF_BIAS = OFF_ABORT + 4;
     static constexpr int TOTAL = OFF_BIAS + 4 * COUT;
     // two sets of TC_T accumulators of COUT columns; a power of two >= 32
-    static constexpr int TCOLS = 2 * TC_T * COUT <= 32 ? 32 : (2 * TC_T * COUT <= 64 ? 64 : (2 * TC_T * COUT <= 128 ? 128 : (2 * TC_T * COUT <= 256 ? 256 : 512)));
-    static_assert(2 * TC_T * COUT <= 512, "tensor memory");
+    static constexpr int ACOLS = TC_SETS * TC_T * COUT;
+    static constexpr int TCOLS = ACOLS <= 32 ? 32 : (ACOLS <= 64 ? 64 : (ACOLS <= 128 ? 128 : (ACOLS <= 256 ? 256 : 512)));
+    static_assert(ACOLS <= 512, "tensor memory");
     static_assert(STAGES >= 3, "shared memory too small for the slab ring");
     static_assert(TOTAL <= TC_SMEM, "shared memory");
 };
@@ -281,12 +289,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * b));   // expect_tx + copies
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty0 + 8 * b));    // one commit
         }
-        for (int a = 0; a < 2; ++a)
+        for (int a = 0; a < TC_SETS; ++a)
         {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(accf0 + 8 * a));     // one commit
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(acce0 + 8 * a));   // 128 epilogue threads
         }
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fin));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(fin), "n"(TC_ISSUERS));   // one commit each
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
@@ -305,31 +313,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // Tiles go in groups of TC_T (the last group may be short).  Slabs run in
     // the order (group, (dz, dy), tile of the group), one ring position each.
     const int FG = ntl / TC_T, rem = ntl % TC_T, NG = FG + (rem ? 1 : 0);
-    if (warp == TC_TMA_WARP)
+    if (warp >= TC_TMA_WARP && warp < TC_TMA_WARP + TC_LOADERS)
     {
         // ---- TMA: per slab, one copy per 8-channel plane; positions outside the grid arrive as zeros ----
         const bool leader = elect_one();
         const uint64_t map = reinterpret_cast<uint64_t>(&xmap);
         if (leader) asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
-        int m = 0;   // slabs issued
         bool stop = false;
-        for (int G = 0; G < NG && !stop; ++G)
+        for (int G = warp - TC_TMA_WARP; G < NG && !stop; G += TC_LOADERS)
         {
             const int Tg = G < FG ? TC_T : rem;
+            int m = 9 * TC_T * G;   // the group's first slab (every earlier group is full)
+            int tx0[TC_T], ty[TC_T], tz[TC_T];   // the group's tiles: first position, row
+#pragma unroll
+            for (int t = 0; t < TC_T; ++t)
+            {
+                const int tile = (int)blockIdx.x + (G * TC_T + t) * (int)gridDim.x;
+                const int r = tile / per_row;
+                tx0[t] = (tile - r * per_row) * TC_M;
+                ty[t] = r % Y;
+                tz[t] = r / Y;
+            }
             for (int g = 0; g < 9 && !stop; ++g)
             {
                 const int dz = g / 3 - 1, dy = g % 3 - 1;
-                for (int t = 0; t < Tg; ++t)
+#pragma unroll
+                for (int t = 0; t < TC_T; ++t)
                 {
+                    if (t >= Tg) break;
                     const int b = m % S;
                     if (m >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((m / S - 1) & 1), abort))
                     {
                         stop = true;
                         break;
                     }
-                    const int tile = (int)blockIdx.x + (G * TC_T + t) * (int)gridDim.x;
-                    const int r = tile / per_row, x0 = (tile - r * per_row) * TC_M;
-                    const int sy = r % Y + dy, sz = r / Y + dz;
+                    const int x0 = tx0[t], sy = ty[t] + dy, sz = tz[t] + dz;
                     if (leader)
                     {
                         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full0 + 8 * b),
@@ -350,7 +368,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
     }
-    else if (warp == TC_MMA_WARP)
+    else if (warp >= TC_MMA_WARP)
     {
         // ---- MMA issue: the whole warp runs the loop (descriptors stay warp-uniform), the elected
         // lane issues every tcgen05.mma and tcgen05.commit ----
@@ -358,12 +376,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) |
                                ((uint32_t)(TC_M >> 4) << 24);
         const bool leader = elect_one();
+        // descriptors as a base plus a byte offset / 16 in the start-address field (shared memory
+        // addresses stay below 2^18, so the 14-bit field never carries)
+        const uint64_t adesc0 = umma_sdesc(slab_a, TC_PLANE, 128);
+        const uint64_t bdesc0 = umma_sdesc(s_base, 128, CH * 128);
         bool go = true;
-        int n = 0;   // slabs consumed
-        for (int G = 0; G < NG && go; ++G)
+        for (int G = warp - TC_MMA_WARP; G < NG && go; G += TC_ISSUERS)
         {
-            const int Tg = G < FG ? TC_T : rem, A = G & 1;
-            if (G >= 2 && !warp_wait(acce0 + 8 * A, (uint32_t)(((G - 2) >> 1) & 1), abort)) break;
+            const int Tg = G < FG ? TC_T : rem, A = G % TC_SETS;
+            int n = 9 * TC_T * G;   // the group's first slab
+            if (G >= TC_SETS &&
+                !warp_wait(acce0 + 8 * A, (uint32_t)(((G - TC_SETS) / TC_SETS) & 1), abort))
+                break;
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t dcol = tbase + (uint32_t)(A * TC_T * COUT);   // tile t at dcol + t COUT
             for (int g = 0; g < 9 && go; ++g)
@@ -379,14 +403,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     for (int ks = 0; ks < CIN / 16; ++ks)
                     {
                         const int tap = g * 3 + sh;
-                        const uint64_t db = umma_sdesc(s_base + tap * L::TAPB + ks * 256, 128, CH * 128);
+                        const uint64_t db = bdesc0 + (uint64_t)((tap * L::TAPB + ks * 256) >> 4);
                         const uint32_t acc = (g > 0 || sh > 0 || ks > 0) ? 1u : 0u;
 #pragma unroll
                         for (int t = 0; t < TC_T; ++t)
                         {
                             if (t >= Tg) break;
-                            const uint32_t a0 = slab_a + ((n + t) % S) * L::SBYTES;
-                            const uint64_t da = umma_sdesc(a0 + sh * 16 + ks * 2 * TC_PLANE, TC_PLANE, 128);
+                            const uint64_t da = adesc0 + (uint64_t)((((n + t) % S) * L::SBYTES + sh * 16 +
+                                                                      ks * 2 * TC_PLANE) >> 4);
                             if (leader)
                                 asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                                              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
@@ -424,9 +448,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ---- epilogue (warps 0-3: tensor-memory lanes 32 warp .. 32 warp + 31) ----
         for (int G = 0; G < NG; ++G)
         {
-            const int Tg = G < FG ? TC_T : rem, A = G & 1;
+            const int Tg = G < FG ? TC_T : rem, A = G % TC_SETS;
             bool ready = false;
-            if (lane == 0) ready = mbar_wait_or_abort(accf0 + 8 * A, (uint32_t)((G >> 1) & 1), abort);
+            if (lane == 0) ready = mbar_wait_or_abort(accf0 + 8 * A, (uint32_t)((G / TC_SETS) & 1), abort);
             if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
             for (int t = 0; t < Tg; ++t)
