@@ -127,20 +127,23 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 // bytes apart in the shared-memory descriptor), so each input row is fetched
 // 9 times per output tile, not 27.  Warp roles, synchronised through
 // mbarriers only (no block-wide barrier in the loop):
-//   warps 4-5  TMA (tiles alternate between them): per slab one
+// Tiles go in groups of four, one per MMA warp, and slabs run in the order
+// (group, (dz, dy), tile), so that the four MMA warps advance together.
+//   warps 4-5  TMA (each takes two tiles of a group): per slab one
 //              cp.async.bulk.tensor copy per plane (box 8
 //              channels x 130 positions of a 5-D view (8, c_in / 8, X, Y, Z)
 //              of the input); positions outside the grid (the x halo, rows
 //              past y or z) arrive as zeros without a memory read; the
 //              buffer's "full" barrier completes on the copies' bytes;
-//   warps 6-7  MMA (tiles alternate between them; warp 6 allocates tensor
+//   warps 6-9  MMA (one tile of each group each; warp 6 allocates tensor
 //              memory): the whole warp runs the loop (so the descriptors stay
 //              warp-uniform) and its elected lane issues tcgen05.mma
 //              (kind::f16, bf16 x bf16 -> f32) for each slab, commits them to
-//              the buffer's "empty" barrier and each finished tile to its
-//              accumulator's "full" barrier (TC_SETS sets in rotation).  With
-//              16-32 output channels an MMA is small and its issue cost,
-//              not the tensor pipe, sets the pace, hence two issuers;
+//              the buffer's "empty" barrier and the finished tile to its
+//              accumulator's "full" barrier (two sets of four accumulators
+//              alternate between groups).  With 16-32 output channels an MMA
+//              is small and its issue cost, not the tensor pipe, sets the
+//              pace, hence four issuers;
 //   warps 0-3  epilogue: tcgen05.ld of row tid (warp w reads lanes 32w..),
 //              release the accumulators, bias, ReLU, store the rows inside X.
 // Every wait is bounded; a timed-out wait raises an abort flag that ends every
@@ -149,16 +152,14 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 constexpr int TC_M = 128;      // GEMM rows per tile
 constexpr int TC_SLAB = 136;   // rows per slab plane (>= 130, a multiple of 8)
 constexpr int TC_PLANE = TC_SLAB * 16;
-constexpr int TC_LOADERS = 2;          // TMA warps (alternate tiles)
-constexpr int TC_ISSUERS = 2;          // MMA-issuing warps (alternate tiles)
-constexpr int TC_SETS = 4;             // accumulator sets in tensor memory (a multiple of TC_ISSUERS)
-constexpr int TC_TMA_WARP = 4, TC_MMA_WARP = 4 + TC_LOADERS;
-constexpr int TC_THREADS = 32 * (4 + TC_LOADERS + TC_ISSUERS);   // epilogue, TMA, MMA warps
-constexpr int TC_BOX = 130;            // positions per slab plane a TMA copy writes
 #ifndef TESSGPU_CONV_TILES
-#define TESSGPU_CONV_TILES 1
+#define TESSGPU_CONV_TILES 4
 #endif
-constexpr int TC_T = TESSGPU_CONV_TILES;   // tiles whose MMAs interleave (independent accumulators)
+constexpr int TC_T = TESSGPU_CONV_TILES;   // tiles per group = MMA-issuing warps
+constexpr int TC_LOADERS = 2;              // TMA warps
+constexpr int TC_TMA_WARP = 4, TC_MMA_WARP = 4 + TC_LOADERS;
+constexpr int TC_THREADS = 32 * (4 + TC_LOADERS + TC_T);   // epilogue, TMA, MMA warps
+constexpr int TC_BOX = 130;            // positions per slab plane a TMA copy writes
 constexpr int TC_SMEM = 227 * 1024;    // dynamic shared memory a CTA may opt into
 
 template <int COUT, int CIN>
@@ -168,15 +169,15 @@ struct TcLayout
     static constexpr int WBYTES = 27 * TAPB;
     static constexpr int SBYTES = (CIN / 8) * TC_PLANE;
     static constexpr int FIT = (TC_SMEM - WBYTES - 512) / SBYTES;
-    static constexpr int STAGES = FIT < 24 ? FIT : 24;
+    static constexpr int STAGES = FIT < 40 ? FIT : 40;
     static constexpr int BAR = WBYTES + STAGES * SBYTES;   // mbarriers, tensor-memory address, abort flag
-    // full[STAGES], empty[STAGES], acc_full[TC_SETS], acc_empty[TC_SETS], fin
+    // full[STAGES], empty[STAGES], acc_full[2][TC_T], acc_empty[2], fin
     static constexpr int OFF_FULL = BAR, OFF_EMPTY = BAR + 8 * STAGES, OFF_ACCF = BAR + 16 * STAGES,
-                         OFF_ACCE = OFF_ACCF + 8 * TC_SETS, OFF_FIN = OFF_ACCE + 8 * TC_SETS, OFF_TMEM = OFF_FIN + 8,
+                         OFF_ACCE = OFF_ACCF + 16 * TC_T, OFF_FIN = OFF_ACCE + 16, OFF_TMEM = OFF_FIN + 8,
                          OFF_ABORT = OFF_TMEM + 4, OFF_BIAS = OFF_ABORT + 4;
     static constexpr int TOTAL = OFF_BIAS + 4 * COUT;
     // two sets of TC_T accumulators of COUT columns; a power of two >= 32
-    static constexpr int ACOLS = TC_SETS * TC_T * COUT;
+    static constexpr int ACOLS = 2 * TC_T * COUT;   // two sets of TC_T accumulators
     static constexpr int TCOLS = ACOLS <= 32 ? 32 : (ACOLS <= 64 ? 64 : (ACOLS <= 128 ? 128 : (ACOLS <= 256 ? 256 : 512)));
     static_assert(ACOLS <= 512, "tensor memory");
     static_assert(STAGES >= 3, "shared memory too small for the slab ring");
@@ -289,12 +290,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * b));   // expect_tx + copies
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty0 + 8 * b));    // one commit
         }
-        for (int a = 0; a < TC_SETS; ++a)
-        {
+        for (int a = 0; a < 2 * TC_T; ++a)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(accf0 + 8 * a));     // one commit
+        for (int a = 0; a < 2; ++a)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(acce0 + 8 * a));   // 128 epilogue threads
-        }
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(fin), "n"(TC_ISSUERS));   // one commit each
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(fin), "n"(TC_T));   // one commit per MMA warp
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
@@ -310,20 +310,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
 
-    // Tiles go in groups of TC_T (the last group may be short).  Slabs run in
-    // the order (group, (dz, dy), tile of the group), one ring position each.
+    // Tiles go in groups of TC_T, one per MMA warp (the last group may be
+    // short).  Slabs run in the order (group, (dz, dy), tile of the group), one
+    // ring position each, so the issuers advance through (dz, dy) together.
     const int FG = ntl / TC_T, rem = ntl % TC_T, NG = FG + (rem ? 1 : 0);
     if (warp >= TC_TMA_WARP && warp < TC_TMA_WARP + TC_LOADERS)
     {
-        // ---- TMA: per slab, one copy per 8-channel plane; positions outside the grid arrive as zeros ----
+        // ---- TMA (tiles t = w, w + TC_LOADERS, .. of each group): per slab one copy per 8-channel
+        // plane; positions outside the grid arrive as zeros ----
+        const int w = warp - TC_TMA_WARP;
         const bool leader = elect_one();
         const uint64_t map = reinterpret_cast<uint64_t>(&xmap);
         if (leader) asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
         bool stop = false;
-        for (int G = warp - TC_TMA_WARP; G < NG && !stop; G += TC_LOADERS)
+        for (int G = 0; G < NG && !stop; ++G)
         {
             const int Tg = G < FG ? TC_T : rem;
-            int m = 9 * TC_T * G;   // the group's first slab (every earlier group is full)
             int tx0[TC_T], ty[TC_T], tz[TC_T];   // the group's tiles: first position, row
 #pragma unroll
             for (int t = 0; t < TC_T; ++t)
@@ -340,7 +342,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
                 for (int t = 0; t < TC_T; ++t)
                 {
+                    if (t % TC_LOADERS != w) continue;
                     if (t >= Tg) break;
+                    const int m = 9 * TC_T * G + g * Tg + t;   // every earlier group is full
                     const int b = m % S;
                     if (m >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((m / S - 1) & 1), abort))
                     {
@@ -363,15 +367,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                 : "memory");
                     }
                     __syncwarp();
-                    ++m;
                 }
             }
         }
     }
     else if (warp >= TC_MMA_WARP)
     {
-        // ---- MMA issue: the whole warp runs the loop (descriptors stay warp-uniform), the elected
-        // lane issues every tcgen05.mma and tcgen05.commit ----
+        // ---- MMA issue (tile t = warp - TC_MMA_WARP of each group): the whole warp runs the loop
+        // (descriptors stay warp-uniform), the elected lane issues every tcgen05.mma and commit ----
+        const int ti = warp - TC_MMA_WARP;
         // D f32; A, B bf16, both K-major; N = COUT, M = 128
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) |
                                ((uint32_t)(TC_M >> 4) << 24);
@@ -381,22 +385,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint64_t adesc0 = umma_sdesc(slab_a, TC_PLANE, 128);
         const uint64_t bdesc0 = umma_sdesc(s_base, 128, CH * 128);
         bool go = true;
-        for (int G = warp - TC_MMA_WARP; G < NG && go; G += TC_ISSUERS)
+        for (int G = 0; G < NG && go; ++G)
         {
-            const int Tg = G < FG ? TC_T : rem, A = G % TC_SETS;
-            int n = 9 * TC_T * G;   // the group's first slab
-            if (G >= TC_SETS &&
-                !warp_wait(acce0 + 8 * A, (uint32_t)(((G - TC_SETS) / TC_SETS) & 1), abort))
-                break;
+            const int Tg = G < FG ? TC_T : rem, A = G & 1;
+            if (ti >= Tg) break;   // only the last group is short
+            // the epilogue has read this accumulator set's tiles of group G - 2
+            if (G >= 2 && !warp_wait(acce0 + 8 * A, (uint32_t)(((G - 2) >> 1) & 1), abort)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t dcol = tbase + (uint32_t)(A * TC_T * COUT);   // tile t at dcol + t COUT
+            const uint32_t dcol = tbase + (uint32_t)((A * TC_T + ti) * COUT);
             for (int g = 0; g < 9 && go; ++g)
             {
-                for (int t = 0; t < Tg && go; ++t)
-                    go = warp_wait(full0 + 8 * ((n + t) % S), (uint32_t)(((n + t) / S) & 1), abort);
+                const int n = 9 * TC_T * G + g * Tg + ti, b = n % S;
+                go = warp_wait(full0 + 8 * b, (uint32_t)((n / S) & 1), abort);
                 if (!go) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                // consecutive MMAs go to different tiles' accumulators
 #pragma unroll
                 for (int sh = 0; sh < 3; ++sh)
 #pragma unroll
@@ -404,33 +406,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     {
                         const int tap = g * 3 + sh;
                         const uint64_t db = bdesc0 + (uint64_t)((tap * L::TAPB + ks * 256) >> 4);
+                        const uint64_t da =
+                            adesc0 + (uint64_t)((b * L::SBYTES + sh * 16 + ks * 2 * TC_PLANE) >> 4);
                         const uint32_t acc = (g > 0 || sh > 0 || ks > 0) ? 1u : 0u;
-#pragma unroll
-                        for (int t = 0; t < TC_T; ++t)
-                        {
-                            if (t >= Tg) break;
-                            const uint64_t da = adesc0 + (uint64_t)((((n + t) % S) * L::SBYTES + sh * 16 +
-                                                                      ks * 2 * TC_PLANE) >> 4);
-                            if (leader)
-                                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
-                                                 dcol + (uint32_t)(t * COUT)),
-                                             "l"(da), "l"(db), "r"(idesc), "r"(acc));
-                        }
+                        if (leader)
+                            asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dcol),
+                                         "l"(da), "l"(db), "r"(idesc), "r"(acc));
                     }
                 if (leader)
-                    for (int t = 0; t < Tg; ++t)
-                        asm volatile(
-                            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                empty0 + 8 * ((n + t) % S))
-                            : "memory");
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     empty0 + 8 * b)
+                                 : "memory");
                 __syncwarp();
-                n += Tg;
             }
             if (!go) break;
             if (leader)
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 accf0 + 8 * A)
+                                 accf0 + 8 * (A * TC_T + ti))
                              : "memory");
             __syncwarp();
         }
@@ -448,13 +441,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ---- epilogue (warps 0-3: tensor-memory lanes 32 warp .. 32 warp + 31) ----
         for (int G = 0; G < NG; ++G)
         {
-            const int Tg = G < FG ? TC_T : rem, A = G % TC_SETS;
-            bool ready = false;
-            if (lane == 0) ready = mbar_wait_or_abort(accf0 + 8 * A, (uint32_t)((G / TC_SETS) & 1), abort);
-            if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            for (int t = 0; t < Tg; ++t)
+            const int Tg = G < FG ? TC_T : rem, A = G & 1;
+            bool ok = true;
+            for (int t = 0; t < Tg && ok; ++t)
             {
+                bool ready = false;
+                if (lane == 0)
+                    ready = mbar_wait_or_abort(accf0 + 8 * (A * TC_T + t), (uint32_t)((G >> 1) & 1), abort);
+                ok = __shfl_sync(0xffffffffu, ready ? 1 : 0, 0) != 0;
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
                 uint32_t acc[COUT];
                 const uint32_t taddr =
                     tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)((A * TC_T + t) * COUT);
@@ -464,7 +460,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 asm volatile("tcgen05.wait::ld.sync.aligned;");
                 if (t == Tg - 1)
                 {
-                    // every accumulator of the group is read: hand them back to the MMA issuer
+                    // every accumulator of the group is read: hand the set back to the MMA warps
                     asm volatile("tcgen05.fence::before_thread_sync;");
                     mbar_arrive(acce0 + 8 * A);
                 }
@@ -493,6 +489,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                 make_float4(f[c], f[c + 1], f[c + 2], f[c + 3]);
                 }
             }
+            if (!ok) break;
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
