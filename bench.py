@@ -384,6 +384,14 @@ def time_surrogate(args, peaks, local):
     torch.cuda.synchronize()
     dtfe_ms = e0.elapsed_time(e1) / 10
     bf16 = float(peaks.get("bf16_tflops", 1900.0))
+    # the network alone on a 256^3 grid (random weights and input): tcgen05 against mma.sync
+    big = {}
+    for eng, name in ((S.ENGINE_TCGEN05, "tcgen05"), (S.ENGINE_MMA_SYNC, "mma_sync")):
+        ms, tf = S.forward_throughput(256, engine=eng)
+        big[name] = dict(ms=ms, tflops=tf, frac_of_bf16_peak=tf / bf16,
+                         layers=[dict(c_in=ci, c_out=co, ms=lm, tflops=lt)
+                                 for ci, co, lm, lt in S.layer_times(256, engine=eng)])
+    r.update(forward_256=dict(grid=256, gflop=S.forward_flops((256, 256, 256)) / 1e9, **big))
     r.update(plain_gpu_ms=dtfe_ms, plain_host_delaunay_s=t_qhull,
              fields_per_s=1e3 / r["forward_ms"], plain_gpu_fields_per_s=1e3 / dtfe_ms,
              plain_with_delaunay_fields_per_s=1.0 / (t_qhull + dtfe_ms * 1e-3),
@@ -391,7 +399,8 @@ def time_surrogate(args, peaks, local):
              speedup_vs_plain_with_delaunay=(t_qhull + dtfe_ms * 1e-3) / (r["forward_ms"] * 1e-3),
              tensor_frac_of_bf16_peak=r["forward_tflops"] / bf16,
              bf16_peak_source="measured MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
-             kernels="mma.sync m16n8k16 bf16 implicit GEMM (forward, data gradient); FP32 weight gradient")
+             kernels="tcgen05 bf16 implicit GEMM with TMEM accumulators, TMA-fed (forward, data gradient); "
+                     "mma.sync m16n8k16 for other channel counts; FP32 weight gradient")
     return r
 
 

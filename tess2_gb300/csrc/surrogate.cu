@@ -8,13 +8,14 @@
 // multiple of 16.
 //
 // conv3d forward (and the data gradient, the same product with the weights
-// flipped and transposed) is an implicit GEMM on the tensor cores:
-// mma.sync m16n8k16 bf16 x bf16 -> f32.  A warp takes 16 consecutive voxels
-// of one x row and every output channel; each tap and 16-channel slice of the
-// input is one k-step, its A fragment read straight from the input (zero
-// outside the grid) and its B fragment from the weights.  The weight gradient
-// reduces over voxels on the CUDA cores (FP32), per tap, with the block's
-// voxel slice staged in shared memory.
+// flipped and transposed) is an implicit GEMM on the tensor cores.  For 16 or
+// 32 channels in and out it runs on tcgen05 (k_conv3d_fwd_tc: TMA-fed slabs,
+// tensor-memory accumulators, warp-specialised); other channel counts, and
+// tessgpu_conv3d_set_engine(1), use mma.sync m16n8k16 (k_conv3d_fwd: a warp
+// takes 16 consecutive voxels of one x row and every output channel, each tap
+// and 16-channel slice of the input one k-step, A fragments read straight from
+// the input).  The weight gradient reduces over voxels on the CUDA cores
+// (FP32), per tap, with the block's voxel slice staged in shared memory.
 #include <cuda.h>   // CUtensorMap and its encoder's types (the encoder comes through the runtime)
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
@@ -174,7 +175,7 @@ struct TcLayout
     // full[STAGES], empty[STAGES], acc_full[2][TC_T], acc_empty[2], fin
     static constexpr int OFF_FULL = BAR, OFF_EMPTY = BAR + 8 * STAGES, OFF_ACCF = BAR + 16 * STAGES,
                          OFF_ACCE = OFF_ACCF + 16 * TC_T, OFF_FIN = OFF_ACCE + 16, OFF_TMEM = OFF_FIN + 8,
-                         OFF_ABORT = OFF_TMEM + 4, OFF_BIAS = OFF_ABORT + 4;
+                         OFF_ABORT = OFF_TMEM + 4, OFF_LAST = OFF_ABORT + 4, OFF_BIAS = OFF_LAST + 4 * STAGES;
     static constexpr int TOTAL = OFF_BIAS + 4 * COUT;
     // two sets of TC_T accumulators of COUT columns; a power of two >= 32
     static constexpr int ACOLS = 2 * TC_T * COUT;   // two sets of TC_T accumulators
@@ -205,16 +206,39 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity)
     return done != 0;
 }
 
-// bounded wait (about a second); gives up when another role raised the abort
-// flag, and raises it when the bound runs out
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr uint64_t TC_WAIT_NS = 2000000000ull;   // a wait gives up after 2 s of wall time
+
+// bounded wait (2 s of wall time, whatever the kernel's speed); gives up when
+// another role raised the abort flag, and raises it when the bound runs out
 __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t parity, volatile int* abort)
 {
-    for (int it = 0; it < 20000; ++it)
+    const uint64_t t0 = global_ns();
+    for (int it = 0; it < (1 << 26); ++it)
     {
         if (mbar_try(mbar, parity)) return true;
         if (*abort) return false;
+        if (global_ns() - t0 > TC_WAIT_NS) break;
     }
     *abort = 1;
+    return false;
+}
+
+// bounded wait that ignores the abort flag (draining copies before exit)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity)
+{
+    const uint64_t t0 = global_ns();
+    for (int it = 0; it < (1 << 26); ++it)
+    {
+        if (mbar_try(mbar, parity)) return true;
+        if (global_ns() - t0 > TC_WAIT_NS) break;
+    }
     return false;
 }
 
@@ -273,6 +297,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const uint32_t accf0 = s_base + L::OFF_ACCF, acce0 = s_base + L::OFF_ACCE, fin = s_base + L::OFF_FIN;
     volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
     float* sbias = reinterpret_cast<float*>(smem + L::OFF_BIAS);
+    int* last_slab = reinterpret_cast<int*>(smem + L::OFF_LAST);   // per ring slot: the last slab copied into it
 
     // all taps' weights -> shared memory: row co of tap t, chunk c at
     // t * TAPB + (co / 8) * (CH * 128) + c * 128 + (co % 8) * 16
@@ -283,6 +308,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         *reinterpret_cast<uint4*>(smem + t * L::TAPB + (r / 8) * (CH * 128) + c * 128 + (r % 8) * 16) = wg[i];
     }
     if (tid < COUT) sbias[tid] = bias ? bias[tid] : 0.0f;
+    for (int b = tid; b < S; b += TC_THREADS) last_slab[b] = -1;
     if (tid == 0)
     {
         for (int b = 0; b < S; ++b)
@@ -354,6 +380,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     const int x0 = tx0[t], sy = ty[t] + dy, sz = tz[t] + dz;
                     if (leader)
                     {
+                        last_slab[b] = m;
                         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full0 + 8 * b),
                                      "r"((uint32_t)(CH * TC_BOX * 16))
                                      : "memory");
@@ -432,8 +459,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(fin)
                          : "memory");
         __syncwarp();
-        for (int it = 0; it < 20000 && !mbar_try(fin, 0u); ++it)
-            ;
+        mbar_wait_bounded(fin, 0u);
         __syncwarp();
     }
     else
@@ -495,6 +521,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
+    // no copy may still be landing in shared memory when the CTA exits (after an abort the MMA
+    // warps may not have consumed every slab): wait for the last copy into each slot
+    for (int b = tid; b < S; b += TC_THREADS)
+    {
+        const int m = last_slab[b];
+        if (m >= 0) mbar_wait_bounded(full0 + 8 * b, (uint32_t)((m / S) & 1));
+    }
+    __syncthreads();
     if (tid == 0 && *abort) atomicExch(err, 1);
     if (warp == TC_MMA_WARP)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));

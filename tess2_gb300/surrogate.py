@@ -252,6 +252,37 @@ def forward_throughput(side, engine=ENGINE_TCGEN05, reps=5, seed=3):
     return ms, forward_flops(net.shape) / (ms * 1e-3) / 1e12
 
 
+def layer_times(side, engine=ENGINE_TCGEN05, reps=5, seed=3):
+    """Per-layer forward times on a side^3 grid of random input (random
+    weights): [(c_in, c_out, ms, TFLOP/s)], CUDA events around each launch."""
+    import torch
+    net = Surrogate((side, side, side), seed=seed)
+    g = torch.Generator(device=net.dev).manual_seed(seed)
+    x = torch.rand(side ** 3, device=net.dev, generator=g)
+    V = side ** 3
+    set_engine(engine)
+    try:
+        net.forward(x)   # fills every layer's input
+        torch.cuda.synchronize()
+        out = []
+        for li, (ci, co) in enumerate(LAYERS):
+            last = li == len(LAYERS) - 1
+            src = net.x16 if li == 0 else net.act[li - 1]
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            for _ in range(reps):
+                conv3d_fwd(src, net.shape, ci, co, net.wb[li], net.b[li], relu=not last,
+                           y_bf16=None if last else net.act[li], y_f32=net.out if last else None)
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms = ev[0].elapsed_time(ev[1]) / reps
+            out.append((ci, co, ms, 2.0 * 27 * ci * co * V / (ms * 1e-3) / 1e12))
+        check()
+    finally:
+        set_engine(ENGINE_TCGEN05)
+    return out
+
+
 def train_and_evaluate(n_train=32, n_val=8, n_particles=262144, side=64, epochs=8, lr=2e-3, seed=7, log=None):
     """Trains on fields the plain path makes and reports validation error, the
     CIC input's own error (the method without the network), and throughputs."""
@@ -302,8 +333,8 @@ def train_and_evaluate(n_train=32, n_val=8, n_particles=262144, side=64, epochs=
     fwd_ms = e0.elapsed_time(e1) / reps
     flops = forward_flops(net.shape)
     fwd_mma_ms = forward_ms(net, x, engine=ENGINE_MMA_SYNC)
-    return dict(forward_mma_sync_ms=fwd_mma_ms, n_train=n_train, n_val=n_val, particles=n_particles, grid=side, epochs=epochs, steps=steps,
+    return dict(n_train=n_train, n_val=n_val, particles=n_particles, grid=side, epochs=epochs, steps=steps,
                 train_mse=losses, val_rel_l2=float(np.mean(errs)), val_rel_l2_max=float(np.max(errs)),
                 cic_rel_l2=float(np.mean(base)), fields_s=t_fields, train_s=t_train,
                 train_step_ms=1e3 * t_train / max(steps, 1), forward_ms=fwd_ms, forward_gflop=flops / 1e9,
-                forward_tflops=flops / (fwd_ms * 1e-3) / 1e12, net=net)
+                forward_tflops=flops / (fwd_ms * 1e-3) / 1e12, forward_mma_sync_ms=fwd_mma_ms, net=net)
