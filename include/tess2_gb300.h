@@ -328,10 +328,11 @@ tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particles, int num_
 
 /* ---- the DTFE surrogate's kernels ------------------------------------ */
 /* A 3-D convolutional network that maps a cloud-in-cell density grid to the
-   DTFE grid.  Device pointers; activations bf16, channels last (voxel
-   (z * Y + y) * X + x, channel fastest); weights bf16 [27 taps][c_out][c_in],
-   tap = (dz * 3 + dy) * 3 + dx for offsets -1..1, zero outside the grid.
-   stream may be NULL.  Nothing is synchronised. */
+   DTFE grid.  Device pointers; activations bf16 (FP32 for the f32
+   outputs), chunk-planar: channel c of voxel v = (z * Y + y) * X + x at
+   element ((c / 8) * V + v) * 8 + c % 8, V = X * Y * Z; weights bf16
+   [27 taps][c_out][c_in], tap = (dz * 3 + dy) * 3 + dx for offsets -1..1,
+   zero outside the grid.  stream may be NULL.  Nothing is synchronised. */
 
 /* y = act(conv3x3x3(x, w) + bias): act = relu when relu != 0; bias may be
    NULL; y_bf16 and/or y_f32 receive it.  X a multiple of 16, c_in of 16,

@@ -1,11 +1,14 @@
 // The DTFE surrogate's kernels: a 3-D convolutional network that maps a
 // cloud-in-cell density grid to the DTFE density grid (log(1 + rho / mean)).
 //
-// Layout: activations channels-last, bf16, voxel index (z * Y + y) * X + x,
-// channel fastest; weights bf16 as [tap][c_out][c_in] (tap = (dz*3 + dy)*3 + dx
-// for offsets dz, dy, dx in -1..1), with an FP32 master copy for the update.
-// Channel counts are multiples of 16 (inputs) and 8 (outputs); X is a
-// multiple of 16.
+// Layout: activations chunk-planar, [c / 8][voxel][8 channels] (channel c of
+// voxel v at ((c / 8) * V + v) * 8 + c % 8, voxel index (z * Y + y) * X + x),
+// bf16, or FP32 for the f32 outputs; weights bf16 as [tap][c_out][c_in]
+// (tap = (dz*3 + dy)*3 + dx for offsets dz, dy, dx in -1..1), with an FP32
+// master copy for the update.  Channel counts are multiples of 16 (inputs)
+// and 8 (outputs); X is a multiple of 16.  A plane of 8 channels is then one
+// contiguous run along x, which is what the tensor-memory kernel's copies
+// fetch.
 //
 // conv3d forward (and the data gradient, the same product with the weights
 // flipped and transposed) is an implicit GEMM on the tensor cores.  For 16 or
@@ -25,6 +28,12 @@
 namespace {
 
 constexpr int MAX_COUT = 64;   // output channels per warp tile (8 n-tiles)
+
+// element index of channel c of voxel v in the chunk-planar layout
+__device__ __forceinline__ long long plidx(long long v, int c, long long V)
+{
+    return ((long long)(c >> 3) * V + v) * 8 + (c & 7);
+}
 
 __device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16* p)
 {
@@ -58,6 +67,7 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
     const int zz = (int)(warp / ((long long)(X / 16) * Y));
     const int x0 = xt * 16;
     const int gid = lane >> 2, tig = lane & 3;
+    const long long V = (long long)X * Y * Z;
     float acc[NT][4];
 #pragma unroll
     for (int n = 0; n < NT; ++n)
@@ -74,10 +84,10 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
         for (int c = 0; c < cin; c += 16)
         {
             uint32_t a[4];
-            a[0] = oka ? ld_pair(x + va * cin + c + tig * 2) : 0u;
-            a[1] = okb ? ld_pair(x + vb * cin + c + tig * 2) : 0u;
-            a[2] = oka ? ld_pair(x + va * cin + c + 8 + tig * 2) : 0u;
-            a[3] = okb ? ld_pair(x + vb * cin + c + 8 + tig * 2) : 0u;
+            a[0] = oka ? ld_pair(x + plidx(va, c + tig * 2, V)) : 0u;
+            a[1] = okb ? ld_pair(x + plidx(vb, c + tig * 2, V)) : 0u;
+            a[2] = oka ? ld_pair(x + plidx(va, c + 8 + tig * 2, V)) : 0u;
+            a[3] = okb ? ld_pair(x + plidx(vb, c + 8 + tig * 2, V)) : 0u;
 #pragma unroll
             for (int n = 0; n < NT; ++n)
             {
@@ -104,13 +114,13 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
         const long long va = v0 + gid, vb = v0 + gid + 8;
         if (y_bf16)
         {
-            *reinterpret_cast<__nv_bfloat162*>(y_bf16 + va * cout + co) = __floats2bfloat162_rn(r[0], r[1]);
-            *reinterpret_cast<__nv_bfloat162*>(y_bf16 + vb * cout + co) = __floats2bfloat162_rn(r[2], r[3]);
+            *reinterpret_cast<__nv_bfloat162*>(y_bf16 + plidx(va, co, V)) = __floats2bfloat162_rn(r[0], r[1]);
+            *reinterpret_cast<__nv_bfloat162*>(y_bf16 + plidx(vb, co, V)) = __floats2bfloat162_rn(r[2], r[3]);
         }
         if (y_f32)
         {
-            y_f32[va * cout + co] = r[0]; y_f32[va * cout + co + 1] = r[1];
-            y_f32[vb * cout + co] = r[2]; y_f32[vb * cout + co + 1] = r[3];
+            *reinterpret_cast<float2*>(y_f32 + plidx(va, co, V)) = make_float2(r[0], r[1]);
+            *reinterpret_cast<float2*>(y_f32 + plidx(vb, co, V)) = make_float2(r[2], r[3]);
         }
     }
 }
@@ -132,8 +142,9 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 // (group, (dz, dy), tile), so that the four MMA warps advance together.
 //   warps 4-5  TMA (each takes two tiles of a group): per slab one
 //              cp.async.bulk.tensor copy per plane (box 8
-//              channels x 130 positions of a 5-D view (8, c_in / 8, X, Y, Z)
-//              of the input); positions outside the grid (the x halo, rows
+//              channels x 130 positions of a 5-D view (8, X, Y, Z, c_in / 8)
+//              of the chunk-planar input: 2,080 contiguous bytes); positions
+//              outside the grid (the x halo, rows
 //              past y or z) arrive as zeros without a memory read; the
 //              buffer's "full" barrier completes on the copies' bytes;
 //   warps 6-9  MMA (one tile of each group each; warp 6 allocates tensor
@@ -290,6 +301,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // tile t: x row r = t / per_row (y = r % Y, z = r / Y), positions x0 = (t % per_row) * 128 ..
     const int per_row = (X + TC_M - 1) / TC_M;
     const int tiles = per_row * Y * Z;   // < 2^31, checked by the launcher
+    const long long V = (long long)X * Y * Z;
     const int ntl = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
     const uint32_t slab_a = s_base + L::WBYTES;   // buffer b at slab_a + b * SBYTES
@@ -390,7 +402,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                 "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
                                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(slab_a + b * L::SBYTES +
                                                                                   c * TC_PLANE),
-                                "l"(map), "r"(0), "r"(c), "r"(x0 - 1), "r"(sy), "r"(sz), "r"(full0 + 8 * b)
+                                "l"(map), "r"(0), "r"(x0 - 1), "r"(sy), "r"(sz), "r"(c), "r"(full0 + 8 * b)
                                 : "memory");
                     }
                     __syncwarp();
@@ -502,17 +514,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         f[c] = __uint_as_float(acc[c]) + sbias[c];
                         if (relu) f[c] = fmaxf(f[c], 0.0f);
                     }
+                    // chunk-planar: 8 channels (16 or 32 bytes) per plane, consecutive threads adjacent
                     if (y_bf16)
 #pragma unroll
                         for (int c = 0; c < COUT; c += 8)
-                            *reinterpret_cast<uint4*>(y_bf16 + vox * COUT + c) =
+                            *reinterpret_cast<uint4*>(y_bf16 + ((c >> 3) * V + vox) * 8) =
                                 make_uint4(pack_bf16(f[c], f[c + 1]), pack_bf16(f[c + 2], f[c + 3]),
                                            pack_bf16(f[c + 4], f[c + 5]), pack_bf16(f[c + 6], f[c + 7]));
                     if (y_f32)
 #pragma unroll
-                        for (int c = 0; c < COUT; c += 4)
-                            *reinterpret_cast<float4*>(y_f32 + vox * COUT + c) =
-                                make_float4(f[c], f[c + 1], f[c + 2], f[c + 3]);
+                        for (int c = 0; c < COUT; c += 8)
+                        {
+                            float4* o = reinterpret_cast<float4*>(y_f32 + ((c >> 3) * V + vox) * 8);
+                            o[0] = make_float4(f[c], f[c + 1], f[c + 2], f[c + 3]);
+                            o[1] = make_float4(f[c + 4], f[c + 5], f[c + 6], f[c + 7]);
+                        }
                 }
             }
             if (!ok) break;
@@ -551,7 +567,7 @@ __global__ void __launch_bounds__(256) k_conv3d_wgrad(const __nv_bfloat16* __res
     for (int i = threadIdx.x; i < VB * cout; i += blockDim.x)
     {
         const long long v = v0 + i / cout;
-        sdy[i] = v < V ? __bfloat162float(dy[v * cout + i % cout]) : 0.0f;
+        sdy[i] = v < V ? __bfloat162float(dy[plidx(v, i % cout, V)]) : 0.0f;
     }
     for (int i = threadIdx.x; i < VB * cin; i += blockDim.x)
     {
@@ -562,7 +578,7 @@ __global__ void __launch_bounds__(256) k_conv3d_wgrad(const __nv_bfloat16* __res
             const int xx = (int)(v % X), yy = (int)((v / X) % Y), zz = (int)(v / ((long long)X * Y));
             const int sx_ = xx + dx, sy = yy + dy_, sz = zz + dz;
             if (sx_ >= 0 && sx_ < X && sy >= 0 && sy < Y && sz >= 0 && sz < Z)
-                val = __bfloat162float(x[(((long long)sz * Y + sy) * X + sx_) * cin + i % cin]);
+                val = __bfloat162float(x[plidx(((long long)sz * Y + sy) * X + sx_, i % cin, V)]);
         }
         sx[i] = val;
     }
@@ -674,11 +690,12 @@ tessgpu_status launch_fwd_tc(const __nv_bfloat16* x, int X, int Y, int Z, const 
     const long long tiles = (long long)((X + TC_M - 1) / TC_M) * Y * Z;
     const EncodeTiled encode = tensor_map_encoder();
     if (tiles >= (1LL << 31) || !encode || ((uintptr_t)x & 15)) return TESSGPU_ERR_UNSUPPORTED;
-    // the input as (8 channels, CIN / 8 chunks, X, Y, Z); a box is one chunk plane of TC_BOX positions
+    // the chunk-planar input as (8 channels, X, Y, Z, CIN / 8 planes); a box is TC_BOX positions
+    // of one plane, 2,080 contiguous bytes
     CUtensorMap xmap;
-    const cuuint64_t dims[5] = { 8, (cuuint64_t)(CIN / 8), (cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z };
-    const cuuint64_t strides[4] = { 16, (cuuint64_t)CIN * 2, (cuuint64_t)X * CIN * 2, (cuuint64_t)X * Y * CIN * 2 };
-    const cuuint32_t box[5] = { 8, 1, (cuuint32_t)TC_BOX, 1, 1 };
+    const cuuint64_t dims[5] = { 8, (cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(CIN / 8) };
+    const cuuint64_t strides[4] = { 16, (cuuint64_t)X * 16, (cuuint64_t)X * Y * 16, (cuuint64_t)X * Y * Z * 16 };
+    const cuuint32_t box[5] = { 8, (cuuint32_t)TC_BOX, 1, 1, 1 };
     const cuuint32_t estride[5] = { 1, 1, 1, 1, 1 };
     if (encode(&xmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, (void*)x, dims, strides, box, estride,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,

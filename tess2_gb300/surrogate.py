@@ -53,6 +53,25 @@ def _p(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+def planar_shape(V, c):
+    """Shape of a chunk-planar activation tensor: channel c of voxel v at [c // 8, v, c % 8]."""
+    return (c // 8, V, 8)
+
+
+def to_planar(a):
+    """(V, c) channels-last numpy array -> (c // 8, V, 8) chunk-planar copy."""
+    a = np.asarray(a)
+    V, c = a.shape
+    return np.ascontiguousarray(a.reshape(V, c // 8, 8).transpose(1, 0, 2))
+
+
+def from_planar(a):
+    """(c // 8, V, 8) chunk-planar numpy array -> (V, c) channels-last copy."""
+    a = np.asarray(a)
+    n, V, _ = a.shape
+    return np.ascontiguousarray(a.transpose(1, 0, 2).reshape(V, n * 8))
+
+
 def conv3d_fwd(x, shape, cin, cout, w_bf16, bias=None, relu=False, y_bf16=None, y_f32=None, stream=None):
     Z, Y, X = shape
     _ok(_lib().tessgpu_conv3d_fwd(_p(x), X, Y, Z, cin, cout, _p(w_bf16), _p(bias), 1 if relu else 0, _p(y_bf16),
@@ -123,12 +142,13 @@ class Surrogate:
         self.step = 0
         self._sync_weights()
         V = self.V
-        self.x16 = torch.zeros((V, 16), dtype=torch.bfloat16, device=device)
-        self.act = [torch.empty((V, co), dtype=torch.bfloat16, device=device) for _, co in LAYERS]
-        self.out = torch.empty((V, LAYERS[-1][1]), dtype=torch.float32, device=device)
+        # activations chunk-planar: (c / 8, V, 8)
+        self.x16 = torch.zeros(planar_shape(V, 16), dtype=torch.bfloat16, device=device)
+        self.act = [torch.empty(planar_shape(V, co), dtype=torch.bfloat16, device=device) for _, co in LAYERS]
+        self.out = torch.empty(planar_shape(V, LAYERS[-1][1]), dtype=torch.float32, device=device)
         cmax = max(max(ci, co) for ci, co in LAYERS)
-        self.g32 = torch.empty(V * cmax, dtype=torch.float32, device=device)   # data gradient, (V, c) in front
-        self.dz = [torch.empty((V, co), dtype=torch.bfloat16, device=device) for _, co in LAYERS]
+        self.g32 = torch.empty(V * cmax, dtype=torch.float32, device=device)   # data gradient, (c/8, V, 8) in front
+        self.dz = [torch.empty(planar_shape(V, co), dtype=torch.bfloat16, device=device) for _, co in LAYERS]
         self.dw = [torch.zeros_like(w) for w in self.w]
         self.db = [torch.zeros_like(b) for b in self.b]
 
@@ -139,14 +159,14 @@ class Surrogate:
     def forward(self, x_log):
         """Prediction (V,) FP32 for the input log-density (V,) FP32 on the device."""
         self.x16.zero_()
-        self.x16[:, 0] = x_log.to(self.torch.bfloat16)
+        self.x16[0, :, 0] = x_log.to(self.torch.bfloat16)
         src = self.x16
         for li, (ci, co) in enumerate(LAYERS):
             last = li == len(LAYERS) - 1
             conv3d_fwd(src, self.shape, ci, co, self.wb[li], self.b[li], relu=not last,
                        y_bf16=None if last else self.act[li], y_f32=self.out if last else None)
             src = self.act[li]
-        return x_log + self.out[:, 0]
+        return x_log + self.out[0, :, 0]
 
     def train_step(self, x_log, y_log, lr=1e-3):
         """One Adam step on the mean squared error of the log-density; returns the loss."""
@@ -156,7 +176,7 @@ class Surrogate:
         loss = float((diff * diff).mean())
         L = len(LAYERS)
         self.dz[L - 1].zero_()
-        self.dz[L - 1][:, 0] = (diff * (2.0 / self.V)).to(torch.bfloat16)
+        self.dz[L - 1][0, :, 0] = (diff * (2.0 / self.V)).to(torch.bfloat16)
         for li in range(L - 1, -1, -1):
             ci, co = LAYERS[li]
             inp = self.x16 if li == 0 else self.act[li - 1]
@@ -165,7 +185,7 @@ class Surrogate:
             conv3d_wgrad(inp, self.dz[li], self.shape, ci, co, self.dw[li], self.db[li])
             if li > 0:
                 # the data gradient: the same convolution with the flipped, transposed weights
-                g = self.g32[:self.V * ci].view(self.V, ci)
+                g = self.g32[:self.V * ci].view(planar_shape(self.V, ci))
                 conv3d_fwd(self.dz[li], self.shape, co, ci, self.wt[li], None, relu=False, y_f32=g)
                 relu_grad(g, self.act[li - 1], self.dz[li - 1])
         self.step += 1

@@ -36,6 +36,18 @@ def test_oracle_gradients_finite_differences():
     assert abs((f(x, w, b + e) - f(x, w, b - e)) / (2 * h) - db[1]) < 1e-6
 
 
+def test_planar_layout_helpers():
+    """to_planar / from_planar: channel c of voxel v at [c // 8, v, c % 8], and back."""
+    from tess2_gb300 import surrogate as S
+    a = np.arange(5 * 32).reshape(5, 32)
+    p = S.to_planar(a)
+    assert p.shape == S.planar_shape(5, 32) == (4, 5, 8)
+    for v in range(5):
+        for c in range(32):
+            assert p[c // 8, v, c % 8] == a[v, c]
+    assert np.array_equal(S.from_planar(p), a)
+
+
 @pytest.fixture
 def engine(request):
     from tess2_gb300 import surrogate as S
@@ -66,26 +78,28 @@ def test_conv3d_kernels_vs_oracle(gpu_ctx, engine, shape, cin, cout):
     b = rng.standard_normal(cout).astype(np.float32)
     dy = _bf16(rng.standard_normal((Z, Y, X, cout)).astype(np.float32))
     dev = "cuda:0"
-    tx = torch.from_numpy(x).to(dev).to(torch.bfloat16).reshape(-1, cin)
+    V = Z * Y * X
+    # the kernels' chunk-planar layout; the oracle's is channels-last
+    tx = torch.from_numpy(S.to_planar(x.reshape(V, cin))).to(dev).to(torch.bfloat16)
     tw = torch.from_numpy(w).to(dev)
     wb = torch.empty((27, cout, cin), dtype=torch.bfloat16, device=dev)
     wt = torch.empty((27, cin, cout), dtype=torch.bfloat16, device=dev)
     S.prepare_weights(tw, cout, cin, wb, wt)
     tb = torch.from_numpy(b).to(dev)
-    y32 = torch.empty((Z * Y * X, cout), device=dev)
+    y32 = torch.empty(S.planar_shape(V, cout), device=dev)
     S.conv3d_fwd(tx, (Z, Y, X), cin, cout, wb, tb, relu=False, y_f32=y32)
     ref = conv3d(x, wq, b)
     torch.cuda.synchronize()
-    assert rel_l2(y32.cpu().numpy(), ref.reshape(-1, cout)) < 1e-5
+    assert rel_l2(S.from_planar(y32.cpu().numpy()), ref.reshape(-1, cout)) < 1e-5
     # relu and bf16 output
-    yb = torch.empty((Z * Y * X, cout), dtype=torch.bfloat16, device=dev)
+    yb = torch.empty(S.planar_shape(V, cout), dtype=torch.bfloat16, device=dev)
     S.conv3d_fwd(tx, (Z, Y, X), cin, cout, wb, tb, relu=True, y_bf16=yb)
-    assert rel_l2(yb.float().cpu().numpy(), np.maximum(ref, 0).reshape(-1, cout)) < 1e-2
+    assert rel_l2(S.from_planar(yb.float().cpu().numpy()), np.maximum(ref, 0).reshape(-1, cout)) < 1e-2
     # data gradient through the flipped weights
-    tdy = torch.from_numpy(dy).to(dev).to(torch.bfloat16).reshape(-1, cout)
-    dx = torch.empty((Z * Y * X, cin), device=dev)
+    tdy = torch.from_numpy(S.to_planar(dy.reshape(V, cout))).to(dev).to(torch.bfloat16)
+    dx = torch.empty(S.planar_shape(V, cin), device=dev)
     S.conv3d_fwd(tdy, (Z, Y, X), cout, cin, wt, None, relu=False, y_f32=dx)
-    assert rel_l2(dx.cpu().numpy(), conv3d_dgrad(dy, wq).reshape(-1, cin)) < 1e-5
+    assert rel_l2(S.from_planar(dx.cpu().numpy()), conv3d_dgrad(dy, wq).reshape(-1, cin)) < 1e-5
     # weight and bias gradient
     dw = torch.zeros((27, cout, cin), device=dev)
     db = torch.zeros(cout, device=dev)
@@ -105,7 +119,7 @@ def test_conv3d_engines_agree_large(gpu_ctx):
     from tess2_gb300 import surrogate as S
     Z, Y, X, c = 64, 48, 80, 32
     g = torch.Generator(device="cuda:0").manual_seed(7)
-    x = torch.randn((Z * Y * X, c), device="cuda:0", generator=g).to(torch.bfloat16)
+    x = torch.randn(S.planar_shape(Z * Y * X, c), device="cuda:0", generator=g).to(torch.bfloat16)
     w = torch.randn((27, c, c), device="cuda:0", generator=g) * 0.1
     wb = torch.empty((27, c, c), dtype=torch.bfloat16, device="cuda:0")
     wt = torch.empty_like(wb)
@@ -114,7 +128,7 @@ def test_conv3d_engines_agree_large(gpu_ctx):
     out = {}
     for e in (S.ENGINE_TCGEN05, S.ENGINE_MMA_SYNC):
         S.set_engine(e)
-        y = torch.full((Z * Y * X, c), float("nan"), device="cuda:0")
+        y = torch.full(S.planar_shape(Z * Y * X, c), float("nan"), device="cuda:0")
         S.conv3d_fwd(x, (Z, Y, X), c, c, wb, b, relu=True, y_f32=y)
         out[e] = y
     S.set_engine(S.ENGINE_TCGEN05)
