@@ -298,11 +298,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     constexpr int S = L::STAGES;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // tile t: x row r = t / per_row (y = r % Y, z = r / Y), positions x0 = (t % per_row) * 128 ..
+    // group q: TC_T tiles on consecutive y rows of one (x range, z): xt = q % per_row,
+    // yb = (q / per_row) % nyb, z = q / (per_row * nyb); tile t covers x0 = xt * 128 .. of row
+    // y = yb * TC_T + t (t < Tg = min(TC_T, Y - yb * TC_T))
     const int per_row = (X + TC_M - 1) / TC_M;
-    const int tiles = per_row * Y * Z;   // < 2^31, checked by the launcher
+    const int nyb = (Y + TC_T - 1) / TC_T;
+    const int groups = per_row * nyb * Z;   // < 2^31, checked by the launcher
     const long long V = (long long)X * Y * Z;
-    const int ntl = (int)blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int NG = (int)blockIdx.x < groups ? (groups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
     const uint32_t slab_a = s_base + L::WBYTES;   // buffer b at slab_a + b * SBYTES
     const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY;
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int b = 0; b < S; ++b)
         {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * b));   // expect_tx + copies
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty0 + 8 * b));    // one commit
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 3;" ::"r"(empty0 + 8 * b));    // three uses
         }
         for (int a = 0; a < 2 * TC_T; ++a)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(accf0 + 8 * a));     // one commit
@@ -348,10 +351,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
 
-    // Tiles go in groups of TC_T, one per MMA warp (the last group may be
-    // short).  Slabs run in the order (group, (dz, dy), tile of the group), one
-    // ring position each, so the issuers advance through (dz, dy) together.
-    const int FG = ntl / TC_T, rem = ntl % TC_T, NG = FG + (rem ? 1 : 0);
+    // A group's tiles share their slabs: for each dz the R = Tg + 2 input rows
+    // y0 - 1 .. y0 + Tg (y0 = yb * TC_T) are one slab each, used by up to three
+    // tiles (as dy = +1, 0, -1), so a group of four loads 18 slabs, not 36.
+    // Slabs run in the order (group, dz, row), one ring position each; a slab's
+    // "empty" barrier expects three arrivals: one commit per consuming tile and
+    // the rest from the loader.
     if (warp >= TC_TMA_WARP && warp < TC_TMA_WARP + TC_LOADERS)
     {
         // ---- TMA (tiles t = w, w + TC_LOADERS, .. of each group): per slab one copy per 8-channel
@@ -361,53 +366,42 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint64_t map = reinterpret_cast<uint64_t>(&xmap);
         if (leader) asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
         bool stop = false;
+        int mbase = 0;   // the group's first slab
         for (int G = 0; G < NG && !stop; ++G)
         {
-            const int Tg = G < FG ? TC_T : rem;
-            int tx0[TC_T], ty[TC_T], tz[TC_T];   // the group's tiles: first position, row
-#pragma unroll
-            for (int t = 0; t < TC_T; ++t)
+            const int q = (int)blockIdx.x + G * (int)gridDim.x;
+            const int xt = q % per_row, yb = (q / per_row) % nyb, z = q / (per_row * nyb);
+            const int Tg = min(TC_T, Y - yb * TC_T), R = Tg + 2;
+            const int x0 = xt * TC_M, y0 = yb * TC_T;
+            for (int j = w; j < 3 * R && !stop; j += TC_LOADERS)
             {
-                const int tile = (int)blockIdx.x + (G * TC_T + t) * (int)gridDim.x;
-                const int r = tile / per_row;
-                tx0[t] = (tile - r * per_row) * TC_M;
-                ty[t] = r % Y;
-                tz[t] = r / Y;
-            }
-            for (int g = 0; g < 9 && !stop; ++g)
-            {
-                const int dz = g / 3 - 1, dy = g % 3 - 1;
-#pragma unroll
-                for (int t = 0; t < TC_T; ++t)
+                const int dz = j / R - 1, rho = j % R;   // input row y0 - 1 + rho of plane z + dz
+                const int m = mbase + j, b = m % S;
+                if (m >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((m / S - 1) & 1), abort))
                 {
-                    if (t % TC_LOADERS != w) continue;
-                    if (t >= Tg) break;
-                    const int m = 9 * TC_T * G + g * Tg + t;   // every earlier group is full
-                    const int b = m % S;
-                    if (m >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((m / S - 1) & 1), abort))
-                    {
-                        stop = true;
-                        break;
-                    }
-                    const int x0 = tx0[t], sy = ty[t] + dy, sz = tz[t] + dz;
-                    if (leader)
-                    {
-                        last_slab[b] = m;
-                        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full0 + 8 * b),
-                                     "r"((uint32_t)(CH * TC_BOX * 16))
-                                     : "memory");
-#pragma unroll
-                        for (int c = 0; c < CH; ++c)
-                            asm volatile(
-                                "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                                " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(slab_a + b * L::SBYTES +
-                                                                                  c * TC_PLANE),
-                                "l"(map), "r"(0), "r"(x0 - 1), "r"(sy), "r"(sz), "r"(c), "r"(full0 + 8 * b)
-                                : "memory");
-                    }
-                    __syncwarp();
+                    stop = true;
+                    break;
                 }
+                // tiles using this row: t in [rho - 2, rho] within the group
+                const int ncons = min(Tg - 1, rho) - max(0, rho - 2) + 1;
+                if (leader)
+                {
+                    last_slab[b] = m;
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full0 + 8 * b),
+                                 "r"((uint32_t)(CH * TC_BOX * 16))
+                                 : "memory");
+#pragma unroll
+                    for (int c = 0; c < CH; ++c)
+                        asm volatile(
+                            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                            " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(slab_a + b * L::SBYTES + c * TC_PLANE),
+                            "l"(map), "r"(0), "r"(x0 - 1), "r"(y0 - 1 + rho), "r"(z + dz), "r"(c), "r"(full0 + 8 * b)
+                            : "memory");
+                    for (int k = ncons; k < 3; ++k) mbar_arrive(empty0 + 8 * b);   // absent consumers
+                }
+                __syncwarp();
             }
+            mbase += 3 * R;
         }
     }
     else if (warp >= TC_MMA_WARP)
@@ -424,17 +418,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint64_t adesc0 = umma_sdesc(slab_a, TC_PLANE, 128);
         const uint64_t bdesc0 = umma_sdesc(s_base, 128, CH * 128);
         bool go = true;
+        int mbase = 0;   // the group's first slab
         for (int G = 0; G < NG && go; ++G)
         {
-            const int Tg = G < FG ? TC_T : rem, A = G & 1;
-            if (ti >= Tg) break;   // only the last group is short
+            const int q = (int)blockIdx.x + G * (int)gridDim.x;
+            const int yb = (q / per_row) % nyb;
+            const int Tg = min(TC_T, Y - yb * TC_T), R = Tg + 2, A = G & 1;
             // the epilogue has read this accumulator set's tiles of group G - 2
             if (G >= 2 && !warp_wait(acce0 + 8 * A, (uint32_t)(((G - 2) >> 1) & 1), abort)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
             const uint32_t dcol = tbase + (uint32_t)((A * TC_T + ti) * COUT);
-            for (int g = 0; g < 9 && go; ++g)
+            // a warp without a tile in a short group still commits (nothing) to its accumulator's
+            // barrier, so that every slot completes one phase per group
+            for (int g = 0; g < 9 && go && ti < Tg; ++g)
             {
-                const int n = 9 * TC_T * G + g * Tg + ti, b = n % S;
+                const int n = mbase + (g / 3) * R + ti + g % 3, b = n % S;   // row y0 + ti + dy
                 go = warp_wait(full0 + 8 * b, (uint32_t)((n / S) & 1), abort);
                 if (!go) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
@@ -465,6 +463,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                                  accf0 + 8 * (A * TC_T + ti))
                              : "memory");
             __syncwarp();
+            mbase += 3 * R;
         }
         // every MMA issued has completed once fin's first phase does
         if (leader)
@@ -479,7 +478,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         // ---- epilogue (warps 0-3: tensor-memory lanes 32 warp .. 32 warp + 31) ----
         for (int G = 0; G < NG; ++G)
         {
-            const int Tg = G < FG ? TC_T : rem, A = G & 1;
+            const int q = (int)blockIdx.x + G * (int)gridDim.x;
+            const int xt = q % per_row, yb = (q / per_row) % nyb, z = q / (per_row * nyb);
+            const int Tg = min(TC_T, Y - yb * TC_T), A = G & 1;
             bool ok = true;
             for (int t = 0; t < Tg && ok; ++t)
             {
@@ -502,11 +503,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     asm volatile("tcgen05.fence::before_thread_sync;");
                     mbar_arrive(acce0 + 8 * A);
                 }
-                const int tile = (int)blockIdx.x + (G * TC_T + t) * (int)gridDim.x;
-                const int r = tile / per_row, ox = (tile - r * per_row) * TC_M + tid;
+                const int ox = xt * TC_M + tid;
                 if (ox < X)
                 {
-                    const long long vox = (long long)r * X + ox;
+                    const long long vox = ((long long)z * Y + yb * TC_T + t) * X + ox;
                     float f[COUT];
 #pragma unroll
                     for (int c = 0; c < COUT; ++c)
@@ -687,7 +687,7 @@ tessgpu_status launch_fwd_tc(const __nv_bfloat16* x, int X, int Y, int Z, const 
     }
     int* err = nullptr;
     if (cudaGetSymbolAddress((void**)&err, g_conv_err) != cudaSuccess) return TESSGPU_ERR_CUDA;
-    const long long tiles = (long long)((X + TC_M - 1) / TC_M) * Y * Z;
+    const long long tiles = (long long)((X + TC_M - 1) / TC_M) * ((Y + TC_T - 1) / TC_T) * Z;   // groups
     const EncodeTiled encode = tensor_map_encoder();
     if (tiles >= (1LL << 31) || !encode || ((uintptr_t)x & 15)) return TESSGPU_ERR_UNSUPPORTED;
     // the chunk-planar input as (8 channels, X, Y, Z, CIN / 8 planes); a box is TC_BOX positions
