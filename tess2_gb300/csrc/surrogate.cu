@@ -135,32 +135,33 @@ __global__ void __launch_bounds__(128) k_conv3d_fwd(const __nv_bfloat16* __restr
 // needs one slab: positions x0 - 1 .. x0 + 128 of the x row shifted by
 // (dy, dz), stored as c_in / 8 planes of 16-byte rows; the three taps
 // dx = -1, 0, 1 read that slab at row offsets 0, 1, 2 (start addresses 16
-// bytes apart in the shared-memory descriptor), so each input row is fetched
-// 9 times per output tile, not 27.  Warp roles, synchronised through
-// mbarriers only (no block-wide barrier in the loop):
-// Tiles go in groups of four, one per MMA warp, and slabs run in the order
-// (group, (dz, dy), tile), so that the four MMA warps advance together.
-//   warps 4-5  TMA (each takes two tiles of a group): per slab one
-//              cp.async.bulk.tensor copy per plane (box 8
-//              channels x 130 positions of a 5-D view (8, X, Y, Z, c_in / 8)
-//              of the chunk-planar input: 2,080 contiguous bytes); positions
-//              outside the grid (the x halo, rows
-//              past y or z) arrive as zeros without a memory read; the
-//              buffer's "full" barrier completes on the copies' bytes;
+// bytes apart in the shared-memory descriptor).  Tiles go in groups of four
+// on consecutive y rows of one (x range, z), one per MMA warp; for each dz the
+// group's six input rows y0 - 1 .. y0 + 4 are one slab each and serve up to
+// three tiles (as dy = +1, 0, -1), so a group loads 18 slabs instead of 36 and
+// an input row is fetched 4.5 times per output tile instead of 27.  Warp
+// roles, synchronised through mbarriers only (no block-wide barrier in the
+// loop):
+//   warps 4-5  TMA (alternate slabs of a group): per slab one
+//              cp.async.bulk.tensor copy per plane (box 8 channels x 130
+//              positions of a 5-D view (8, X, Y, Z, c_in / 8) of the
+//              chunk-planar input: 2,080 contiguous bytes); positions outside
+//              the grid (the x halo, rows past y or z) arrive as zeros without
+//              a memory read; the buffer's "full" barrier completes on the
+//              copies' bytes, its "empty" barrier on three arrivals (one commit
+//              per consuming tile, the loader standing in for absent ones);
 //   warps 6-9  MMA (one tile of each group each; warp 6 allocates tensor
 //              memory): the whole warp runs the loop (so the descriptors stay
 //              warp-uniform) and its elected lane issues tcgen05.mma
 //              (kind::f16, bf16 x bf16 -> f32) for each slab, commits them to
 //              the buffer's "empty" barrier and the finished tile to its
 //              accumulator's "full" barrier (two sets of four accumulators
-//              alternate between groups).  With 16-32 output channels an MMA
-//              is small and its issue cost, not the tensor pipe, sets the
-//              pace, hence four issuers;
+//              alternate between groups);
 //   warps 0-3  epilogue: tcgen05.ld of row tid (warp w reads lanes 32w..),
 //              release the accumulators, bias, ReLU, store the rows inside X.
 // Every wait is bounded; a timed-out wait raises an abort flag that ends every
-// role's loop, the kernel reports it in *err, waits a bounded time for its
-// MMAs and frees its tensor memory.
+// role's loop, the kernel reports it in *err, waits for the copies in flight
+// and its MMAs (bounded) and frees its tensor memory.
 constexpr int TC_M = 128;      // GEMM rows per tile
 constexpr int TC_SLAB = 136;   // rows per slab plane (>= 130, a multiple of 8)
 constexpr int TC_PLANE = TC_SLAB * 16;
