@@ -396,6 +396,8 @@ def time_surrogate(args, peaks, local):
              fields_per_s=1e3 / r["forward_ms"], plain_gpu_fields_per_s=1e3 / dtfe_ms,
              plain_with_delaunay_fields_per_s=1.0 / (t_qhull + dtfe_ms * 1e-3),
              speedup_vs_plain_gpu=dtfe_ms / r["forward_ms"],
+             fields_per_s_graph=1e3 / r["forward_graph_ms"],
+             speedup_vs_plain_gpu_graph=dtfe_ms / r["forward_graph_ms"],
              speedup_vs_plain_with_delaunay=(t_qhull + dtfe_ms * 1e-3) / (r["forward_ms"] * 1e-3),
              tensor_frac_of_bf16_peak=r["forward_tflops"] / bf16,
              bf16_peak_source="measured MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",

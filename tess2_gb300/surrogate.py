@@ -53,6 +53,16 @@ def _p(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+def _s(stream):
+    """The CUDA stream for a call: torch's current stream unless one is given
+    (so that the kernels follow torch's ordering and can be captured in a CUDA
+    graph)."""
+    if stream is not None:
+        return stream
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
 def planar_shape(V, c):
     """Shape of a chunk-planar activation tensor: channel c of voxel v at [c // 8, v, c % 8]."""
     return (c // 8, V, 8)
@@ -75,7 +85,7 @@ def from_planar(a):
 def conv3d_fwd(x, shape, cin, cout, w_bf16, bias=None, relu=False, y_bf16=None, y_f32=None, stream=None):
     Z, Y, X = shape
     _ok(_lib().tessgpu_conv3d_fwd(_p(x), X, Y, Z, cin, cout, _p(w_bf16), _p(bias), 1 if relu else 0, _p(y_bf16),
-                                  _p(y_f32), stream), "tessgpu_conv3d_fwd")
+                                  _p(y_f32), _s(stream)), "tessgpu_conv3d_fwd")
 
 
 ENGINE_TCGEN05, ENGINE_MMA_SYNC = 0, 1
@@ -90,25 +100,27 @@ def set_engine(engine):
 
 def check(stream=None):
     """Synchronises; raises if a tcgen05 convolution gave up on a bounded wait."""
-    _ok(_lib().tessgpu_conv3d_check(stream), "tessgpu_conv3d_check")
+    _ok(_lib().tessgpu_conv3d_check(_s(stream)), "tessgpu_conv3d_check")
 
 
 def conv3d_wgrad(x, dy, shape, cin, cout, dw, db=None, stream=None):
     Z, Y, X = shape
-    _ok(_lib().tessgpu_conv3d_wgrad(_p(x), _p(dy), X, Y, Z, cin, cout, _p(dw), _p(db), stream), "tessgpu_conv3d_wgrad")
+    _ok(_lib().tessgpu_conv3d_wgrad(_p(x), _p(dy), X, Y, Z, cin, cout, _p(dw), _p(db), _s(stream)),
+        "tessgpu_conv3d_wgrad")
 
 
 def prepare_weights(w, cout, cin, w_bf16, wt_bf16, stream=None):
-    _ok(_lib().tessgpu_conv3d_prepare_weights(_p(w), cout, cin, _p(w_bf16), _p(wt_bf16), stream),
+    _ok(_lib().tessgpu_conv3d_prepare_weights(_p(w), cout, cin, _p(w_bf16), _p(wt_bf16), _s(stream)),
         "tessgpu_conv3d_prepare_weights")
 
 
 def relu_grad(g, y, out, stream=None):
-    _ok(_lib().tessgpu_relu_grad(_p(g), _p(y), g.numel(), _p(out), stream), "tessgpu_relu_grad")
+    _ok(_lib().tessgpu_relu_grad(_p(g), _p(y), g.numel(), _p(out), _s(stream)), "tessgpu_relu_grad")
 
 
 def adam(w, g, m, v, lr, step, b1=0.9, b2=0.999, eps=1e-8, stream=None):
-    _ok(_lib().tessgpu_adam(_p(w), _p(g), _p(m), _p(v), w.numel(), lr, b1, b2, eps, step, stream), "tessgpu_adam")
+    _ok(_lib().tessgpu_adam(_p(w), _p(g), _p(m), _p(v), w.numel(), lr, b1, b2, eps, step, _s(stream)),
+        "tessgpu_adam")
 
 
 def forward_flops(shape):
@@ -167,6 +179,27 @@ class Surrogate:
                        y_bf16=None if last else self.act[li], y_f32=self.out if last else None)
             src = self.act[li]
         return x_log + self.out[0, :, 0]
+
+    def forward_graph(self, x_log):
+        """forward() replayed from a CUDA graph captured on the first call (the
+        five convolution launches and the elementwise work, no host work per
+        call).  Returns a view of the graph's own output buffer, overwritten by
+        the next call; weights updated in place since are seen."""
+        torch = self.torch
+        if getattr(self, "_graph", None) is None:
+            self._gx = x_log.detach().clone()
+            side = torch.cuda.Stream(device=self.dev)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                self.forward(self._gx)   # launch set-up (attributes, first use) outside the capture
+            torch.cuda.current_stream().wait_stream(side)
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                self._gy = self.forward(self._gx)
+            self._graph = graph
+        self._gx.copy_(x_log)
+        self._graph.replay()
+        return self._gy
 
     def train_step(self, x_log, y_log, lr=1e-3):
         """One Adam step on the mean squared error of the log-density; returns the loss."""
@@ -239,20 +272,22 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-def forward_ms(net, x, engine=ENGINE_TCGEN05, reps=10):
+def forward_ms(net, x, engine=ENGINE_TCGEN05, reps=10, graph=False):
     """Mean forward time (ms, CUDA events) of net on the resident input x with
-    the given convolution engine; the engine is reset to tcgen05 after."""
+    the given convolution engine (graph: replayed from a CUDA graph); the
+    engine is reset to tcgen05 after."""
     import torch
     set_engine(engine)
+    fwd = net.forward_graph if graph else net.forward
     try:
         for _ in range(3):
-            net.forward(x)
+            fwd(x)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(reps):
-            net.forward(x)
+            fwd(x)
         e1.record()
         torch.cuda.synchronize()
         check()
@@ -353,8 +388,10 @@ def train_and_evaluate(n_train=32, n_val=8, n_particles=262144, side=64, epochs=
     fwd_ms = e0.elapsed_time(e1) / reps
     flops = forward_flops(net.shape)
     fwd_mma_ms = forward_ms(net, x, engine=ENGINE_MMA_SYNC)
+    fwd_graph_ms = forward_ms(net, x, graph=True)
     return dict(n_train=n_train, n_val=n_val, particles=n_particles, grid=side, epochs=epochs, steps=steps,
                 train_mse=losses, val_rel_l2=float(np.mean(errs)), val_rel_l2_max=float(np.max(errs)),
                 cic_rel_l2=float(np.mean(base)), fields_s=t_fields, train_s=t_train,
                 train_step_ms=1e3 * t_train / max(steps, 1), forward_ms=fwd_ms, forward_gflop=flops / 1e9,
-                forward_tflops=flops / (fwd_ms * 1e-3) / 1e12, forward_mma_sync_ms=fwd_mma_ms, net=net)
+                forward_tflops=flops / (fwd_ms * 1e-3) / 1e12, forward_mma_sync_ms=fwd_mma_ms,
+                forward_graph_ms=fwd_graph_ms, net=net)

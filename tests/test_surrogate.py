@@ -139,6 +139,24 @@ def test_conv3d_engines_agree_large(gpu_ctx):
 
 
 @pytest.mark.gpu
+def test_forward_graph_matches_forward(gpu_ctx):
+    """The CUDA-graph replay gives the eager forward's output bit for bit, and
+    sees weights updated in place after the capture."""
+    import torch
+    from tess2_gb300 import surrogate as S
+    net = S.Surrogate((16, 12, 32), seed=4)
+    g = torch.Generator(device="cuda:0").manual_seed(5)
+    x1 = torch.rand(16 * 12 * 32, device="cuda:0", generator=g)
+    x2 = torch.rand(16 * 12 * 32, device="cuda:0", generator=g)
+    eager = net.forward(x1).clone()
+    assert torch.equal(net.forward_graph(x1).clone(), eager)
+    assert torch.equal(net.forward_graph(x2).clone(), net.forward(x2).clone())
+    net.train_step(x1, x2, lr=1e-2)   # new weights, same buffers
+    assert torch.equal(net.forward_graph(x1).clone(), net.forward(x1).clone())
+    S.check()
+
+
+@pytest.mark.gpu
 def test_surrogate_learns(gpu_ctx):
     """A few Adam steps on a handful of small fields lower the loss, and the
     trained network beats its own input (the CIC grid) against DTFE on the
