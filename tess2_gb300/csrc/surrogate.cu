@@ -551,6 +551,251 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
 }
 
+// ---------------------------------------------------------------------------
+// the weight gradient on the tensor cores (tcgen05)
+// ---------------------------------------------------------------------------
+// dw[tap][co][ci] += sum_v dy[v][co] x[v + tap][ci].  A tile is 128 voxels
+// x0 .. x0 + 127 of one x row; for the tap (dz, dy, dx) its share is
+// sum_r dyT[r][co] slab[r + dx + 1][ci], with dyT the tile of the output
+// gradient (zero past X) and slab positions x0 - 1 .. x0 + 128 of the input row
+// shifted by (dy, dz), both chunk-planar.  As one MMA per 16 rows r: D[co][ci]
+// with A = dyT (M = 128: c_out rows and zero planes up to 128), B = the slab
+// read from row dx + 1 (N = c_in), both MN-major straight from the planes
+// (LBO = 8 rows, SBO = one plane).  A CTA takes one dz (blockIdx.x % 3) and
+// keeps the nine taps of that dz in tensor memory across all of its tiles (9
+// accumulators of c_in columns); at the end warps 0-3 read them (lane = c_out)
+// and add them to dw, one atomic per weight and CTA.  Warp 4 loads a tile
+// (the dyT planes and three slabs) by TMA into one of two stages while warp 5
+// issues the previous tile's 72 MMAs.  Waits are bounded as in the forward
+// kernel.
+constexpr int WG_TILE = 128;
+constexpr int WG_APLANE = WG_TILE * 16;            // one plane of dyT
+constexpr int WG_ABYTES = 16 * WG_APLANE;          // 16 planes: M = 128 (unused planes stay zero)
+constexpr int WG_THREADS_TC = 192;                 // warps 0-3 epilogue, 4 TMA, 5 MMA
+constexpr int WG_MIN_SMEM = 120 * 1024;            // one CTA per SM (its tensor memory is the SM's half)
+
+template <int COUT, int CIN>
+struct WgLayout
+{
+    static constexpr int CH = CIN / 8;
+    static constexpr int SBYTES = CH * TC_PLANE;             // one slab
+    static constexpr int STAGE = WG_ABYTES + 3 * SBYTES;     // dyT + the three slabs of a dz
+    static constexpr int BAR = 2 * STAGE;                    // full[2], empty[2], fin, tmem, abort, last[2]
+    static constexpr int OFF_FULL = BAR, OFF_EMPTY = BAR + 16, OFF_FIN = BAR + 32, OFF_TMEM = BAR + 40,
+                         OFF_ABORT = BAR + 44, OFF_LAST = BAR + 48;
+    static constexpr int USED = OFF_LAST + 8;
+    static constexpr int TOTAL = USED > WG_MIN_SMEM ? USED : WG_MIN_SMEM;
+    static constexpr int ACOLS = 9 * CIN;
+    static constexpr int TCOLS = ACOLS <= 128 ? 128 : (ACOLS <= 256 ? 256 : 512);
+    static constexpr uint32_t TX = (uint32_t)((COUT / 8) * WG_TILE * 16 + 3 * CH * TC_BOX * 16);
+    static_assert(ACOLS <= 512, "tensor memory");
+    static_assert(TOTAL <= TC_SMEM, "shared memory");
+};
+
+template <int COUT, int CIN>
+__global__ void __launch_bounds__(WG_THREADS_TC, 1)
+    k_conv3d_wgrad_tc(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap dymap, int X,
+                      int Y, int Z, float* dw, int* err)
+{
+    using L = WgLayout<COUT, CIN>;
+    constexpr int CH = L::CH;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int per_row = (X + WG_TILE - 1) / WG_TILE;
+    const int tiles = per_row * Y * Z;   // < 2^31, checked by the launcher
+    const int dz = (int)(blockIdx.x % 3) - 1, lanes = (int)gridDim.x / 3, me = (int)blockIdx.x / 3;
+    const int ntl = me < tiles ? (tiles - 1 - me) / lanes + 1 : 0;
+    const uint32_t s_base = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY, fin = s_base + L::OFF_FIN;
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
+    int* last = reinterpret_cast<int*>(smem + L::OFF_LAST);   // per stage: the last tile loaded into it
+
+    // the dyT planes past c_out stay zero for the whole kernel
+    for (int i = tid; i < 2 * (16 - COUT / 8) * WG_APLANE / 16; i += blockDim.x)
+    {
+        const int per = (16 - COUT / 8) * WG_APLANE / 16, s = i / per, j = i % per;
+        reinterpret_cast<uint4*>(smem + s * L::STAGE + (COUT / 8) * WG_APLANE)[j] = make_uint4(0, 0, 0, 0);
+    }
+    if (tid < 2) last[tid] = -1;
+    if (tid == 0)
+    {
+        for (int s = 0; s < 2; ++s)
+        {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * s));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(empty0 + 8 * s));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fin));
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 5)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_base + L::OFF_TMEM),
+                     "r"(L::TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
+    bool ok = true;
+
+    if (warp == 4)
+    {
+        // ---- TMA: per tile the dyT planes and, for dy = -1, 0, 1, the slab of row (y + dy, z + dz) ----
+        const bool leader = elect_one();
+        const uint64_t xm = reinterpret_cast<uint64_t>(&xmap), dm = reinterpret_cast<uint64_t>(&dymap);
+        for (int k = 0; k < ntl; ++k)
+        {
+            const int s = k & 1;
+            if (k >= 2 && !warp_wait(empty0 + 8 * s, (uint32_t)(((k - 2) >> 1) & 1), abort)) break;
+            const int t = me + k * lanes, r = t / per_row, x0 = (t - r * per_row) * WG_TILE;
+            const int y = r % Y, z = r / Y;
+            const uint32_t st = s_base + s * L::STAGE;
+            if (leader)
+            {
+                last[s] = k;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(full0 + 8 * s),
+                             "r"(L::TX)
+                             : "memory");
+#pragma unroll
+                for (int p = 0; p < COUT / 8; ++p)
+                    asm volatile(
+                        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(st + p * WG_APLANE),
+                        "l"(dm), "r"(0), "r"(x0), "r"(y), "r"(z), "r"(p), "r"(full0 + 8 * s)
+                        : "memory");
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+#pragma unroll
+                    for (int c = 0; c < CH; ++c)
+                        asm volatile(
+                            "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                            " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(st + WG_ABYTES + d * L::SBYTES +
+                                                                              c * TC_PLANE),
+                            "l"(xm), "r"(0), "r"(x0 - 1), "r"(y + d - 1), "r"(z + dz), "r"(c), "r"(full0 + 8 * s)
+                            : "memory");
+            }
+            __syncwarp();
+        }
+    }
+    else if (warp == 5)
+    {
+        // ---- MMA: D[tap (dy, dx)][co][ci] += dyT^T slab, 8 MMAs of 16 rows per tap and tile ----
+        // D f32; A, B bf16, both MN-major (bits 15, 16); N = CIN, M = 128
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                               ((uint32_t)(CIN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+        const bool leader = elect_one();
+        const uint64_t adesc0 = umma_sdesc(s_base, 128, WG_APLANE);
+        const uint64_t bdesc0 = umma_sdesc(s_base + WG_ABYTES, 128, TC_PLANE);
+        for (int k = 0; k < ntl && ok; ++k)
+        {
+            const int s = k & 1;
+            ok = warp_wait(full0 + 8 * s, (uint32_t)((k >> 1) & 1), abort);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+#pragma unroll
+                for (int sh = 0; sh < 3; ++sh)
+#pragma unroll
+                    for (int ks = 0; ks < WG_TILE / 16; ++ks)
+                    {
+                        const uint64_t da = adesc0 + (uint64_t)((s * L::STAGE + ks * 256) >> 4);
+                        const uint64_t db =
+                            bdesc0 + (uint64_t)((s * L::STAGE + d * L::SBYTES + sh * 16 + ks * 256) >> 4);
+                        const uint32_t acc = (k > 0 || ks > 0) ? 1u : 0u;
+                        if (leader)
+                            asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(
+                                             tbase + (uint32_t)((d * 3 + sh) * CIN)),
+                                         "l"(da), "l"(db), "r"(idesc), "r"(acc));
+                    }
+            if (leader)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 empty0 + 8 * s)
+                             : "memory");
+            __syncwarp();
+        }
+        if (leader)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(fin)
+                         : "memory");
+        __syncwarp();
+        if (!mbar_wait_bounded(fin, 0u)) *abort = 1;
+        __syncwarp();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // no copy may still be landing when the CTA reads or exits
+    if (tid < 2 && last[tid] >= 0) mbar_wait_bounded(full0 + 8 * tid, (uint32_t)((last[tid] >> 1) & 1));
+    __syncthreads();
+    const bool good = *abort == 0;
+    if (warp < 4 && good && ntl > 0)
+    {
+        // lane 32 warp + l = row co of every accumulator
+        const int co = tid;
+#pragma unroll 1
+        for (int tap = 0; tap < 9; ++tap)
+        {
+            uint32_t v[CIN];
+#pragma unroll
+            for (int c = 0; c < CIN; c += 16)
+                tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(tap * CIN + c), v + c);
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+            if (co < COUT)
+            {
+                float* out = dw + ((long long)((dz + 1) * 9 + tap) * COUT + co) * CIN;
+#pragma unroll
+                for (int c = 0; c < CIN; ++c) atomicAdd(out + c, __uint_as_float(v[c]));
+            }
+        }
+    }
+    if (tid == 0 && !good) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 5)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
+}
+
+// db[co] += sum_v dy[v][co] (chunk-planar dy): block partial sums, one atomic per channel and block
+__global__ void __launch_bounds__(256) k_bias_grad(const __nv_bfloat16* __restrict__ dy, long long V, int cout,
+                                                   float* db)
+{
+    __shared__ float part[8][32];
+    const int plane = blockIdx.y;   // 8 channels
+    float acc[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    {
+        const uint4 q = reinterpret_cast<const uint4*>(dy + ((long long)plane * V + v) * 8)[0];
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&q);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+        {
+            const float2 f = __bfloat1622float2(h[i]);
+            acc[2 * i] += f.x;
+            acc[2 * i + 1] += f.y;
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+    {
+        float a = acc[i];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) part[i][wid] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8)
+    {
+        float a = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) a += part[threadIdx.x][w];
+        atomicAdd(&db[plane * 8 + threadIdx.x], a);
+    }
+}
+
 // dw[tap][co][ci] += sum_v dy[v][co] x[v + tap][ci]; db[co] += sum_v dy[v][co]
 // (FP32 accumulation).  Block: one tap, VB voxels of one x row band; thread
 // (co, ci) pairs.
@@ -708,6 +953,54 @@ tessgpu_status launch_fwd_tc(const __nv_bfloat16* x, int X, int Y, int Z, const 
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
+// a chunk-planar activation (c channels) as (8 channels, X, Y, Z, c / 8); a box is rows positions of one plane
+bool planar_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int rows)
+{
+    const EncodeTiled encode = tensor_map_encoder();
+    if (!encode || ((uintptr_t)base & 15)) return false;
+    const cuuint64_t dims[5] = { 8, (cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(c / 8) };
+    const cuuint64_t strides[4] = { 16, (cuuint64_t)X * 16, (cuuint64_t)X * Y * 16, (cuuint64_t)X * Y * Z * 16 };
+    const cuuint32_t box[5] = { 8, (cuuint32_t)rows, 1, 1, 1 };
+    const cuuint32_t estride[5] = { 1, 1, 1, 1, 1 };
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int COUT, int CIN>
+tessgpu_status launch_wgrad_tc(const __nv_bfloat16* x, const __nv_bfloat16* dy, int X, int Y, int Z, float* dw,
+                               cudaStream_t s)
+{
+    using L = WgLayout<COUT, CIN>;
+    static int sms_of[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
+    if (!sms_of[dev])
+    {
+        int optin = 0, sms = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (optin < L::TOTAL || sms < 3) return TESSGPU_ERR_UNSUPPORTED;
+        if (cudaFuncSetAttribute(k_conv3d_wgrad_tc<COUT, CIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 L::TOTAL) != cudaSuccess)
+            return TESSGPU_ERR_CUDA;
+        sms_of[dev] = sms;
+    }
+    int* err = nullptr;
+    if (cudaGetSymbolAddress((void**)&err, g_conv_err) != cudaSuccess) return TESSGPU_ERR_CUDA;
+    const long long tiles = (long long)((X + WG_TILE - 1) / WG_TILE) * Y * Z;
+    CUtensorMap xmap, dymap;
+    if (tiles >= (1LL << 31) || !planar_map(&xmap, x, X, Y, Z, CIN, TC_BOX) ||
+        !planar_map(&dymap, dy, X, Y, Z, COUT, WG_TILE))
+        return TESSGPU_ERR_UNSUPPORTED;
+    // one CTA per SM, a third of them per dz
+    long long lanes = sms_of[dev] / 3;
+    if (lanes > tiles) lanes = tiles;
+    k_conv3d_wgrad_tc<COUT, CIN><<<(unsigned)(3 * lanes), WG_THREADS_TC, L::TOTAL, s>>>(xmap, dymap, X, Y, Z, dw,
+                                                                                      err);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
 }  // namespace
 
 extern "C" tessgpu_status tessgpu_conv3d_set_engine(int engine)
@@ -771,9 +1064,28 @@ extern "C" tessgpu_status tessgpu_conv3d_wgrad(const void* x, const void* dy, in
     if (!x || !dy || !dw || X <= 0 || Y <= 0 || Z <= 0 || cin <= 0 || cout <= 0 || cin * cout > 64 * 64)
         return TESSGPU_ERR_INVALID;
     const long long V = (long long)X * Y * Z;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (g_conv_engine == 0)
+    {
+        // tcgen05 for 16 or 32 channels in and out (TESSGPU_ERR_UNSUPPORTED: the FP32 kernel below)
+        const __nv_bfloat16* xx = (const __nv_bfloat16*)x;
+        const __nv_bfloat16* dd = (const __nv_bfloat16*)dy;
+        tessgpu_status st = TESSGPU_ERR_UNSUPPORTED;
+        if (cin == 16 && cout == 16) st = launch_wgrad_tc<16, 16>(xx, dd, X, Y, Z, dw, s);
+        if (cin == 16 && cout == 32) st = launch_wgrad_tc<32, 16>(xx, dd, X, Y, Z, dw, s);
+        if (cin == 32 && cout == 16) st = launch_wgrad_tc<16, 32>(xx, dd, X, Y, Z, dw, s);
+        if (cin == 32 && cout == 32) st = launch_wgrad_tc<32, 32>(xx, dd, X, Y, Z, dw, s);
+        if (st == TESSGPU_OK && db)
+        {
+            long long nb = (V + 255) / 256;
+            if (nb > 256) nb = 256;
+            k_bias_grad<<<dim3((unsigned)nb, (unsigned)(cout / 8)), 256, 0, s>>>(dd, V, cout, db);
+            st = cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+        }
+        if (st != TESSGPU_ERR_UNSUPPORTED) return st;
+    }
     dim3 grid((unsigned)((V + VB - 1) / VB), 27);
     const size_t smem = sizeof(float) * VB * (cin + cout);
-    cudaStream_t s = (cudaStream_t)stream;
     if (smem > 48 * 1024)
         cudaFuncSetAttribute(k_conv3d_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_conv3d_wgrad<<<grid, 256, smem, s>>>((const __nv_bfloat16*)x, (const __nv_bfloat16*)dy, X, Y, Z, cin, cout, dw,
