@@ -343,7 +343,9 @@ tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particles, int num_
 tessgpu_status tessgpu_conv3d_fwd(const void* x, int X, int Y, int Z, int c_in, int c_out, const void* w,
                                   const float* bias, int relu, void* y_bf16, float* y_f32, void* stream);
 /* dw[tap][co][ci] += sum_v dy[v][co] x[v + tap][ci] and db[co] += sum_v dy[v][co]
-   (FP32; db may be NULL); c_in * c_out <= 4096 */
+   (FP32 sums; db may be NULL); c_in * c_out <= 4096.  tcgen05 (bf16 products,
+   FP32 accumulation in tensor memory) when c_in and c_out are 16 or 32, FP32
+   on the CUDA cores otherwise. */
 tessgpu_status tessgpu_conv3d_wgrad(const void* x, const void* dy, int X, int Y, int Z, int c_in, int c_out,
                                     float* dw, float* db, void* stream);
 /* bf16 weights for the forward pass and, flipped and transposed
@@ -351,7 +353,8 @@ tessgpu_status tessgpu_conv3d_wgrad(const void* x, const void* dy, int X, int Y,
 tessgpu_status tessgpu_conv3d_prepare_weights(const float* w, int c_out, int c_in, void* w_bf16, void* wt_bf16,
                                               void* stream);
 /* engine 0 (the default): tcgen05 where the channel counts allow; 1: the
-   mma.sync kernel for every shape.  Process-wide. */
+   mma.sync forward and the FP32 weight gradient for every shape.
+   Process-wide. */
 tessgpu_status tessgpu_conv3d_set_engine(int engine);
 /* Synchronises stream; TESSGPU_ERR_TIMEOUT (and the flag cleared) when a
    tcgen05 convolution gave up on a bounded wait since the last check. */
