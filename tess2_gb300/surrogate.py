@@ -338,6 +338,37 @@ def layer_times(side, engine=ENGINE_TCGEN05, reps=5, seed=3):
     return out
 
 
+def wgrad_times(side, engine=ENGINE_TCGEN05, reps=3, seed=5):
+    """Per-layer weight-gradient times on a side^3 grid of random activations
+    and output gradients: [(c_in, c_out, ms, TFLOP/s)] (2 * 27 * c_in * c_out
+    FLOP per voxel), CUDA events around each launch."""
+    import torch
+    V = side ** 3
+    g = torch.Generator(device="cuda:0").manual_seed(seed)
+    set_engine(engine)
+    out = []
+    try:
+        for ci, co in LAYERS:
+            x = torch.randn(planar_shape(V, ci), device="cuda:0", generator=g).to(torch.bfloat16)
+            dy = torch.randn(planar_shape(V, co), device="cuda:0", generator=g).to(torch.bfloat16)
+            dw = torch.zeros((27, co, ci), device="cuda:0")
+            db = torch.zeros(co, device="cuda:0")
+            conv3d_wgrad(x, dy, (side, side, side), ci, co, dw, db)
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            for _ in range(reps):
+                conv3d_wgrad(x, dy, (side, side, side), ci, co, dw, db)
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms = ev[0].elapsed_time(ev[1]) / reps
+            out.append((ci, co, ms, 2.0 * 27 * ci * co * V / (ms * 1e-3) / 1e12))
+        check()
+    finally:
+        set_engine(ENGINE_TCGEN05)
+    return out
+
+
 def train_and_evaluate(n_train=32, n_val=8, n_particles=262144, side=64, epochs=8, lr=2e-3, seed=7, log=None):
     """Trains on fields the plain path makes and reports validation error, the
     CIC input's own error (the method without the network), and throughputs."""
