@@ -27,6 +27,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -92,7 +93,9 @@ class ClockSampler:
 
     def __init__(self, device=0):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples (the JSON line carries their summary); BENCH_CLOCKS_DIR keeps them elsewhere
+        self.path = os.path.join(os.environ.get("BENCH_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"clocks_{os.getpid()}.csv")
         self.device = device
 
     def start(self):
@@ -506,7 +509,7 @@ def run_gpu(args):
 
     extra = {}
     if not args.no_extra:
-        # plain FP64 GPU path: the comparison target, and the judge at full size
+        # plain FP64 GPU path: the comparison target, and the accuracy reference at full size
         for _ in range(2):
             step(MODE_FP64)
         torch.cuda.synchronize()

@@ -228,7 +228,7 @@ class Oracle:
 
 
 class Restated(Oracle):
-    """Extra calls that only the restated oracle has (FP64 judges, DTFE, predicates)."""
+    """Extra calls that only the restated oracle has (FP64 references, DTFE, predicates)."""
 
     def __init__(self):
         super().__init__("oracle")

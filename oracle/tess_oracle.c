@@ -19,7 +19,7 @@
  * example the double sqrt in volume()'s face-area sum, src/volume.cpp:34,
  * where <cmath>'s global sqrt takes a double).
  *
- * Part 2 holds the FP64 judges for the stages the reference does not have.
+ * Part 2 holds the FP64 references for the stages the reference does not have.
  */
 #include "tess_oracle.h"
 #include <stdlib.h>
@@ -1218,7 +1218,7 @@ void orc_reorder_neighbors(orc_tet* tets, int num_tets)
 }
 
 /* ------------------------------------------------------------------ */
-/* part 2: FP64 judges                                                */
+/* part 2: FP64 references                                                */
 /* ------------------------------------------------------------------ */
 
 void orc_fill_circumcenters_f64(const float* particles, const orc_tet* tets, int num_tets, double* out)

@@ -11,7 +11,7 @@
  *     its outputs are bit-identical to the reference's own build
  *     (oracle/_ref/libtess_ref.so).  It is pinned against golden vectors
  *     produced by that build (tests/golden/).
- *  2. FP64 judges for the new, non-reference stages (Voronoi volumes in FP64,
+ *  2. FP64 references for the new, non-reference stages (Voronoi volumes in FP64,
  *     DTFE vertex densities and tet-linear grid interpolation).  The DTFE
  *     point-to-tet assignment uses exact orientation signs for float32
  *     inputs with a symbolic perturbation of the grid point, so it is a
@@ -119,7 +119,7 @@ float orc_box_distance(const float* box6, const float* c);
 /* src/tess-qhull.c:161-225, in place */
 void  orc_reorder_neighbors(orc_tet* tets, int num_tets);
 
-/* ---- part 2: FP64 judges ---- */
+/* ---- part 2: FP64 references ---- */
 void  orc_fill_circumcenters_f64(const float* particles, const orc_tet* tets, int num_tets, double* out);
 void  orc_volumes_f64(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,
                       const float* particles, double* out);

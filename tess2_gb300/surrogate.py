@@ -1,7 +1,7 @@
 """The DTFE surrogate: a small 3-D convolutional network that maps the cheap
 cloud-in-cell density grid (DENSE_CIC, no Delaunay needed) of a particle set
 to its DTFE density grid, both as log(1 + rho / mean rho).  The plain DTFE
-path makes the training fields, judges the network's error, and is the
+path makes the training fields, measures the network's error, and is the
 fallback.
 
 Five 3x3x3 convolutions, channels 16 -> 16 -> 32 -> 32 -> 16 -> 16 (the input
