@@ -48,6 +48,72 @@ def test_planar_layout_helpers():
     assert np.array_equal(S.from_planar(p), a)
 
 
+def _slab(x, x0, y, z, n):
+    """Positions x0 - 1 .. x0 - 2 + n of input row (y, z), zero outside the grid (x: Z, Y, X, C)."""
+    Z, Y, X, C = x.shape
+    out = np.zeros((n, C))
+    if 0 <= y < Y and 0 <= z < Z:
+        lo, hi = max(x0 - 1, 0), min(x0 - 1 + n, X)
+        if hi > lo:
+            out[lo - (x0 - 1):hi - (x0 - 1)] = x[z, y, lo:hi]
+    return out
+
+
+@pytest.mark.parametrize("shape", [(3, 6, 16), (2, 5, 140), (1, 1, 16)])
+def test_tcgen05_forward_decomposition(shape):
+    """The tcgen05 forward's decomposition, restated on the CPU: groups of four
+    tiles of 128 voxels on consecutive y rows; per dz the group's rows
+    y0 - 1 .. y0 + Tg are one slab each; tile t, tap (dz, dy, dx) reads slab
+    row t + dy + 1 from position dx + 1 on.  Equals the FP64 convolution."""
+    from oracle.surrogate_oracle import conv3d
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(shape + (16,))
+    w = rng.standard_normal((27, 8, 16))
+    Z, Y, X = shape
+    y = np.full((Z, Y, X, 8), np.nan)
+    per_row, T = (X + 127) // 128, 4
+    for q in range(per_row * ((Y + T - 1) // T) * Z):
+        xt, yb, z = q % per_row, (q // per_row) % ((Y + T - 1) // T), q // (per_row * ((Y + T - 1) // T))
+        Tg, x0, y0 = min(T, Y - yb * T), xt * 128, yb * T
+        slabs = {(dz, rho): _slab(x, x0, y0 - 1 + rho, z + dz, 130) for dz in (-1, 0, 1) for rho in range(Tg + 2)}
+        for t in range(Tg):
+            acc = np.zeros((128, 8))
+            for g in range(9):
+                dz, dy = g // 3 - 1, g % 3 - 1
+                for sh in range(3):
+                    acc += slabs[(dz, t + dy + 1)][sh:sh + 128] @ w[g * 3 + sh].T
+            n = min(128, X - x0)
+            y[z, y0 + t, x0:x0 + n] = acc[:n]
+    assert np.abs(y - conv3d(x, w)).max() < 1e-9
+
+
+@pytest.mark.parametrize("shape", [(3, 4, 16), (2, 3, 140)])
+def test_tcgen05_wgrad_decomposition(shape):
+    """The tcgen05 weight gradient's decomposition, restated on the CPU: one
+    accumulator per tap of a dz, D[co][ci] += dyT^T slab[r + dx + 1] over the
+    tiles of 128 voxels (dy zero past X).  Equals the FP64 weight gradient."""
+    from oracle.surrogate_oracle import conv3d_wgrad
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal(shape + (16,))
+    dyv = rng.standard_normal(shape + (8,))
+    Z, Y, X = shape
+    dw = np.zeros((27, 8, 16))
+    per_row = (X + 127) // 128
+    for dz in (-1, 0, 1):
+        for t in range(per_row * Y * Z):
+            r = t // per_row
+            x0, yy, zz = (t % per_row) * 128, r % Y, r // Y
+            A = np.zeros((128, 8))
+            n = min(128, X - x0)
+            A[:n] = dyv[zz, yy, x0:x0 + n]
+            for d in range(3):
+                slab = _slab(x, x0, yy + d - 1, zz + dz, 130)
+                for sh in range(3):
+                    dw[(dz + 1) * 9 + d * 3 + sh] += A.T @ slab[sh:sh + 128]
+    ref, _ = conv3d_wgrad(x, dyv)
+    assert np.abs(dw - ref).max() < 1e-9
+
+
 @pytest.fixture
 def engine(request):
     from tess2_gb300 import surrogate as S
