@@ -317,11 +317,12 @@ tessgpu_status tessgpu_batch_debug_outputs(tessgpu_ctx* ctx, tessgpu_batch* batc
    mode is tessgpu_mode; stream may be NULL.  The function allocates nothing:
    its scratch is a static device array shared by all calls, which keeps the
    last call's contents (each call clears what it uses), so calls that
-   overlap on the GPU race and must be serialised by the caller.  The first
-   call on a device looks up that array's device address; make it before
-   any stream capture.  More than TESSGPU_NOALLOC_MAX_PARTICLES particles is
-   rejected with TESSGPU_ERR_INVALID.  Returns after the densities are
-   written (the call synchronises the stream). */
+   overlap on the GPU race and must be serialised by the caller.  Each call
+   looks up that array's address on the current device.  More than
+   TESSGPU_NOALLOC_MAX_PARTICLES particles is rejected with
+   TESSGPU_ERR_INVALID.  Returns after the densities are written: the call
+   synchronises the stream and reads a status word back, so it cannot be
+   used while the stream is being captured into a CUDA graph. */
 tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particles, int num_particles, const int* d_tets,
                                               int num_tets, const float* bounds6, float mass, int mode,
                                               float* d_rho, void* stream);

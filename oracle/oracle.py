@@ -249,6 +249,15 @@ class Restated(Oracle):
         self._l.f("fill_circumcenters_f64")(_ptr(particles), _ptr(tets), ctypes.c_int(tets.shape[0]), _ptr(out))
         return out
 
+    def volume_areas(self, particles, tets, vert_to_tet, n=None):
+        """volume() (src/volume.cpp:13-54) and each cell's summed face area, in float."""
+        n = vert_to_tet.shape[0] if n is None else n
+        vol = np.empty(n, np.float32)
+        area = np.empty(n, np.float32)
+        self._l.f("volume_areas")(ctypes.c_int(n), _ptr(vert_to_tet), _ptr(tets), ctypes.c_int(tets.shape[0]),
+                                  _ptr(particles), _ptr(vol), _ptr(area))
+        return vol, area
+
     def volumes_f64(self, particles, tets, vert_to_tet, n=None):
         n = vert_to_tet.shape[0] if n is None else n
         out = np.empty(n, np.float64)

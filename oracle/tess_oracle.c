@@ -257,16 +257,19 @@ int orc_fill_edge_link(int v, int u, int ut, const orc_tet* tets, int* link, int
     return n <= cap ? n : -n - 1;
 }
 
-/* src/volume.cpp:13-54 */
-float orc_volume(int v, const int* vert_to_tet, const orc_tet* tets, int num_tets,
-                 const float* particles, const float* cc)
+/* src/volume.cpp:13-54; *area_out (may be NULL) receives the sum of the
+   cell's face areas in face order, in float (the quantity volume() weights
+   by the edge lengths; tess2 itself does not return it) */
+static float volume_area(int v, const int* vert_to_tet, const orc_tet* tets, const float* particles,
+                         const float* cc, float* area_out)
 {
-    (void)num_tets;
     int vt = vert_to_tet[v];
     ivec nbrs = {0}, link = {0};
     int finite;
     int nf = neighbor_edges_iv(v, tets, vt, &nbrs, &finite);
-    float vol = 0;
+    float vol = 0, area_sum = 0;
+    if (area_out)
+        *area_out = -1;
     if (!finite)
     {
         iv_free(&nbrs);
@@ -292,10 +295,20 @@ float orc_volume(int v, const int* vert_to_tet, const orc_tet* tets, int num_tet
         }
         float dist = dist3(&particles[3 * u], &particles[3 * v]);
         vol += area * dist / 6;
+        area_sum += area;
     }
     iv_free(&nbrs);
     iv_free(&link);
+    if (area_out)
+        *area_out = area_sum;
     return vol;
+}
+
+float orc_volume(int v, const int* vert_to_tet, const orc_tet* tets, int num_tets,
+                 const float* particles, const float* cc)
+{
+    (void)num_tets;
+    return volume_area(v, vert_to_tet, tets, particles, cc, NULL);
 }
 
 void orc_volumes(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,
@@ -305,6 +318,26 @@ void orc_volumes(int n, const int* vert_to_tet, const orc_tet* tets, int num_tet
     orc_fill_circumcenters(particles, tets, num_tets, cc);
     for (int v = 0; v < n; ++v)
         out[v] = vert_to_tet[v] < 0 ? -1.0f : orc_volume(v, vert_to_tet, tets, num_tets, particles, cc);
+    free(cc);
+}
+
+/* volumes and total face areas of cells [0, n) (-1 for both where the cell
+   is infinite or the vertex is in no tet) */
+void orc_volume_areas(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,
+                      const float* particles, float* vol, float* area)
+{
+    float* cc = (float*)malloc(sizeof(float) * 3 * (size_t)(num_tets ? num_tets : 1));
+    orc_fill_circumcenters(particles, tets, num_tets, cc);
+    for (int v = 0; v < n; ++v)
+    {
+        if (vert_to_tet[v] < 0)
+        {
+            vol[v] = -1.0f;
+            area[v] = -1.0f;
+        }
+        else
+            vol[v] = volume_area(v, vert_to_tet, tets, particles, cc, &area[v]);
+    }
     free(cc);
 }
 

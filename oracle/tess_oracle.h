@@ -55,6 +55,8 @@ float orc_volume(int v, const int* vert_to_tet, const orc_tet* tets, int num_tet
                  const float* particles, const float* circumcenters);
 void  orc_volumes(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,
                   const float* particles, float* out);
+void  orc_volume_areas(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,
+                       const float* particles, float* vol, float* area);
 
 void  orc_grid_step_params(int num_given_bounds, const float* given_mins, const float* given_maxs,
                            const float* data_mins, const float* data_maxs,

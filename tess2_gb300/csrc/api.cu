@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 #include "kernels.h"
+#include "dtfe_common.cuh"
 
 using namespace tg;
 
@@ -661,7 +662,7 @@ static tessgpu_status finish_status(tessgpu_ctx* ctx)
     return TESSGPU_OK;
 }
 
-static const float kTau = 4.0e-5f;   // mixed DTFE: FP64 for tets whose FP32 bound exceeds tau*|6V|
+static const float kTau = DTFE_TAU;   // mixed DTFE: FP64 for tets whose FP32 bound exceeds tau*|6V|
 
 extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* bt, const tessgpu_dense_params* p,
                                               float* d_grid, tessgpu_dense_info* info)
@@ -795,11 +796,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int) * (nb + 1), s));
         // fixed-point scale of the star-volume sums: any star volume is below
         // the volume of the particles' bounding box; allow 8x the data box
-        double vbox = 48.0;   // 6V sums of up to 8x the data box
-        for (int i = 0; i < 3; ++i)
-            vbox *= std::max((double)dmax[i] - (double)dmin[i], 1e-30);
-        const int bits = 61 - (int)std::ceil(std::log2(vbox));
-        const double scale = std::ldexp(1.0, bits);
+        const double scale = star_sum_scale(dmin, dmax);   // 6V sums of up to 8x the data box
         // once the launch variant is known, blocks run their stages on two
         // streams in turn (as the host pipeline does), so one block's star
         // volumes overlap another's rasteriser
@@ -1342,11 +1339,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     }
     tiles = tiles && covered == G;
 
-    double vbox = 48.0;
-    for (int i = 0; i < 3; ++i)
-        vbox *= std::max((double)dmax[i] - (double)dmin[i], 1e-30);
-    const int bits = 61 - (int)std::ceil(std::log2(vbox));
-    const double scale = std::ldexp(1.0, bits);
+    const double scale = star_sum_scale(dmin, dmax);
 
     ctx->nmarks = 0;
     ctx->nsev = 0;

@@ -24,14 +24,13 @@
 // Compiled with -fmad=false: FMAs appear only where written (fmaf/fma), so
 // the error bounds below hold as derived.
 #include "kernels.h"
+#include "dtfe_common.cuh"
 #include <float.h>
 #include <math.h>
 
 namespace tg {
 
 constexpr unsigned FULL = 0xffffffffu;
-constexpr float EPS32 = 5.9604645e-08f;      // 2^-24
-constexpr double EPS64 = 1.1102230246251565e-16;  // 2^-53
 
 __device__ __forceinline__ int find_blk(const BlockDesc* b, int nb, int t)
 {
@@ -167,32 +166,6 @@ __device__ __noinline__ int numerator_sign_exact(const float a[4][3], int k, con
 // ---------------------------------------------------------------------------
 // star volumes and densities
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double tet_vol6_f64(float3 a0, float3 a1, float3 a2, float3 a3)
-{
-    double e[3][3] = { { (double)a1.x - a0.x, (double)a1.y - a0.y, (double)a1.z - a0.z },
-                       { (double)a2.x - a0.x, (double)a2.y - a0.y, (double)a2.z - a0.z },
-                       { (double)a3.x - a0.x, (double)a3.y - a0.y, (double)a3.z - a0.z } };
-    return e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) + e[0][1] * (e[1][2] * e[2][0] - e[1][0] * e[2][2]) +
-           e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
-}
-
-// FP32 6*volume with a bound on its rounding error (Shewchuk's orient3d bound
-// over the translated coordinates, padded)
-__device__ __forceinline__ float tet_vol6_f32(float3 a0, float3 a1, float3 a2, float3 a3, float& bound)
-{
-    float e1x = a1.x - a0.x, e1y = a1.y - a0.y, e1z = a1.z - a0.z;
-    float e2x = a2.x - a0.x, e2y = a2.y - a0.y, e2z = a2.z - a0.z;
-    float e3x = a3.x - a0.x, e3y = a3.y - a0.y, e3z = a3.z - a0.z;
-    float m1a = e2y * e3z, m1b = e2z * e3y;
-    float m2a = e2z * e3x, m2b = e2x * e3z;
-    float m3a = e2x * e3y, m3b = e2y * e3x;
-    float det = e1x * (m1a - m1b) + e1y * (m2a - m2b) + e1z * (m3a - m3b);
-    float perm = fabsf(e1x) * (fabsf(m1a) + fabsf(m1b)) + fabsf(e1y) * (fabsf(m2a) + fabsf(m2b)) +
-                 fabsf(e1z) * (fabsf(m3a) + fabsf(m3b));
-    bound = 10.0f * EPS32 * perm;
-    return det;
-}
-
 // Star volumes W_v are sums of the volumes of v's tets (accumulated as 6V,
 // the orientation determinants).  Each term is rounded once to a multiple of
 // 2^-scale_bits and added with 64-bit integer
@@ -207,21 +180,7 @@ __global__ void k_star_volumes(int mode, int total, const float4* pos, const int
     {
         const int4 vi = __ldg(&tv[t]);
         const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
-        double vol;
-        if (mode == TESSGPU_MODE_FP64)
-            vol = fabs(tet_vol6_f64(a0, a1, a2, a3));
-        else
-        {
-            float bound;
-            const float d = tet_vol6_f32(a0, a1, a2, a3, bound);
-            if (bound > tau * fabsf(d))
-            {
-                vol = fabs(tet_vol6_f64(a0, a1, a2, a3));
-                nfix++;
-            }
-            else
-                vol = (double)fabsf(d);
-        }
+        const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a0, a1, a2, a3, &nfix);
         const unsigned long long q = (unsigned long long)__double2ll_rn(vol * scale);
         atomicAdd(&W[vi.x], q);
         atomicAdd(&W[vi.y], q);

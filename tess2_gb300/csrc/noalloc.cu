@@ -16,52 +16,29 @@
 // different streams or host threads) race on it and must be serialised by
 // the caller.
 //
-// The first call on a device looks up the array's device address there
-// (cudaGetSymbolAddress, with that device current); make that first call
-// before any stream capture.
+// Host code cannot pass the array's symbol to a kernel: in host code the name
+// is a host-side stand-in, not a device address.  Every call therefore looks
+// up the array's address on the current device with cudaGetSymbolAddress
+// (nothing is cached, so a device reset or a different current context never
+// leaves a stale address behind).  A call synchronises its stream and reads a
+// status word back, so it cannot be recorded into a CUDA graph.
 //
-// The arithmetic is that of the DTFE path in dtfe.cu: 6V per tet in FP32
-// (FP64 when the FP32 error bound exceeds tau |6V|, or in FP64 mode), summed
-// exactly as fixed-point integers, rho = 24 m / sum.
+// The arithmetic is the DTFE path's (dtfe_common.cuh, shared with dtfe.cu):
+// 6V per tet in FP32 (FP64 when the FP32 error bound exceeds tau |6V|, or in
+// FP64 mode), summed exactly as fixed-point integers, rho = 24 m / sum.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
-#include <mutex>
 #include "../../include/tess2_gb300.h"
+#include "dtfe_common.cuh"
 
 static __device__ __align__(256) unsigned long long noalloc_star_sums[TESSGPU_NOALLOC_MAX_PARTICLES];
 static __device__ __align__(256) int noalloc_flags[8];
 
 namespace {
 
-constexpr float kEps32 = 5.9604645e-08f;   // 2^-24
-constexpr float kTau = 4.0e-5f;            // the DTFE path's FP64 fix-up threshold
-constexpr int kMaxDevices = 64;
-
-__device__ __forceinline__ double vol6_f64(const float* a, const float* b, const float* c, const float* d)
-{
-    const double e[3][3] = { { (double)b[0] - a[0], (double)b[1] - a[1], (double)b[2] - a[2] },
-                             { (double)c[0] - a[0], (double)c[1] - a[1], (double)c[2] - a[2] },
-                             { (double)d[0] - a[0], (double)d[1] - a[1], (double)d[2] - a[2] } };
-    return e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) + e[0][1] * (e[1][2] * e[2][0] - e[1][0] * e[2][2]) +
-           e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
-}
-
-__device__ __forceinline__ float vol6_f32(const float* a, const float* b, const float* c, const float* d, float& bound)
-{
-    const float e1x = b[0] - a[0], e1y = b[1] - a[1], e1z = b[2] - a[2];
-    const float e2x = c[0] - a[0], e2y = c[1] - a[1], e2z = c[2] - a[2];
-    const float e3x = d[0] - a[0], e3y = d[1] - a[1], e3z = d[2] - a[2];
-    const float m1a = e2y * e3z, m1b = e2z * e3y;
-    const float m2a = e2z * e3x, m2b = e2x * e3z;
-    const float m3a = e2x * e3y, m3b = e2y * e3x;
-    const float det = e1x * (m1a - m1b) + e1y * (m2a - m2b) + e1z * (m3a - m3b);
-    const float perm = fabsf(e1x) * (fabsf(m1a) + fabsf(m1b)) + fabsf(e1y) * (fabsf(m2a) + fabsf(m2b)) +
-                       fabsf(e1z) * (fabsf(m3a) + fabsf(m3b));
-    bound = 10.0f * kEps32 * perm;
-    return det;
-}
+using tg::tet_abs_vol6;
 
 // one thread per tet, reading tess2's tet_t records and x,y,z particles directly
 __global__ void k_noalloc_star(const float* xyz, int np, const int* tets, int nt, int mode, double scale,
@@ -76,19 +53,13 @@ __global__ void k_noalloc_star(const float* xyz, int np, const int* tets, int nt
             atomicExch(&flags[0], 1);
             continue;
         }
-        const float* p0 = xyz + 3 * (size_t)v[0];
-        const float* p1 = xyz + 3 * (size_t)v[1];
-        const float* p2 = xyz + 3 * (size_t)v[2];
-        const float* p3 = xyz + 3 * (size_t)v[3];
-        double vol;
-        if (mode == TESSGPU_MODE_FP64)
-            vol = fabs(vol6_f64(p0, p1, p2, p3));
-        else
+        float3 a[4];
+        for (int k = 0; k < 4; ++k)
         {
-            float bound;
-            const float d = vol6_f32(p0, p1, p2, p3, bound);
-            vol = bound > kTau * fabsf(d) ? fabs(vol6_f64(p0, p1, p2, p3)) : (double)fabsf(d);
+            const float* q = xyz + 3 * (size_t)v[k];
+            a[k] = make_float3(q[0], q[1], q[2]);
         }
+        const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a[0], a[1], a[2], a[3], nullptr);
         const unsigned long long q = (unsigned long long)__double2ll_rn(vol * scale);
         for (int k = 0; k < 4; ++k)
             atomicAdd(&sums[v[k]], q);
@@ -107,10 +78,6 @@ __global__ void k_noalloc_rho(const unsigned long long* sums, int np, float mass
         rho[v] = s > 0.0 ? (float)(24.0 * (double)mass / s) : 0.0f;
     }
 }
-
-std::mutex g_setup_mutex;
-unsigned long long* g_sums_addr[kMaxDevices];
-int* g_flags_addr[kMaxDevices];
 
 }  // namespace
 
@@ -132,36 +99,18 @@ extern "C" tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particle
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)
         return TESSGPU_ERR_NO_DEVICE;
-    if (dev < 0 || dev >= kMaxDevices)
-        return TESSGPU_ERR_UNSUPPORTED;
-    unsigned long long* sums;
-    int* flags;
+    // the scratch arrays' device addresses on the current device
+    void* sums_addr = nullptr;
+    void* flags_addr = nullptr;
+    if (cudaGetSymbolAddress(&sums_addr, noalloc_star_sums) != cudaSuccess ||
+        cudaGetSymbolAddress(&flags_addr, noalloc_flags) != cudaSuccess)
     {
-        // the symbol's device address on this device (host code cannot use
-        // the symbol itself: it names a host-side stand-in)
-        std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_sums_addr[dev])
-        {
-            void* a = nullptr;
-            void* f = nullptr;
-            if (cudaGetSymbolAddress(&a, noalloc_star_sums) != cudaSuccess ||
-                cudaGetSymbolAddress(&f, noalloc_flags) != cudaSuccess)
-            {
-                cudaGetLastError();
-                return TESSGPU_ERR_CUDA;
-            }
-            g_sums_addr[dev] = (unsigned long long*)a;
-            g_flags_addr[dev] = (int*)f;
-        }
-        sums = g_sums_addr[dev];
-        flags = g_flags_addr[dev];
+        cudaGetLastError();
+        return TESSGPU_ERR_CUDA;
     }
-    // fixed-point scale: any 6V star sum stays below 2^62 (as in the batch path)
-    double vbox = 48.0;
-    for (int i = 0; i < 3; ++i)
-        vbox *= fmax((double)bounds6[3 + i] - (double)bounds6[i], 1e-30);
-    const int bits = 61 - (int)std::ceil(std::log2(vbox));
-    const double scale = std::ldexp(1.0, bits);
+    unsigned long long* sums = (unsigned long long*)sums_addr;
+    int* flags = (int*)flags_addr;
+    const double scale = tg::star_sum_scale(bounds6, bounds6 + 3);
 
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * (size_t)num_particles, s) != cudaSuccess ||

@@ -52,6 +52,18 @@ def test_volumes_bitexact(gpu_ctx, name):
 
 
 @pytest.mark.parametrize("name", SINGLE)
+def test_face_areas_bitexact(gpu_ctx, oracle, name):
+    """tessgpu_volumes' areas output: each cell's face areas (volume()'s fan
+    sums, src/volume.cpp:25-47) added in face order, against the oracle."""
+    d = load_single(name)
+    v, a = gpu_ctx.volume(d["vert_to_tet"], d["tets"], d["particles"], areas=True)
+    rv, ra = oracle.volume_areas(d["particles"], d["tets"], d["vert_to_tet"])
+    assert np.array_equal(bits(v), bits(rv))
+    assert np.array_equal(bits(a), bits(ra))
+    assert np.all(a[v > 0] > 0)
+
+
+@pytest.mark.parametrize("name", SINGLE)
 def test_volumes_f64_vs_oracle(gpu_ctx, oracle, name):
     d = load_single(name)
     v = gpu_ctx.volume_f64(d["vert_to_tet"], d["tets"], d["particles"])

@@ -31,13 +31,14 @@ def batch_rho(ctx, d):
     return rho
 
 
-def noalloc_rho(d, mode=0):
+def noalloc_rho(d, blk, mode=0):
     import torch
     from tess2_gb300.api import lib
     p = torch.from_numpy(np.ascontiguousarray(d["particles"], np.float32)).cuda()
     t = torch.from_numpy(np.ascontiguousarray(d["tets"], np.int32)).cuda()
     rho = torch.full((p.shape[0],), -1.0, dtype=torch.float32, device="cuda")
-    bounds = (ctypes.c_float * 6)(0, 0, 0, 1, 1, 1)
+    # the data bounds dense() derives for this one block: its own bounds
+    bounds = (ctypes.c_float * 6)(*[float(x) for x in blk["data_min"]], *[float(x) for x in blk["data_max"]])
     torch.cuda.synchronize()
     s = lib().tessgpu_dtfe_densities_noalloc(p.data_ptr(), p.shape[0], t.data_ptr(), t.shape[0], bounds, 1.0, mode,
                                              rho.data_ptr(), None)
@@ -45,14 +46,19 @@ def noalloc_rho(d, mode=0):
     return rho.cpu().numpy()
 
 
-def test_noalloc_matches_batch_path_twice(gpu_ctx):
-    # two calls in a row through the C ABI, on blocks of different sizes
+def test_noalloc_matches_batch_path_twice(gpu_ctx, oracle):
+    # two calls in a row through the C ABI, on blocks of different sizes: the
+    # same arithmetic and fixed-point sums as the batch path, so the same bits
     for name in ("c1_uniform4096_seed1", "mix2048_seed7"):
         d = load_single(name)
+        blk = single_block(d)[0]
         ref = batch_rho(gpu_ctx, d)
-        got = noalloc_rho(d)
+        got = noalloc_rho(d, blk)
         assert np.all(np.isfinite(got))
-        assert np.allclose(got, ref, rtol=1e-6, atol=0.0)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+        # and the FP64 oracle's densities, within FP32 rounding of the result
+        orc = oracle.dtfe(single_block(d), [8, 8, 8], want_owner=False)["rho"]
+        assert np.allclose(got, orc, rtol=2e-6, atol=0.0)
 
 
 def test_noalloc_rejects_oversize():
