@@ -49,6 +49,11 @@ def parse():
     ap.add_argument("--grid", type=int, default=512)
     ap.add_argument("--blocks", type=int, default=2, help="blocks per axis")
     ap.add_argument("--ghost", type=float, default=0.05)
+    ap.add_argument("--frac-uniform", type=float, default=0.5, help="fraction of uniform background particles")
+    ap.add_argument("--clumps", type=int, default=256, help="Gaussian clumps")
+    ap.add_argument("--sigma", type=float, default=0.01, help="clump sigma")
+    ap.add_argument("--sigma-range", type=float, nargs=2, default=None,
+                    help="clump sigmas log-uniform in [lo, hi] instead of --sigma")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -57,18 +62,24 @@ def parse():
                     help="skip training and timing the DTFE surrogate network")
     ap.add_argument("--surrogate-fields", type=int, default=24, help="training fields for the surrogate")
     ap.add_argument("--surrogate-epochs", type=int, default=10)
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the sampled checks against the CPU oracle at the benchmark's size")
     ap.add_argument("--no-rows", action="store_true",
                     help="skip the timings of the stages around the path (reorder_neighbors, incomplete_cells, "
                          "projection, WriteGrid)")
     return ap.parse_args()
 
 
-def prepare(args):
+def prepare(args, timings=False):
     from tess2_gb300 import host
     t0 = time.time()
-    pts = host.mixture_particles(args.particles, args.seed, frac_uniform=0.5, n_clumps=256, sigma=0.01)
+    pts = host.mixture_particles(args.particles, args.seed, frac_uniform=args.frac_uniform, n_clumps=args.clumps,
+                                 sigma=args.sigma, sigma_range=tuple(args.sigma_range) if args.sigma_range else None)
     blocks = host.decompose(pts, (args.blocks,) * 3, args.ghost)
+    t1 = time.time()
     blocks = host.tessellate(blocks, processes=min(len(blocks), os.cpu_count() or 1))
+    if timings:
+        return blocks, time.time() - t0, time.time() - t1
     return blocks, time.time() - t0
 
 
@@ -76,7 +87,10 @@ def workload_config(args, blocks):
     T = sum(int(b["tets"].shape[0]) for b in blocks)
     N = sum(int(b["particles"].shape[0]) for b in blocks)
     G = args.grid ** 3
-    return dict(workload=f"DTFE {args.particles} particles (50% uniform + 50% 256 clumps sigma 0.01) -> "
+    sig = (f"sigma log-uniform {args.sigma_range[0]}..{args.sigma_range[1]}" if args.sigma_range
+           else f"sigma {args.sigma}")
+    mix = f"{100 * args.frac_uniform:.0f}% uniform + {100 * (1 - args.frac_uniform):.0f}% {args.clumps} clumps {sig}"
+    return dict(workload=f"DTFE {args.particles} particles ({mix}) -> "
                          f"{args.grid}^3 float32, {args.blocks}x{args.blocks}x{args.blocks} blocks, ghost {args.ghost}",
                 particles=args.particles, particles_with_ghosts=N, tets=T, grid=[args.grid] * 3,
                 blocks=args.blocks ** 3, ghost=args.ghost, seed=args.seed, mode="mixed FP32 + FP64 fix-up",
@@ -142,19 +156,23 @@ class ClockSampler:
 _W = {}
 
 
-def _worker_init(block, data6, gni):
-    _W["block"] = block
-    _W["data6"] = data6
-    _W["gni"] = gni
+def _ref_init(block, share, data6, gni):
+    """A reference-arm worker: one block's share of cells, the block's
+    circumcenters computed once."""
+    from oracle.oracle import TessCells
+    _W["tc"] = TessCells(block, data6, gni)
+    _W["share"] = np.asarray(share, np.int32)
 
 
-def _tess_sample(ncells):
-    from oracle.oracle import Restated
-    b = dict(_W["block"])
-    b["num_orig"] = min(ncells, b["num_orig"])
+def _ref_cells(frac, seed):
+    """DENSE_TESS on a seeded random fraction of this worker's cells: (seconds, cells)."""
+    share = _W["share"]
+    rng = np.random.default_rng(seed)
+    n = int(round(frac * share.size))
+    cells = np.sort(rng.choice(share, size=n, replace=False)) if n < share.size else share
     t0 = time.perf_counter()
-    Restated().dense(0, [b], _W["gni"], data6=_W["data6"])
-    return time.perf_counter() - t0, b["num_orig"]
+    _W["tc"].run(cells)
+    return time.perf_counter() - t0, int(cells.size)
 
 
 def data_bounds6(blocks):
@@ -186,54 +204,98 @@ def dtfe_cpu_baseline(blocks, gni, stride=16):
                        f"for all {len(blocks)} blocks")
 
 
-def run_reference(args):
-    """--impl reference: the reference's DENSE_TESS (restated bit-exactly in
-    oracle/) on the host cores, one process per block, a sample of cells each."""
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    blocks, prep_s = prepare(args)
-    gni = [args.grid] * 3
+def dense_tess_cpu(blocks, gni, steps, warmup, target_s=2.0):
+    """The reference estimator (restated DENSE_TESS) on every host core: a step
+    processes all cells when that takes at most 4 s, else a seeded random
+    sample sized from two pilots to take about target_s.  Returns (dict, step
+    seconds list)."""
     d6 = data_bounds6(blocks)
-    cores = min(len(blocks), os.cpu_count() or 1)
+    cores = os.cpu_count() or 1
     total_cells = sum(b["num_orig"] for b in blocks)
-    sample_cells = max(200, min(4000, total_cells // (len(blocks) * 50)))
+    shares = ref_workers(blocks, max(cores, len(blocks)))
     ctx = mp.get_context("spawn")
-    pools = [ctx.Pool(1, initializer=_worker_init, initargs=(b, d6, gni)) for b in blocks]
+    t0 = time.perf_counter()
+    pools = [ctx.Pool(1, initializer=_ref_init, initargs=(blocks[bi], share, d6, gni)) for bi, share in shares]
     try:
-        def step():
+        def step(frac, seed):
             t0 = time.perf_counter()
-            rs = [p.apply_async(_tess_sample, (sample_cells,)) for p in pools]
+            rs = [p.apply_async(_ref_cells, (frac, seed * 1000 + w)) for w, p in enumerate(pools)]
             out = [r.get() for r in rs]
-            wall = time.perf_counter() - t0
-            done = sum(n for _, n in out)
-            return wall, done
+            return time.perf_counter() - t0, sum(n for _, n in out)
 
-        for _ in range(args.warmup):
-            step()
-        walls = []
-        done = 0
-        for _ in range(args.steps):
-            w, done = step()
+        step(0.0, 0)   # workers up, circumcenters done
+        init_s = time.perf_counter() - t0
+        # pilots at two fractions: step time ~ a + b * fraction
+        w1, _ = step(0.005, 1)
+        w2, _ = step(0.02, 2)
+        b = max((w2 - w1) / 0.015, 1e-6)
+        a = max(w1 - 0.005 * b, 0.0)
+        frac = 1.0 if a + b <= 4.0 else float(min(1.0, max(0.005, (target_s - a) / b)))
+        for k in range(warmup):
+            step(frac, 10 + k)
+        walls, dones = [], []
+        for k in range(steps):
+            w, done = step(frac, 100 + k)
             walls.append(w)
+            dones.append(done)
     finally:
         for p in pools:
             p.close()
             p.join()
     wall = statistics.mean(walls)
-    # the blocks run in parallel (one process each); scale to all cells
-    t_full = wall * total_cells / done
+    f_eff = statistics.mean(dones) / total_cells
     G = float(np.prod(gni))
-    value = G / t_full
+    value = G * f_eff / wall
+    sample = ("reference DENSE_TESS estimator (restated bit-exactly), "
+              + (f"all {total_cells} cells of the {len(blocks)} blocks per step" if frac >= 1.0 else
+                 f"a seeded random {100 * f_eff:.2f}% of the {total_cells} cells per step (every block, a fresh "
+                 f"sample each step); full pass = step time / fraction")
+              + f", on {len(pools)} processes of {cores} host cores")
+    return dict(value=value, unit=UNIT, cores=len(pools), kind="port", sample=sample, full_pass_s=wall / f_eff,
+                step_s=wall, fraction=f_eff, worker_setup_s=init_s), walls
+
+
+def ref_workers(blocks, procs):
+    """procs workers spread over the blocks in proportion to their cells
+    (at least one each); a block's cells are dealt out to its workers in turn."""
+    cells = np.array([b["num_orig"] for b in blocks], np.float64)
+    nw = np.maximum(1, np.floor(procs * cells / cells.sum())).astype(int)
+    while nw.sum() < procs:
+        nw[np.argmax(cells / nw)] += 1
+    out = []
+    for bi, b in enumerate(blocks):
+        idx = np.arange(b["num_orig"], dtype=np.int32)
+        for w in range(nw[bi]):
+            out.append((bi, idx[w::nw[bi]]))
+    return out
+
+
+def run_reference(args):
+    """--impl reference: the reference's estimator for this path, dense()
+    DENSE_TESS (restated bit-exactly in oracle/, the reference's own sources
+    not being on the GPU host), on every host core.  A step processes every
+    cell of the 8 blocks when that takes at most 4 s, else a seeded random
+    sample of each block's cells (a fresh sample per step, the same fraction
+    everywhere) sized from two pilots to take about 2 s; value = the grid
+    points per second at which the whole workload finishes (G x fraction /
+    step time)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    blocks, prep_s, qhull_s = prepare(args, timings=True)
+    gni = [args.grid] * 3
+    r, walls = dense_tess_cpu(blocks, gni, args.steps, args.warmup)
+    value = r["value"]
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
-                ms_per_step=1e3 * t_full, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
+                ms_per_step=1e3 * r["step_s"], higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
                 data="synthetic", impl="reference", config=workload_config(args, blocks),
-                cpu_baseline=dict(value=value, unit=UNIT, cores=cores, kind="port",
-                                  sample=f"reference DENSE_TESS estimator (restated bit-exactly), first {sample_cells} "
-                                         f"cells of each of {len(blocks)} blocks in parallel processes per step, "
-                                         f"scaled to all {total_cells} cells"),
+                cpu_baseline=dict(value=value, unit=UNIT, cores=r["cores"], kind="port", sample=r["sample"]),
                 e2e=dict(value=value, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                full_pass_s=r["full_pass_s"], cells_per_s=sum(b["num_orig"] for b in blocks) / r["full_pass_s"],
+                particles_per_s=args.particles / r["full_pass_s"], delaunay_s=qhull_s,
+                delaunay_note=f"host Qhull of the {len(blocks)} blocks, one process per block (wall), not in value",
+                worker_setup_s=r["worker_setup_s"],
                 note="the reference has no DTFE; its own estimator for this path (dense() DENSE_TESS) is timed")
     print(json.dumps(line), flush=True)
 
@@ -410,6 +472,52 @@ def time_surrogate(args, peaks, local):
 
 
 # ---------------------------------------------------------------------------
+# parity at the benchmark's size, on samples the CPU oracle can recompute
+# ---------------------------------------------------------------------------
+def full_size_parity(ctx, blocks, gni, grid, DENSE_DTFE, DENSE_TESS, MODE_MIXED, MODE_FP64, stride=16,
+                     cells_per_block=1000):
+    """DTFE owners and values of every 16th tet of each block against the FP64
+    oracle (mixed and FP64 modes), and the DENSE_TESS per-cell grid-point
+    counts of a seeded random sample of every block's cells against the
+    restated reference (oracle/parity.py)."""
+    import torch
+    from oracle import parity
+    t0 = time.perf_counter()
+    G = grid.numel()
+    b = ctx.upload(blocks)
+    b.keep_debug(True)
+    out = {}
+    for mode in (MODE_MIXED, MODE_FP64):
+        b.dense(DENSE_DTFE, gni, grid.data_ptr(), mode=mode, want_info=False)
+        _, own, _ = b.debug_outputs(grid_points=G)
+        out[mode] = (grid.cpu().numpy(), own)
+    total = sum(int(x["num_orig"]) for x in blocks)
+    b.dense(DENSE_TESS, gni, grid.data_ptr(), want_info=False)
+    counts, _, _ = b.debug_outputs(cells=total)
+    b.free()
+    torch.cuda.synchronize()
+    smp = parity.dtfe_oracle_sample(blocks, gni, stride)
+    res = {}
+    for mode, name, tol in ((MODE_MIXED, "dtfe_mixed", 1e-6), (MODE_FP64, "dtfe_fp64", 1e-12)):
+        r = parity.dtfe_compare(out[mode][0], out[mode][1], smp, stride)
+        r["bound"] = tol
+        r["ok"] = bool(r["owners_equal"] and r["no_extra"] and r["rel_l2"] <= tol)
+        res[name] = r
+    del out, smp
+    cells = parity.tess_cell_sample(blocks, cells_per_block, seed=11)
+    ref = parity.tess_counts_oracle(blocks, gni, cells)
+    off, same, n = 0, 0, 0
+    for blk, c, r in zip(blocks, cells, ref):
+        same += int(np.count_nonzero(counts[off + c] == r))
+        n += int(c.size)
+        off += int(blk["num_orig"])
+    res["dense_tess_cell_counts"] = dict(cells=n, equal=same, ok=same == n, seed=11,
+                                         sample=f"{cells_per_block} random cells of each block")
+    res["seconds"] = time.perf_counter() - t0
+    return res
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def run_gpu(args):
@@ -553,11 +661,20 @@ def run_gpu(args):
                                        achieved_gflops=tf / (mst * 1e-3) / 1e9,
                                        fp32_frac_of_nominal=tf / (mst * 1e-3) / fp32_nominal)
 
-    # roofline of the dominant kernel: the mixed rasteriser
-    # algorithmic bytes per launch: tet vertices 16 B/tet, particle positions
-    # 16 B and densities 4 B per particle (each read once), 4 B per grid point written
+    # roofline of the dominant kernel: the mixed rasteriser.  Algorithmic bytes
+    # per launch of the brick kernel: the pair list 4 B per (tet, brick) pair,
+    # tet vertex indices 16 B per tet, particle position 16 B and density 4 B
+    # per particle (each read once), 4 B per grid point written (every point of
+    # the blocks' boxes, zeros included); the row kernel writes only the
+    # assigned points (the grid is zeroed by a separate memset).
     assigned = info["grid_pts_assigned"]
-    raster_bytes = 16.0 * T + 20.0 * N + 4.0 * assigned
+    pairs = info.get("brick_pairs", 0)
+    if pairs:
+        raster_bytes = 4.0 * pairs + 16.0 * T + 20.0 * N + 4.0 * G
+        rkernel = "k_raster_bricks<float,...> (mixed DTFE brick rasteriser), duration from the serial stage pass"
+    else:
+        raster_bytes = 16.0 * T + 20.0 * N + 4.0 * assigned
+        rkernel = "k_raster<float,...> (mixed DTFE row rasteriser), duration from the serial stage pass"
 
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     r_ms = stage_ms.get("raster", float("nan"))
@@ -565,12 +682,12 @@ def run_gpu(args):
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "dtfe_raster_traffic.json")))
-        if prof.get("grid") == args.grid and prof.get("particles") == args.particles:
+        if prof.get("grid") == args.grid and prof.get("particles") == args.particles and \
+                prof.get("brick") == bool(pairs):
             traffic = prof.get("dram_bytes_per_launch")
     except Exception:
         pass
-    roofline = dict(bound="hbm", kernel="k_raster<float,...> (mixed DTFE rasteriser), duration from the serial stage pass",
-                    achieved=achieved, peak=hbm,
+    roofline = dict(bound="hbm", kernel=rkernel, achieved=achieved, peak=hbm,
                     unit="GB/s", frac=achieved / hbm, traffic=traffic, algorithmic_bytes=raster_bytes,
                     kernel_ms=r_ms, peak_source=peak_src + " MEASURED_PEAKS.json hbm_gbs" if peak_src == "measured"
                     else "fallback 6.8 TB/s")
@@ -603,8 +720,27 @@ def run_gpu(args):
             ctx.dense(DENSE_DTFE, hblocks, gni, out=out)
         te = (time.perf_counter() - t0) / ke
         h2d = sum(b["particles"].nbytes + b["tets"].nbytes for b in blocks)
+        # the same call on pageable host memory, as tess2's malloc'd block
+        # arrays and new[]'d density array are
+        pblocks = []
+        for b in blocks:
+            nb = dict(b)
+            nb.pop("vert_to_tet", None)
+            nb["particles"] = np.array(b["particles"], copy=True)
+            nb["tets"] = np.array(b["tets"], copy=True)
+            pblocks.append(nb)
+        pout = np.empty((args.grid,) * 3, np.float32)
+        for _ in range(2):
+            ctx.dense(DENSE_DTFE, pblocks, gni, out=pout)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            ctx.dense(DENSE_DTFE, pblocks, gni, out=pout)
+        tp = (time.perf_counter() - t0) / ke
         e2e = dict(value=G / te, unit=UNIT, ms_per_step=te * 1e3, h2d_bytes_per_step=int(h2d),
-                   d2h_bytes_per_step=int(4 * G), api="tessgpu_dense (host buffers)")
+                   d2h_bytes_per_step=int(4 * G), api="tessgpu_dense (host buffers, pinned)",
+                   pageable=dict(value=G / tp, ms_per_step=tp * 1e3,
+                                 api="tessgpu_dense (pageable numpy arrays, as tess2's malloc/new[] buffers)"))
+        del pblocks, pout
 
     rows = None
     if not args.no_rows:
@@ -612,6 +748,16 @@ def run_gpu(args):
         extra["rows"] = rows
     if not args.no_surrogate:
         extra["surrogate"] = time_surrogate(args, peaks, local)
+
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = full_size_parity(ctx, blocks, gni, grid, DENSE_DTFE, DENSE_TESS, MODE_MIXED, MODE_FP64)
+    if rank == 0 and not args.no_extra and not args.no_cpu:
+        # the reference's estimator on the host cores: the like-for-like pair of dense_tess_gpu
+        dt, _ = dense_tess_cpu(blocks, gni, steps=3, warmup=1)
+        extra["dense_tess_cpu"] = dt
+        if "dense_tess_gpu" in extra:
+            extra["dense_tess_gpu_over_cpu"] = extra["dense_tess_gpu"]["value"] / dt["value"]
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -621,14 +767,25 @@ def run_gpu(args):
             cpu = dict(value=None, unit=UNIT, cores=1, kind="port", sample=f"failed: {e}")
 
     if rank == 0:
+        # the long detail objects on a comment line first; the JSON line itself stays short
+        details = dict(rows=extra.pop("rows", None), surrogate=extra.get("surrogate"),
+                       raster_variant_ms=info["raster_variant_ms"], config=cfg)
+        print("# details " + json.dumps(details), flush=True)
+        sur = extra.pop("surrogate", None)
+        if sur:
+            extra["surrogate"] = {k: sur.get(k) for k in ("val_rel_l2", "cic_rel_l2", "fields_per_s",
+                                                          "speedup_vs_plain_gpu", "speedup_vs_plain_with_delaunay",
+                                                          "tensor_frac_of_bf16_peak", "train_step_ms")}
+        cfg_short = {k: cfg[k] for k in ("workload", "particles", "particles_with_ghosts", "tets", "blocks", "mode",
+                                         "l2")}
         line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
                     ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f32",
-                    data="synthetic", config=cfg, roofline=roofline, cpu_baseline=cpu, e2e=e2e,
+                    data="synthetic", config=cfg_short, roofline=roofline, cpu_baseline=cpu, e2e=e2e,
                     gpu_launches=int(launches), clocks=clk, particles_per_s=world * args.particles / (ms * 1e-3),
-                    stage_ms=stage_ms, step_roofline=step_roof, fp64_fixup_tets=info["fp64_tets"],
-                    exact_tests=info["exact_tests"], grid_pts_assigned=assigned,
+                    stage_ms=stage_ms, step_roofline=step_roof, parity=parity, fp64_fixup_tets=info["fp64_tets"],
+                    exact_tests=info["exact_tests"], grid_pts_assigned=assigned, brick_pairs=pairs,
                     rows_visited=info["rows_visited"], points_tested=info["points_tested"],
-                    raster_variant=info["raster_variant"], raster_variant_ms=info["raster_variant_ms"], host_prep_s=prep_s, **extra)
+                    raster_variant=info["raster_variant"], host_prep_s=prep_s, **extra)
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

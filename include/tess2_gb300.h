@@ -45,7 +45,9 @@ typedef enum tessgpu_status
     TESSGPU_ERR_BAD_MESH       = 7,   /* an index out of range or a broken adjacency */
     TESSGPU_ERR_UNSUPPORTED    = 8,
     TESSGPU_ERR_IO             = 9,   /* a file could not be opened or written */
-    TESSGPU_ERR_TIMEOUT        = 10   /* a bounded wait inside a kernel ran out */
+    TESSGPU_ERR_TIMEOUT        = 10,  /* a bounded wait inside a kernel ran out */
+    TESSGPU_ERR_CAPACITY       = 11   /* a device work list outgrew its buffer (the DTFE
+                                         calls retry once with a larger one) */
 } tessgpu_status;
 
 /* bounds of the device loops; larger inputs report the overflow codes */
@@ -127,6 +129,7 @@ typedef struct tessgpu_dense_info
     long long grid_floats;      /* floats of the device grid tessgpu_batch_dense wrote */
     long long cell_probes;      /* DENSE_TESS: PtInCell calls of the scanline (src/dense.cpp:1475-1701) */
     long long face_tests;       /* DENSE_TESS: face-plane tests of those calls (probes x faces) */
+    long long brick_pairs;      /* DTFE, brick rasteriser: (tet, brick) candidate pairs binned */
 } tessgpu_dense_info;
 
 /* ---- context ---------------------------------------------------------- */
@@ -253,6 +256,29 @@ void           tessgpu_batch_free(tessgpu_batch* batch);
 tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* batch,
                                    const tessgpu_dense_params* params, float* d_grid,
                                    tessgpu_dense_info* info);
+
+/* ---- independent particle sets ---------------------------------------- */
+
+/* Floats of the output of tessgpu_batch_dense_sets for nsets sets whose grids
+   have glo_num_idx[3b..3b+2] points; offsets (may be NULL) receives each set's
+   first float.  -1 for a grid with fewer than 2 points on an axis. */
+long long      tessgpu_sets_grid_floats(int nsets, const int* glo_num_idx, long long* offsets);
+
+/* DTFE of many independent particle sets at once: every block of the batch is
+   one set, processed as dense() over that block alone (its bounds are the data
+   bounds) onto its own grid of glo_num_idx[3b..3b+2] points, written to device
+   memory d_out + offsets[b] (tessgpu_sets_grid_floats), x fastest.  The
+   reference runs DIY blocks independently through master.foreach
+   (src/dense.cpp:130-164); here all sets share each stage's launch, and the
+   rasteriser is one persistent launch whose CTAs take (brick, chunk) items of
+   every set from one device counter.  graph != 0: the step is recorded into
+   a CUDA graph on the first call with these sets, grids and output, and
+   replayed by later calls (the brick shape is autotuned on the first call of
+   a context, outside the graph).  The batch's descriptors must not change
+   while it keeps a recorded step.  info may be NULL. */
+tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_batch* batch, const int* glo_num_idx,
+                                        float mass, float eps, int mode, float* d_out, int graph,
+                                        tessgpu_dense_info* info);
 
 /* incomplete_cells for every block of a device batch: block b's links are
    links[link_offsets[b] .. link_offsets[b+1]) (host arrays, at most 64 per

@@ -348,3 +348,37 @@ class Restated(Oracle):
         del keep
         return dict(grid=grid, owner=owner, rho=rho[:nv] if rho is not None else None, assigned=int(n),
                     grid_min=g6[:3].copy(), grid_step=g6[3:].copy())
+
+
+class TessCells:
+    """The reference estimator's per-cell work (DENSE_TESS, IterateCells,
+    src/dense.cpp:220-313) for one block on chosen cells, through the restated
+    oracle; the block's circumcenters are computed once, here.  Used to time
+    the reference on samples of cells."""
+
+    def __init__(self, block, data6, glo_num_idx, mass=1.0, eps=1e-4):
+        self.o = Restated()
+        self.arr, self.keep = make_blocks([block])
+        t = np.ascontiguousarray(block["tets"], np.int32)
+        p = np.ascontiguousarray(block["particles"], np.float32)
+        self.cc = np.empty((max(t.shape[0], 1), 3), np.float32)
+        self.o._l.f("fill_circumcenters")(_ptr(p), _ptr(t), ctypes.c_int(t.shape[0]), _ptr(self.cc))
+        self.keep += [t, p]
+        self.d6 = np.ascontiguousarray(data6, np.float32)
+        self.gni = np.ascontiguousarray(glo_num_idx, np.int32)
+        self.grid = np.zeros(int(np.prod(self.gni)), np.float32)
+        self.mass, self.eps = mass, eps
+        self.fn = self.o._l.f("dense_tess_cells")
+        self.fn.restype = ctypes.c_long
+
+    def run(self, cells, counts=False):
+        """Cells (particle indices of the block) through CellBounds, CellGridPts and
+        the deposits; returns how many deposited (and, with counts, each cell's
+        CellGridPts result: -1 skipped, else its grid points)."""
+        c = np.ascontiguousarray(cells, np.int32)
+        cnt = np.empty(c.shape[0], np.int32) if counts else None
+        n = int(self.fn(self.arr, _ptr(self.cc), _ptr(c), ctypes.c_int(c.shape[0]), _ptr(self.d6),
+                        _ptr(self.gni), ctypes.c_float(self.mass), ctypes.c_float(self.eps), _ptr(self.grid),
+                        _ptr(cnt)))
+        return (n, cnt) if counts else n
+

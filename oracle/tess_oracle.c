@@ -801,6 +801,44 @@ int orc_cell_grid_pts(const orc_block* b, int cell, const float* data_mins, cons
     return n;
 }
 
+/* DENSE_TESS's per-cell work (IterateCells, src/dense.cpp:220-313: CellBounds,
+   CellGridPts, the deposits) for a list of one block's cells, with the block's
+   circumcenters cc computed beforehand; the deposits go into grid (the global
+   grid, x fastest; may be NULL) and each cell's CellGridPts result into
+   counts (may be NULL: -1 skipped cell, else the grid points it deposited
+   to).  Returns the cells that deposited.  For timing the reference estimator
+   on samples of cells and checking samples of a large run. */
+long orc_dense_tess_cells(const orc_block* b, const float* cc, const int* cells, int ncells, const float* data6,
+                          const int* glo_num_idx, float mass, float eps, float* grid, int* counts)
+{
+    float gmin[3], gmax[3], step[3];
+    orc_grid_step_params(0, NULL, NULL, data6, data6 + 3, gmin, gmax, step, glo_num_idx);
+    const float div = step[0] * step[1] * step[2];
+    cell_ws w;
+    memset(&w, 0, sizeof(w));
+    long done = 0;
+    for (int k = 0; k < ncells; ++k)
+    {
+        const int n = iterate_cell(b, cells[k], cc, &w, data6, data6 + 3, gmin, step, mass, eps, NULL);
+        if (counts)
+            counts[k] = n;
+        if (n <= 0)
+            continue;
+        done++;
+        for (int i = 0; i < n && grid; ++i)
+        {
+            const int* gi = &w.gidx[3 * i];
+            if (gi[0] < 0 || gi[1] < 0 || gi[2] < 0 || gi[0] >= glo_num_idx[0] || gi[1] >= glo_num_idx[1] ||
+                gi[2] >= glo_num_idx[2])
+                continue;
+            float* d = &grid[((size_t)gi[2] * glo_num_idx[1] + gi[1]) * glo_num_idx[0] + gi[0]];
+            *d = (float)((double)*d + w.gmass[i] / div);
+        }
+    }
+    ws_free(&w);
+    return done;
+}
+
 /* ------------------------------------------------------------------ */
 /* part 1: dense() over blocks                                        */
 /* ------------------------------------------------------------------ */

@@ -55,6 +55,8 @@ float orc_volume(int v, const int* vert_to_tet, const orc_tet* tets, int num_tet
                  const float* particles, const float* circumcenters);
 void  orc_volumes(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,
                   const float* particles, float* out);
+long  orc_dense_tess_cells(const orc_block* b, const float* cc, const int* cells, int ncells, const float* data6,
+                           const int* glo_num_idx, float mass, float eps, float* grid, int* counts);
 void  orc_volume_areas(int n, const int* vert_to_tet, const orc_tet* tets, int num_tets,
                        const float* particles, float* vol, float* area);
 

@@ -26,7 +26,7 @@ MODE_MIXED, MODE_FP64 = 0, 1
 
 _STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "no CUDA device", 4: "star overflow",
            5: "face overflow", 6: "edge ring overflow", 7: "malformed mesh", 8: "unsupported", 9: "I/O error",
-           10: "a bounded wait inside a kernel ran out"}
+           10: "a bounded wait inside a kernel ran out", 11: "a device work list outgrew its buffer"}
 
 
 class TessGpuError(RuntimeError):
@@ -82,7 +82,7 @@ class DenseInfo(ctypes.Structure):
                 ("points_tested", ctypes.c_longlong), ("raster_variant", ctypes.c_int),
                 ("raster_variant_ms", ctypes.c_float * 8), ("grid_layers", ctypes.c_int),
                 ("grid_floats", ctypes.c_longlong), ("cell_probes", ctypes.c_longlong),
-                ("face_tests", ctypes.c_longlong)]
+                ("face_tests", ctypes.c_longlong), ("brick_pairs", ctypes.c_longlong)]
 
     def as_dict(self):
         return dict(data_mins=np.array(self.data_mins[:], np.float32), data_maxs=np.array(self.data_maxs[:], np.float32),
@@ -94,7 +94,8 @@ class DenseInfo(ctypes.Structure):
                     exact_tests=self.exact_tests, rows_visited=self.rows_visited,
                     points_tested=self.points_tested, raster_variant=self.raster_variant,
                     raster_variant_ms=list(self.raster_variant_ms), grid_layers=self.grid_layers,
-                    grid_floats=self.grid_floats, cell_probes=self.cell_probes, face_tests=self.face_tests)
+                    grid_floats=self.grid_floats, cell_probes=self.cell_probes, face_tests=self.face_tests,
+                    brick_pairs=self.brick_pairs)
 
 
 _LIB = None
@@ -144,6 +145,8 @@ def lib():
             "tessgpu_write_last_grid": (_I, [_VP, ctypes.c_char_p]),
             "tessgpu_incomplete_cells": (_I, [_VP, _VP, _I, _VP, _I, _VP, _VP]),
             "tessgpu_batch_incomplete_cells": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+            "tessgpu_sets_grid_floats": (ctypes.c_longlong, [_I, _VP, _VP]),
+            "tessgpu_batch_dense_sets": (_I, [_VP, _VP, _VP, ctypes.c_float, ctypes.c_float, _I, _VP, _I, _VP]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -364,6 +367,16 @@ class Context:
         self._check(lib().tessgpu_write_last_grid(self._h, os.fsencode(path)))
 
 
+def sets_offsets(glo_num_idx):
+    """(total floats, per-set first float) of the output of Batch.dense_sets."""
+    gni = np.ascontiguousarray(np.asarray(glo_num_idx, np.int32).reshape(-1, 3))
+    off = np.zeros(len(gni), np.int64)
+    n = lib().tessgpu_sets_grid_floats(len(gni), _p(gni), _p(off))
+    if n < 0:
+        raise ValueError("a set's grid has fewer than 2 points on an axis")
+    return int(n), off
+
+
 def grid_floats(blocks, alg, glo_num_idx, project=False, **kw):
     """(floats, layers) of the device grid Batch.dense writes for these blocks."""
     arr, keep = make_blocks(blocks)
@@ -408,6 +421,19 @@ class Batch:
         info = DenseInfo() if want_info else None
         self.ctx._check(lib().tessgpu_batch_dense(self.ctx.handle, self._h, ctypes.byref(p), ctypes.c_void_p(d_grid),
                                                   ctypes.byref(info) if info is not None else None))
+        return info.as_dict() if info is not None else None
+
+    def dense_sets(self, glo_num_idx, d_out, mass=1.0, eps=1e-4, mode=MODE_MIXED, graph=False, want_info=True):
+        """DTFE of every block as an independent set onto its own grid (glo_num_idx:
+        one (nx, ny, nz) per block) into device memory at d_out, set b at
+        sets_offsets(glo_num_idx)[b]; graph=True records the step into a CUDA graph
+        once and replays it."""
+        gni = np.ascontiguousarray(np.asarray(glo_num_idx, np.int32).reshape(-1, 3))
+        info = DenseInfo() if want_info else None
+        self.ctx._check(lib().tessgpu_batch_dense_sets(self.ctx.handle, self._h, _p(gni), ctypes.c_float(mass),
+                                                       ctypes.c_float(eps), int(mode), ctypes.c_void_p(d_out),
+                                                       1 if graph else 0,
+                                                       ctypes.byref(info) if info is not None else None))
         return info.as_dict() if info is not None else None
 
     def incomplete_cells(self, links6_per_block, d_masks, wrap3_per_block=None, last_neighbor=None):

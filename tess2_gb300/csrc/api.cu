@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,6 +55,10 @@ struct tessgpu_ctx
     cudaStream_t             h2d = nullptr, d2h = nullptr, cs2 = nullptr;
     std::vector<cudaEvent_t> pipe_ev;
     cudaEvent_t              first_ev[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
+    // brick rasteriser: pair-list size the last call needed (0: not known yet)
+    long long                pair_cap_hint = 0;
+    bool                     in_retry = false;
+    bool                     rows = false;          // TESSGPU_RASTER=rows when the context was made
 };
 
 // an event on stream s for a span (timing on), its index; -1 otherwise
@@ -155,6 +160,14 @@ static tessgpu_status cuda_check(tessgpu_ctx* c, cudaError_t e, const char* what
         if (_s != TESSGPU_OK) return _s;                                \
     } while (0)
 
+// TESSGPU_RASTER=rows selects the per-tet row kernel (k_raster) with its
+// separate FP64 fix-up pass; the default is the brick kernel.
+static bool raster_rows()
+{
+    const char* e = getenv("TESSGPU_RASTER");
+    return e && std::strcmp(e, "rows") == 0;
+}
+
 static void* pool_get(tessgpu_ctx* c, int slot, size_t bytes, cudaError_t* e)
 {
     if ((int)c->pool.size() <= slot)
@@ -188,6 +201,7 @@ extern "C" tessgpu_status tessgpu_create(int device, void* stream, tessgpu_ctx**
     tessgpu_ctx* ctx = new tessgpu_ctx;
     ctx->device = device;
     ctx->stream = (cudaStream_t)stream;
+    ctx->rows = raster_rows();
     tessgpu_status s;
     if ((s = cuda_check(ctx, cudaSetDevice(device), "cudaSetDevice")) != TESSGPU_OK ||
         (s = cuda_check(ctx, cudaMalloc(&ctx->d_status, sizeof(Status)), "cudaMalloc")) != TESSGPU_OK ||
@@ -433,6 +447,10 @@ struct tessgpu_batch
     int*                   d_owner = nullptr;
     long long              owner_n = 0;
     int                    last_alg = -1;
+    // independent particle sets (tessgpu_batch_dense_sets): the recorded step and what it was recorded for
+    cudaGraph_t            sets_graph = nullptr;
+    cudaGraphExec_t        sets_exec = nullptr;
+    std::vector<long long> sets_key;
     std::vector<void*>     owned;            // device allocations to free (non-pooled)
 };
 
@@ -441,7 +459,7 @@ enum PoolSlot
     SLOT_BLOCKS, SLOT_COFF, SLOT_POS, SLOT_TV, SLOT_TN, SLOT_V2T, SLOT_CC, SLOT_CC64, SLOT_W, SLOT_RHO32,
     SLOT_RHO64, SLOT_FIX, SLOT_FIXN, SLOT_STAGE, SLOT_RAWPTR, SLOT_RAWV2T, SLOT_GRID, SLOT_CELLS, SLOT_OUT,
     SLOT_OUT2, SLOT_COUNT, SLOT_ZLAYER, SLOT_GRID3, SLOT_PROJ, SLOT_LINKS, SLOT_LINKOFF, SLOT_MASK,
-    SLOT_SENDS, SLOT_ORDER, SLOT_OKEY, SLOT_OHIST, SLOT_OCNT
+    SLOT_SENDS, SLOT_ORDER, SLOT_OKEY, SLOT_OHIST, SLOT_OCNT, SLOT_BRICKS, SLOT_PAIRS
 };
 
 static cudaError_t balloc(tessgpu_batch* bt, int slot, size_t bytes, void** out)
@@ -469,6 +487,8 @@ extern "C" void tessgpu_batch_free(tessgpu_batch* bt)
 {
     if (!bt) return;
     cudaSetDevice(bt->ctx->device);
+    if (bt->sets_exec) cudaGraphExecDestroy(bt->sets_exec);
+    if (bt->sets_graph) cudaGraphDestroy(bt->sets_graph);
     for (void* p : bt->owned)
         cudaFree(p);
     delete bt;
@@ -655,14 +675,194 @@ static tessgpu_status finish_status(tessgpu_ctx* ctx)
     {
         static const char* names[] = { "ok", "invalid", "cuda", "no device", "vertex star larger than TESSGPU_MAX_STAR",
                                        "Voronoi cell with more than TESSGPU_MAX_FACES faces",
-                                       "edge ring longer than TESSGPU_MAX_LINK", "malformed mesh", "unsupported" };
-        const char* nm = (st.code > 0 && st.code < 9) ? names[st.code] : "error";
+                                       "edge ring longer than TESSGPU_MAX_LINK", "malformed mesh", "unsupported",
+                                       "i/o", "bounded wait ran out", "device work list larger than its buffer" };
+        const char* nm = (st.code > 0 && st.code < 12) ? names[st.code] : "error";
         return set_err(ctx, (tessgpu_status)st.code, std::string(nm) + " at item " + std::to_string(st.detail));
     }
     return TESSGPU_OK;
 }
 
 static const float kTau = DTFE_TAU;   // mixed DTFE: FP64 for tets whose FP32 bound exceeds tau*|6V|
+
+// ---------------------------------------------------------------------------
+// DTFE rasteriser selection and the brick rasteriser's host side
+// ---------------------------------------------------------------------------
+// true when the blocks' grid boxes are disjoint and cover the whole grid, so
+// that writing every box writes every grid point
+static bool boxes_tile(const std::vector<BlockDesc>& hb, const int* gni)
+{
+    long long covered = 0;
+    const int nb = (int)hb.size();
+    for (int i = 0; i < nb; ++i)
+    {
+        long long v = 1;
+        for (int k = 0; k < 3; ++k)
+        {
+            const int n = hb[i].gmax_idx[k] - hb[i].gmin_idx[k] + 1;
+            if (n <= 0) return false;
+            v *= n;
+        }
+        covered += v;
+        for (int j = 0; j < i; ++j)
+        {
+            bool meet = true;
+            for (int k = 0; k < 3; ++k)
+                if (hb[i].gmax_idx[k] < hb[j].gmin_idx[k] || hb[j].gmax_idx[k] < hb[i].gmin_idx[k]) meet = false;
+            if (meet) return false;
+        }
+    }
+    return covered == (long long)gni[0] * gni[1] * gni[2];
+}
+
+// every block rasterises into the call's one grid (offset 0)
+static void set_block_grids(std::vector<BlockDesc>& hb, const GridDesc& g)
+{
+    for (BlockDesc& d : hb)
+    {
+        for (int k = 0; k < 3; ++k)
+        {
+            d.grid.gmin[k] = g.gmin[k];
+            d.grid.step[k] = g.step[k];
+            d.grid.inv_step[k] = g.inv_step[k];
+            d.grid.n[k] = g.n[k];
+        }
+        d.grid.off = 0;
+    }
+}
+
+// cut every block's grid box into bricks of the variant's shape (aligned to
+// the global grid); returns the number of bricks of all blocks
+static long long assign_bricks(std::vector<BlockDesc>& hb, int variant)
+{
+    int sh[3];
+    brick_shape(variant, &sh[0], &sh[1], &sh[2]);
+    long long base = 0;
+    for (BlockDesc& d : hb)
+    {
+        d.brick_base = (int)base;
+        long long n = 1;
+        for (int k = 0; k < 3; ++k)
+        {
+            if (d.gmin_idx[k] > d.gmax_idx[k])
+            {
+                d.brick_lo[k] = 0;
+                d.brick_n[k] = 0;
+            }
+            else
+            {
+                d.brick_lo[k] = d.gmin_idx[k] >> sh[k];
+                d.brick_n[k] = (d.gmax_idx[k] >> sh[k]) - d.brick_lo[k] + 1;
+            }
+            n *= d.brick_n[k];
+        }
+        base += n;
+    }
+    return base;
+}
+
+// the brick rasteriser's scratch (context pool): per-brick counts, offsets,
+// cursors and item offsets, per-segment items and counters, the pair cursor,
+// and the pair list (2 pairs per tet to start with; grown to what a call
+// needed when it overflowed)
+static tessgpu_status brick_bins(tessgpu_ctx* ctx, long long nbricks, int nb, long long T, BrickBins* b)
+{
+    cudaError_t e;
+    const size_t nbr = (size_t)std::max(nbricks, 1LL);
+    char* raw = (char*)pool_get(ctx, SLOT_BRICKS, 16 + sizeof(int) * (4 * nbr + 2 * (size_t)nb), &e);
+    CK(e);
+    b->pair_cursor = (unsigned long long*)raw;
+    int* base = (int*)(raw + 16);
+    b->cnt = base;
+    b->off = base + nbr;
+    b->cur = base + 2 * nbr;
+    b->item_off = base + 3 * nbr;
+    b->seg_items = base + 4 * nbr;
+    b->counters = b->seg_items + nb;
+    long long cap = std::max(ctx->pair_cap_hint, 2 * T + 65536);
+    // TESSGPU_PAIR_CAP: a first size for tests of the overflow retry
+    const char* env = getenv("TESSGPU_PAIR_CAP");
+    if (env && *env && ctx->pair_cap_hint == 0)
+        cap = std::max(atoll(env), 1LL);
+    cap = std::min(cap, (long long)INT32_MAX);
+    b->pairs = (int*)pool_get(ctx, SLOT_PAIRS, sizeof(int) * (size_t)cap, &e);
+    CK(e);
+    b->pair_cap = cap;
+    return TESSGPU_OK;
+}
+
+// segment [k0, k1) of blocks: bin its tets into its bricks, then rasterise
+static void bricks_bin(tessgpu_ctx* ctx, int variant, const BlockDesc* d_blocks, const std::vector<BlockDesc>& hb,
+                       int k0, int k1, long long nbricks, const BrickBins& bins, const float4* pos, const int4* tv,
+                       const GridDesc& g, float* grid, cudaStream_t s)
+{
+    const int nb = (int)hb.size();
+    const int bb0 = hb[k0].brick_base, bb1 = k1 < nb ? hb[k1].brick_base : (int)nbricks;
+    const int t0 = hb[k0].t_off, t1 = hb[k1 - 1].t_off + hb[k1 - 1].nt;
+    launch_bin_bricks(variant, d_blocks, nb, k0, bb0, bb1, t0, t1 - t0, pos, tv, g, bins, grid, ctx->d_status, s);
+    ctx->launches += t1 > t0 ? 4 : 1;
+}
+
+// the same in three steps, the count fused into the star volumes:
+// bricks_reset, bricks_star (star volumes of tets [t0, t0 + nt) and their
+// pair counts; may run in parts), bricks_place (scan, scatter, zeroing)
+static void bricks_reset(tessgpu_ctx* ctx, const std::vector<BlockDesc>& hb, int k0, int k1, long long nbricks,
+                         const BrickBins& bins, cudaStream_t s)
+{
+    const int nb = (int)hb.size();
+    const int bb0 = hb[k0].brick_base, bb1 = k1 < nb ? hb[k1].brick_base : (int)nbricks;
+    launch_bin_reset(bins, k0, bb0, bb1, s);
+    (void)ctx;
+}
+
+static void bricks_star(tessgpu_ctx* ctx, int mode, int variant, const BlockDesc* d_blocks, int nb, long long t0,
+                        long long nt, const float4* pos, const int4* tv, unsigned long long* W, double scale,
+                        const GridDesc& g, const BrickBins& bins, cudaStream_t s)
+{
+    if (nt <= 0) return;
+    launch_star_bin(mode, variant, d_blocks, nb, (int)t0, (int)nt, pos, tv, W, scale, g, bins.cnt, ctx->d_status, s);
+    ctx->launches++;
+}
+
+static void bricks_place(tessgpu_ctx* ctx, int variant, const BlockDesc* d_blocks, const std::vector<BlockDesc>& hb,
+                         int k0, int k1, long long nbricks, const BrickBins& bins, const float4* pos, const int4* tv,
+                         const GridDesc& g, float* grid, cudaStream_t s)
+{
+    const int nb = (int)hb.size();
+    const int bb0 = hb[k0].brick_base, bb1 = k1 < nb ? hb[k1].brick_base : (int)nbricks;
+    const int t0 = hb[k0].t_off, t1 = hb[k1 - 1].t_off + hb[k1 - 1].nt;
+    launch_bin_place(variant, d_blocks, nb, k0, bb0, bb1, t0, t1 - t0, pos, tv, g, bins, grid, ctx->d_status, s);
+    ctx->launches += t1 > t0 && bb1 > bb0 ? 3 : 1;
+}
+
+static void bricks_raster(tessgpu_ctx* ctx, int mode, int variant, const BlockDesc* d_blocks,
+                          const std::vector<BlockDesc>& hb, int k0, int k1, long long nbricks, const BrickBins& bins,
+                          const float4* pos, const int4* tv, const float* rho32, const double* rho64,
+                          const GridDesc& g, float* grid, int* owner, cudaStream_t s)
+{
+    const int nb = (int)hb.size();
+    const int bb0 = hb[k0].brick_base, bb1 = k1 < nb ? hb[k1].brick_base : (int)nbricks;
+    if (bb1 <= bb0) return;
+    launch_raster_bricks(mode, variant, d_blocks, nb, k0, bb0, bb1, bins, pos, tv, rho32, rho64, g, grid, owner,
+                         ctx->d_status, s);
+    ctx->launches++;
+}
+
+// after a call failed with TESSGPU_ERR_CAPACITY: size the pair list for what
+// it needed (the cursor holds the pairs every segment asked for)
+static void grow_pairs(tessgpu_ctx* ctx)
+{
+    if ((int)ctx->pool.size() <= SLOT_BRICKS || !ctx->pool[SLOT_BRICKS].first) return;
+    unsigned long long need = 0;
+    if (cudaMemcpy(&need, ctx->pool[SLOT_BRICKS].first, sizeof(need), cudaMemcpyDeviceToHost) == cudaSuccess)
+        ctx->pair_cap_hint = std::max(ctx->pair_cap_hint, (long long)(need + need / 4 + 65536));
+    cudaGetLastError();
+}
+
+static tessgpu_status dtfe_batch_bricks(tessgpu_ctx* ctx, tessgpu_batch* bt, const tessgpu_dense_params* p,
+                                        const GridDesc& g, const float* gmax, float* target, float* d_grid,
+                                        const int* d_zl, int L, long long Gout, int var, long long nbricks,
+                                        tessgpu_dense_info* info);
 
 extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* bt, const tessgpu_dense_params* p,
                                               float* d_grid, tessgpu_dense_info* info)
@@ -699,6 +899,19 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             d.gmin_idx[k] = std::max(d.gmin_idx[k], 0);
             d.gmax_idx[k] = std::min(d.gmax_idx[k], p->glo_num_idx[k] - 1);
         }
+    }
+    set_block_grids(bt->hb, g);
+    // DTFE with the brick rasteriser: the bricks of the chosen (or first) variant
+    const bool bricks = p->alg == TESSGPU_DENSE_DTFE && !ctx->rows;
+    int bvar = -1;
+    long long nbricks = 0;
+    if (bricks)
+    {
+        bvar = bt->raster_variant[p->mode] >= 0 ? bt->raster_variant[p->mode] : ctx->raster_variant[p->mode];
+        const char* env = getenv("TESSGPU_RASTER_VARIANT");
+        if (bvar < 0 && env && *env)
+            bvar = ctx->raster_variant[p->mode] = std::min(std::max(atoi(env), 0), brick_variants() - 1);
+        nbricks = assign_bricks(bt->hb, bvar < 0 ? 0 : bvar);
     }
     CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
@@ -740,8 +953,13 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     ctx->nsev = 0;
     ctx->spans.clear();
     mark(ctx, "start");
-    CK(cudaMemsetAsync(target, 0, sizeof(float) * Gtarget, s));
-    mark(ctx, "grid_zero");
+    // the brick rasteriser writes every point of the blocks' boxes (zeros
+    // included); the grid needs zeroing only where the boxes leave gaps
+    if (!bricks || !boxes_tile(bt->hb, p->glo_num_idx))
+    {
+        CK(cudaMemsetAsync(target, 0, sizeof(float) * Gtarget, s));
+        mark(ctx, "grid_zero");
+    }
     bt->last_alg = p->alg;
 
     if (p->alg == TESSGPU_DENSE_TESS)
@@ -775,6 +993,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
     }
     else
     {
+        if (bricks)
+            return dtfe_batch_bricks(ctx, bt, p, g, gmax, target, d_grid, d_zl, L, Gout, bvar, nbricks, info);
         if (!bt->W || bt->pooled)
         {
             BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
@@ -1008,6 +1228,433 @@ dtfe_done:
         info->face_tests = (long long)ctx->h_status->face_tests;
     }
     return st;
+}
+
+// DTFE on a device batch with the brick rasteriser.  Stages: bin the tets
+// into bricks, star volumes, densities, rasterise (FP64 values of the
+// ill-conditioned tets inline).  Once the brick shape is known (autotuned on
+// the first call per context and mode) the blocks alternate between two
+// streams, each block its own segment of the bins; TESSGPU_BATCH_OVERLAP=0
+// runs each stage over all blocks in one launch instead.
+static tessgpu_status dtfe_batch_bricks(tessgpu_ctx* ctx, tessgpu_batch* bt, const tessgpu_dense_params* p,
+                                        const GridDesc& g, const float* gmax, float* target, float* d_grid,
+                                        const int* d_zl, int L, long long Gout, int var, long long nbricks,
+                                        tessgpu_dense_info* info)
+{
+    cudaStream_t s = ctx->stream;
+    const int nb = bt->nb;
+    const long long G = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
+    if (!bt->W || bt->pooled)
+    {
+        BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
+        BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
+        BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
+    }
+    int* owner = nullptr;
+    if (bt->keep_debug)
+    {
+        if (!bt->d_owner || bt->owner_n < G || bt->pooled)
+            BALLOC(SLOT_OUT, sizeof(int) * G, bt->d_owner);
+        CK(cudaMemsetAsync(bt->d_owner, 0xff, sizeof(int) * G, s));
+        bt->owner_n = G;
+        owner = bt->d_owner;
+    }
+    const double scale = star_sum_scale(g.dmin, g.dmax);
+    unsigned long long* W = (unsigned long long*)bt->W;
+    BrickBins bins;
+    tessgpu_status st;
+    if ((st = brick_bins(ctx, nbricks, nb, bt->T, &bins)) != TESSGPU_OK)
+        return st;
+    CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
+    CK(cudaMemsetAsync(W, 0, sizeof(unsigned long long) * (bt->N ? bt->N : 1), s));
+    const char* ov = getenv("TESSGPU_BATCH_OVERLAP");
+    const bool overlap = var >= 0 && !(ov && *ov && atoi(ov) == 0) && !p->project && nb > 1;
+    if (overlap)
+    {
+        if (!ctx->cs2) CK(cudaStreamCreateWithFlags(&ctx->cs2, cudaStreamNonBlocking));
+        while ((int)ctx->pipe_ev.size() < 2 * nb + 2)
+        {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            ctx->pipe_ev.push_back(e);
+        }
+        CK(cudaEventRecord(ctx->pipe_ev[2 * nb + 1], s));
+        CK(cudaStreamWaitEvent(ctx->cs2, ctx->pipe_ev[2 * nb + 1], 0));
+        for (int k = 0; k < nb; ++k)
+        {
+            const BlockDesc& d = bt->hb[k];
+            cudaStream_t sk = (k & 1) ? ctx->cs2 : s;
+            const int e0 = smark(ctx, sk);
+            bricks_reset(ctx, bt->hb, k, k + 1, nbricks, bins, sk);
+            bricks_star(ctx, p->mode, var, bt->d_blocks, nb, d.t_off, d.nt, bt->pos, bt->tv, W, scale, g, bins, sk);
+            const int e1 = smark(ctx, sk);
+            bricks_place(ctx, var, bt->d_blocks, bt->hb, k, k + 1, nbricks, bins, bt->pos, bt->tv, g, target, sk);
+            const int e2 = smark(ctx, sk);
+            if (d.np)
+            {
+                launch_densities(W + d.p_off, d.np, p->mass, 1.0 / scale, bt->rho32 + d.p_off, bt->rho64 + d.p_off,
+                                 ctx->d_status, sk);
+                ctx->launches++;
+            }
+            const int e3 = smark(ctx, sk);
+            bricks_raster(ctx, p->mode, var, bt->d_blocks, bt->hb, k, k + 1, nbricks, bins, bt->pos, bt->tv,
+                          bt->rho32, bt->rho64, g, target, owner, sk);
+            const int e4 = smark(ctx, sk);
+            span(ctx, "star_volumes_bin_count", e0, e1);
+            span(ctx, "bin_place", e1, e2);
+            span(ctx, "densities", e2, e3);
+            span(ctx, "raster", e3, e4);
+            CK(cudaEventRecord(ctx->pipe_ev[nb + k], sk));
+        }
+        for (int k = nb - 1; k >= 0; --k)
+            if (k & 1)
+            {
+                CK(cudaStreamWaitEvent(s, ctx->pipe_ev[nb + k], 0));
+                break;
+            }
+        mark(ctx, "dtfe_blocks");
+    }
+    else
+    {
+        if (var >= 0)
+        {
+            bricks_reset(ctx, bt->hb, 0, nb, nbricks, bins, s);
+            bricks_star(ctx, p->mode, var, bt->d_blocks, nb, 0, bt->T, bt->pos, bt->tv, W, scale, g, bins, s);
+            mark(ctx, "star_volumes_bin_count");
+            bricks_place(ctx, var, bt->d_blocks, bt->hb, 0, nb, nbricks, bins, bt->pos, bt->tv, g, target, s);
+            mark(ctx, "bin_place");
+        }
+        else
+        {
+            launch_star_volumes(p->mode, (int)bt->T, bt->pos, bt->tv, W, scale, kTau, ctx->d_status, s);
+            ctx->launches += bt->T ? 1 : 0;
+            mark(ctx, "star_volumes");
+        }
+        launch_densities(W, (int)bt->N, p->mass, 1.0 / scale, bt->rho32, bt->rho64, ctx->d_status, s);
+        mark(ctx, "densities");
+        ctx->launches += bt->N ? 1 : 0;
+        if (var < 0)
+        {
+            // autotune the brick shape: bin and rasterise with each, twice (the
+            // first launch of a kernel also pays its module load); keep the fastest
+            float best = 1e30f;
+            cudaEvent_t e0, e1;
+            CK(cudaEventCreate(&e0));
+            CK(cudaEventCreate(&e1));
+            for (int v = 0; v < brick_variants(); ++v)
+            {
+                const long long nbv = assign_bricks(bt->hb, v);
+                CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
+                if ((st = brick_bins(ctx, nbv, nb, bt->T, &bins)) != TESSGPU_OK)
+                    return st;
+                float vbest = 1e30f;
+                for (int rep = 0; rep < 2; ++rep)
+                {
+                    CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
+                    CK(cudaEventRecord(e0, s));
+                    bricks_bin(ctx, v, bt->d_blocks, bt->hb, 0, nb, nbv, bins, bt->pos, bt->tv, g, target, s);
+                    bricks_raster(ctx, p->mode, v, bt->d_blocks, bt->hb, 0, nb, nbv, bins, bt->pos, bt->tv,
+                                  bt->rho32, bt->rho64, g, target, owner, s);
+                    CK(cudaEventRecord(e1, s));
+                    CK(cudaEventSynchronize(e1));
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    vbest = std::min(vbest, ms);
+                }
+                if (v < 8) ctx->tune_ms[p->mode][v] = vbest;
+                if (vbest < best) { best = vbest; var = v; }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            CK(cudaStreamSynchronize(s));
+            const Status& hs = *ctx->h_status;
+            CK(cudaMemcpy(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost));
+            if (hs.code && hs.code != TESSGPU_ERR_CAPACITY)
+                return finish_status(ctx);
+            if (hs.code == TESSGPU_ERR_CAPACITY)
+                grow_pairs(ctx);
+            ctx->raster_variant[p->mode] = var;
+            bt->raster_variant[p->mode] = var;
+            // the run itself, with the chosen shape
+            return tessgpu_batch_dense(ctx, bt, p, d_grid, info);
+        }
+        bricks_raster(ctx, p->mode, var, bt->d_blocks, bt->hb, 0, nb, nbricks, bins, bt->pos, bt->tv, bt->rho32,
+                      bt->rho64, g, target, owner, s);
+        mark(ctx, "raster");
+    }
+    bt->raster_variant[p->mode] = var;
+    if (p->project)
+    {
+        // surface density: the column integral of rho over each layer's z range
+        launch_project_layers(target, p->glo_num_idx[0], p->glo_num_idx[1], d_zl + p->glo_num_idx[2], L, g.step[2],
+                              d_grid, s);
+        ctx->launches++;
+        mark(ctx, "project_layers");
+    }
+    if (info)
+    {
+        CK(cudaMemsetAsync(ctx->d_max, 0, sizeof(float), s));
+        launch_grid_max(d_grid, Gout, ctx->d_max, s);
+        ctx->launches++;
+        mark(ctx, "grid_max");
+    }
+    st = finish_status(ctx);
+    if (st == TESSGPU_ERR_CAPACITY && !ctx->in_retry)
+    {
+        // the pair list was too small: size it for this call and run again
+        grow_pairs(ctx);
+        ctx->in_retry = true;
+        st = tessgpu_batch_dense(ctx, bt, p, d_grid, info);
+        ctx->in_retry = false;
+        return st;
+    }
+    if (st != TESSGPU_OK || !info)
+        return st;
+    float mx = 0.0f;
+    CK(cudaMemcpy(&mx, ctx->d_max, sizeof(float), cudaMemcpyDeviceToHost));
+    std::memset(info, 0, sizeof(*info));
+    for (int i = 0; i < 3; ++i)
+    {
+        info->data_mins[i] = g.dmin[i]; info->data_maxs[i] = g.dmax[i];
+        info->grid_phys_mins[i] = g.gmin[i]; info->grid_phys_maxs[i] = gmax[i]; info->grid_step_size[i] = g.step[i];
+    }
+    const Status& hs = *ctx->h_status;
+    info->max_dense = mx;
+    info->tot_mass = hs.tot_mass;
+    info->grid_pts_assigned = (long long)hs.assigned;
+    info->fp64_tets = (long long)hs.fp64_tets;
+    info->exact_tests = (long long)hs.exact_tests;
+    info->rows_visited = (long long)hs.rows;
+    info->points_tested = (long long)hs.candidates;
+    info->raster_variant = var;
+    for (int v = 0; v < 8; ++v)
+        info->raster_variant_ms[v] = ctx->tune_ms[p->mode][v];
+    info->grid_layers = L;
+    info->grid_floats = Gout;
+    unsigned long long pairs = 0;
+    CK(cudaMemcpy(&pairs, bins.pair_cursor, sizeof(pairs), cudaMemcpyDeviceToHost));
+    info->brick_pairs = (long long)pairs;
+    return TESSGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// independent particle sets, each block with its own grid
+// ---------------------------------------------------------------------------
+extern "C" long long tessgpu_sets_grid_floats(int nsets, const int* glo_num_idx, long long* offsets)
+{
+    if (nsets <= 0 || !glo_num_idx) return -1;
+    long long tot = 0;
+    for (int b = 0; b < nsets; ++b)
+    {
+        if (offsets) offsets[b] = tot;
+        long long n = 1;
+        for (int k = 0; k < 3; ++k)
+        {
+            if (glo_num_idx[3 * b + k] < 2) return -1;
+            n *= glo_num_idx[3 * b + k];
+        }
+        tot += n;
+    }
+    return tot;
+}
+
+// DTFE of every block of the batch as an independent set: block b is
+// dense() over that one block onto its own glo_num_idx[3b..3b+2] grid, at
+// d_out + offset b (tessgpu_sets_grid_floats).  Stages over all sets at once:
+// star volumes with the brick pair counts, densities, the bins' scan and
+// scatter, one persistent rasteriser launch whose CTAs take (brick, chunk)
+// items of every set from one device counter.  graph != 0 records the step
+// into a CUDA graph on the first call with these sets and replays it after
+// (the brick shape is autotuned first, without the graph).
+extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_batch* bt, const int* glo_num_idx,
+                                                   float mass, float eps, int mode, float* d_out, int graph,
+                                                   tessgpu_dense_info* info)
+{
+    if (!ctx || !bt || !glo_num_idx || !d_out || (mode != TESSGPU_MODE_MIXED && mode != TESSGPU_MODE_FP64))
+        return set_err(ctx, TESSGPU_ERR_INVALID, "bad dense_sets arguments");
+    if (ctx->rows)
+        return set_err(ctx, TESSGPU_ERR_UNSUPPORTED, "independent sets need the brick rasteriser");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int nb = bt->nb;
+    std::vector<long long> off(nb);
+    const long long Gtot = tessgpu_sets_grid_floats(nb, glo_num_idx, off.data());
+    if (Gtot < 0)
+        return set_err(ctx, TESSGPU_ERR_INVALID, "a set's grid has fewer than 2 points on an axis");
+    // each set's grid: dense() over its one block (DataBounds = its bounds)
+    float umin[3] = { 0, 0, 0 }, umax[3] = { 0, 0, 0 };
+    for (int b = 0; b < nb; ++b)
+    {
+        tessgpu_dense_params p;
+        std::memset(&p, 0, sizeof(p));
+        p.alg = TESSGPU_DENSE_DTFE;
+        p.mode = mode;
+        p.mass = mass;
+        p.eps = eps;
+        for (int k = 0; k < 3; ++k) p.glo_num_idx[k] = glo_num_idx[3 * b + k];
+        float dmin[3], dmax[3], gmin[3], gmax[3], step[3];
+        data_bounds(1, &bt->blocks[b], &p, dmin, dmax);
+        grid_step_params(&p, dmin, dmax, gmin, gmax, step);
+        BlockDesc& d = bt->hb[b];
+        block_grid_params(bt->blocks[b], gmin, step, eps, dmin, dmax, p.glo_num_idx, d.gmin_idx, d.gmax_idx,
+                          d.gnum_idx);
+        for (int k = 0; k < 3; ++k)
+        {
+            d.gmin_idx[k] = std::max(d.gmin_idx[k], 0);
+            d.gmax_idx[k] = std::min(d.gmax_idx[k], p.glo_num_idx[k] - 1);
+            d.grid.gmin[k] = gmin[k];
+            d.grid.step[k] = step[k];
+            d.grid.inv_step[k] = 1.0f / step[k];
+            d.grid.n[k] = p.glo_num_idx[k];
+            if (b == 0 || dmin[k] < umin[k]) umin[k] = dmin[k];
+            if (b == 0 || dmax[k] > umax[k]) umax[k] = dmax[k];
+        }
+        d.grid.off = off[b];
+    }
+    // one fixed-point scale for every set (the largest box): sums stay exact
+    const double scale = star_sum_scale(umin, umax);
+    GridDesc g0;
+    std::memset(&g0, 0, sizeof(g0));
+    for (int k = 0; k < 3; ++k)
+    {
+        g0.dmin[k] = umin[k];
+        g0.dmax[k] = umax[k];
+    }
+    int var = bt->raster_variant[mode] >= 0 ? bt->raster_variant[mode] : ctx->raster_variant[mode];
+    const char* env = getenv("TESSGPU_RASTER_VARIANT");
+    if (var < 0 && env && *env)
+        var = ctx->raster_variant[mode] = std::min(std::max(atoi(env), 0), brick_variants() - 1);
+    if (!bt->W || bt->pooled)
+    {
+        BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
+        BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
+        BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
+    }
+    unsigned long long* W = (unsigned long long*)bt->W;
+    BrickBins bins;
+    tessgpu_status st;
+    if (var < 0)
+    {
+        // autotune the brick shape on these sets (bin + rasterise, twice each)
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
+        CK(cudaMemsetAsync(W, 0, sizeof(unsigned long long) * (bt->N ? bt->N : 1), s));
+        launch_star_volumes(mode, (int)bt->T, bt->pos, bt->tv, W, scale, kTau, ctx->d_status, s);
+        launch_densities(W, (int)bt->N, mass, 1.0 / scale, bt->rho32, bt->rho64, ctx->d_status, s);
+        ctx->launches += 2;
+        float best = 1e30f;
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        for (int v = 0; v < brick_variants(); ++v)
+        {
+            const long long nbv = assign_bricks(bt->hb, v);
+            CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
+            if ((st = brick_bins(ctx, nbv, nb, bt->T, &bins)) != TESSGPU_OK)
+                return st;
+            float vbest = 1e30f;
+            for (int rep = 0; rep < 2; ++rep)
+            {
+                CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
+                CK(cudaEventRecord(e0, s));
+                bricks_bin(ctx, v, bt->d_blocks, bt->hb, 0, nb, nbv, bins, bt->pos, bt->tv, g0, d_out, s);
+                bricks_raster(ctx, mode, v, bt->d_blocks, bt->hb, 0, nb, nbv, bins, bt->pos, bt->tv, bt->rho32,
+                              bt->rho64, g0, d_out, nullptr, s);
+                CK(cudaEventRecord(e1, s));
+                CK(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                vbest = std::min(vbest, ms);
+            }
+            if (v < 8) ctx->tune_ms[mode][v] = vbest;
+            if (vbest < best) { best = vbest; var = v; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        CK(cudaMemcpy(ctx->h_status, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost));
+        if (ctx->h_status->code == TESSGPU_ERR_CAPACITY)
+            grow_pairs(ctx);
+        else if (ctx->h_status->code)
+            return finish_status(ctx);
+        ctx->raster_variant[mode] = var;
+    }
+    bt->raster_variant[mode] = var;
+    const long long nbricks = assign_bricks(bt->hb, var);
+    if ((st = brick_bins(ctx, nbricks, nb, bt->T, &bins)) != TESSGPU_OK)
+        return st;
+    // what a recorded step depends on: the sets' grids, the mode, the shape and the scratch
+    std::vector<long long> key = { (long long)mode, (long long)var, (long long)(size_t)d_out,
+                                   (long long)(size_t)bins.pairs, bins.pair_cap,
+                                   (long long)(size_t)bins.cnt, (long long)(size_t)bt->W };
+    for (int i = 0; i < 3 * nb; ++i) key.push_back(glo_num_idx[i]);
+    long long mbits = 0, ebits = 0;
+    std::memcpy(&mbits, &mass, sizeof(float));
+    std::memcpy(&ebits, &eps, sizeof(float));
+    key.push_back(mbits);
+    key.push_back(ebits);
+    // the descriptors go up before the step (a graph cannot hold a copy from pageable memory)
+    CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
+    auto record = [&]() {
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
+        CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
+        CK(cudaMemsetAsync(W, 0, sizeof(unsigned long long) * (bt->N ? bt->N : 1), s));
+        bricks_reset(ctx, bt->hb, 0, nb, nbricks, bins, s);
+        bricks_star(ctx, mode, var, bt->d_blocks, nb, 0, bt->T, bt->pos, bt->tv, W, scale, g0, bins, s);
+        bricks_place(ctx, var, bt->d_blocks, bt->hb, 0, nb, nbricks, bins, bt->pos, bt->tv, g0, d_out, s);
+        launch_densities(W, (int)bt->N, mass, 1.0 / scale, bt->rho32, bt->rho64, ctx->d_status, s);
+        ctx->launches += bt->N ? 1 : 0;
+        bricks_raster(ctx, mode, var, bt->d_blocks, bt->hb, 0, nb, nbricks, bins, bt->pos, bt->tv, bt->rho32,
+                      bt->rho64, g0, d_out, nullptr, s);
+        return TESSGPU_OK;
+    };
+    const long long launches0 = ctx->launches;
+    if (graph)
+    {
+        if (!bt->sets_exec || bt->sets_key != key)
+        {
+            if (bt->sets_exec) { cudaGraphExecDestroy(bt->sets_exec); bt->sets_exec = nullptr; }
+            if (bt->sets_graph) { cudaGraphDestroy(bt->sets_graph); bt->sets_graph = nullptr; }
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            tessgpu_status rs = record();
+            cudaGraph_t gr = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+            if (rs != TESSGPU_OK) { if (gr) cudaGraphDestroy(gr); return rs; }
+            CK(ce);
+            bt->sets_graph = gr;
+            CK(cudaGraphInstantiate(&bt->sets_exec, gr, 0));
+            bt->sets_key = key;
+        }
+        ctx->launches = launches0;   // counted per replay below
+        CK(cudaGraphLaunch(bt->sets_exec, s));
+        ctx->launches += bt->T ? 6 : 2;
+    }
+    else if ((st = record()) != TESSGPU_OK)
+        return st;
+    st = finish_status(ctx);
+    if (st == TESSGPU_ERR_CAPACITY && !ctx->in_retry)
+    {
+        grow_pairs(ctx);
+        ctx->in_retry = true;
+        st = tessgpu_batch_dense_sets(ctx, bt, glo_num_idx, mass, eps, mode, d_out, graph, info);
+        ctx->in_retry = false;
+        return st;
+    }
+    if (st != TESSGPU_OK || !info)
+        return st;
+    std::memset(info, 0, sizeof(*info));
+    const Status& hs = *ctx->h_status;
+    info->grid_pts_assigned = (long long)hs.assigned;
+    info->fp64_tets = (long long)hs.fp64_tets;
+    info->exact_tests = (long long)hs.exact_tests;
+    info->rows_visited = (long long)hs.rows;
+    info->points_tested = (long long)hs.candidates;
+    info->raster_variant = var;
+    for (int v = 0; v < 8; ++v)
+        info->raster_variant_ms[v] = ctx->tune_ms[mode][v];
+    info->grid_floats = Gtot;
+    unsigned long long pairs = 0;
+    CK(cudaMemcpy(&pairs, bins.pair_cursor, sizeof(pairs), cudaMemcpyDeviceToHost));
+    info->brick_pairs = (long long)pairs;
+    return TESSGPU_OK;
 }
 
 extern "C" tessgpu_status tessgpu_batch_debug_outputs(tessgpu_ctx* ctx, tessgpu_batch* bt, int* cell_counts,
@@ -1274,6 +1921,16 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         return set_err(ctx, TESSGPU_ERR_INVALID, "batch larger than 2^31 particles or tets");
     const long long area = (long long)p->glo_num_idx[0] * p->glo_num_idx[1];
     const long long G = area * p->glo_num_idx[2];
+    set_block_grids(hb, g);
+    const bool bricks = !ctx->rows;
+    const long long nbricks = bricks ? assign_bricks(hb, variant) : 0;
+    BrickBins bins;
+    std::memset(&bins, 0, sizeof(bins));
+    if (bricks)
+    {
+        tessgpu_status bs = brick_bins(ctx, nbricks, nb, T, &bins);
+        if (bs != TESSGPU_OK) return bs;
+    }
     cudaError_t e = cudaSuccess;
     auto get = [&](int slot, size_t bytes) { cudaError_t ee; void* q = pool_get(ctx, slot, bytes, &ee);
                                              if (ee != cudaSuccess) e = ee; return q; };
@@ -1284,8 +1941,8 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     unsigned long long* W = (unsigned long long*)get(SLOT_W, sizeof(double) * std::max(N, 1LL));
     float* rho32 = (float*)get(SLOT_RHO32, sizeof(float) * std::max(N, 1LL));
     double* rho64 = (double*)get(SLOT_RHO64, sizeof(double) * std::max(N, 1LL));
-    int* fix = (int*)get(SLOT_FIX, sizeof(int) * std::max(T, 1LL));
-    int* fixn = (int*)get(SLOT_FIXN, sizeof(int) * nb);   // one fix-list length per block
+    int* fix = bricks ? nullptr : (int*)get(SLOT_FIX, sizeof(int) * std::max(T, 1LL));
+    int* fixn = (int*)get(SLOT_FIXN, sizeof(int) * nb);   // one fix-list length per block (row kernel)
     float* grid = (float*)get(SLOT_GRID, sizeof(float) * G);
     CK(e);
     *d_grid_out = grid;
@@ -1317,27 +1974,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     }
     // when the blocks' grid boxes tile the grid (the usual case), each box
     // goes down as soon as its block is done, so only the last box trails
-    bool tiles = true;
-    long long covered = 0;
-    for (int i = 0; i < nb && tiles; ++i)
-    {
-        long long v = 1;
-        for (int k = 0; k < 3; ++k)
-        {
-            const int n = hb[i].gmax_idx[k] - hb[i].gmin_idx[k] + 1;
-            if (n <= 0) tiles = false;
-            v *= n;
-        }
-        covered += v;
-        for (int j = 0; j < i && tiles; ++j)
-        {
-            bool meet = true;
-            for (int k = 0; k < 3; ++k)
-                if (hb[i].gmax_idx[k] < hb[j].gmin_idx[k] || hb[j].gmax_idx[k] < hb[i].gmin_idx[k]) meet = false;
-            if (meet) tiles = false;
-        }
-    }
-    tiles = tiles && covered == G;
+    const bool tiles = boxes_tile(hb, p->glo_num_idx);
 
     const double scale = star_sum_scale(dmin, dmax);
 
@@ -1390,8 +2027,12 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     }
     CK(cudaMemcpyAsync(d_blocks, hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
-    CK(cudaMemsetAsync(grid, 0, sizeof(float) * G, s));
+    // the brick rasteriser writes every point of the blocks' boxes
+    if (!bricks || !tiles)
+        CK(cudaMemsetAsync(grid, 0, sizeof(float) * G, s));
     CK(cudaMemsetAsync(fixn, 0, sizeof(int) * nb, s));
+    if (bricks)
+        CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
     // blocks alternate between two compute streams, so one block's launches
     // fill the SMs the previous block's last waves leave idle; they share
     // nothing but read-only descriptors, the status word (atomics) and the grid,
@@ -1413,6 +2054,8 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             CK(cudaMemsetAsync(W + d.p_off, 0, sizeof(unsigned long long) * d.np, s));
             ctx->launches++;
         }
+        if (bricks)
+            bricks_reset(ctx, hb, b, b + 1, nbricks, bins, s);
         for (int i = 0; i < (k == 0 ? kFirstParts : 1); ++i)
         {
             // the tets in the parts they came up in (one part after the first block)
@@ -1422,16 +2065,28 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             if (t1 <= t0) continue;
             k_ingest_verts<<<grid_small(t1 - t0), 256, 0, s>>>(stage_tets + 2 * ((size_t)d.t_off + t0), (int)(t1 - t0),
                                                                 d.np, d.p_off, tv + d.t_off + t0, ctx->d_status);
-            launch_star_volumes(p->mode, (int)(t1 - t0), pos, tv + d.t_off + t0, W, scale, kTau, ctx->d_status, s);
-            ctx->launches += 2;
+            ctx->launches++;
+            if (bricks)
+                bricks_star(ctx, p->mode, variant, d_blocks, nb, d.t_off + t0, t1 - t0, pos, tv, W, scale, g, bins, s);
+            else
+            {
+                launch_star_volumes(p->mode, (int)(t1 - t0), pos, tv + d.t_off + t0, W, scale, kTau, ctx->d_status,
+                                    s);
+                ctx->launches++;
+            }
         }
+        if (bricks)
+            bricks_place(ctx, variant, d_blocks, hb, b, b + 1, nbricks, bins, pos, tv, g, grid, s);
         if (d.np)
         {
             launch_densities(W + d.p_off, d.np, p->mass, 1.0 / scale, rho32 + d.p_off, rho64 + d.p_off,
                              ctx->d_status, s);
             ctx->launches++;
         }
-        if (d.nt)
+        if (bricks)
+            bricks_raster(ctx, p->mode, variant, d_blocks, hb, b, b + 1, nbricks, bins, pos, tv, rho32, rho64, g,
+                          grid, nullptr, s);
+        else if (d.nt)
         {
             // the block's FP64 fix-up list: its own segment of the list buffer
             launch_raster(p->mode, variant, d_blocks, nb, d.nt, pos, tv, rho32, rho64, g, kTau, grid, nullptr,
@@ -1522,6 +2177,12 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             info->raster_variant_ms[v] = ctx->tune_ms[p->mode][v];
         info->grid_layers = 0;
         info->grid_floats = G;
+        if (bricks)
+        {
+            unsigned long long pairs = 0;
+            CK(cudaMemcpy(&pairs, bins.pair_cursor, sizeof(pairs), cudaMemcpyDeviceToHost));
+            info->brick_pairs = (long long)pairs;
+        }
     }
     return TESSGPU_OK;
 }
@@ -1543,6 +2204,15 @@ extern "C" tessgpu_status tessgpu_dense(tessgpu_ctx* ctx, int nblocks, const tes
             float* d_grid = nullptr;
             tessgpu_status s = dense_dtfe_pipelined(ctx, nblocks, blocks, p, ctx->raster_variant[p->mode],
                                                     global_grid, info, &d_grid);
+            if (s == TESSGPU_ERR_CAPACITY && !ctx->in_retry)
+            {
+                // the brick pair list was too small: size it for this call and run again
+                grow_pairs(ctx);
+                ctx->in_retry = true;
+                s = dense_dtfe_pipelined(ctx, nblocks, blocks, p, ctx->raster_variant[p->mode], global_grid, info,
+                                         &d_grid);
+                ctx->in_retry = false;
+            }
             if (s == TESSGPU_OK)
             {
                 ctx->last_grid = d_grid;

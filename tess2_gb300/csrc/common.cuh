@@ -12,6 +12,17 @@ namespace tg {
 //   tn   int4[T]    tet neighbours (tn.i opposite tv.i), global tet indices, -1 on the hull
 //   v2t  int[N]     a tet containing each particle (the highest-numbered), -1 if none
 //   cc   float4[T]  circumcenters (DENSE_TESS / volume only)
+// the grid a block's DTFE rasteriser writes: grid positions x_i = i * step +
+// gmin per axis, n points per axis, x fastest, starting at float offset off of
+// the output (every block of a dense() call shares one grid; a batch of
+// independent particle sets gives each set its own)
+struct BlockGrid
+{
+    float     gmin[3], step[3], inv_step[3];
+    int       n[3];
+    long long off;
+};
+
 struct BlockDesc
 {
     int   gid;
@@ -20,6 +31,11 @@ struct BlockDesc
     int   t_off, nt;             // first tet, tets
     int   c_off;                 // first cell in the batch's cell numbering (original particles)
     int   gmin_idx[3], gmax_idx[3], gnum_idx[3];   // BlockGridParams of the current grid
+    // DTFE brick rasteriser: the bricks covering the grid box, brick_n[0] x
+    // brick_n[1] x brick_n[2] of them from brick coordinates brick_lo, numbered
+    // from brick_base in the batch's brick numbering (x fastest)
+    int   brick_base, brick_lo[3], brick_n[3];
+    BlockGrid grid;
 };
 
 struct GridDesc

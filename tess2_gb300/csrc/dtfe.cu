@@ -26,6 +26,7 @@
 #include "kernels.h"
 #include "dtfe_common.cuh"
 #include <float.h>
+#include <limits.h>
 #include <math.h>
 
 namespace tg {
@@ -172,27 +173,6 @@ __device__ __noinline__ int numerator_sign_exact(const float a[4][3], int k, con
 // atomics: the sum is exact and independent of the order of the additions,
 // so W (and rho) is bit-reproducible.  scale_bits keeps any star volume below
 // 2^62 (the host derives it from the data bounds).
-__global__ void k_star_volumes(int mode, int total, const float4* pos, const int4* tv, unsigned long long* W,
-                               double scale, float tau, Status* st)
-{
-    unsigned long long nfix = 0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x)
-    {
-        const int4 vi = __ldg(&tv[t]);
-        const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
-        const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a0, a1, a2, a3, &nfix);
-        const unsigned long long q = (unsigned long long)__double2ll_rn(vol * scale);
-        atomicAdd(&W[vi.x], q);
-        atomicAdd(&W[vi.y], q);
-        atomicAdd(&W[vi.z], q);
-        atomicAdd(&W[vi.w], q);
-    }
-    for (int o = 16; o > 0; o >>= 1)
-        nfix += __shfl_xor_sync(FULL, nfix, o);
-    if ((threadIdx.x & 31) == 0 && nfix)
-        atomicAdd(&st->fp64_tets, nfix);
-}
-
 // rho_v = (D+1) m / W_v = 4 m / W_v, 0 for a vertex in no tet.  The sums
 // hold 6x the volumes (the determinants), so rho = 24 m / sum.
 __global__ void k_densities(const unsigned long long* W, int n, float mass, double inv_scale, float* rho32,
@@ -360,12 +340,14 @@ template <typename T> __device__ __forceinline__ T comp4(const typename Vec4<T>:
 }
 
 // the tet's vertices and the index box of grid points it can hold inside its
-// block's grid box; true when that box is empty
-__device__ __forceinline__ bool tet_box(const BlockDesc* blocks, int nb, const float4* pos, const int4* tv,
-                                        const GridDesc& g, int t, int& b, int* vid, float a[4][3], float* lo,
-                                        float* hi, int* ilo, int* ihi)
+// block's grid box (positions from the block's grid; g is not read); true when
+// that box is empty.  Box = the grid points whose
+// float position x_i = i*step + gmin satisfies lo <= x_i < hi on every axis:
+// the perturbed point x_i + (e, e^2, e^3) can only be inside the tet then.
+__device__ __forceinline__ bool tet_box_in(const BlockDesc& bd, const float4* pos, const int4* tv,
+                                           const GridDesc& g, int t, int* vid, float a[4][3], float* lo,
+                                           float* hi, int* ilo, int* ihi)
 {
-    b = find_blk(blocks, nb, t);
     const int4 vi = __ldg(&tv[t]);
     vid[0] = vi.x; vid[1] = vi.y; vid[2] = vi.z; vid[3] = vi.w;
 #pragma unroll
@@ -380,13 +362,22 @@ __device__ __forceinline__ bool tet_box(const BlockDesc* blocks, int nb, const f
     {
         lo[d] = fminf(fminf(a[0][d], a[1][d]), fminf(a[2][d], a[3][d]));
         hi[d] = fmaxf(fmaxf(a[0][d], a[1][d]), fmaxf(a[2][d], a[3][d]));
-        const int olo = blocks[b].gmin_idx[d], ohi = blocks[b].gmax_idx[d];
-        ilo[d] = first_at_or_above(lo[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi);
-        ihi[d] = first_at_or_above(hi[d], g.gmin[d], g.step[d], g.inv_step[d], olo, ohi + 1) - 1;
+        const int olo = bd.gmin_idx[d], ohi = bd.gmax_idx[d];
+        const BlockGrid& gb = bd.grid;
+        ilo[d] = first_at_or_above(lo[d], gb.gmin[d], gb.step[d], gb.inv_step[d], olo, ohi);
+        ihi[d] = first_at_or_above(hi[d], gb.gmin[d], gb.step[d], gb.inv_step[d], olo, ohi + 1) - 1;
         if (ihi[d] > ohi) ihi[d] = ohi;
         if (ilo[d] > ihi[d]) empty = true;
     }
     return empty;
+}
+
+__device__ __forceinline__ bool tet_box(const BlockDesc* blocks, int nb, const float4* pos, const int4* tv,
+                                        const GridDesc& g, int t, int& b, int* vid, float a[4][3], float* lo,
+                                        float* hi, int* ilo, int* ihi)
+{
+    b = find_blk(blocks, nb, t);
+    return tet_box_in(blocks[b], pos, tv, g, t, vid, a, lo, hi, ilo, ihi);
 }
 
 // Each tet's rows run along the axis of its smallest projected area (fewest
@@ -998,13 +989,6 @@ static int grid_for(long long n, int block, int per_sm)
     return (int)(need < cap ? need : cap);
 }
 
-void launch_star_volumes(int mode, int total, const float4* pos, const int4* tv, unsigned long long* W,
-                         double scale, float tau, Status* st, cudaStream_t s)
-{
-    if (total <= 0) return;
-    k_star_volumes<<<grid_for(total, 256, 8), 256, 0, s>>>(mode, total, pos, tv, W, scale, tau, st);
-}
-
 void launch_densities(const unsigned long long* W, int n, float mass, double inv_scale, float* rho32, double* rho64,
                       Status* st, cudaStream_t s)
 {
@@ -1173,6 +1157,933 @@ void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total, const float
     const long long work = (long long)((total / 16 + 31) / 32) * 32 * 32;
     raster_variant<float, true, true>(0, work, s, d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32, rho64, g,
                                       0.0f, grid, owner, nullptr, nullptr, st);
+}
+
+
+// ===========================================================================
+// brick rasteriser
+// ===========================================================================
+// Work decomposition.  The grid box of every block is cut into bricks of
+// BX x BY x BZ grid points (powers of two) aligned to the global grid and
+// clipped at the box's edges.  A brick's candidates are the tets whose grid
+// box (tet_box_in) overlaps it, found by a counting sort of the (tet, brick)
+// pairs: count, scan, scatter.  One CTA takes one brick: it rasterises the
+// brick's candidates into a tile in shared memory and writes the tile out
+// once, whole, in x rows of BX floats, with zeros where no tet owns a point;
+// so no grid zeroing pass is needed and each grid sector is written once.
+// A brick with more than BRICK_CHUNK candidates (a dense clump) is split into
+// several items of that many; its region is zeroed first and each item
+// writes only the points its own tets hold.
+//
+// Inside the CTA each warp takes 32 candidates at a time, one per lane, and
+// sets them up into its shared-memory slots: grid box clipped to the brick,
+// orientation, the numerator planes and error bounds of the point-in-tet
+// test, interpolation weights, the x bounds of a row as affine functions of
+// (y, z), the edge slopes of the z slices.  The 32 tets' work is then spread
+// over the lanes level by level, so that no lane waits on another tet's long
+// loop: the z slices of all 32 tets (a lane per slice: the y range of the
+// tet's cross-section there), the rows of 32 slices (a lane per row: the x
+// range its face bounds allow), the points of 32 rows (a lane per point: the
+// filtered test, exact arithmetic when the filter cannot decide, and the
+// interpolated value written to the tile).  A level finds its parent through
+// an owner table the parent lanes fill.  Owners, tests and values are those
+// of k_raster: the same predicates, bounds and expressions.
+constexpr int BRICK_CHUNK = 2048;
+constexpr unsigned BRICK_UNSET = 0xffffffffu;   // a NaN no arithmetic produces
+
+template <typename T, int SX, int SY, int SZ>
+struct __align__(32) BrickWarp
+{
+    typedef typename Vec4<T>::type T4;
+    T4     C[4][32];                // s c_k (x, y, z) and B_k
+    T4     W[32];                   // s rho_k / 6V
+    T4     RN[32];                  // level 3: the row's R_k (the y and z part of s N_k)
+    double F[4][32];                // FP64 fix-up tets: rho_0 and the field's gradient
+    float4 P[4][32];                // vertices; w: lo x, hi x, lo y, hi y of the tet's box
+    float4 XA[32], XB[32], XG[32];  // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
+    float  IDZ[6][32];              // 1 / (z_v - z_u) of the six edges (0 for an edge in a z plane)
+    int4   I0[32];                  // box clipped to the brick: x0, x1, y0, y1
+    int4   I1[32];                  // z0 (clipped), box's first y and z, flags
+    int    TG[32];                  // tet index
+    int4   SL[32];                  // level 2: the slice's (slot, z, first y)
+    int4   RW[32];                  // level 3: the row's (slot, y, z, first x)
+    int    pre1[33], pre2[33], pre3[33];
+    unsigned char own1[32 << SZ], own2[32 << SY], own3[32 << SX];
+};
+
+// brick b's block (blocks' bricks are numbered in block order)
+__device__ __forceinline__ int brick_block(const BlockDesc* blocks, int nb, int b)
+{
+    int lo = 0, hi = nb - 1;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (blocks[mid].brick_base <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// grid points [r0, r1] of brick b of block bd
+__device__ __forceinline__ void brick_region(const BlockDesc& bd, int b, int sx, int sy, int sz, int* r0, int* r1)
+{
+    const int l = b - bd.brick_base;
+    const int bx = l % bd.brick_n[0], by = (l / bd.brick_n[0]) % bd.brick_n[1], bz = l / (bd.brick_n[0] * bd.brick_n[1]);
+    const int c[3] = { bx, by, bz }, sh[3] = { sx, sy, sz };
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        const int s0 = (bd.brick_lo[d] + c[d]) << sh[d];
+        r0[d] = max(s0, bd.gmin_idx[d]);
+        r1[d] = min(s0 + (1 << sh[d]) - 1, bd.gmax_idx[d]);
+    }
+}
+
+// the bricks tet t's grid box overlaps: brick coordinates relative to the block
+__device__ __forceinline__ bool tet_bricks(const BlockDesc& bd, const float4* pos, const int4* tv, const GridDesc& g,
+                                           int t, int sx, int sy, int sz, int* b0, int* b1)
+{
+    int vid[4], ilo[3], ihi[3];
+    float a[4][3], lo[3], hi[3];
+    if (tet_box_in(bd, pos, tv, g, t, vid, a, lo, hi, ilo, ihi))
+        return false;
+    const int sh[3] = { sx, sy, sz };
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        b0[d] = (ilo[d] >> sh[d]) - bd.brick_lo[d];
+        b1[d] = (ihi[d] >> sh[d]) - bd.brick_lo[d];
+    }
+    return true;
+}
+
+// q added to W[key] by the lanes that hold key: one atomic per distinct key
+// and warp (consecutive tets share vertices, so a warp's 32 tets touch about
+// 40 vertices, not 128).  The group's sum is exact (64-bit integers, summed
+// as three 21-bit pieces with the warp's integer reduction), so W is the same
+// as with one atomic per term.  Every lane of the warp calls this; inactive
+// lanes pass active = false.
+__device__ __forceinline__ void warp_add_u64(unsigned long long* W, int key, unsigned long long q, bool active)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned grp = __match_any_sync(FULL, active ? key : -1 - lane);
+    const unsigned s0 = __reduce_add_sync(grp, (unsigned)(q & 0x1fffffull));
+    const unsigned s1 = __reduce_add_sync(grp, (unsigned)((q >> 21) & 0x1fffffull));
+    const unsigned s2 = __reduce_add_sync(grp, (unsigned)(q >> 42));
+    if (active && lane == __ffs(grp) - 1)
+        atomicAdd(&W[key], (unsigned long long)s0 + ((unsigned long long)s1 << 21) + ((unsigned long long)s2 << 42));
+}
+
+// Star volumes of tets [t0, t0 + nt); with BIN, also the brick rasteriser's
+// pair counts of those tets (the same vertex loads serve both).
+template <bool BIN>
+__global__ void k_star_volumes(int mode, int t0, int nt, const float4* pos, const int4* tv, unsigned long long* W,
+                               double scale, Status* st, const BlockDesc* blocks, int nb, GridDesc g, int sx, int sy,
+                               int sz, int* cnt)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long nfix = 0;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < nt; base += (long long)gridDim.x * blockDim.x)
+    {
+        const long long it = base + threadIdx.x;
+        const bool active = it < nt;
+        int4 vi = make_int4(0, 0, 0, 0);
+        unsigned long long q = 0;
+        if (active)
+        {
+            vi = __ldg(&tv[t0 + it]);
+            const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
+            const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a0, a1, a2, a3, &nfix);
+            q = (unsigned long long)__double2ll_rn(vol * scale);
+        }
+        warp_add_u64(W, vi.x, q, active);
+        warp_add_u64(W, vi.y, q, active);
+        warp_add_u64(W, vi.z, q, active);
+        warp_add_u64(W, vi.w, q, active);
+        if (BIN)
+        {
+            int b0[3], b1[3], key = -1;
+            bool any = false, single = false;
+            const BlockDesc* bd = nullptr;
+            if (active)
+            {
+                const int t = t0 + (int)it;
+                bd = &blocks[find_blk(blocks, nb, t)];
+                any = tet_bricks(*bd, pos, tv, g, t, sx, sy, sz, b0, b1);
+                if (any)
+                {
+                    single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
+                    if (single)
+                        key = bd->brick_base + (b0[2] * bd->brick_n[1] + b0[1]) * bd->brick_n[0] + b0[0];
+                }
+            }
+            const unsigned grp = __match_any_sync(FULL, key);
+            if (key >= 0 && lane == __ffs(grp) - 1)
+                atomicAdd(&cnt[key], __popc(grp));
+            if (any && !single)
+                for (int z = b0[2]; z <= b1[2]; ++z)
+                    for (int y = b0[1]; y <= b1[1]; ++y)
+                        for (int x = b0[0]; x <= b1[0]; ++x)
+                            atomicAdd(&cnt[bd->brick_base + (z * bd->brick_n[1] + y) * bd->brick_n[0] + x], 1);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        nfix += __shfl_xor_sync(FULL, nfix, o);
+    if (lane == 0 && nfix)
+        atomicAdd(&st->fp64_tets, nfix);
+}
+
+// (tet, brick) pairs per brick.  Tets that fall in one brick (most) are
+// counted with one atomic per brick and warp.
+__global__ void k_bin_count(const BlockDesc* blocks, int nb, int t0, int nt, const float4* pos, const int4* tv,
+                            GridDesc g, int sx, int sy, int sz, int* cnt)
+{
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < nt; base += (long long)gridDim.x * blockDim.x)
+    {
+        const long long it = base + threadIdx.x;
+        int b0[3], b1[3], key = -1;
+        bool any = false, single = false;
+        const BlockDesc* bd = nullptr;
+        if (it < nt)
+        {
+            const int t = t0 + (int)it;
+            bd = &blocks[find_blk(blocks, nb, t)];
+            any = tet_bricks(*bd, pos, tv, g, t, sx, sy, sz, b0, b1);
+            if (any)
+            {
+                single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
+                if (single)
+                    key = bd->brick_base + (b0[2] * bd->brick_n[1] + b0[1]) * bd->brick_n[0] + b0[0];
+            }
+        }
+        const unsigned grp = __match_any_sync(FULL, key);
+        if (key >= 0 && lane == __ffs(grp) - 1)
+            atomicAdd(&cnt[key], __popc(grp));
+        if (any && !single)
+            for (int z = b0[2]; z <= b1[2]; ++z)
+                for (int y = b0[1]; y <= b1[1]; ++y)
+                    for (int x = b0[0]; x <= b1[0]; ++x)
+                        atomicAdd(&cnt[bd->brick_base + (z * bd->brick_n[1] + y) * bd->brick_n[0] + x], 1);
+    }
+}
+
+// Bricks [bb0, bb1) of one segment (blocks whose tets are binned together):
+// exclusive prefixes of the pair counts (placed in the pair list at an
+// offset taken from the shared cursor) and of the items (ceil(count /
+// BRICK_CHUNK), at least one per brick).  One CTA of 1024 threads.
+__global__ void __launch_bounds__(1024)
+k_bin_scan(int bb0, int bb1, int seg, const int* cnt, int* off, int* cur, int* item_off, int* seg_items,
+           unsigned long long* pair_cursor, long long pair_cap, Status* st)
+{
+    __shared__ long long pc[1024], pi[1024];
+    __shared__ long long s_base;
+    __shared__ int s_ok;
+    const int n = bb1 - bb0;
+    const int per = (n + 1023) / 1024;
+    const int lo = min(n, (int)threadIdx.x * per), hi = min(n, lo + per);
+    long long sc = 0, si = 0;
+    for (int i = lo; i < hi; ++i)
+    {
+        const int c = cnt[bb0 + i];
+        sc += c;
+        si += c > 0 ? (c + BRICK_CHUNK - 1) / BRICK_CHUNK : 1;
+    }
+    pc[threadIdx.x] = sc;
+    pi[threadIdx.x] = si;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1)
+    {
+        const long long a = threadIdx.x >= (unsigned)o ? pc[threadIdx.x - o] : 0;
+        const long long b = threadIdx.x >= (unsigned)o ? pi[threadIdx.x - o] : 0;
+        __syncthreads();
+        pc[threadIdx.x] += a;
+        pi[threadIdx.x] += b;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        const long long tot = pc[1023];
+        const unsigned long long base = atomicAdd(pair_cursor, (unsigned long long)tot);
+        const bool ok = (long long)base + tot <= pair_cap;
+        if (!ok)
+            fail(st, TESSGPU_ERR_CAPACITY, (int)min(tot, (long long)INT_MAX));
+        s_base = (long long)base;
+        s_ok = ok;
+        seg_items[seg] = ok ? (int)pi[1023] : 0;
+    }
+    __syncthreads();
+    if (!s_ok)
+        return;
+    long long rc = s_base + pc[threadIdx.x] - sc, ri = pi[threadIdx.x] - si;
+    for (int i = lo; i < hi; ++i)
+    {
+        const int c = cnt[bb0 + i];
+        off[bb0 + i] = (int)rc;
+        cur[bb0 + i] = (int)rc;
+        item_off[bb0 + i] = (int)ri;
+        rc += c;
+        ri += c > 0 ? (c + BRICK_CHUNK - 1) / BRICK_CHUNK : 1;
+    }
+}
+
+// the pairs themselves: each brick's tets, in the order the atomics give
+__global__ void k_bin_scatter(const BlockDesc* blocks, int nb, int t0, int nt, const float4* pos, const int4* tv,
+                              GridDesc g, int sx, int sy, int sz, int* cur, int* pairs, long long pair_cap)
+{
+    const int lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < nt; base += (long long)gridDim.x * blockDim.x)
+    {
+        const long long it = base + threadIdx.x;
+        int b0[3], b1[3], key = -1, t = -1;
+        bool any = false, single = false;
+        const BlockDesc* bd = nullptr;
+        if (it < nt)
+        {
+            t = t0 + (int)it;
+            bd = &blocks[find_blk(blocks, nb, t)];
+            any = tet_bricks(*bd, pos, tv, g, t, sx, sy, sz, b0, b1);
+            if (any)
+            {
+                single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
+                if (single)
+                    key = bd->brick_base + (b0[2] * bd->brick_n[1] + b0[1]) * bd->brick_n[0] + b0[0];
+            }
+        }
+        const unsigned grp = __match_any_sync(FULL, key);
+        const int leader = __ffs(grp) - 1;
+        int slot = 0;
+        if (key >= 0 && lane == leader)
+            slot = atomicAdd(&cur[key], __popc(grp));
+        slot = __shfl_sync(FULL, slot, leader) + __popc(grp & ((1u << lane) - 1u));
+        if (key >= 0 && slot < pair_cap)
+            pairs[slot] = t;
+        if (any && !single)
+            for (int z = b0[2]; z <= b1[2]; ++z)
+                for (int y = b0[1]; y <= b1[1]; ++y)
+                    for (int x = b0[0]; x <= b1[0]; ++x)
+                    {
+                        const int q = atomicAdd(&cur[bd->brick_base + (z * bd->brick_n[1] + y) * bd->brick_n[0] + x], 1);
+                        if (q < pair_cap)
+                            pairs[q] = t;
+                    }
+    }
+}
+
+// the regions of the split bricks are zeroed before their items run
+__global__ void k_zero_split(const BlockDesc* blocks, int nb, int bb0, int bb1, int seg, const int* item_off,
+                             const int* seg_items, int sx, int sy, int sz, GridDesc g, float* grid)
+{
+    for (int b = bb0 + blockIdx.x; b < bb1; b += gridDim.x)
+    {
+        const int i1 = b + 1 < bb1 ? item_off[b + 1] : seg_items[seg];
+        if (i1 - item_off[b] <= 1)
+            continue;
+        const BlockDesc& bd = blocks[brick_block(blocks, nb, b)];
+        int r0[3], r1[3];
+        brick_region(bd, b, sx, sy, sz, r0, r1);
+        const int nx = r1[0] - r0[0] + 1, ny = r1[1] - r0[1] + 1, nz = r1[2] - r0[2] + 1;
+        const BlockGrid& gb = bd.grid;
+        for (int i = threadIdx.x; i < nx * ny * nz; i += blockDim.x)
+        {
+            const int x = i % nx, y = (i / nx) % ny, z = i / (nx * ny);
+            grid[gb.off + ((size_t)(r0[2] + z) * gb.n[1] + (r0[1] + y)) * gb.n[0] + (r0[0] + x)] = 0.0f;
+        }
+    }
+}
+
+// exclusive prefix of v over the warp into pre[0..32]; returns the total
+__device__ __forceinline__ int warp_prefix(int v, int lane, int* pre)
+{
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const int u = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += u;
+    }
+    pre[lane + 1] = incl;
+    if (lane == 0) pre[0] = 0;
+    return __shfl_sync(FULL, incl, 31);
+}
+
+struct BrickCounts
+{
+    unsigned long long exact = 0, assigned = 0, fix = 0, rows = 0, cand = 0;
+};
+
+// one warp, up to 32 candidates [ci0, ci1) of the brick r0..r1
+template <typename T, int SX, int SY, int SZ>
+__device__ __forceinline__ void brick_batch(BrickWarp<T, SX, SY, SZ>& S, float* tile, const int* r0, const int* r1,
+                                            int ci0, int ci1, const int* pairs, const BlockDesc& bd,
+                                            const float4* pos, const int4* tv, const float* rho32,
+                                            const double* rho64, const GridDesc& g0, int* owner, int fixup,
+                                            BrickCounts& cn)
+{
+    typedef typename Vec4<T>::type T4;
+    constexpr bool F32 = sizeof(T) == 4;
+    const int lane = threadIdx.x & 31;
+    const BlockGrid& g = bd.grid;   // the block's own grid
+    int ns = 0;
+    if (ci0 + lane < ci1)
+    {
+        const int t = __ldg(&pairs[ci0 + lane]);
+        int vid[4], ilo[3], ihi[3];
+        float a[4][3], lo[3], hi[3];
+        const bool empty = tet_box_in(bd, pos, tv, g0, t, vid, a, lo, hi, ilo, ihi);
+        const int cx0 = max(ilo[0], r0[0]), cx1 = min(ihi[0], r1[0]);
+        const int cy0 = max(ilo[1], r0[1]), cy1 = min(ihi[1], r1[1]);
+        const int cz0 = max(ilo[2], r0[2]), cz1 = min(ihi[2], r1[2]);
+        if (!empty && cx0 <= cx1 && cy0 <= cy1 && cz0 <= cz1)
+        {
+            const float3 A0 = make_float3(a[0][0], a[0][1], a[0][2]), A1 = make_float3(a[1][0], a[1][1], a[1][2]);
+            const float3 A2 = make_float3(a[2][0], a[2][1], a[2][2]), A3 = make_float3(a[3][0], a[3][1], a[3][2]);
+            int s;
+            T v6;
+            if (F32)
+            {
+                float vb;
+                const float v6f = tet_vol6_f32(A0, A1, A2, A3, vb);
+                v6 = v6f;
+                if (v6f > vb) s = 1;
+                else if (v6f < -vb) s = -1;
+                else s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1], a[2][2],
+                                  a[3][0], a[3][1], a[3][2]);
+            }
+            else
+            {
+                v6 = (T)tet_vol6_f64(A0, A1, A2, A3);
+                s = tet_sign(a[0][0], a[0][1], a[0][2], a[1][0], a[1][1], a[1][2], a[2][0], a[2][1], a[2][2],
+                             a[3][0], a[3][1], a[3][2]);
+            }
+            if (s != 0)   // s == 0: flat tet, no interior
+            {
+                T c[4][3], Bk[4];
+                numerators_setup<T>(a, lo, hi, c, Bk);
+                const bool fix = F32 && fixup && (float)(Bk[0] + Bk[1] + Bk[2] + Bk[3]) > DTFE_TAU * fabsf((float)v6);
+                if (fix && cx0 == ilo[0] && cy0 == ilo[1] && cz0 == ilo[2])
+                    cn.fix++;   // counted in the brick that holds the box's first corner
+                T4 w4;
+                const float r6 = F32 ? __frcp_rn((float)v6) : 0.0f;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                {
+                    const T wk = (T)s * (F32 ? (T)(__ldg(&rho32[vid[k]]) * r6) : (T)__ldg(&rho64[vid[k]]) / v6);
+                    if (k == 0) w4.x = wk;
+                    else if (k == 1) w4.y = wk;
+                    else if (k == 2) w4.z = wk;
+                    else w4.w = wk;
+                }
+                S.W[lane] = w4;
+                if (fix)
+                {
+                    // values in FP64: rho(p) = rho_0 + (p - a0) . G with G = sum_k rho_k c_k / 6V
+                    double e[3][3], f1[3], f2[3], cc[4][3];
+                    for (int k = 0; k < 3; ++k)
+                        for (int d = 0; d < 3; ++d)
+                            e[k][d] = (double)a[k + 1][d] - (double)a[0][d];
+                    for (int d = 0; d < 3; ++d)
+                    {
+                        f1[d] = (double)a[3][d] - (double)a[1][d];
+                        f2[d] = (double)a[2][d] - (double)a[1][d];
+                    }
+                    for (int jj = 0; jj < 3; ++jj)
+                    {
+                        const int ja = (jj + 1) % 3, jb = (jj + 2) % 3;
+                        cc[0][jj] = f1[ja] * f2[jb] - f1[jb] * f2[ja];
+                        cc[1][jj] = e[1][ja] * e[2][jb] - e[1][jb] * e[2][ja];
+                        cc[2][jj] = e[2][ja] * e[0][jb] - e[2][jb] * e[0][ja];
+                        cc[3][jj] = e[0][ja] * e[1][jb] - e[0][jb] * e[1][ja];
+                    }
+                    const double v6d = e[0][0] * cc[1][0] + e[0][1] * cc[1][1] + e[0][2] * cc[1][2];
+                    double G[3] = { 0.0, 0.0, 0.0 };
+                    for (int k = 0; k < 4; ++k)
+                    {
+                        const double wk = __ldg(&rho64[vid[k]]) / v6d;
+                        for (int d = 0; d < 3; ++d)
+                            G[d] += wk * cc[k][d];
+                    }
+                    S.F[0][lane] = __ldg(&rho64[vid[0]]);
+                    S.F[1][lane] = G[0];
+                    S.F[2][lane] = G[1];
+                    S.F[3][lane] = G[2];
+                }
+                S.P[0][lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
+                S.P[1][lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
+                S.P[2][lane] = make_float4(a[2][0], a[2][1], a[2][2], lo[1]);
+                S.P[3][lane] = make_float4(a[3][0], a[3][1], a[3][2], hi[1]);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                {
+                    // the orientation folded in (s = +-1 exactly): inside when every s N_k > B_k
+                    const T sg = (T)s;
+                    T4 ck;
+                    ck.x = sg * c[k][0]; ck.y = sg * c[k][1]; ck.z = sg * c[k][2]; ck.w = Bk[k];
+                    S.C[k][lane] = ck;
+                }
+                // row-wise x bounds (see k_raster): bnd_k = bx - s B_k / c_kx - R_k / c_kx,
+                // affine in the row's offsets (dy, dz) from the box's first row, widened by E
+                int masks = 0;
+                {
+                    const int nyb = ihi[1] - ilo[1] + 1, nzb = ihi[2] - ilo[2] + 1;
+                    const float h1 = g.step[1], h2 = g.step[2];
+                    const float py0 = ilo[1] * h1 + g.gmin[1], pz0 = ilo[2] * h2 + g.gmin[2];
+                    const float ymx = fmaxf(fabsf(py0), fabsf(ihi[1] * h1 + g.gmin[1]));
+                    const float zmx = fmaxf(fabsf(pz0), fabsf(ihi[2] * h2 + g.gmin[2]));
+                    const float xmx = fmaxf(fabsf(lo[0]), fabsf(hi[0]));
+                    float xa[4], xb[4], xg[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                    {
+                        const int base = k == 0 ? 1 : 0;
+                        const float bx = a[base][0], by = a[base][1], bz = a[base][2];
+                        const float cx = (float)c[k][0], cy = (float)c[k][1], cz = (float)c[k][2];
+                        const float B = (float)Bk[k];
+                        if (cx == 0.0f)
+                        {
+                            xa[k] = 0.0f; xb[k] = 0.0f; xg[k] = 0.0f;
+                            masks |= 1 << (4 + k);   // no x bound from this face
+                            continue;
+                        }
+                        const float icx = __frcp_rn(cx);
+                        const float R0 = cy * (py0 - by) + cz * (pz0 - bz);
+                        const float alpha = bx - (float)s * B * icx - R0 * icx;
+                        const float beta = -cy * h1 * icx, gamma = -cz * h2 * icx;
+                        const float E = 32.0f * EPS32 *
+                            (fabsf(bx) + xmx + fabsf(alpha) + fabsf(B * icx) + fabsf(R0 * icx) +
+                             fabsf(beta) * nyb + fabsf(gamma) * nzb +
+                             (fabsf(cy) * (ymx + fabsf(by)) + fabsf(cz) * (zmx + fabsf(bz))) * fabsf(icx)) +
+                            1e-30f;
+                        const bool lo_face = (float)s * cx > 0.0f;
+                        masks |= lo_face ? 1 << k : 0;
+                        xa[k] = lo_face ? alpha - E : alpha + E;
+                        xb[k] = beta;
+                        xg[k] = gamma;
+                    }
+                    S.XA[lane] = make_float4(xa[0], xa[1], xa[2], xa[3]);
+                    S.XB[lane] = make_float4(xb[0], xb[1], xb[2], xb[3]);
+                    S.XG[lane] = make_float4(xg[0], xg[1], xg[2], xg[3]);
+                }
+#pragma unroll
+                for (int e = 0; e < 6; ++e)
+                {
+                    const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
+                    const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
+                    const float dz = a[v][2] - a[u][2];
+                    S.IDZ[e][lane] = dz != 0.0f ? __frcp_rn(dz) : 0.0f;
+                }
+                S.I0[lane] = make_int4(cx0, cx1, cy0, cy1);
+                S.I1[lane] = make_int4(cz0, ilo[1], ilo[2], masks | (s > 0 ? 1 << 8 : 0) | (fix ? 1 << 9 : 0));
+                S.TG[lane] = t;
+                ns = cz1 - cz0 + 1;
+            }
+        }
+    }
+    // ---- level 1: the z slices of the 32 tets, a lane per slice
+    const int Z = warp_prefix(ns, lane, S.pre1);
+    __syncwarp();
+    for (int i = 0; i < ns; ++i)
+        S.own1[S.pre1[lane] + i] = (unsigned char)lane;
+    __syncwarp();
+    for (int zb = 0; zb < Z; zb += 32)
+    {
+        const int it = zb + lane;
+        int ny = 0, j = 0, z = 0, y0 = 0;
+        if (it < Z)
+        {
+            j = S.own1[it];
+            const int4 I0 = S.I0[j], I1 = S.I1[j];
+            z = I1.x + (it - S.pre1[j]);
+            // the y range of the tet's cross-section at z, from the edges that
+            // cross the plane, widened by a rounding margin (an extra row is only
+            // visited, a dropped row would lose points)
+            float a[4][3];
+            float4 P4[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+            {
+                P4[k] = S.P[k][j];
+                a[k][0] = P4[k].x; a[k][1] = P4[k].y; a[k][2] = P4[k].z;
+            }
+            const float lo1 = P4[2].w, hi1 = P4[3].w;
+            const float pz = z * g.step[2] + g.gmin[2];
+            float ylo = FLT_MAX, yhi = -FLT_MAX;
+#pragma unroll
+            for (int e = 0; e < 6; ++e)
+            {
+                const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
+                const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
+                const float za = a[u][2], zb2 = a[v][2];
+                if (pz < fminf(za, zb2) || pz > fmaxf(za, zb2))
+                    continue;
+                float y0f, y1f;
+                if (za == zb2)
+                {
+                    y0f = a[u][1];
+                    y1f = a[v][1];
+                }
+                else
+                {
+                    const float tt = fminf(fmaxf((pz - za) * S.IDZ[e][j], 0.0f), 1.0f);
+                    y0f = y1f = fmaf(tt, a[v][1] - a[u][1], a[u][1]);
+                }
+                ylo = fminf(ylo, fminf(y0f, y1f));
+                yhi = fmaxf(yhi, fmaxf(y0f, y1f));
+            }
+            if (ylo <= yhi)
+            {
+                const float ginv = g.inv_step[1], gmn = g.gmin[1];
+                const float my = 64.0f * EPS32 * (fmaxf(fabsf(ylo), fabsf(yhi)) + hi1 - lo1);
+                const float f0 = (ylo - my - gmn) * ginv;
+                const float f1 = (yhi + my - gmn) * ginv;
+                const float mm = 1e-3f + 8.0f * EPS32 *
+                    ((fabsf(gmn) + fmaxf(fabsf(ylo), fabsf(yhi))) * ginv + fmaxf(fabsf(f0), fabsf(f1)));
+                const int y0i = max(I0.z, (int)ceilf(fmaxf(f0 - mm, (float)(I0.z - 1))));
+                const int y1i = min(I0.w, (int)floorf(fminf(f1 + mm, (float)(I0.w + 1))));
+                if (y1i >= y0i)
+                {
+                    ny = y1i - y0i + 1;
+                    y0 = y0i;
+                }
+            }
+        }
+        // ---- level 2: the rows of these 32 slices, a lane per row
+        const int R = warp_prefix(ny, lane, S.pre2);
+        S.SL[lane] = make_int4(j, z, y0, 0);
+        __syncwarp();
+        for (int i = 0; i < ny; ++i)
+            S.own2[S.pre2[lane] + i] = (unsigned char)lane;
+        __syncwarp();
+        for (int rb = 0; rb < R; rb += 32)
+        {
+            const int r = rb + lane;
+            int n = 0;
+            if (r < R)
+            {
+                cn.rows++;
+                const int q = S.own2[r];
+                const int4 sl = S.SL[q];
+                const int jj = sl.x, zz = sl.y, yy = sl.z + (r - S.pre2[q]);
+                const int4 I0 = S.I0[jj], I1 = S.I1[jj];
+                const float4 A0 = S.P[0][jj], A1 = S.P[1][jj];
+                float xmin = A0.w, xmax = A1.w;
+                {
+                    const float4 XA = S.XA[jj], XB = S.XB[jj], XG = S.XG[jj];
+                    const float fdy = (float)(yy - I1.y), fdz = (float)(zz - I1.z);
+                    const int m = I1.w & 0xff;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                    {
+                        const float bnd = fmaf(comp4<float>(XG, k), fdz, fmaf(comp4<float>(XB, k), fdy, comp4<float>(XA, k)));
+                        if ((m >> (4 + k)) & 1) continue;
+                        if ((m >> k) & 1) xmin = fmaxf(xmin, bnd);
+                        else xmax = fminf(xmax, bnd);
+                    }
+                }
+                int i0 = 0, i1 = -1;
+                if (xmin <= xmax)
+                {
+                    // grid indices inside [xmin, xmax], widened by mg grid steps
+                    const float ginv0 = g.inv_step[0], gmn0 = g.gmin[0];
+                    const float f0 = (xmin - gmn0) * ginv0;
+                    const float f1 = (xmax - gmn0) * ginv0;
+                    const float mg = 1e-3f + 8.0f * EPS32 * ((fabsf(gmn0) + fmaxf(fabsf(xmin), fabsf(xmax))) * ginv0 +
+                                                             fmaxf(fabsf(f0), fabsf(f1)));
+                    i0 = max(I0.x, (int)ceilf(fmaxf(f0 - mg, (float)(I0.x - 1))));
+                    i1 = min(I0.y, (int)floorf(fminf(f1 + mg, (float)(I0.y + 1))));
+                }
+                if (i0 <= i1)
+                {
+                    n = i1 - i0 + 1;
+                    const float pyf = yy * g.step[1] + g.gmin[1];
+                    const float pzf = zz * g.step[2] + g.gmin[2];
+                    T RN[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                    {
+                        const T4 ck = S.C[k][jj];
+                        const float by = k == 0 ? A1.y : A0.y, bz = k == 0 ? A1.z : A0.z;
+                        const T qy = (T)pyf - (T)by, qz = (T)pzf - (T)bz;
+                        RN[k] = Real<T>::fma_(ck.y, qy, ck.z * qz);
+                    }
+                    T4 rn;
+                    rn.x = RN[0]; rn.y = RN[1]; rn.z = RN[2]; rn.w = RN[3];
+                    S.RN[lane] = rn;
+                    S.RW[lane] = make_int4(jj, yy, zz, i0);
+                }
+            }
+            // ---- level 3: the points of these 32 rows, a lane per point
+            const int P = warp_prefix(n, lane, S.pre3);
+            __syncwarp();
+            for (int i = 0; i < n; ++i)
+                S.own3[S.pre3[lane] + i] = (unsigned char)lane;
+            __syncwarp();
+            for (int pb = 0; pb < P; pb += 32)
+            {
+                const int pi = pb + lane;
+                if (pi >= P)
+                    continue;
+                cn.cand++;
+                const int u = S.own3[pi];
+                const int4 rw = S.RW[u];
+                const T4 rn = S.RN[u];
+                const int jj = rw.x, yy = rw.y, zz = rw.z, xx = rw.w + (pi - S.pre3[u]);
+                const float4 A0 = S.P[0][jj], A1 = S.P[1][jj];
+                const int flags = S.I1[jj].w;
+                const float pxf = xx * g.step[0] + g.gmin[0];
+                const T px = pxf;
+                const T4 c0 = S.C[0][jj], c1 = S.C[1][jj], c2 = S.C[2][jj], c3 = S.C[3][jj];
+                T N[4];
+                N[0] = Real<T>::fma_(c0.x, px - (T)A1.x, rn.x);
+                const T qx = px - (T)A0.x;
+                N[1] = Real<T>::fma_(c1.x, qx, rn.y);
+                N[2] = Real<T>::fma_(c2.x, qx, rn.z);
+                N[3] = Real<T>::fma_(c3.x, qx, rn.w);
+                const T Bk[4] = { c0.w, c1.w, c2.w, c3.w };
+                bool in = true, out = false;
+                unsigned open = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                {
+                    const bool ik = N[k] > Bk[k];
+                    in = in && ik;
+                    out = out || (N[k] < -Bk[k]);
+                    open |= (ik ? 0u : 1u) << k;
+                }
+                if (out)
+                    continue;
+                const float pyf = yy * g.step[1] + g.gmin[1];
+                const float pzf = zz * g.step[2] + g.gmin[2];
+                if (!in)
+                {
+                    cn.exact++;
+                    const float4 A2 = S.P[2][jj], A3 = S.P[3][jj];
+                    const int sgn = (flags >> 8) & 1 ? 1 : -1;
+                    if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf, pyf,
+                                      pzf, sgn, open))
+                        continue;
+                }
+                float f;
+                if (F32 && ((flags >> 9) & 1))
+                    f = (float)(S.F[0][jj] + ((double)pxf - (double)A0.x) * S.F[1][jj] +
+                                ((double)pyf - (double)A0.y) * S.F[2][jj] + ((double)pzf - (double)A0.z) * S.F[3][jj]);
+                else
+                {
+                    const T4 W4 = S.W[jj];
+                    f = (float)Real<T>::fma_(N[0], W4.x, Real<T>::fma_(N[1], W4.y, Real<T>::fma_(N[2], W4.z, N[3] * W4.w)));
+                }
+                tile[((zz - r0[2]) << (SX + SY)) + ((yy - r0[1]) << SX) + (xx - r0[0])] = f;
+                if (owner)
+                    owner[g.off + ((size_t)zz * g.n[1] + yy) * g.n[0] + xx] = S.TG[jj] - bd.t_off;
+                cn.assigned++;
+            }
+            __syncwarp();
+        }
+        __syncwarp();
+    }
+    __syncwarp();
+}
+
+template <typename T, int SX, int SY, int SZ, int NW>
+__global__ void __launch_bounds__(NW * 32, 2)
+k_raster_bricks(const BlockDesc* blocks, int nb, int seg, int bb0, int bb1, const int* cnt, const int* off,
+                const int* item_off, const int* seg_items, int* item_counter, const int* pairs, const float4* pos,
+                const int4* tv, const float* rho32, const double* rho64, GridDesc g, float* grid, int* owner,
+                int fixup, Status* st)
+{
+    constexpr int BX = 1 << SX, BY = 1 << SY, BZ = 1 << SZ, BP = BX * BY * BZ;
+    extern __shared__ __align__(32) unsigned char brick_smem[];
+    float* tile = (float*)brick_smem;
+    BrickWarp<T, SX, SY, SZ>* W = (BrickWarp<T, SX, SY, SZ>*)(brick_smem + BP * sizeof(float));
+    __shared__ int s_item;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    BrickCounts cn;
+    const int total = seg_items[seg];
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(item_counter, 1);
+        __syncthreads();
+        const int item = s_item;
+        if (item >= total)
+            break;
+        // the item's brick: the last b with item_off[b] <= item
+        int lo = bb0, hi = bb1 - 1;
+        while (lo < hi)
+        {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(&item_off[mid]) <= item) lo = mid; else hi = mid - 1;
+        }
+        const int b = lo;
+        const int ib = __ldg(&item_off[b]);
+        const int nitems = (b + 1 < bb1 ? __ldg(&item_off[b + 1]) : total) - ib;
+        const bool split = nitems > 1;
+        const int chunk = item - ib;
+        const int c0 = __ldg(&off[b]) + chunk * BRICK_CHUNK;
+        const int c1 = __ldg(&off[b]) + min(__ldg(&cnt[b]), (chunk + 1) * BRICK_CHUNK);
+        const BlockDesc& bd = blocks[brick_block(blocks, nb, b)];
+        int r0[3], r1[3];
+        brick_region(bd, b, SX, SY, SZ, r0, r1);
+        const float init = split ? __uint_as_float(BRICK_UNSET) : 0.0f;
+        for (int i = threadIdx.x; i < BP; i += NW * 32)
+            tile[i] = init;
+        __syncthreads();
+        for (int base = c0 + wid * 32; base < c1; base += NW * 32)
+            brick_batch<T, SX, SY, SZ>(W[wid], tile, r0, r1, base, min(base + 32, c1), pairs, bd, pos, tv, rho32,
+                                       rho64, g, owner, fixup, cn);
+        __syncthreads();
+        const int nx = r1[0] - r0[0] + 1, ny = r1[1] - r0[1] + 1, nz = r1[2] - r0[2] + 1;
+        for (int i = threadIdx.x; i < BP; i += NW * 32)
+        {
+            const int x = i & (BX - 1), y = (i >> SX) & (BY - 1), z = i >> (SX + SY);
+            if (x < nx && y < ny && z < nz)
+            {
+                const float v = tile[i];
+                if (!split || __float_as_uint(v) != BRICK_UNSET)
+                    grid[bd.grid.off + ((size_t)(r0[2] + z) * bd.grid.n[1] + (r0[1] + y)) * bd.grid.n[0] +
+                         (r0[0] + x)] = v;
+            }
+        }
+        (void)BZ;
+    }
+    unsigned long long v[5] = { cn.rows, cn.cand, cn.exact, cn.assigned, cn.fix };
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+        for (int o = 16; o > 0; o >>= 1)
+            v[k] += __shfl_xor_sync(FULL, v[k], o);
+    if (lane == 0)
+    {
+        if (v[0]) atomicAdd(&st->rows, v[0]);
+        if (v[1]) atomicAdd(&st->candidates, v[1]);
+        if (v[2]) atomicAdd(&st->exact_tests, v[2]);
+        if (v[3]) atomicAdd(&st->assigned, v[3]);
+        if (v[4]) atomicAdd(&st->fp64_tets, v[4]);
+    }
+}
+
+// brick shapes the autotuner tries: log2 of BX, BY, BZ, and warps per CTA
+struct BrickVariant { int sx, sy, sz, nw; };
+static const BrickVariant kBrickVariants[] = { { 5, 4, 4, 6 }, { 5, 3, 4, 4 }, { 5, 4, 3, 4 }, { 5, 3, 3, 4 } };
+constexpr int N_BRICK_VARIANTS = sizeof(kBrickVariants) / sizeof(kBrickVariants[0]);
+
+int brick_variants() { return N_BRICK_VARIANTS; }
+
+void brick_shape(int variant, int* sx, int* sy, int* sz)
+{
+    const BrickVariant& v = kBrickVariants[variant < 0 || variant >= N_BRICK_VARIANTS ? 0 : variant];
+    *sx = v.sx;
+    *sy = v.sy;
+    *sz = v.sz;
+}
+
+void launch_bin_reset(const BrickBins& bins, int seg, int bb0, int bb1, cudaStream_t s)
+{
+    if (bb1 > bb0)
+        cudaMemsetAsync(bins.cnt + bb0, 0, sizeof(int) * (size_t)(bb1 - bb0), s);
+    cudaMemsetAsync(bins.counters + seg, 0, sizeof(int), s);
+}
+
+void launch_bin_place(int variant, const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1, int t0, int nt,
+                      const float4* pos, const int4* tv, const GridDesc& g, const BrickBins& bins, float* grid,
+                      Status* st, cudaStream_t s)
+{
+    int sx, sy, sz;
+    brick_shape(variant, &sx, &sy, &sz);
+    k_bin_scan<<<1, 1024, 0, s>>>(bb0, bb1, seg, bins.cnt, bins.off, bins.cur, bins.item_off, bins.seg_items,
+                                  bins.pair_cursor, bins.pair_cap, st);
+    if (nt > 0 && bb1 > bb0)
+    {
+        k_bin_scatter<<<grid_for(nt, 256, 8), 256, 0, s>>>(d_blocks, nb, t0, nt, pos, tv, g, sx, sy, sz, bins.cur,
+                                                           bins.pairs, bins.pair_cap);
+        k_zero_split<<<grid_for((long long)(bb1 - bb0) * 256, 256, 4), 256, 0, s>>>(
+            d_blocks, nb, bb0, bb1, seg, bins.item_off, bins.seg_items, sx, sy, sz, g, grid);
+    }
+}
+
+void launch_bin_bricks(int variant, const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1, int t0, int nt,
+                       const float4* pos, const int4* tv, const GridDesc& g, const BrickBins& bins, float* grid,
+                       Status* st, cudaStream_t s)
+{
+    int sx, sy, sz;
+    brick_shape(variant, &sx, &sy, &sz);
+    launch_bin_reset(bins, seg, bb0, bb1, s);
+    if (nt > 0 && bb1 > bb0)
+        k_bin_count<<<grid_for(nt, 256, 8), 256, 0, s>>>(d_blocks, nb, t0, nt, pos, tv, g, sx, sy, sz, bins.cnt);
+    launch_bin_place(variant, d_blocks, nb, seg, bb0, bb1, t0, nt, pos, tv, g, bins, grid, st, s);
+}
+
+template <typename T, int SX, int SY, int SZ, int NW>
+static void raster_bricks_t(const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1, long long nbricks,
+                            const BrickBins& bins, const float4* pos, const int4* tv, const float* rho32,
+                            const double* rho64, const GridDesc& g, float* grid, int* owner, int fixup, Status* st,
+                            cudaStream_t s)
+{
+    constexpr int BP = 1 << (SX + SY + SZ);
+    const size_t smem = BP * sizeof(float) + NW * sizeof(BrickWarp<T, SX, SY, SZ>);
+    static bool attr = false;   // per process and instance; set before the first launch
+    if (!attr)
+    {
+        cudaFuncSetAttribute(k_raster_bricks<T, SX, SY, SZ, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr = true;
+    }
+    int dev = 0, sms = 152, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raster_bricks<T, SX, SY, SZ, NW>, NW * 32, smem);
+    long long nblk = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    // items >= bricks; more CTAs than items only exit
+    if (nblk > nbricks + 64) nblk = nbricks + 64;
+    if (nblk < 1) nblk = 1;
+    k_raster_bricks<T, SX, SY, SZ, NW><<<(int)nblk, NW * 32, smem, s>>>(
+        d_blocks, nb, seg, bb0, bb1, bins.cnt, bins.off, bins.item_off, bins.seg_items, bins.counters + seg,
+        bins.pairs, pos, tv, rho32, rho64, g, grid, owner, fixup, st);
+}
+
+void launch_raster_bricks(int mode, int variant, const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1,
+                          const BrickBins& bins, const float4* pos, const int4* tv, const float* rho32,
+                          const double* rho64, const GridDesc& g, float* grid, int* owner, Status* st,
+                          cudaStream_t s)
+{
+    if (bb1 <= bb0) return;
+    const long long nbr = bb1 - bb0;
+#define TG_BRICKS(SX, SY, SZ, NW)                                                                                   \
+    do {                                                                                                            \
+        if (mode == TESSGPU_MODE_FP64)                                                                              \
+            raster_bricks_t<double, SX, SY, SZ, NW>(d_blocks, nb, seg, bb0, bb1, nbr, bins, pos, tv, rho32, rho64, \
+                                                    g, grid, owner, 0, st, s);                                     \
+        else                                                                                                        \
+            raster_bricks_t<float, SX, SY, SZ, NW>(d_blocks, nb, seg, bb0, bb1, nbr, bins, pos, tv, rho32, rho64,  \
+                                                   g, grid, owner, 1, st, s);                                      \
+    } while (0)
+    switch (variant)
+    {
+    case 1: TG_BRICKS(5, 3, 4, 4); break;
+    case 2: TG_BRICKS(5, 4, 3, 4); break;
+    case 3: TG_BRICKS(5, 3, 3, 4); break;
+    default: TG_BRICKS(5, 4, 4, 6); break;
+    }
+#undef TG_BRICKS
+}
+
+void launch_star_volumes(int mode, int total, const float4* pos, const int4* tv, unsigned long long* W,
+                         double scale, float tau, Status* st, cudaStream_t s)
+{
+    (void)tau;   // DTFE_TAU
+    if (total <= 0) return;
+    GridDesc g0;
+    k_star_volumes<false><<<grid_for(total, 256, 8), 256, 0, s>>>(mode, 0, total, pos, tv, W, scale, st, nullptr, 0,
+                                                                    g0, 0, 0, 0, nullptr);
+}
+
+void launch_star_bin(int mode, int variant, const BlockDesc* d_blocks, int nb, int t0, int nt, const float4* pos,
+                     const int4* tv, unsigned long long* W, double scale, const GridDesc& g, int* cnt, Status* st,
+                     cudaStream_t s)
+{
+    if (nt <= 0) return;
+    int sx, sy, sz;
+    brick_shape(variant, &sx, &sy, &sz);
+    k_star_volumes<true><<<grid_for(nt, 256, 8), 256, 0, s>>>(mode, t0, nt, pos, tv, W, scale, st, d_blocks, nb, g,
+                                                               sx, sy, sz, cnt);
 }
 
 }  // namespace tg

@@ -45,6 +45,38 @@ int  raster_variants();
 void order_bricks(const GridDesc& g, int* nbx, int* nby, int* nbz);
 void launch_tet_order(const float4* pos, const int4* tv, int total, const GridDesc& g, int* key, int* hist,
                       int* order, cudaStream_t s);
+// brick rasteriser: bins of (tet, brick) pairs per segment of blocks, then
+// one CTA per brick (dtfe.cu)
+struct BrickBins
+{
+    int* cnt;                        // per brick: pairs
+    int* off;                        // per brick: first pair in the pair list
+    int* cur;                        // per brick: scatter cursor
+    int* item_off;                   // per brick: first item within its segment
+    int* seg_items;                  // per segment: items
+    int* counters;                   // per segment: items taken by the rasteriser's CTAs
+    int* pairs;                      // tet indices, brick by brick
+    long long pair_cap;
+    unsigned long long* pair_cursor; // pairs placed so far (all segments of a call)
+};
+int  brick_variants();
+void brick_shape(int variant, int* sx, int* sy, int* sz);
+void launch_bin_reset(const BrickBins& bins, int seg, int bb0, int bb1, cudaStream_t s);
+// star volumes of tets [t0, t0 + nt) fused with their pair counts
+void launch_star_bin(int mode, int variant, const BlockDesc* d_blocks, int nb, int t0, int nt, const float4* pos,
+                     const int4* tv, unsigned long long* W, double scale, const GridDesc& g, int* cnt, Status* st,
+                     cudaStream_t s);
+// scan (pair and item offsets), scatter, zeroing of split bricks' regions
+void launch_bin_place(int variant, const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1, int t0, int nt,
+                      const float4* pos, const int4* tv, const GridDesc& g, const BrickBins& bins, float* grid,
+                      Status* st, cudaStream_t s);
+void launch_bin_bricks(int variant, const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1, int t0, int nt,
+                       const float4* pos, const int4* tv, const GridDesc& g, const BrickBins& bins, float* grid,
+                       Status* st, cudaStream_t s);
+void launch_raster_bricks(int mode, int variant, const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1,
+                          const BrickBins& bins, const float4* pos, const int4* tv, const float* rho32,
+                          const double* rho64, const GridDesc& g, float* grid, int* owner, Status* st,
+                          cudaStream_t s);
 void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos, const int4* tv,
                        const float* rho32, const double* rho64, const GridDesc& g, float* grid, int* owner,
                        const int* fix_list, const int* fix_count, Status* st, cudaStream_t s);

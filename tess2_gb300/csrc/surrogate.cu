@@ -242,14 +242,24 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t parit
     return false;
 }
 
-// bounded wait that ignores the abort flag (draining copies before exit)
+// The waits for work already issued -- the last copy into each ring slot and
+// the commit of every MMA -- before the CTA frees its tensor memory and
+// exits.  A copy of a valid box always lands and an issued MMA always
+// completes, so these run long only when the kernel itself is slowed (an
+// instrumented profiler replay serialises and slows it by orders of
+// magnitude); giving up early there is the one way this kernel could free
+// tensor memory or exit with asynchronous work still writing to it, so they
+// allow 30 s, not the 2 s of the pipeline's waits.
+constexpr uint64_t TC_DRAIN_NS = 30000000000ull;
+
+// bounded wait that ignores the abort flag (draining copies and MMAs before exit)
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity)
 {
     const uint64_t t0 = global_ns();
-    for (int it = 0; it < (1 << 26); ++it)
+    for (int it = 0; it < (1 << 30); ++it)
     {
         if (mbar_try(mbar, parity)) return true;
-        if (global_ns() - t0 > TC_WAIT_NS) break;
+        if (global_ns() - t0 > TC_DRAIN_NS) break;
     }
     return false;
 }

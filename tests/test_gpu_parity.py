@@ -504,3 +504,150 @@ def test_offset_domain_gpu(gpu_ctx, oracle, given):
     o = oracle.dtfe(blocks, gni, given=g)
     assert np.array_equal(owner, o["owner"].ravel())
     assert rel_l2(d.cpu().numpy(), o["grid"].ravel()) < 1e-6
+
+
+# ---------------------------------------------------------------------------
+# the brick rasteriser (default) against the row kernel and the oracle
+# ---------------------------------------------------------------------------
+def _fresh_ctx(env):
+    """A context made with the given environment switches (the rasteriser
+    kind and launch variant are fixed when a context is made or first used)."""
+    import os
+    from tess2_gb300.api import Context
+    old = {k: os.environ.get(k) for k in env}
+    os.environ.update({k: v for k, v in env.items() if v is not None})
+    for k, v in env.items():
+        if v is None:
+            os.environ.pop(k, None)
+    try:
+        ctx = Context(0)
+        return ctx, old
+    except Exception:
+        _restore(old)
+        raise
+
+
+def _restore(old):
+    import os
+    for k, v in old.items():
+        if v is None:
+            os.environ.pop(k, None)
+        else:
+            os.environ[k] = v
+
+
+def _dtfe_batch(ctx, blocks, gni, mode, want_owner=True):
+    """DTFE of a device batch on a fresh context: the first call picks the
+    launch variant, the second is the one checked (grid preset to -7)."""
+    import torch
+    from tess2_gb300.api import DENSE_DTFE
+    b = ctx.upload(blocks)
+    b.keep_debug(want_owner)
+    grid = torch.full((gni[2], gni[1], gni[0]), -7.0, dtype=torch.float32, device="cuda")
+    b.dense(DENSE_DTFE, gni, grid.data_ptr(), mode=mode)
+    grid.fill_(-7.0)
+    info = b.dense(DENSE_DTFE, gni, grid.data_ptr(), mode=mode)
+    owner = None
+    if want_owner:
+        _, owner, _ = b.debug_outputs(grid_points=grid.numel())
+        owner = owner.reshape(grid.shape)
+    g = grid.cpu().numpy()
+    b.free()
+    return g, owner, info
+
+
+@pytest.mark.parametrize("variant", ["0", "1", "2", "3"])
+@pytest.mark.parametrize("mode,tol", [(0, 1e-6), (1, 1e-12)])
+def test_dtfe_brick_variants_vs_oracle(oracle, variant, mode, tol):
+    """Every brick shape the autotuner may pick: owners equal to the FP64
+    oracle's, values within the mode's bound, every grid point written (the
+    grid starts at -7 and the brick kernel writes zeros itself)."""
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    gni = [int(x) for x in d["glo_num_idx"]]
+    ref = oracle.dtfe(blocks, gni)
+    ctx, old = _fresh_ctx({"TESSGPU_RASTER": None, "TESSGPU_RASTER_VARIANT": variant})
+    try:
+        g, owner, info = _dtfe_batch(ctx, blocks, gni, mode)
+    finally:
+        _restore(old)
+    assert info["raster_variant"] == int(variant)
+    assert np.array_equal(owner, ref["owner"])
+    assert info["grid_pts_assigned"] == ref["assigned"]
+    assert rel_l2(g, ref["grid"]) < tol
+    assert np.all(g[ref["owner"] < 0] == 0)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_dtfe_bricks_match_row_kernel(mode):
+    """The brick kernel and the per-tet row kernel (TESSGPU_RASTER=rows): the
+    same owners and counts, and values within the mode's FP32 rounding of each
+    other (the row kernel evaluates each tet along its own row axis, so the
+    three-term dot products round in a different order)."""
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    gni = [61, 47, 55]
+    out = []
+    for env in ({"TESSGPU_RASTER": "rows", "TESSGPU_RASTER_VARIANT": None},
+                {"TESSGPU_RASTER": None, "TESSGPU_RASTER_VARIANT": None}):
+        ctx, old = _fresh_ctx(env)
+        try:
+            out.append(_dtfe_batch(ctx, blocks, gni, mode))
+        finally:
+            _restore(old)
+    (g0, o0, i0), (g1, o1, i1) = out
+    assert np.array_equal(o0, o1)
+    for k in ("grid_pts_assigned", "fp64_tets", "exact_tests"):
+        assert i0[k] == i1[k], k
+    assert rel_l2(g1, g0) < (1e-6 if mode == 0 else 1e-12)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_dtfe_lattice_ties_gpu(oracle, mode):
+    """Particles on a lattice whose points coincide with grid points, plus
+    jittered ones: every shared-face, edge and vertex tie occurs, and the GPU
+    must give each grid point the oracle's owner (the perturbation rule)."""
+    from tess2_gb300 import host
+    g1 = np.arange(5, dtype=np.float32) / 4
+    lat = np.stack(np.meshgrid(g1, g1, g1, indexing="ij"), -1).reshape(-1, 3)
+    jit = host.uniform_particles(40, 5) * np.float32(0.9) + np.float32(0.05)
+    for pts in (lat, np.concatenate([lat, jit])):
+        tets = host.delaunay_tets(pts)
+        blk = [dict(gid=0, particles=pts, tets=tets, vert_to_tet=host.vert_to_tet_host(len(pts), tets),
+                    num_orig=len(pts), bounds_min=np.zeros(3, np.float32), bounds_max=np.ones(3, np.float32),
+                    data_min=np.zeros(3, np.float32), data_max=np.ones(3, np.float32))]
+        gni = [17, 17, 17]   # step 1/16: the lattice is on grid points
+        ref = oracle.dtfe(blk, gni)
+        ctx, old = _fresh_ctx({"TESSGPU_RASTER": None, "TESSGPU_RASTER_VARIANT": "3"})
+        try:
+            g, owner, info = _dtfe_batch(ctx, blk, gni, mode)
+        finally:
+            _restore(old)
+        assert np.array_equal(owner, ref["owner"])
+        assert rel_l2(g, ref["grid"]) < (1e-6 if mode == 0 else 1e-12)
+        assert info["exact_tests"] > 0
+
+
+def test_dtfe_split_bricks_and_pair_retry(oracle):
+    """Two particles per grid point put tens of thousands of candidate tets
+    into each brick, so every brick's work is split into items of 2048 (the
+    regions zeroed first); a pair list sized far too small
+    (TESSGPU_PAIR_CAP) makes the call retry with the size it needed."""
+    from tess2_gb300 import host
+    pts = host.uniform_particles(30000, 9)
+    tets = host.delaunay_tets(pts)
+    blk = [dict(gid=0, particles=pts, tets=tets, vert_to_tet=host.vert_to_tet_host(len(pts), tets),
+                num_orig=len(pts), bounds_min=np.zeros(3, np.float32), bounds_max=np.ones(3, np.float32),
+                data_min=np.zeros(3, np.float32), data_max=np.ones(3, np.float32))]
+    gni = [24, 24, 24]
+    ref = oracle.dtfe(blk, gni)
+    for env in ({"TESSGPU_RASTER_VARIANT": "0", "TESSGPU_PAIR_CAP": None},
+                {"TESSGPU_RASTER_VARIANT": "0", "TESSGPU_PAIR_CAP": "1000"}):
+        ctx, old = _fresh_ctx(dict(env, TESSGPU_RASTER=None))
+        try:
+            g, owner, info = _dtfe_batch(ctx, blk, gni, 0)
+            # and once more through the host-buffer call on the same context
+            r = ctx.dense(2, blk, gni)
+        finally:
+            _restore(old)
+        assert np.array_equal(owner, ref["owner"])
+        assert rel_l2(g, ref["grid"]) < 1e-6
+        assert np.array_equal(r["grid"], g)

@@ -266,3 +266,22 @@ def test_offset_domain_matches_reference(oracle, given, alg):
     assert np.array_equal(bits(r["grid"]), bits(ref["grid"]))
     assert np.array_equal(r["grid_step"], ref["grid_step"]) and np.array_equal(r["grid_min"], ref["grid_min"])
     assert r["grid"].sum() > 0
+
+
+def test_sampled_parity_helpers_against_full_oracle(oracle):
+    """oracle/parity.py: the sampled DTFE (every 4th tet) agrees with the full
+    FP64 oracle's owners restricted to those tets, and the cell-list DENSE_TESS
+    gives the reference's golden per-cell counts."""
+    from conftest import load_blocks, load_single, single_block
+    from oracle import parity
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    gni = [int(x) for x in d["glo_num_idx"]]
+    full = oracle.dtfe(blocks, gni)
+    smp = parity.dtfe_oracle_sample(blocks, gni, 4, processes=1)
+    r = parity.dtfe_compare(full["grid"].ravel(), full["owner"].ravel(), smp, 4)
+    assert r["points"] > 0 and r["owners_equal"] and r["no_extra"] and r["rel_l2"] == 0.0
+    s = load_single("mix2048_seed7")
+    blk = single_block(s)
+    cells = parity.tess_cell_sample(blk, 500, seed=3)
+    cnt = parity.tess_counts_oracle(blk, [int(x) for x in s["glo_num_idx"]], cells, processes=1)
+    assert np.array_equal(cnt[0], s["tess_cell_counts"][cells[0]])
