@@ -328,7 +328,7 @@ tessgpu_status tessgpu_batch_debug_outputs(tessgpu_ctx* ctx, tessgpu_batch* batc
 /* ---- allocation-free entry point -------------------------------------- */
 
 /* Largest particle count tessgpu_dtfe_densities_noalloc accepts: its scratch
-   is a fixed 16 MiB array inside the library. */
+   is a fixed 32 MiB array inside the library (two 64-bit words per particle). */
 #define TESSGPU_NOALLOC_MAX_PARTICLES (1 << 21)
 
 /* DTFE vertex densities of one block (rho_v = 4 m / star volume, as the

@@ -53,6 +53,7 @@ struct tessgpu_ctx
     long long                last_grid_floats = 0;
     // the pipelined host-buffer DTFE call: copy streams and events
     cudaStream_t             h2d = nullptr, d2h = nullptr, cs2 = nullptr;
+    cudaStream_t             cap = nullptr;         // stream CUDA graphs are recorded on
     std::vector<cudaEvent_t> pipe_ev;
     cudaEvent_t              first_ev[5] = { nullptr, nullptr, nullptr, nullptr, nullptr };
     // brick rasteriser: pair-list size the last call needed (0: not known yet)
@@ -240,6 +241,7 @@ extern "C" void tessgpu_destroy(tessgpu_ctx* ctx)
     if (ctx->h2d) cudaStreamDestroy(ctx->h2d);
     if (ctx->d2h) cudaStreamDestroy(ctx->d2h);
     if (ctx->cs2) cudaStreamDestroy(ctx->cs2);
+    if (ctx->cap) cudaStreamDestroy(ctx->cap);
     delete ctx;
 }
 
@@ -427,7 +429,7 @@ struct tessgpu_batch
     double*                cc64 = nullptr;
     bool                   cc_ok = false, cc64_ok = false;
     // DTFE scratch
-    double*                W = nullptr;
+    StarSum*               W = nullptr;
     float*                 rho32 = nullptr;
     double*                rho64 = nullptr;
     int*                   fix_list = nullptr;
@@ -816,7 +818,7 @@ static void bricks_reset(tessgpu_ctx* ctx, const std::vector<BlockDesc>& hb, int
 }
 
 static void bricks_star(tessgpu_ctx* ctx, int mode, int variant, const BlockDesc* d_blocks, int nb, long long t0,
-                        long long nt, const float4* pos, const int4* tv, unsigned long long* W, double scale,
+                        long long nt, const float4* pos, const int4* tv, StarSum* W, double scale,
                         const GridDesc& g, const BrickBins& bins, cudaStream_t s)
 {
     if (nt <= 0) return;
@@ -997,7 +999,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             return dtfe_batch_bricks(ctx, bt, p, g, gmax, target, d_grid, d_zl, L, Gout, bvar, nbricks, info);
         if (!bt->W || bt->pooled)
         {
-            BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
+            BALLOC(SLOT_W, sizeof(StarSum) * (bt->N ? bt->N : 1), bt->W);
             BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
             BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
             BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
@@ -1012,7 +1014,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             bt->owner_n = G;
             owner = bt->d_owner;
         }
-        CK(cudaMemsetAsync(bt->W, 0, sizeof(unsigned long long) * bt->N, s));
+        CK(cudaMemsetAsync(bt->W, 0, sizeof(StarSum) * bt->N, s));
         CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int) * (nb + 1), s));
         // fixed-point scale of the star-volume sums: any star volume is below
         // the volume of the particles' bounding box; allow 8x the data box
@@ -1042,11 +1044,11 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
                     cudaStream_t sk = (k & 1) ? ctx->cs2 : s;
                     const int t0 = smark(ctx, sk);
                     if (d.nt)
-                        launch_star_volumes(p->mode, d.nt, bt->pos, bt->tv + d.t_off, (unsigned long long*)bt->W, scale,
+                        launch_star_volumes(p->mode, d.nt, bt->pos, bt->tv + d.t_off, (StarSum*)bt->W, scale,
                                             kTau, ctx->d_status, sk);
                     const int t1 = smark(ctx, sk);
                     if (d.np)
-                        launch_densities((const unsigned long long*)bt->W + d.p_off, d.np, p->mass, 1.0 / scale,
+                        launch_densities((const StarSum*)bt->W + d.p_off, d.np, p->mass, 1.0 / scale,
                                          bt->rho32 + d.p_off, bt->rho64 + d.p_off, ctx->d_status, sk);
                     const int t2 = smark(ctx, sk);
                     int t3 = -1, t4 = -1;
@@ -1080,10 +1082,10 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
                 goto dtfe_done;
             }
         }
-        launch_star_volumes(p->mode, (int)bt->T, bt->pos, bt->tv, (unsigned long long*)bt->W, scale, kTau,
+        launch_star_volumes(p->mode, (int)bt->T, bt->pos, bt->tv, (StarSum*)bt->W, scale, kTau,
                             ctx->d_status, s);
         mark(ctx, "star_volumes");
-        launch_densities((const unsigned long long*)bt->W, (int)bt->N, p->mass, 1.0 / scale, bt->rho32, bt->rho64,
+        launch_densities((const StarSum*)bt->W, (int)bt->N, p->mass, 1.0 / scale, bt->rho32, bt->rho64,
                          ctx->d_status, s);
         mark(ctx, "densities");
         // TESSGPU_RASTER_ORDER=1 rasterises the tets brick by brick (kept with a
@@ -1246,7 +1248,7 @@ static tessgpu_status dtfe_batch_bricks(tessgpu_ctx* ctx, tessgpu_batch* bt, con
     const long long G = (long long)p->glo_num_idx[0] * p->glo_num_idx[1] * p->glo_num_idx[2];
     if (!bt->W || bt->pooled)
     {
-        BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
+        BALLOC(SLOT_W, sizeof(StarSum) * (bt->N ? bt->N : 1), bt->W);
         BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
         BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
     }
@@ -1260,13 +1262,13 @@ static tessgpu_status dtfe_batch_bricks(tessgpu_ctx* ctx, tessgpu_batch* bt, con
         owner = bt->d_owner;
     }
     const double scale = star_sum_scale(g.dmin, g.dmax);
-    unsigned long long* W = (unsigned long long*)bt->W;
+    StarSum* W = (StarSum*)bt->W;
     BrickBins bins;
     tessgpu_status st;
     if ((st = brick_bins(ctx, nbricks, nb, bt->T, &bins)) != TESSGPU_OK)
         return st;
     CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(W, 0, sizeof(unsigned long long) * (bt->N ? bt->N : 1), s));
+    CK(cudaMemsetAsync(W, 0, sizeof(StarSum) * (bt->N ? bt->N : 1), s));
     const char* ov = getenv("TESSGPU_BATCH_OVERLAP");
     const bool overlap = var >= 0 && !(ov && *ov && atoi(ov) == 0) && !p->project && nb > 1;
     if (overlap)
@@ -1526,18 +1528,18 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
         var = ctx->raster_variant[mode] = std::min(std::max(atoi(env), 0), brick_variants() - 1);
     if (!bt->W || bt->pooled)
     {
-        BALLOC(SLOT_W, sizeof(double) * (bt->N ? bt->N : 1), bt->W);
+        BALLOC(SLOT_W, sizeof(StarSum) * (bt->N ? bt->N : 1), bt->W);
         BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
         BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
     }
-    unsigned long long* W = (unsigned long long*)bt->W;
+    StarSum* W = (StarSum*)bt->W;
     BrickBins bins;
     tessgpu_status st;
     if (var < 0)
     {
         // autotune the brick shape on these sets (bin + rasterise, twice each)
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
-        CK(cudaMemsetAsync(W, 0, sizeof(unsigned long long) * (bt->N ? bt->N : 1), s));
+        CK(cudaMemsetAsync(W, 0, sizeof(StarSum) * (bt->N ? bt->N : 1), s));
         launch_star_volumes(mode, (int)bt->T, bt->pos, bt->tv, W, scale, kTau, ctx->d_status, s);
         launch_densities(W, (int)bt->N, mass, 1.0 / scale, bt->rho32, bt->rho64, ctx->d_status, s);
         ctx->launches += 2;
@@ -1593,17 +1595,17 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
     key.push_back(ebits);
     // the descriptors go up before the step (a graph cannot hold a copy from pageable memory)
     CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
-    auto record = [&]() {
-        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
-        CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
-        CK(cudaMemsetAsync(W, 0, sizeof(unsigned long long) * (bt->N ? bt->N : 1), s));
-        bricks_reset(ctx, bt->hb, 0, nb, nbricks, bins, s);
-        bricks_star(ctx, mode, var, bt->d_blocks, nb, 0, bt->T, bt->pos, bt->tv, W, scale, g0, bins, s);
-        bricks_place(ctx, var, bt->d_blocks, bt->hb, 0, nb, nbricks, bins, bt->pos, bt->tv, g0, d_out, s);
-        launch_densities(W, (int)bt->N, mass, 1.0 / scale, bt->rho32, bt->rho64, ctx->d_status, s);
+    auto record = [&](cudaStream_t rs) {
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), rs));
+        CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), rs));
+        CK(cudaMemsetAsync(W, 0, sizeof(StarSum) * (bt->N ? bt->N : 1), rs));
+        bricks_reset(ctx, bt->hb, 0, nb, nbricks, bins, rs);
+        bricks_star(ctx, mode, var, bt->d_blocks, nb, 0, bt->T, bt->pos, bt->tv, W, scale, g0, bins, rs);
+        bricks_place(ctx, var, bt->d_blocks, bt->hb, 0, nb, nbricks, bins, bt->pos, bt->tv, g0, d_out, rs);
+        launch_densities(W, (int)bt->N, mass, 1.0 / scale, bt->rho32, bt->rho64, ctx->d_status, rs);
         ctx->launches += bt->N ? 1 : 0;
         bricks_raster(ctx, mode, var, bt->d_blocks, bt->hb, 0, nb, nbricks, bins, bt->pos, bt->tv, bt->rho32,
-                      bt->rho64, g0, d_out, nullptr, s);
+                      bt->rho64, g0, d_out, nullptr, rs);
         return TESSGPU_OK;
     };
     const long long launches0 = ctx->launches;
@@ -1613,10 +1615,14 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
         {
             if (bt->sets_exec) { cudaGraphExecDestroy(bt->sets_exec); bt->sets_exec = nullptr; }
             if (bt->sets_graph) { cudaGraphDestroy(bt->sets_graph); bt->sets_graph = nullptr; }
-            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            tessgpu_status rs = record();
+            // recorded on the context's own capture stream (the legacy default
+            // stream cannot be captured), launched on the context's stream
+            if (!ctx->cap) CK(cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking));
+            CK(cudaStreamSynchronize(s));
+            CK(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal));
+            tessgpu_status rs = record(ctx->cap);
             cudaGraph_t gr = nullptr;
-            const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+            const cudaError_t ce = cudaStreamEndCapture(ctx->cap, &gr);
             if (rs != TESSGPU_OK) { if (gr) cudaGraphDestroy(gr); return rs; }
             CK(ce);
             bt->sets_graph = gr;
@@ -1627,7 +1633,7 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
         CK(cudaGraphLaunch(bt->sets_exec, s));
         ctx->launches += bt->T ? 6 : 2;
     }
-    else if ((st = record()) != TESSGPU_OK)
+    else if ((st = record(s)) != TESSGPU_OK)
         return st;
     st = finish_status(ctx);
     if (st == TESSGPU_ERR_CAPACITY && !ctx->in_retry)
@@ -1938,7 +1944,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     float4* pos = (float4*)get(SLOT_POS, sizeof(float4) * std::max(N, 1LL));
     int4* tv = (int4*)get(SLOT_TV, sizeof(int4) * std::max(T, 1LL));
     char* stage = (char*)get(SLOT_STAGE, 32 * (size_t)T + 12 * (size_t)N + 16);
-    unsigned long long* W = (unsigned long long*)get(SLOT_W, sizeof(double) * std::max(N, 1LL));
+    StarSum* W = (StarSum*)get(SLOT_W, sizeof(StarSum) * std::max(N, 1LL));
     float* rho32 = (float*)get(SLOT_RHO32, sizeof(float) * std::max(N, 1LL));
     double* rho64 = (double*)get(SLOT_RHO64, sizeof(double) * std::max(N, 1LL));
     int* fix = bricks ? nullptr : (int*)get(SLOT_FIX, sizeof(int) * std::max(T, 1LL));
@@ -2051,7 +2057,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         if (d.np)
         {
             k_pack_block<<<grid_small(d.np), 256, 0, s>>>(stage_xyz + 3 * (size_t)d.p_off, d.np, pos + d.p_off);
-            CK(cudaMemsetAsync(W + d.p_off, 0, sizeof(unsigned long long) * d.np, s));
+            CK(cudaMemsetAsync(W + d.p_off, 0, sizeof(StarSum) * d.np, s));
             ctx->launches++;
         }
         if (bricks)

@@ -175,15 +175,15 @@ __device__ __noinline__ int numerator_sign_exact(const float a[4][3], int k, con
 // 2^62 (the host derives it from the data bounds).
 // rho_v = (D+1) m / W_v = 4 m / W_v, 0 for a vertex in no tet.  The sums
 // hold 6x the volumes (the determinants), so rho = 24 m / sum.
-__global__ void k_densities(const unsigned long long* W, int n, float mass, double inv_scale, float* rho32,
-                            double* rho64, Status* st)
+__global__ void k_densities(const StarSum* W, int n, float mass, double inv_scale, float* rho32, double* rho64,
+                            Status* st)
 {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
     {
-        const long long wi = (long long)W[v];
-        if (wi < 0)
+        const StarSum wv = W[v];
+        if (wv.hi >= (1ull << 62))
             fail(st, TESSGPU_ERR_UNSUPPORTED, v);   // star volume past the fixed-point range
-        const double w = (double)wi * inv_scale;
+        const double w = star_value(wv.hi, wv.lo, inv_scale);
         const double r = w > 0.0 ? 24.0 * (double)mass / w : 0.0;
         rho32[v] = (float)r;
         rho64[v] = r;
@@ -989,7 +989,7 @@ static int grid_for(long long n, int block, int per_sm)
     return (int)(need < cap ? need : cap);
 }
 
-void launch_densities(const unsigned long long* W, int n, float mass, double inv_scale, float* rho32, double* rho64,
+void launch_densities(const StarSum* W, int n, float mass, double inv_scale, float* rho32, double* rho64,
                       Status* st, cudaStream_t s)
 {
     if (n <= 0) return;
@@ -1256,27 +1256,34 @@ __device__ __forceinline__ bool tet_bricks(const BlockDesc& bd, const float4* po
     return true;
 }
 
-// q added to W[key] by the lanes that hold key: one atomic per distinct key
-// and warp (consecutive tets share vertices, so a warp's 32 tets touch about
-// 40 vertices, not 128).  The group's sum is exact (64-bit integers, summed
-// as three 21-bit pieces with the warp's integer reduction), so W is the same
-// as with one atomic per term.  Every lane of the warp calls this; inactive
-// lanes pass active = false.
-__device__ __forceinline__ void warp_add_u64(unsigned long long* W, int key, unsigned long long q, bool active)
+// the term (hi, lo) added to W[key] by the lanes that hold key: one pair of
+// atomics per distinct key and warp (consecutive tets share vertices, so a
+// warp's 32 tets touch about 40 vertices, not 128).  The group's sums are
+// exact: hi (< 2^61) and lo (<= 2^40) summed as 21-bit pieces with the warp's
+// integer reduction.  W ends up the same as with one atomic per term.  Every
+// lane of the warp calls this; inactive lanes pass active = false.
+__device__ __forceinline__ void warp_add_star(StarSum* W, int key, unsigned long long hi, unsigned long long lo,
+                                              bool active)
 {
     const int lane = threadIdx.x & 31;
     const unsigned grp = __match_any_sync(FULL, active ? key : -1 - lane);
-    const unsigned s0 = __reduce_add_sync(grp, (unsigned)(q & 0x1fffffull));
-    const unsigned s1 = __reduce_add_sync(grp, (unsigned)((q >> 21) & 0x1fffffull));
-    const unsigned s2 = __reduce_add_sync(grp, (unsigned)(q >> 42));
+    constexpr unsigned long long M21 = 0x1fffffull;
+    const unsigned h0 = __reduce_add_sync(grp, (unsigned)(hi & M21));
+    const unsigned h1 = __reduce_add_sync(grp, (unsigned)((hi >> 21) & M21));
+    const unsigned h2 = __reduce_add_sync(grp, (unsigned)(hi >> 42));
+    const unsigned l0 = __reduce_add_sync(grp, (unsigned)(lo & M21));
+    const unsigned l1 = __reduce_add_sync(grp, (unsigned)(lo >> 21));
     if (active && lane == __ffs(grp) - 1)
-        atomicAdd(&W[key], (unsigned long long)s0 + ((unsigned long long)s1 << 21) + ((unsigned long long)s2 << 42));
+    {
+        atomicAdd(&W[key].hi, (unsigned long long)h0 + ((unsigned long long)h1 << 21) + ((unsigned long long)h2 << 42));
+        atomicAdd(&W[key].lo, (unsigned long long)l0 + ((unsigned long long)l1 << 21));
+    }
 }
 
 // Star volumes of tets [t0, t0 + nt); with BIN, also the brick rasteriser's
 // pair counts of those tets (the same vertex loads serve both).
 template <bool BIN>
-__global__ void k_star_volumes(int mode, int t0, int nt, const float4* pos, const int4* tv, unsigned long long* W,
+__global__ void k_star_volumes(int mode, int t0, int nt, const float4* pos, const int4* tv, StarSum* W,
                                double scale, Status* st, const BlockDesc* blocks, int nb, GridDesc g, int sx, int sy,
                                int sz, int* cnt)
 {
@@ -1287,18 +1294,18 @@ __global__ void k_star_volumes(int mode, int t0, int nt, const float4* pos, cons
         const long long it = base + threadIdx.x;
         const bool active = it < nt;
         int4 vi = make_int4(0, 0, 0, 0);
-        unsigned long long q = 0;
+        unsigned long long qh = 0, ql = 0;
         if (active)
         {
             vi = __ldg(&tv[t0 + it]);
             const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
             const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a0, a1, a2, a3, &nfix);
-            q = (unsigned long long)__double2ll_rn(vol * scale);
+            star_term(vol, scale, qh, ql);
         }
-        warp_add_u64(W, vi.x, q, active);
-        warp_add_u64(W, vi.y, q, active);
-        warp_add_u64(W, vi.z, q, active);
-        warp_add_u64(W, vi.w, q, active);
+        warp_add_star(W, vi.x, qh, ql, active);
+        warp_add_star(W, vi.y, qh, ql, active);
+        warp_add_star(W, vi.z, qh, ql, active);
+        warp_add_star(W, vi.w, qh, ql, active);
         if (BIN)
         {
             int b0[3], b1[3], key = -1;
@@ -1413,7 +1420,17 @@ k_bin_scan(int bb0, int bb1, int seg, const int* cnt, int* off, int* cur, int* i
     }
     __syncthreads();
     if (!s_ok)
+    {
+        // the list is too small: no item runs (seg_items is 0), and every
+        // cursor points past the list so the scatter writes nothing
+        for (int i = lo; i < hi; ++i)
+        {
+            off[bb0 + i] = (int)min(pair_cap, (long long)INT_MAX);
+            cur[bb0 + i] = (int)min(pair_cap, (long long)INT_MAX);
+            item_off[bb0 + i] = 0;
+        }
         return;
+    }
     long long rc = s_base + pc[threadIdx.x] - sc, ri = pi[threadIdx.x] - si;
     for (int i = lo; i < hi; ++i)
     {
@@ -1455,7 +1472,7 @@ __global__ void k_bin_scatter(const BlockDesc* blocks, int nb, int t0, int nt, c
         if (key >= 0 && lane == leader)
             slot = atomicAdd(&cur[key], __popc(grp));
         slot = __shfl_sync(FULL, slot, leader) + __popc(grp & ((1u << lane) - 1u));
-        if (key >= 0 && slot < pair_cap)
+        if (key >= 0 && slot >= 0 && slot < pair_cap)
             pairs[slot] = t;
         if (any && !single)
             for (int z = b0[2]; z <= b1[2]; ++z)
@@ -1463,7 +1480,7 @@ __global__ void k_bin_scatter(const BlockDesc* blocks, int nb, int t0, int nt, c
                     for (int x = b0[0]; x <= b1[0]; ++x)
                     {
                         const int q = atomicAdd(&cur[bd->brick_base + (z * bd->brick_n[1] + y) * bd->brick_n[0] + x], 1);
-                        if (q < pair_cap)
+                        if (q >= 0 && q < pair_cap)
                             pairs[q] = t;
                     }
     }
@@ -2065,7 +2082,7 @@ void launch_raster_bricks(int mode, int variant, const BlockDesc* d_blocks, int 
 #undef TG_BRICKS
 }
 
-void launch_star_volumes(int mode, int total, const float4* pos, const int4* tv, unsigned long long* W,
+void launch_star_volumes(int mode, int total, const float4* pos, const int4* tv, StarSum* W,
                          double scale, float tau, Status* st, cudaStream_t s)
 {
     (void)tau;   // DTFE_TAU
@@ -2076,7 +2093,7 @@ void launch_star_volumes(int mode, int total, const float4* pos, const int4* tv,
 }
 
 void launch_star_bin(int mode, int variant, const BlockDesc* d_blocks, int nb, int t0, int nt, const float4* pos,
-                     const int4* tv, unsigned long long* W, double scale, const GridDesc& g, int* cnt, Status* st,
+                     const int4* tv, StarSum* W, double scale, const GridDesc& g, int* cnt, Status* st,
                      cudaStream_t s)
 {
     if (nt <= 0) return;

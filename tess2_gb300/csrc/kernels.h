@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "common.cuh"
+#include "dtfe_common.cuh"
 
 namespace tg {
 
@@ -33,9 +34,9 @@ void launch_project_layers(const float* grid, int nx, int ny, const int* zs, int
 void launch_sum_layers(const float* layers, int num_layers, long long area, float* out, cudaStream_t s);
 
 // dtfe.cu  (built with -fmad=false; FMAs only where written)
-void launch_star_volumes(int mode, int total_tets, const float4* pos, const int4* tv, unsigned long long* W,
+void launch_star_volumes(int mode, int total_tets, const float4* pos, const int4* tv, StarSum* W,
                          double scale, float tau, Status* st, cudaStream_t s);
-void launch_densities(const unsigned long long* W, int total_particles, float mass, double inv_scale, float* rho32,
+void launch_densities(const StarSum* W, int total_particles, float mass, double inv_scale, float* rho32,
                       double* rho64, Status* st, cudaStream_t s);
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
@@ -64,7 +65,7 @@ void brick_shape(int variant, int* sx, int* sy, int* sz);
 void launch_bin_reset(const BrickBins& bins, int seg, int bb0, int bb1, cudaStream_t s);
 // star volumes of tets [t0, t0 + nt) fused with their pair counts
 void launch_star_bin(int mode, int variant, const BlockDesc* d_blocks, int nb, int t0, int nt, const float4* pos,
-                     const int4* tv, unsigned long long* W, double scale, const GridDesc& g, int* cnt, Status* st,
+                     const int4* tv, StarSum* W, double scale, const GridDesc& g, int* cnt, Status* st,
                      cudaStream_t s);
 // scan (pair and item offsets), scatter, zeroing of split bricks' regions
 void launch_bin_place(int variant, const BlockDesc* d_blocks, int nb, int seg, int bb0, int bb1, int t0, int nt,

@@ -9,9 +9,9 @@
 // per-vertex star-volume sums) lives in a fixed array compiled into the
 // library.
 //
-// That array, noalloc_star_sums, holds TESSGPU_NOALLOC_MAX_PARTICLES 64-bit
-// sums (16 MiB); every GPU that loads the library keeps it until the process
-// exits.  All calls share it and it keeps the last call's contents, so each
+// That array, noalloc_star_sums, holds TESSGPU_NOALLOC_MAX_PARTICLES star
+// sums of two 64-bit words each (32 MiB); every GPU that loads the library
+// keeps it until the process exits.  All calls share it and it keeps the last call's contents, so each
 // call clears the part it uses first; two calls that overlap on the GPU (on
 // different streams or host threads) race on it and must be serialised by
 // the caller.
@@ -33,16 +33,17 @@
 #include "../../include/tess2_gb300.h"
 #include "dtfe_common.cuh"
 
-static __device__ __align__(256) unsigned long long noalloc_star_sums[TESSGPU_NOALLOC_MAX_PARTICLES];
+static __device__ __align__(256) tg::StarSum noalloc_star_sums[TESSGPU_NOALLOC_MAX_PARTICLES];
 static __device__ __align__(256) int noalloc_flags[8];
 
 namespace {
 
+using tg::StarSum;
 using tg::tet_abs_vol6;
 
 // one thread per tet, reading tess2's tet_t records and x,y,z particles directly
 __global__ void k_noalloc_star(const float* xyz, int np, const int* tets, int nt, int mode, double scale,
-                               unsigned long long* sums, int* flags)
+                               StarSum* sums, int* flags)
 {
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x)
     {
@@ -60,21 +61,24 @@ __global__ void k_noalloc_star(const float* xyz, int np, const int* tets, int nt
             a[k] = make_float3(q[0], q[1], q[2]);
         }
         const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a[0], a[1], a[2], a[3], nullptr);
-        const unsigned long long q = (unsigned long long)__double2ll_rn(vol * scale);
+        unsigned long long qh, ql;
+        tg::star_term(vol, scale, qh, ql);
         for (int k = 0; k < 4; ++k)
-            atomicAdd(&sums[v[k]], q);
+        {
+            atomicAdd(&sums[v[k]].hi, qh);
+            atomicAdd(&sums[v[k]].lo, ql);
+        }
     }
 }
 
-__global__ void k_noalloc_rho(const unsigned long long* sums, int np, float mass, double inv_scale, float* rho,
-                              int* flags)
+__global__ void k_noalloc_rho(const StarSum* sums, int np, float mass, double inv_scale, float* rho, int* flags)
 {
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x)
     {
-        const long long w = (long long)sums[v];
-        if (w < 0)
+        const StarSum w = sums[v];
+        if (w.hi >= (1ull << 62))
             atomicExch(&flags[1], 1);
-        const double s = (double)w * inv_scale;
+        const double s = tg::star_value(w.hi, w.lo, inv_scale);
         rho[v] = s > 0.0 ? (float)(24.0 * (double)mass / s) : 0.0f;
     }
 }
@@ -108,12 +112,12 @@ extern "C" tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particle
         cudaGetLastError();
         return TESSGPU_ERR_CUDA;
     }
-    unsigned long long* sums = (unsigned long long*)sums_addr;
+    StarSum* sums = (StarSum*)sums_addr;
     int* flags = (int*)flags_addr;
     const double scale = tg::star_sum_scale(bounds6, bounds6 + 3);
 
     cudaStream_t s = (cudaStream_t)stream;
-    if (cudaMemsetAsync(sums, 0, sizeof(unsigned long long) * (size_t)num_particles, s) != cudaSuccess ||
+    if (cudaMemsetAsync(sums, 0, sizeof(StarSum) * (size_t)num_particles, s) != cudaSuccess ||
         cudaMemsetAsync(flags, 0, sizeof(int) * 8, s) != cudaSuccess)
         return TESSGPU_ERR_CUDA;
     if (num_tets)
