@@ -686,7 +686,7 @@ def run_gpu(args):
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "dtfe_raster_traffic.json")))
         if prof.get("grid") == args.grid and prof.get("particles") == args.particles and \
-                prof.get("brick") == bool(pairs):
+                bool(prof.get("brick", False)) == bool(pairs):
             traffic = prof.get("dram_bytes_per_launch")
     except Exception:
         pass

@@ -59,7 +59,8 @@ struct tessgpu_ctx
     // brick rasteriser: pair-list size the last call needed (0: not known yet)
     long long                pair_cap_hint = 0;
     bool                     in_retry = false;
-    bool                     rows = false;          // TESSGPU_RASTER=rows when the context was made
+    bool                     rows = true;           // the row kernel for dense() (raster_rows() when made)
+    int                      sets_variant[2] = { -1, -1 };   // brick shape of tessgpu_batch_dense_sets, per mode
 };
 
 // an event on stream s for a span (timing on), its index; -1 otherwise
@@ -161,12 +162,16 @@ static tessgpu_status cuda_check(tessgpu_ctx* c, cudaError_t e, const char* what
         if (_s != TESSGPU_OK) return _s;                                \
     } while (0)
 
-// TESSGPU_RASTER=rows selects the per-tet row kernel (k_raster) with its
-// separate FP64 fix-up pass; the default is the brick kernel.
+// The DTFE rasteriser of dense() calls: the per-tet row kernel (k_raster, with
+// its separate FP64 fix-up pass) unless TESSGPU_RASTER=bricks selects the
+// brick kernel (k_raster_bricks).  The row kernel is the faster one on this
+// GPU (its per-tet set-up runs once per tet; the brick kernel repeats it for
+// every brick a tet overlaps and bins the tets first).  Independent sets
+// (tessgpu_batch_dense_sets) always use the brick kernel.
 static bool raster_rows()
 {
     const char* e = getenv("TESSGPU_RASTER");
-    return e && std::strcmp(e, "rows") == 0;
+    return !(e && std::strcmp(e, "bricks") == 0);
 }
 
 static void* pool_get(tessgpu_ctx* c, int slot, size_t bytes, cudaError_t* e)
@@ -1474,8 +1479,6 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
 {
     if (!ctx || !bt || !glo_num_idx || !d_out || (mode != TESSGPU_MODE_MIXED && mode != TESSGPU_MODE_FP64))
         return set_err(ctx, TESSGPU_ERR_INVALID, "bad dense_sets arguments");
-    if (ctx->rows)
-        return set_err(ctx, TESSGPU_ERR_UNSUPPORTED, "independent sets need the brick rasteriser");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     const int nb = bt->nb;
@@ -1522,10 +1525,10 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
         g0.dmin[k] = umin[k];
         g0.dmax[k] = umax[k];
     }
-    int var = bt->raster_variant[mode] >= 0 ? bt->raster_variant[mode] : ctx->raster_variant[mode];
+    int var = ctx->sets_variant[mode];
     const char* env = getenv("TESSGPU_RASTER_VARIANT");
     if (var < 0 && env && *env)
-        var = ctx->raster_variant[mode] = std::min(std::max(atoi(env), 0), brick_variants() - 1);
+        var = ctx->sets_variant[mode] = std::min(std::max(atoi(env), 0), brick_variants() - 1);
     if (!bt->W || bt->pooled)
     {
         BALLOC(SLOT_W, sizeof(StarSum) * (bt->N ? bt->N : 1), bt->W);
@@ -1577,9 +1580,8 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
             grow_pairs(ctx);
         else if (ctx->h_status->code)
             return finish_status(ctx);
-        ctx->raster_variant[mode] = var;
+        ctx->sets_variant[mode] = var;
     }
-    bt->raster_variant[mode] = var;
     const long long nbricks = assign_bricks(bt->hb, var);
     if ((st = brick_bins(ctx, nbricks, nb, bt->T, &bins)) != TESSGPU_OK)
         return st;

@@ -1197,7 +1197,6 @@ struct __align__(32) BrickWarp
     typedef typename Vec4<T>::type T4;
     T4     C[4][32];                // s c_k (x, y, z) and B_k
     T4     W[32];                   // s rho_k / 6V
-    T4     RN[32];                  // level 3: the row's R_k (the y and z part of s N_k)
     double F[4][32];                // FP64 fix-up tets: rho_0 and the field's gradient
     float4 P[4][32];                // vertices; w: lo x, hi x, lo y, hi y of the tet's box
     float4 XA[32], XB[32], XG[32];  // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
@@ -1205,10 +1204,8 @@ struct __align__(32) BrickWarp
     int4   I0[32];                  // box clipped to the brick: x0, x1, y0, y1
     int4   I1[32];                  // z0 (clipped), box's first y and z, flags
     int    TG[32];                  // tet index
-    int4   SL[32];                  // level 2: the slice's (slot, z, first y)
-    int4   RW[32];                  // level 3: the row's (slot, y, z, first x)
-    int    pre1[33], pre2[33], pre3[33];
-    unsigned char own1[32 << SZ], own2[32 << SY], own3[32 << SX];
+    int    pre1[33];                // exclusive prefix of the tets' slice counts
+    unsigned char own1[32 << SZ];   // the tet slot of every slice
 };
 
 // brick b's block (blocks' bricks are numbered in block order)
@@ -1256,28 +1253,13 @@ __device__ __forceinline__ bool tet_bricks(const BlockDesc& bd, const float4* po
     return true;
 }
 
-// the term (hi, lo) added to W[key] by the lanes that hold key: one pair of
-// atomics per distinct key and warp (consecutive tets share vertices, so a
-// warp's 32 tets touch about 40 vertices, not 128).  The group's sums are
-// exact: hi (< 2^61) and lo (<= 2^40) summed as 21-bit pieces with the warp's
-// integer reduction.  W ends up the same as with one atomic per term.  Every
-// lane of the warp calls this; inactive lanes pass active = false.
-__device__ __forceinline__ void warp_add_star(StarSum* W, int key, unsigned long long hi, unsigned long long lo,
-                                              bool active)
+// the term (hi, lo) added to W[key]: two 64-bit integer atomics.  (Merging
+// the terms of the warp's lanes that share a vertex first, with match and
+// reduce instructions, made the kernel five times slower on this GPU.)
+__device__ __forceinline__ void add_star(StarSum* W, int key, unsigned long long hi, unsigned long long lo)
 {
-    const int lane = threadIdx.x & 31;
-    const unsigned grp = __match_any_sync(FULL, active ? key : -1 - lane);
-    constexpr unsigned long long M21 = 0x1fffffull;
-    const unsigned h0 = __reduce_add_sync(grp, (unsigned)(hi & M21));
-    const unsigned h1 = __reduce_add_sync(grp, (unsigned)((hi >> 21) & M21));
-    const unsigned h2 = __reduce_add_sync(grp, (unsigned)(hi >> 42));
-    const unsigned l0 = __reduce_add_sync(grp, (unsigned)(lo & M21));
-    const unsigned l1 = __reduce_add_sync(grp, (unsigned)(lo >> 21));
-    if (active && lane == __ffs(grp) - 1)
-    {
-        atomicAdd(&W[key].hi, (unsigned long long)h0 + ((unsigned long long)h1 << 21) + ((unsigned long long)h2 << 42));
-        atomicAdd(&W[key].lo, (unsigned long long)l0 + ((unsigned long long)l1 << 21));
-    }
+    atomicAdd(&W[key].hi, hi);
+    atomicAdd(&W[key].lo, lo);
 }
 
 // Star volumes of tets [t0, t0 + nt); with BIN, also the brick rasteriser's
@@ -1289,48 +1271,28 @@ __global__ void k_star_volumes(int mode, int t0, int nt, const float4* pos, cons
 {
     const int lane = threadIdx.x & 31;
     unsigned long long nfix = 0;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < nt; base += (long long)gridDim.x * blockDim.x)
+    for (long long it = (long long)blockIdx.x * blockDim.x + threadIdx.x; it < nt;
+         it += (long long)gridDim.x * blockDim.x)
     {
-        const long long it = base + threadIdx.x;
-        const bool active = it < nt;
-        int4 vi = make_int4(0, 0, 0, 0);
-        unsigned long long qh = 0, ql = 0;
-        if (active)
-        {
-            vi = __ldg(&tv[t0 + it]);
-            const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
-            const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a0, a1, a2, a3, &nfix);
-            star_term(vol, scale, qh, ql);
-        }
-        warp_add_star(W, vi.x, qh, ql, active);
-        warp_add_star(W, vi.y, qh, ql, active);
-        warp_add_star(W, vi.z, qh, ql, active);
-        warp_add_star(W, vi.w, qh, ql, active);
+        const int4 vi = __ldg(&tv[t0 + it]);
+        const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
+        const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a0, a1, a2, a3, &nfix);
+        unsigned long long qh, ql;
+        star_term(vol, scale, qh, ql);
+        add_star(W, vi.x, qh, ql);
+        add_star(W, vi.y, qh, ql);
+        add_star(W, vi.z, qh, ql);
+        add_star(W, vi.w, qh, ql);
         if (BIN)
         {
-            int b0[3], b1[3], key = -1;
-            bool any = false, single = false;
-            const BlockDesc* bd = nullptr;
-            if (active)
-            {
-                const int t = t0 + (int)it;
-                bd = &blocks[find_blk(blocks, nb, t)];
-                any = tet_bricks(*bd, pos, tv, g, t, sx, sy, sz, b0, b1);
-                if (any)
-                {
-                    single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
-                    if (single)
-                        key = bd->brick_base + (b0[2] * bd->brick_n[1] + b0[1]) * bd->brick_n[0] + b0[0];
-                }
-            }
-            const unsigned grp = __match_any_sync(FULL, key);
-            if (key >= 0 && lane == __ffs(grp) - 1)
-                atomicAdd(&cnt[key], __popc(grp));
-            if (any && !single)
+            const int t = t0 + (int)it;
+            const BlockDesc& bd = blocks[find_blk(blocks, nb, t)];
+            int b0[3], b1[3];
+            if (tet_bricks(bd, pos, tv, g, t, sx, sy, sz, b0, b1))
                 for (int z = b0[2]; z <= b1[2]; ++z)
                     for (int y = b0[1]; y <= b1[1]; ++y)
                         for (int x = b0[0]; x <= b1[0]; ++x)
-                            atomicAdd(&cnt[bd->brick_base + (z * bd->brick_n[1] + y) * bd->brick_n[0] + x], 1);
+                            atomicAdd(&cnt[bd.brick_base + (z * bd.brick_n[1] + y) * bd.brick_n[0] + x], 1);
         }
     }
     for (int o = 16; o > 0; o >>= 1)
@@ -1339,38 +1301,20 @@ __global__ void k_star_volumes(int mode, int t0, int nt, const float4* pos, cons
         atomicAdd(&st->fp64_tets, nfix);
 }
 
-// (tet, brick) pairs per brick.  Tets that fall in one brick (most) are
-// counted with one atomic per brick and warp.
+// (tet, brick) pairs per brick
 __global__ void k_bin_count(const BlockDesc* blocks, int nb, int t0, int nt, const float4* pos, const int4* tv,
                             GridDesc g, int sx, int sy, int sz, int* cnt)
 {
-    const int lane = threadIdx.x & 31;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < nt; base += (long long)gridDim.x * blockDim.x)
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nt; it += gridDim.x * blockDim.x)
     {
-        const long long it = base + threadIdx.x;
-        int b0[3], b1[3], key = -1;
-        bool any = false, single = false;
-        const BlockDesc* bd = nullptr;
-        if (it < nt)
-        {
-            const int t = t0 + (int)it;
-            bd = &blocks[find_blk(blocks, nb, t)];
-            any = tet_bricks(*bd, pos, tv, g, t, sx, sy, sz, b0, b1);
-            if (any)
-            {
-                single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
-                if (single)
-                    key = bd->brick_base + (b0[2] * bd->brick_n[1] + b0[1]) * bd->brick_n[0] + b0[0];
-            }
-        }
-        const unsigned grp = __match_any_sync(FULL, key);
-        if (key >= 0 && lane == __ffs(grp) - 1)
-            atomicAdd(&cnt[key], __popc(grp));
-        if (any && !single)
+        const int t = t0 + it;
+        const BlockDesc& bd = blocks[find_blk(blocks, nb, t)];
+        int b0[3], b1[3];
+        if (tet_bricks(bd, pos, tv, g, t, sx, sy, sz, b0, b1))
             for (int z = b0[2]; z <= b1[2]; ++z)
                 for (int y = b0[1]; y <= b1[1]; ++y)
                     for (int x = b0[0]; x <= b1[0]; ++x)
-                        atomicAdd(&cnt[bd->brick_base + (z * bd->brick_n[1] + y) * bd->brick_n[0] + x], 1);
+                        atomicAdd(&cnt[bd.brick_base + (z * bd.brick_n[1] + y) * bd.brick_n[0] + x], 1);
     }
 }
 
@@ -1447,39 +1391,17 @@ k_bin_scan(int bb0, int bb1, int seg, const int* cnt, int* off, int* cur, int* i
 __global__ void k_bin_scatter(const BlockDesc* blocks, int nb, int t0, int nt, const float4* pos, const int4* tv,
                               GridDesc g, int sx, int sy, int sz, int* cur, int* pairs, long long pair_cap)
 {
-    const int lane = threadIdx.x & 31;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < nt; base += (long long)gridDim.x * blockDim.x)
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nt; it += gridDim.x * blockDim.x)
     {
-        const long long it = base + threadIdx.x;
-        int b0[3], b1[3], key = -1, t = -1;
-        bool any = false, single = false;
-        const BlockDesc* bd = nullptr;
-        if (it < nt)
-        {
-            t = t0 + (int)it;
-            bd = &blocks[find_blk(blocks, nb, t)];
-            any = tet_bricks(*bd, pos, tv, g, t, sx, sy, sz, b0, b1);
-            if (any)
-            {
-                single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
-                if (single)
-                    key = bd->brick_base + (b0[2] * bd->brick_n[1] + b0[1]) * bd->brick_n[0] + b0[0];
-            }
-        }
-        const unsigned grp = __match_any_sync(FULL, key);
-        const int leader = __ffs(grp) - 1;
-        int slot = 0;
-        if (key >= 0 && lane == leader)
-            slot = atomicAdd(&cur[key], __popc(grp));
-        slot = __shfl_sync(FULL, slot, leader) + __popc(grp & ((1u << lane) - 1u));
-        if (key >= 0 && slot >= 0 && slot < pair_cap)
-            pairs[slot] = t;
-        if (any && !single)
+        const int t = t0 + it;
+        const BlockDesc& bd = blocks[find_blk(blocks, nb, t)];
+        int b0[3], b1[3];
+        if (tet_bricks(bd, pos, tv, g, t, sx, sy, sz, b0, b1))
             for (int z = b0[2]; z <= b1[2]; ++z)
                 for (int y = b0[1]; y <= b1[1]; ++y)
                     for (int x = b0[0]; x <= b1[0]; ++x)
                     {
-                        const int q = atomicAdd(&cur[bd->brick_base + (z * bd->brick_n[1] + y) * bd->brick_n[0] + x], 1);
+                        const int q = atomicAdd(&cur[bd.brick_base + (z * bd.brick_n[1] + y) * bd.brick_n[0] + x], 1);
                         if (q >= 0 && q < pair_cap)
                             pairs[q] = t;
                     }
@@ -1695,7 +1617,8 @@ __device__ __forceinline__ void brick_batch(BrickWarp<T, SX, SY, SZ>& S, float* 
             }
         }
     }
-    // ---- level 1: the z slices of the 32 tets, a lane per slice
+    // ---- the z slices of the 32 tets, a lane per slice; the lane walks the
+    // slice's rows and their points itself, with the tet's tables in registers
     const int Z = warp_prefix(ns, lane, S.pre1);
     __syncwarp();
     for (int i = 0; i < ns; ++i)
@@ -1704,25 +1627,20 @@ __device__ __forceinline__ void brick_batch(BrickWarp<T, SX, SY, SZ>& S, float* 
     for (int zb = 0; zb < Z; zb += 32)
     {
         const int it = zb + lane;
-        int ny = 0, j = 0, z = 0, y0 = 0;
-        if (it < Z)
+        if (it >= Z)
+            continue;
+        const int j = S.own1[it];
+        const int4 I0 = S.I0[j], I1 = S.I1[j];
+        const int zz = I1.x + (it - S.pre1[j]);
+        const float4 A0 = S.P[0][j], A1 = S.P[1][j], A2 = S.P[2][j], A3 = S.P[3][j];
+        const float pzf = zz * g.step[2] + g.gmin[2];
+        // the y range of the tet's cross-section at z, from the edges that cross
+        // the plane, widened by a rounding margin (an extra row is only visited,
+        // a dropped row would lose points)
+        int y0 = 0, y1 = -1;
         {
-            j = S.own1[it];
-            const int4 I0 = S.I0[j], I1 = S.I1[j];
-            z = I1.x + (it - S.pre1[j]);
-            // the y range of the tet's cross-section at z, from the edges that
-            // cross the plane, widened by a rounding margin (an extra row is only
-            // visited, a dropped row would lose points)
-            float a[4][3];
-            float4 P4[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-            {
-                P4[k] = S.P[k][j];
-                a[k][0] = P4[k].x; a[k][1] = P4[k].y; a[k][2] = P4[k].z;
-            }
-            const float lo1 = P4[2].w, hi1 = P4[3].w;
-            const float pz = z * g.step[2] + g.gmin[2];
+            const float a[4][3] = { { A0.x, A0.y, A0.z }, { A1.x, A1.y, A1.z }, { A2.x, A2.y, A2.z },
+                                    { A3.x, A3.y, A3.z } };
             float ylo = FLT_MAX, yhi = -FLT_MAX;
 #pragma unroll
             for (int e = 0; e < 6; ++e)
@@ -1730,7 +1648,7 @@ __device__ __forceinline__ void brick_batch(BrickWarp<T, SX, SY, SZ>& S, float* 
                 const int u = e < 3 ? 0 : (e < 5 ? 1 : 2);
                 const int v = e < 3 ? e + 1 : (e < 5 ? e - 1 : 3);
                 const float za = a[u][2], zb2 = a[v][2];
-                if (pz < fminf(za, zb2) || pz > fmaxf(za, zb2))
+                if (pzf < fminf(za, zb2) || pzf > fmaxf(za, zb2))
                     continue;
                 float y0f, y1f;
                 if (za == zb2)
@@ -1740,7 +1658,7 @@ __device__ __forceinline__ void brick_batch(BrickWarp<T, SX, SY, SZ>& S, float* 
                 }
                 else
                 {
-                    const float tt = fminf(fmaxf((pz - za) * S.IDZ[e][j], 0.0f), 1.0f);
+                    const float tt = fminf(fmaxf((pzf - za) * S.IDZ[e][j], 0.0f), 1.0f);
                     y0f = y1f = fmaf(tt, a[v][1] - a[u][1], a[u][1]);
                 }
                 ylo = fminf(ylo, fminf(y0f, y1f));
@@ -1749,112 +1667,70 @@ __device__ __forceinline__ void brick_batch(BrickWarp<T, SX, SY, SZ>& S, float* 
             if (ylo <= yhi)
             {
                 const float ginv = g.inv_step[1], gmn = g.gmin[1];
-                const float my = 64.0f * EPS32 * (fmaxf(fabsf(ylo), fabsf(yhi)) + hi1 - lo1);
+                const float my = 64.0f * EPS32 * (fmaxf(fabsf(ylo), fabsf(yhi)) + A3.w - A2.w);
                 const float f0 = (ylo - my - gmn) * ginv;
                 const float f1 = (yhi + my - gmn) * ginv;
                 const float mm = 1e-3f + 8.0f * EPS32 *
                     ((fabsf(gmn) + fmaxf(fabsf(ylo), fabsf(yhi))) * ginv + fmaxf(fabsf(f0), fabsf(f1)));
-                const int y0i = max(I0.z, (int)ceilf(fmaxf(f0 - mm, (float)(I0.z - 1))));
-                const int y1i = min(I0.w, (int)floorf(fminf(f1 + mm, (float)(I0.w + 1))));
-                if (y1i >= y0i)
-                {
-                    ny = y1i - y0i + 1;
-                    y0 = y0i;
-                }
+                y0 = max(I0.z, (int)ceilf(fmaxf(f0 - mm, (float)(I0.z - 1))));
+                y1 = min(I0.w, (int)floorf(fminf(f1 + mm, (float)(I0.w + 1))));
             }
         }
-        // ---- level 2: the rows of these 32 slices, a lane per row
-        const int R = warp_prefix(ny, lane, S.pre2);
-        S.SL[lane] = make_int4(j, z, y0, 0);
-        __syncwarp();
-        for (int i = 0; i < ny; ++i)
-            S.own2[S.pre2[lane] + i] = (unsigned char)lane;
-        __syncwarp();
-        for (int rb = 0; rb < R; rb += 32)
+        if (y0 > y1)
+            continue;
+        const float4 XA = S.XA[j], XB = S.XB[j], XG = S.XG[j];
+        const T4 c0 = S.C[0][j], c1 = S.C[1][j], c2 = S.C[2][j], c3 = S.C[3][j];
+        const int m = I1.w & 0xff;
+        const bool fix = F32 && ((I1.w >> 9) & 1);
+        const float fdz = (float)(zz - I1.z);
+        const float ginv0 = g.inv_step[0], gmn0 = g.gmin[0];
+        for (int yy = y0; yy <= y1; ++yy)
         {
-            const int r = rb + lane;
-            int n = 0;
-            if (r < R)
+            cn.rows++;
+            // the row's x range from the four faces' bounds, then the grid
+            // indices inside it widened by mg grid steps (see k_raster)
+            float xmin = A0.w, xmax = A1.w;
+            const float fdy = (float)(yy - I1.y);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
             {
-                cn.rows++;
-                const int q = S.own2[r];
-                const int4 sl = S.SL[q];
-                const int jj = sl.x, zz = sl.y, yy = sl.z + (r - S.pre2[q]);
-                const int4 I0 = S.I0[jj], I1 = S.I1[jj];
-                const float4 A0 = S.P[0][jj], A1 = S.P[1][jj];
-                float xmin = A0.w, xmax = A1.w;
-                {
-                    const float4 XA = S.XA[jj], XB = S.XB[jj], XG = S.XG[jj];
-                    const float fdy = (float)(yy - I1.y), fdz = (float)(zz - I1.z);
-                    const int m = I1.w & 0xff;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                    {
-                        const float bnd = fmaf(comp4<float>(XG, k), fdz, fmaf(comp4<float>(XB, k), fdy, comp4<float>(XA, k)));
-                        if ((m >> (4 + k)) & 1) continue;
-                        if ((m >> k) & 1) xmin = fmaxf(xmin, bnd);
-                        else xmax = fminf(xmax, bnd);
-                    }
-                }
-                int i0 = 0, i1 = -1;
-                if (xmin <= xmax)
-                {
-                    // grid indices inside [xmin, xmax], widened by mg grid steps
-                    const float ginv0 = g.inv_step[0], gmn0 = g.gmin[0];
-                    const float f0 = (xmin - gmn0) * ginv0;
-                    const float f1 = (xmax - gmn0) * ginv0;
-                    const float mg = 1e-3f + 8.0f * EPS32 * ((fabsf(gmn0) + fmaxf(fabsf(xmin), fabsf(xmax))) * ginv0 +
-                                                             fmaxf(fabsf(f0), fabsf(f1)));
-                    i0 = max(I0.x, (int)ceilf(fmaxf(f0 - mg, (float)(I0.x - 1))));
-                    i1 = min(I0.y, (int)floorf(fminf(f1 + mg, (float)(I0.y + 1))));
-                }
-                if (i0 <= i1)
-                {
-                    n = i1 - i0 + 1;
-                    const float pyf = yy * g.step[1] + g.gmin[1];
-                    const float pzf = zz * g.step[2] + g.gmin[2];
-                    T RN[4];
-#pragma unroll
-                    for (int k = 0; k < 4; ++k)
-                    {
-                        const T4 ck = S.C[k][jj];
-                        const float by = k == 0 ? A1.y : A0.y, bz = k == 0 ? A1.z : A0.z;
-                        const T qy = (T)pyf - (T)by, qz = (T)pzf - (T)bz;
-                        RN[k] = Real<T>::fma_(ck.y, qy, ck.z * qz);
-                    }
-                    T4 rn;
-                    rn.x = RN[0]; rn.y = RN[1]; rn.z = RN[2]; rn.w = RN[3];
-                    S.RN[lane] = rn;
-                    S.RW[lane] = make_int4(jj, yy, zz, i0);
-                }
+                const float bnd = fmaf(comp4<float>(XG, k), fdz, fmaf(comp4<float>(XB, k), fdy, comp4<float>(XA, k)));
+                if ((m >> (4 + k)) & 1) continue;
+                if ((m >> k) & 1) xmin = fmaxf(xmin, bnd);
+                else xmax = fminf(xmax, bnd);
             }
-            // ---- level 3: the points of these 32 rows, a lane per point
-            const int P = warp_prefix(n, lane, S.pre3);
-            __syncwarp();
-            for (int i = 0; i < n; ++i)
-                S.own3[S.pre3[lane] + i] = (unsigned char)lane;
-            __syncwarp();
-            for (int pb = 0; pb < P; pb += 32)
+            if (xmin > xmax)
+                continue;
+            const float f0 = (xmin - gmn0) * ginv0;
+            const float f1 = (xmax - gmn0) * ginv0;
+            const float mg = 1e-3f + 8.0f * EPS32 * ((fabsf(gmn0) + fmaxf(fabsf(xmin), fabsf(xmax))) * ginv0 +
+                                                     fmaxf(fabsf(f0), fabsf(f1)));
+            const int i0 = max(I0.x, (int)ceilf(fmaxf(f0 - mg, (float)(I0.x - 1))));
+            const int i1 = min(I0.y, (int)floorf(fminf(f1 + mg, (float)(I0.y + 1))));
+            if (i0 > i1)
+                continue;
+            const float pyf = yy * g.step[1] + g.gmin[1];
+            T RN[4];
             {
-                const int pi = pb + lane;
-                if (pi >= P)
-                    continue;
+                const T q1y = (T)pyf - (T)A1.y, q1z = (T)pzf - (T)A1.z;
+                const T q0y = (T)pyf - (T)A0.y, q0z = (T)pzf - (T)A0.z;
+                RN[0] = Real<T>::fma_(c0.y, q1y, c0.z * q1z);
+                RN[1] = Real<T>::fma_(c1.y, q0y, c1.z * q0z);
+                RN[2] = Real<T>::fma_(c2.y, q0y, c2.z * q0z);
+                RN[3] = Real<T>::fma_(c3.y, q0y, c3.z * q0z);
+            }
+            float* trow = tile + ((zz - r0[2]) << (SX + SY)) + ((yy - r0[1]) << SX) - r0[0];
+            for (int xx = i0; xx <= i1; ++xx)
+            {
                 cn.cand++;
-                const int u = S.own3[pi];
-                const int4 rw = S.RW[u];
-                const T4 rn = S.RN[u];
-                const int jj = rw.x, yy = rw.y, zz = rw.z, xx = rw.w + (pi - S.pre3[u]);
-                const float4 A0 = S.P[0][jj], A1 = S.P[1][jj];
-                const int flags = S.I1[jj].w;
-                const float pxf = xx * g.step[0] + g.gmin[0];
+                const float pxf = xx * g.step[0] + gmn0;
                 const T px = pxf;
-                const T4 c0 = S.C[0][jj], c1 = S.C[1][jj], c2 = S.C[2][jj], c3 = S.C[3][jj];
                 T N[4];
-                N[0] = Real<T>::fma_(c0.x, px - (T)A1.x, rn.x);
+                N[0] = Real<T>::fma_(c0.x, px - (T)A1.x, RN[0]);
                 const T qx = px - (T)A0.x;
-                N[1] = Real<T>::fma_(c1.x, qx, rn.y);
-                N[2] = Real<T>::fma_(c2.x, qx, rn.z);
-                N[3] = Real<T>::fma_(c3.x, qx, rn.w);
+                N[1] = Real<T>::fma_(c1.x, qx, RN[1]);
+                N[2] = Real<T>::fma_(c2.x, qx, RN[2]);
+                N[3] = Real<T>::fma_(c3.x, qx, RN[3]);
                 const T Bk[4] = { c0.w, c1.w, c2.w, c3.w };
                 bool in = true, out = false;
                 unsigned open = 0;
@@ -1868,34 +1744,29 @@ __device__ __forceinline__ void brick_batch(BrickWarp<T, SX, SY, SZ>& S, float* 
                 }
                 if (out)
                     continue;
-                const float pyf = yy * g.step[1] + g.gmin[1];
-                const float pzf = zz * g.step[2] + g.gmin[2];
                 if (!in)
                 {
                     cn.exact++;
-                    const float4 A2 = S.P[2][jj], A3 = S.P[3][jj];
-                    const int sgn = (flags >> 8) & 1 ? 1 : -1;
-                    if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf, pyf,
-                                      pzf, sgn, open))
+                    const int sgn = (I1.w >> 8) & 1 ? 1 : -1;
+                    if (!inside_exact(A0.x, A0.y, A0.z, A1.x, A1.y, A1.z, A2.x, A2.y, A2.z, A3.x, A3.y, A3.z, pxf,
+                                      pyf, pzf, sgn, open))
                         continue;
                 }
                 float f;
-                if (F32 && ((flags >> 9) & 1))
-                    f = (float)(S.F[0][jj] + ((double)pxf - (double)A0.x) * S.F[1][jj] +
-                                ((double)pyf - (double)A0.y) * S.F[2][jj] + ((double)pzf - (double)A0.z) * S.F[3][jj]);
+                if (fix)
+                    f = (float)(S.F[0][j] + ((double)pxf - (double)A0.x) * S.F[1][j] +
+                                ((double)pyf - (double)A0.y) * S.F[2][j] + ((double)pzf - (double)A0.z) * S.F[3][j]);
                 else
                 {
-                    const T4 W4 = S.W[jj];
+                    const T4 W4 = S.W[j];
                     f = (float)Real<T>::fma_(N[0], W4.x, Real<T>::fma_(N[1], W4.y, Real<T>::fma_(N[2], W4.z, N[3] * W4.w)));
                 }
-                tile[((zz - r0[2]) << (SX + SY)) + ((yy - r0[1]) << SX) + (xx - r0[0])] = f;
+                trow[xx] = f;
                 if (owner)
-                    owner[g.off + ((size_t)zz * g.n[1] + yy) * g.n[0] + xx] = S.TG[jj] - bd.t_off;
+                    owner[g.off + ((size_t)zz * g.n[1] + yy) * g.n[0] + xx] = S.TG[j] - bd.t_off;
                 cn.assigned++;
             }
-            __syncwarp();
         }
-        __syncwarp();
     }
     __syncwarp();
 }
@@ -1979,7 +1850,7 @@ k_raster_bricks(const BlockDesc* blocks, int nb, int seg, int bb0, int bb1, cons
 
 // brick shapes the autotuner tries: log2 of BX, BY, BZ, and warps per CTA
 struct BrickVariant { int sx, sy, sz, nw; };
-static const BrickVariant kBrickVariants[] = { { 5, 4, 4, 6 }, { 5, 3, 4, 4 }, { 5, 4, 3, 4 }, { 5, 3, 3, 4 } };
+static const BrickVariant kBrickVariants[] = { { 5, 4, 4, 8 }, { 5, 3, 4, 8 }, { 5, 4, 3, 8 }, { 5, 3, 3, 8 } };
 constexpr int N_BRICK_VARIANTS = sizeof(kBrickVariants) / sizeof(kBrickVariants[0]);
 
 int brick_variants() { return N_BRICK_VARIANTS; }
@@ -2074,10 +1945,10 @@ void launch_raster_bricks(int mode, int variant, const BlockDesc* d_blocks, int 
     } while (0)
     switch (variant)
     {
-    case 1: TG_BRICKS(5, 3, 4, 4); break;
-    case 2: TG_BRICKS(5, 4, 3, 4); break;
-    case 3: TG_BRICKS(5, 3, 3, 4); break;
-    default: TG_BRICKS(5, 4, 4, 6); break;
+    case 1: TG_BRICKS(5, 3, 4, 8); break;
+    case 2: TG_BRICKS(5, 4, 3, 8); break;
+    case 3: TG_BRICKS(5, 3, 3, 8); break;
+    default: TG_BRICKS(5, 4, 4, 8); break;
     }
 #undef TG_BRICKS
 }

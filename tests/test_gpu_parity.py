@@ -559,13 +559,13 @@ def _dtfe_batch(ctx, blocks, gni, mode, want_owner=True):
 @pytest.mark.parametrize("variant", ["0", "1", "2", "3"])
 @pytest.mark.parametrize("mode,tol", [(0, 1e-6), (1, 1e-12)])
 def test_dtfe_brick_variants_vs_oracle(oracle, variant, mode, tol):
-    """Every brick shape the autotuner may pick: owners equal to the FP64
+    """Every brick shape the autotuner may pick (TESSGPU_RASTER=bricks): owners equal to the FP64
     oracle's, values within the mode's bound, every grid point written (the
     grid starts at -7 and the brick kernel writes zeros itself)."""
     d, blocks = load_blocks("blocks8_mix8192_seed3")
     gni = [int(x) for x in d["glo_num_idx"]]
     ref = oracle.dtfe(blocks, gni)
-    ctx, old = _fresh_ctx({"TESSGPU_RASTER": None, "TESSGPU_RASTER_VARIANT": variant})
+    ctx, old = _fresh_ctx({"TESSGPU_RASTER": "bricks", "TESSGPU_RASTER_VARIANT": variant})
     try:
         g, owner, info = _dtfe_batch(ctx, blocks, gni, mode)
     finally:
@@ -587,7 +587,7 @@ def test_dtfe_bricks_match_row_kernel(mode):
     gni = [61, 47, 55]
     out = []
     for env in ({"TESSGPU_RASTER": "rows", "TESSGPU_RASTER_VARIANT": None},
-                {"TESSGPU_RASTER": None, "TESSGPU_RASTER_VARIANT": None}):
+                {"TESSGPU_RASTER": "bricks", "TESSGPU_RASTER_VARIANT": None}):
         ctx, old = _fresh_ctx(env)
         try:
             out.append(_dtfe_batch(ctx, blocks, gni, mode))
@@ -616,7 +616,7 @@ def test_dtfe_lattice_ties_gpu(oracle, mode):
                     data_min=np.zeros(3, np.float32), data_max=np.ones(3, np.float32))]
         gni = [17, 17, 17]   # step 1/16: the lattice is on grid points
         ref = oracle.dtfe(blk, gni)
-        ctx, old = _fresh_ctx({"TESSGPU_RASTER": None, "TESSGPU_RASTER_VARIANT": "3"})
+        ctx, old = _fresh_ctx({"TESSGPU_RASTER": "bricks", "TESSGPU_RASTER_VARIANT": "3"})
         try:
             g, owner, info = _dtfe_batch(ctx, blk, gni, mode)
         finally:
@@ -641,7 +641,7 @@ def test_dtfe_split_bricks_and_pair_retry(oracle):
     ref = oracle.dtfe(blk, gni)
     for env in ({"TESSGPU_RASTER_VARIANT": "0", "TESSGPU_PAIR_CAP": None},
                 {"TESSGPU_RASTER_VARIANT": "0", "TESSGPU_PAIR_CAP": "1000"}):
-        ctx, old = _fresh_ctx(dict(env, TESSGPU_RASTER=None))
+        ctx, old = _fresh_ctx(dict(env, TESSGPU_RASTER="bricks"))
         try:
             g, owner, info = _dtfe_batch(ctx, blk, gni, 0)
             # and once more through the host-buffer call on the same context
