@@ -1023,7 +1023,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int) * (nb + 1), s));
         // fixed-point scale of the star-volume sums: any star volume is below
         // the volume of the particles' bounding box; allow 8x the data box
-        const double scale = star_sum_scale(dmin, dmax);   // 6V sums of up to 8x the data box
+        const double scale = star_sum_scale(dmin, dmax, p->mode == TESSGPU_MODE_FP64);
         // once the launch variant is known, blocks run their stages on two
         // streams in turn (as the host pipeline does), so one block's star
         // volumes overlap another's rasteriser
@@ -1266,7 +1266,7 @@ static tessgpu_status dtfe_batch_bricks(tessgpu_ctx* ctx, tessgpu_batch* bt, con
         bt->owner_n = G;
         owner = bt->d_owner;
     }
-    const double scale = star_sum_scale(g.dmin, g.dmax);
+    const double scale = star_sum_scale(g.dmin, g.dmax, p->mode == TESSGPU_MODE_FP64);
     StarSum* W = (StarSum*)bt->W;
     BrickBins bins;
     tessgpu_status st;
@@ -1465,6 +1465,139 @@ extern "C" long long tessgpu_sets_grid_floats(int nsets, const int* glo_num_idx,
     return tot;
 }
 
+// The independent sets on the row rasteriser: star volumes, densities, grid
+// zeroing, one rasteriser launch over every set's tets and its FP64 fix-up
+// pass (the block descriptors carry each set's grid); recorded into a CUDA
+// graph when asked, as the brick path is.
+static tessgpu_status dense_sets_rows(tessgpu_ctx* ctx, tessgpu_batch* bt, const int* glo_num_idx, float mass,
+                                      float eps, int mode, float* d_out, int graph, tessgpu_dense_info* info,
+                                      double scale, const GridDesc& g0, long long Gtot)
+{
+    cudaStream_t s = ctx->stream;
+    const int nb = bt->nb;
+    if (!bt->W || bt->pooled)
+    {
+        BALLOC(SLOT_W, sizeof(StarSum) * (bt->N ? bt->N : 1), bt->W);
+        BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
+        BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
+    }
+    if (!bt->fix_list || bt->pooled)
+    {
+        BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
+        BALLOC(SLOT_FIXN, sizeof(int) * (nb + 1), bt->fix_count);
+    }
+    StarSum* W = bt->W;
+    CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
+    int var = ctx->raster_variant[mode];
+    const char* env = getenv("TESSGPU_RASTER_VARIANT");
+    if (var < 0 && env && *env)
+        var = ctx->raster_variant[mode] = std::min(std::max(atoi(env), 0), raster_variants() - 1);
+    auto densities = [&](cudaStream_t rs) {
+        CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), rs));
+        CK(cudaMemsetAsync(W, 0, sizeof(StarSum) * (bt->N ? bt->N : 1), rs));
+        launch_star_volumes(mode, (int)bt->T, bt->pos, bt->tv, W, scale, kTau, ctx->d_status, rs);
+        launch_densities(W, (int)bt->N, mass, 1.0 / scale, bt->rho32, bt->rho64, ctx->d_status, rs);
+        ctx->launches += (bt->T ? 1 : 0) + (bt->N ? 1 : 0);
+        return TESSGPU_OK;
+    };
+    auto raster = [&](cudaStream_t rs, int v) {
+        CK(cudaMemsetAsync(d_out, 0, sizeof(float) * Gtot, rs));
+        CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), rs));
+        launch_raster(mode, v, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g0, kTau,
+                      d_out, nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs);
+        ctx->launches += bt->T ? 1 : 0;
+        if (mode != TESSGPU_MODE_FP64)
+        {
+            launch_raster_fix(bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g0, d_out,
+                              nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs);
+            ctx->launches += bt->T ? 1 : 0;
+        }
+        return TESSGPU_OK;
+    };
+    tessgpu_status st;
+    if (var < 0)
+    {
+        // autotune the launch variant on these sets (twice each: the first
+        // launch of a kernel also pays its module load)
+        if ((st = densities(s)) != TESSGPU_OK) return st;
+        float best = 1e30f;
+        cudaEvent_t e0, e1;
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        for (int v = 0; v < raster_variants(); ++v)
+        {
+            float vbest = 1e30f;
+            for (int rep = 0; rep < 2; ++rep)
+            {
+                CK(cudaEventRecord(e0, s));
+                if ((st = raster(s, v)) != TESSGPU_OK) return st;
+                CK(cudaEventRecord(e1, s));
+                CK(cudaEventSynchronize(e1));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                vbest = std::min(vbest, ms);
+            }
+            if (v < 8) ctx->tune_ms[mode][v] = vbest;
+            if (vbest < best) { best = vbest; var = v; }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if ((st = finish_status(ctx)) != TESSGPU_OK) return st;
+        ctx->raster_variant[mode] = var;
+    }
+    std::vector<long long> key = { 1000 + (long long)mode, (long long)var, (long long)(size_t)d_out,
+                                   (long long)(size_t)bt->W, (long long)(size_t)bt->fix_list };
+    for (int i = 0; i < 3 * nb; ++i) key.push_back(glo_num_idx[i]);
+    long long mbits = 0, ebits = 0;
+    std::memcpy(&mbits, &mass, sizeof(float));
+    std::memcpy(&ebits, &eps, sizeof(float));
+    key.push_back(mbits);
+    key.push_back(ebits);
+    auto record = [&](cudaStream_t rs) {
+        tessgpu_status r = densities(rs);
+        return r != TESSGPU_OK ? r : raster(rs, var);
+    };
+    const long long launches0 = ctx->launches;
+    if (graph)
+    {
+        if (!bt->sets_exec || bt->sets_key != key)
+        {
+            if (bt->sets_exec) { cudaGraphExecDestroy(bt->sets_exec); bt->sets_exec = nullptr; }
+            if (bt->sets_graph) { cudaGraphDestroy(bt->sets_graph); bt->sets_graph = nullptr; }
+            if (!ctx->cap) CK(cudaStreamCreateWithFlags(&ctx->cap, cudaStreamNonBlocking));
+            CK(cudaStreamSynchronize(s));
+            CK(cudaStreamBeginCapture(ctx->cap, cudaStreamCaptureModeThreadLocal));
+            tessgpu_status rs = record(ctx->cap);
+            cudaGraph_t gr = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(ctx->cap, &gr);
+            if (rs != TESSGPU_OK) { if (gr) cudaGraphDestroy(gr); return rs; }
+            CK(ce);
+            bt->sets_graph = gr;
+            CK(cudaGraphInstantiate(&bt->sets_exec, gr, 0));
+            bt->sets_key = key;
+        }
+        ctx->launches = launches0;
+        CK(cudaGraphLaunch(bt->sets_exec, s));
+        ctx->launches += bt->T ? (mode == TESSGPU_MODE_FP64 ? 3 : 4) : 1;
+    }
+    else if ((st = record(s)) != TESSGPU_OK)
+        return st;
+    if ((st = finish_status(ctx)) != TESSGPU_OK || !info)
+        return st;
+    std::memset(info, 0, sizeof(*info));
+    const Status& hs = *ctx->h_status;
+    info->grid_pts_assigned = (long long)hs.assigned;
+    info->fp64_tets = (long long)hs.fp64_tets;
+    info->exact_tests = (long long)hs.exact_tests;
+    info->rows_visited = (long long)hs.rows;
+    info->points_tested = (long long)hs.candidates;
+    info->raster_variant = var;
+    for (int v = 0; v < 8; ++v)
+        info->raster_variant_ms[v] = ctx->tune_ms[mode][v];
+    info->grid_floats = Gtot;
+    return TESSGPU_OK;
+}
+
 // DTFE of every block of the batch as an independent set: block b is
 // dense() over that one block onto its own glo_num_idx[3b..3b+2] grid, at
 // d_out + offset b (tessgpu_sets_grid_floats).  Stages over all sets at once:
@@ -1517,7 +1650,7 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
         d.grid.off = off[b];
     }
     // one fixed-point scale for every set (the largest box): sums stay exact
-    const double scale = star_sum_scale(umin, umax);
+    const double scale = star_sum_scale(umin, umax, mode == TESSGPU_MODE_FP64);
     GridDesc g0;
     std::memset(&g0, 0, sizeof(g0));
     for (int k = 0; k < 3; ++k)
@@ -1525,6 +1658,8 @@ extern "C" tessgpu_status tessgpu_batch_dense_sets(tessgpu_ctx* ctx, tessgpu_bat
         g0.dmin[k] = umin[k];
         g0.dmax[k] = umax[k];
     }
+    if (ctx->rows)
+        return dense_sets_rows(ctx, bt, glo_num_idx, mass, eps, mode, d_out, graph, info, scale, g0, Gtot);
     int var = ctx->sets_variant[mode];
     const char* env = getenv("TESSGPU_RASTER_VARIANT");
     if (var < 0 && env && *env)
@@ -1984,7 +2119,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     // goes down as soon as its block is done, so only the last box trails
     const bool tiles = boxes_tile(hb, p->glo_num_idx);
 
-    const double scale = star_sum_scale(dmin, dmax);
+    const double scale = star_sum_scale(dmin, dmax, p->mode == TESSGPU_MODE_FP64);
 
     ctx->nmarks = 0;
     ctx->nsev = 0;

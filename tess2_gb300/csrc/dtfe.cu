@@ -181,7 +181,7 @@ __global__ void k_densities(const StarSum* W, int n, float mass, double inv_scal
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
     {
         const StarSum wv = W[v];
-        if (wv.hi >= (1ull << 62))
+        if (star_overflow(wv.hi, wv.lo))
             fail(st, TESSGPU_ERR_UNSUPPORTED, v);   // star volume past the fixed-point range
         const double w = star_value(wv.hi, wv.lo, inv_scale);
         const double r = w > 0.0 ? 24.0 * (double)mass / w : 0.0;
@@ -318,6 +318,7 @@ struct __align__(32) RasterSmem
     // per tet of the current batch (lane = tet slot)
     float4 A0[32], A1[32];                   // vertices 0, 1 (row-axis order); .w = bbox lo, hi along the row axis
     int    TG[32];                           // global tet index (the exact path reloads vertices 2, 3)
+    int    BK[32];                           // the tet's block (its grid)
     T4     C[4][32];                         // c_k.x, c_k.y, c_k.z, B_k
     T4     W[32];                            // rho_k / 6V
     float4 XA[32], XB[32], XG[32];           // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
@@ -409,7 +410,7 @@ template <typename T, bool VAL64, typename SM>
 __device__ __forceinline__ void raster_point(const SM& S, int j, int xi, int yi, int zi, float pyf,
                                              float pzf, const float4& A0, const float4& A1, const int4& I1,
                                              const T* cx, const T* RN, const T* Bk, float hx, float gx, int ra,
-                                             const GridDesc& g, const int4* tv, const float4* pos, float* grid,
+                                             const BlockGrid& g, const int4* tv, const float4* pos, float* grid,
                                              int* owner, unsigned long long& nexact, unsigned long long& nassigned)
 {
     typedef typename Vec4<T>::type T4;
@@ -474,7 +475,7 @@ __device__ __forceinline__ void raster_point(const SM& S, int j, int xi, int yi,
     }
     int gx_, gy_, gz_;
     unperm3(ra, xi, yi, zi, gx_, gy_, gz_);
-    const size_t gi = ((size_t)gz_ * g.n[1] + gy_) * g.n[0] + gx_;
+    const size_t gi = g.off + ((size_t)gz_ * g.n[1] + gy_) * g.n[0] + gx_;
     grid[gi] = f;
     if (owner)
         owner[gi] = I1.z;
@@ -651,9 +652,11 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         perm3(ra, ilo[0], ilo[1], ilo[2], ilo[0], ilo[1], ilo[2]);
                         perm3(ra, ihi[0], ihi[1], ihi[2], ihi[0], ihi[1], ihi[2]);
                         float gst[3], gmn[3], ginv[3];
-                        perm3(ra, g.step[0], g.step[1], g.step[2], gst[0], gst[1], gst[2]);
-                        perm3(ra, g.gmin[0], g.gmin[1], g.gmin[2], gmn[0], gmn[1], gmn[2]);
-                        perm3(ra, g.inv_step[0], g.inv_step[1], g.inv_step[2], ginv[0], ginv[1], ginv[2]);
+                        const BlockGrid& gb = blocks[b].grid;
+                        S.BK[lane] = b;
+                        perm3(ra, gb.step[0], gb.step[1], gb.step[2], gst[0], gst[1], gst[2]);
+                        perm3(ra, gb.gmin[0], gb.gmin[1], gb.gmin[2], gmn[0], gmn[1], gmn[2]);
+                        perm3(ra, gb.inv_step[0], gb.inv_step[1], gb.inv_step[2], ginv[0], ginv[1], ginv[2]);
                         S.A0[lane] = make_float4(a[0][0], a[0][1], a[0][2], lo[0]);
                         S.A1[lane] = make_float4(a[1][0], a[1][1], a[1][2], hi[0]);
 #pragma unroll
@@ -853,10 +856,11 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                     {
                         // the tet's axes: row axis ra, then y, z (see perm3)
                         const int ra = (I1.w >> 9) & 3;
+                        const BlockGrid& gb = blocks[S.BK[j]].grid;
                         float gst[3], gmn[3], ginv0;
-                        perm3(ra, g.step[0], g.step[1], g.step[2], gst[0], gst[1], gst[2]);
-                        perm3(ra, g.gmin[0], g.gmin[1], g.gmin[2], gmn[0], gmn[1], gmn[2]);
-                        ginv0 = ra == 0 ? g.inv_step[0] : (ra == 1 ? g.inv_step[1] : g.inv_step[2]);
+                        perm3(ra, gb.step[0], gb.step[1], gb.step[2], gst[0], gst[1], gst[2]);
+                        perm3(ra, gb.gmin[0], gb.gmin[1], gb.gmin[2], gmn[0], gmn[1], gmn[2]);
+                        ginv0 = ra == 0 ? gb.inv_step[0] : (ra == 1 ? gb.inv_step[1] : gb.inv_step[2]);
                         // grid indices inside [xmin, xmax]: an index estimate widened by m
                         // grid steps, where m exceeds the rounding of the estimate and of the
                         // float grid positions (2 eps |pos| each), so no point in the range is
@@ -905,7 +909,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                             else
                                 for (int xi = i0; xi <= i1; ++xi)
                                     raster_point<T, VAL64>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0],
-                                                           gmn[0], ra, g, tv, pos, grid, owner, nexact, nassigned);
+                                                           gmn[0], ra, gb, tv, pos, grid, owner, nexact, nassigned);
                         }
                     }
                 }
@@ -932,9 +936,10 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         const float4 A0 = S.A0[jj], A1 = S.A1[jj];
                         const int4 I1 = S.I1[jj];
                         const int ra = (I1.w >> 9) & 3;
+                        const BlockGrid& gb = blocks[S.BK[jj]].grid;
                         float gst[3], gmn[3];
-                        perm3(ra, g.step[0], g.step[1], g.step[2], gst[0], gst[1], gst[2]);
-                        perm3(ra, g.gmin[0], g.gmin[1], g.gmin[2], gmn[0], gmn[1], gmn[2]);
+                        perm3(ra, gb.step[0], gb.step[1], gb.step[2], gst[0], gst[1], gst[2]);
+                        perm3(ra, gb.gmin[0], gb.gmin[1], gb.gmin[2], gmn[0], gmn[1], gmn[2]);
                         const float pyf = yi * gst[1] + gmn[1];
                         const float pzf = zi * gst[2] + gmn[2];
                         T cx[4], Bk[4], RN[4];
@@ -947,7 +952,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                             RN[k] = S.RN[k][rs];
                         }
                         raster_point<T, VAL64>(S, jj, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0], gmn[0], ra,
-                                               g, tv, pos, grid, owner, nexact, nassigned);
+                                               gb, tv, pos, grid, owner, nexact, nassigned);
                     }
                 }
                 __syncwarp();
@@ -1253,12 +1258,14 @@ __device__ __forceinline__ bool tet_bricks(const BlockDesc& bd, const float4* po
     return true;
 }
 
-// the term (hi, lo) added to W[key]: two 64-bit integer atomics.  (Merging
+// the term (hi, lo) added to W[key]: one or two 64-bit integer atomics.  (Merging
 // the terms of the warp's lanes that share a vertex first, with match and
 // reduce instructions, made the kernel five times slower on this GPU.)
-__device__ __forceinline__ void add_star(StarSum* W, int key, unsigned long long hi, unsigned long long lo)
+__device__ __forceinline__ void add_star(StarSum* W, int key, unsigned long long hi, unsigned long long lo,
+                                         bool two_words)
 {
-    atomicAdd(&W[key].hi, hi);
+    if (two_words)
+        atomicAdd(&W[key].hi, hi);
     atomicAdd(&W[key].lo, lo);
 }
 
@@ -1277,12 +1284,13 @@ __global__ void k_star_volumes(int mode, int t0, int nt, const float4* pos, cons
         const int4 vi = __ldg(&tv[t0 + it]);
         const float3 a0 = ld3(pos, vi.x), a1 = ld3(pos, vi.y), a2 = ld3(pos, vi.z), a3 = ld3(pos, vi.w);
         const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a0, a1, a2, a3, &nfix);
+        const bool two = mode == TESSGPU_MODE_FP64;
         unsigned long long qh, ql;
-        star_term(vol, scale, qh, ql);
-        add_star(W, vi.x, qh, ql);
-        add_star(W, vi.y, qh, ql);
-        add_star(W, vi.z, qh, ql);
-        add_star(W, vi.w, qh, ql);
+        star_term(vol, scale, two, qh, ql);
+        add_star(W, vi.x, qh, ql, two);
+        add_star(W, vi.y, qh, ql, two);
+        add_star(W, vi.z, qh, ql, two);
+        add_star(W, vi.w, qh, ql, two);
         if (BIN)
         {
             const int t = t0 + (int)it;

@@ -66,25 +66,34 @@ __device__ __forceinline__ double tet_abs_vol6(int mode_fp64, float3 a0, float3 
 }
 
 // Star-volume sums W_v = sum of 6V over v's tets, as exact fixed-point
-// integers of up to 101 bits held in two 64-bit words.  A term q = 6V * scale
-// (scale a power of two, so q is the double's own bits, an integer for any
-// 6V above scale^-1 * 2^52 and rounded once below that) is split into
-// hi = floor(q / 2^40) and lo = q - hi * 2^40, and the his and los are summed
-// separately with 64-bit integer atomics: a lo sum of up to 2^24 terms stays
-// below 2^64 and the hi sum of any star below 2^61, so the sums are exact and
-// independent of the order of the additions, and W (hence rho) is
-// bit-reproducible.  With 2^-95 as the quantum for a unit box, even the
-// smallest tets of a dense clump keep FP64 accuracy.
+// integers: every term is rounded once to a multiple of the quantum 1/scale
+// (scale a power of two) and the terms are added with 64-bit integer
+// atomics, so the sums are exact and independent of the order of the
+// additions, and W (hence rho) is bit-reproducible.
+//
+// Mixed mode: one 64-bit word (lo), scale such that any sum stays below
+// 2^62 -- a quantum of 2^-55 for a unit box, finer than the FP32 volumes it
+// sums.  FP64 mode: up to 101 bits in two words -- the term q = 6V * scale is
+// split into hi = floor(q / 2^40) and lo = q - hi * 2^40, summed separately
+// (a lo sum of up to 2^24 terms stays below 2^64, the hi sum of any star
+// below 2^61) -- a quantum of 2^-95 for a unit box, so even the smallest tets
+// of a dense clump keep FP64 accuracy.
 struct StarSum
 {
     unsigned long long hi, lo;
 };
 constexpr double STAR_LO = 1099511627776.0;   // 2^40
 
-__host__ __device__ __forceinline__ void star_term(double vol6, double scale, unsigned long long& hi,
+__host__ __device__ __forceinline__ void star_term(double vol6, double scale, bool two_words, unsigned long long& hi,
                                                    unsigned long long& lo)
 {
     const double x = vol6 * scale;            // exact (power-of-two scale)
+    if (!two_words)
+    {
+        hi = 0;
+        lo = (unsigned long long)rint(x);
+        return;
+    }
     const double h = floor(x / STAR_LO);      // exact
     hi = (unsigned long long)h;
     lo = (unsigned long long)rint(x - h * STAR_LO);   // the difference is exact; rint rounds q's fraction
@@ -95,9 +104,15 @@ __host__ __device__ __forceinline__ double star_value(unsigned long long hi, uns
     return ((double)hi * STAR_LO + (double)lo) * inv_scale;
 }
 
+// true when a sum left the range its scale was chosen for
+__host__ __device__ __forceinline__ bool star_overflow(unsigned long long hi, unsigned long long lo)
+{
+    return hi >= (1ull << 62) || lo >= (1ull << 63);
+}
+
 // the fixed-point scale: 2^bits with any 6V sum of up to 8x the data box
-// below 2^101 (so every hi sum stays below 2^61)
-inline double star_sum_scale(const float* dmin, const float* dmax)
+// below 2^62 (one word, mixed mode) or 2^101 (two words, FP64 mode)
+inline double star_sum_scale(const float* dmin, const float* dmax, bool two_words)
 {
     double vbox = 48.0;
     for (int i = 0; i < 3; ++i)
@@ -105,7 +120,7 @@ inline double star_sum_scale(const float* dmin, const float* dmax)
         const double ext = (double)dmax[i] - (double)dmin[i];
         vbox *= ext > 1e-30 ? ext : 1e-30;
     }
-    const int bits = 101 - (int)ceil(log2(vbox));
+    const int bits = (two_words ? 101 : 61) - (int)ceil(log2(vbox));
     return ldexp(1.0, bits);
 }
 

@@ -25,7 +25,8 @@
 //
 // The arithmetic is the DTFE path's (dtfe_common.cuh, shared with dtfe.cu):
 // 6V per tet in FP32 (FP64 when the FP32 error bound exceeds tau |6V|, or in
-// FP64 mode), summed exactly as fixed-point integers, rho = 24 m / sum.
+// FP64 mode), summed exactly as fixed-point integers (one 64-bit word in
+// mixed mode, two in FP64 mode), rho = 24 m / sum.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cmath>
@@ -61,11 +62,13 @@ __global__ void k_noalloc_star(const float* xyz, int np, const int* tets, int nt
             a[k] = make_float3(q[0], q[1], q[2]);
         }
         const double vol = tet_abs_vol6(mode == TESSGPU_MODE_FP64, a[0], a[1], a[2], a[3], nullptr);
+        const bool two = mode == TESSGPU_MODE_FP64;
         unsigned long long qh, ql;
-        tg::star_term(vol, scale, qh, ql);
+        tg::star_term(vol, scale, two, qh, ql);
         for (int k = 0; k < 4; ++k)
         {
-            atomicAdd(&sums[v[k]].hi, qh);
+            if (two)
+                atomicAdd(&sums[v[k]].hi, qh);
             atomicAdd(&sums[v[k]].lo, ql);
         }
     }
@@ -76,7 +79,7 @@ __global__ void k_noalloc_rho(const StarSum* sums, int np, float mass, double in
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < np; v += gridDim.x * blockDim.x)
     {
         const StarSum w = sums[v];
-        if (w.hi >= (1ull << 62))
+        if (tg::star_overflow(w.hi, w.lo))
             atomicExch(&flags[1], 1);
         const double s = tg::star_value(w.hi, w.lo, inv_scale);
         rho[v] = s > 0.0 ? (float)(24.0 * (double)mass / s) : 0.0f;
@@ -114,7 +117,7 @@ extern "C" tessgpu_status tessgpu_dtfe_densities_noalloc(const float* d_particle
     }
     StarSum* sums = (StarSum*)sums_addr;
     int* flags = (int*)flags_addr;
-    const double scale = tg::star_sum_scale(bounds6, bounds6 + 3);
+    const double scale = tg::star_sum_scale(bounds6, bounds6 + 3, mode == TESSGPU_MODE_FP64);
 
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemsetAsync(sums, 0, sizeof(StarSum) * (size_t)num_particles, s) != cudaSuccess ||

@@ -1,7 +1,7 @@
 """Many independent particle sets in one call (tessgpu_batch_dense_sets): each
 block is its own dense() over its own grid, all sets share every stage's
-launch and one persistent rasteriser launch; with graph=True the step is
-recorded into a CUDA graph once and replayed.
+launch (one rasteriser launch over all of them, row or brick kernel); with
+graph=True the step is recorded into a CUDA graph once and replayed.
 
 Each set's grid must equal what a one-block tessgpu_batch_dense of that set
 writes (bit for bit: same arithmetic, same fixed-point scale for sets in the
@@ -30,17 +30,34 @@ def make_sets(n, seed):
     return blocks, gni
 
 
+def make_ctx(kind):
+    """A context whose dense() rasteriser is kind ("rows" or "bricks")."""
+    import os
+    from tess2_gb300.api import Context
+    old = os.environ.get("TESSGPU_RASTER")
+    os.environ["TESSGPU_RASTER"] = kind
+    try:
+        return Context(0)
+    finally:
+        if old is None:
+            os.environ.pop("TESSGPU_RASTER", None)
+        else:
+            os.environ["TESSGPU_RASTER"] = old
+
+
+@pytest.mark.parametrize("kind", ["rows", "bricks"])
 @pytest.mark.parametrize("mode,tol", [(0, 1e-6), (1, 1e-12)])
-def test_sets_match_single_block_runs_and_oracle(gpu_ctx, oracle, mode, tol):
+def test_sets_match_single_block_runs_and_oracle(oracle, kind, mode, tol):
     import torch
     from tess2_gb300.api import DENSE_DTFE, sets_offsets
+    gpu_ctx = make_ctx(kind)
     blocks, gni = make_sets(7, 31)
     total, off = sets_offsets(gni)
     out = torch.full((total,), -7.0, dtype=torch.float32, device="cuda")
     b = gpu_ctx.upload(blocks)
     info = b.dense_sets(gni, out.data_ptr(), mode=mode)
     got = out.cpu().numpy()
-    assert info["grid_floats"] == total and info["brick_pairs"] > 0
+    assert info["grid_floats"] == total and (info["brick_pairs"] > 0) == (kind == "bricks")
     assigned = 0
     for i, blk in enumerate(blocks):
         n = int(np.prod(gni[i]))
@@ -58,11 +75,13 @@ def test_sets_match_single_block_runs_and_oracle(gpu_ctx, oracle, mode, tol):
     b.free()
 
 
-def test_sets_graph_replay(gpu_ctx):
+@pytest.mark.parametrize("kind", ["rows", "bricks"])
+def test_sets_graph_replay(kind):
     """The recorded step replays to the same grids, call after call, and a
     replay after the output was overwritten rewrites every point."""
     import torch
     from tess2_gb300.api import sets_offsets
+    gpu_ctx = make_ctx(kind)
     blocks, gni = make_sets(5, 8)
     total, off = sets_offsets(gni)
     b = gpu_ctx.upload(blocks)
@@ -77,4 +96,5 @@ def test_sets_graph_replay(gpu_ctx):
         assert torch.equal(out, ref), k
     for k in ("grid_pts_assigned", "exact_tests", "fp64_tets", "brick_pairs"):
         assert infos[0][k] == infos[1][k] == infos[2][k], k
+    assert infos[0]["grid_pts_assigned"] > 0
     b.free()
