@@ -1488,10 +1488,7 @@ static tessgpu_status dense_sets_rows(tessgpu_ctx* ctx, tessgpu_batch* bt, const
     }
     StarSum* W = bt->W;
     CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
-    int var = ctx->raster_variant[mode];
-    const char* env = getenv("TESSGPU_RASTER_VARIANT");
-    if (var < 0 && env && *env)
-        var = ctx->raster_variant[mode] = std::min(std::max(atoi(env), 0), raster_variants() - 1);
+    const int var = 1;   // the per-block-grid row kernel has one launch configuration
     auto densities = [&](cudaStream_t rs) {
         CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), rs));
         CK(cudaMemsetAsync(W, 0, sizeof(StarSum) * (bt->N ? bt->N : 1), rs));
@@ -1504,47 +1501,17 @@ static tessgpu_status dense_sets_rows(tessgpu_ctx* ctx, tessgpu_batch* bt, const
         CK(cudaMemsetAsync(d_out, 0, sizeof(float) * Gtot, rs));
         CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), rs));
         launch_raster(mode, v, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g0, kTau,
-                      d_out, nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs);
+                      d_out, nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs, nullptr, nullptr, 0, true);
         ctx->launches += bt->T ? 1 : 0;
         if (mode != TESSGPU_MODE_FP64)
         {
             launch_raster_fix(bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g0, d_out,
-                              nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs);
+                              nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs, true);
             ctx->launches += bt->T ? 1 : 0;
         }
         return TESSGPU_OK;
     };
     tessgpu_status st;
-    if (var < 0)
-    {
-        // autotune the launch variant on these sets (twice each: the first
-        // launch of a kernel also pays its module load)
-        if ((st = densities(s)) != TESSGPU_OK) return st;
-        float best = 1e30f;
-        cudaEvent_t e0, e1;
-        CK(cudaEventCreate(&e0));
-        CK(cudaEventCreate(&e1));
-        for (int v = 0; v < raster_variants(); ++v)
-        {
-            float vbest = 1e30f;
-            for (int rep = 0; rep < 2; ++rep)
-            {
-                CK(cudaEventRecord(e0, s));
-                if ((st = raster(s, v)) != TESSGPU_OK) return st;
-                CK(cudaEventRecord(e1, s));
-                CK(cudaEventSynchronize(e1));
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                vbest = std::min(vbest, ms);
-            }
-            if (v < 8) ctx->tune_ms[mode][v] = vbest;
-            if (vbest < best) { best = vbest; var = v; }
-        }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        if ((st = finish_status(ctx)) != TESSGPU_OK) return st;
-        ctx->raster_variant[mode] = var;
-    }
     std::vector<long long> key = { 1000 + (long long)mode, (long long)var, (long long)(size_t)d_out,
                                    (long long)(size_t)bt->W, (long long)(size_t)bt->fix_list };
     for (int i = 0; i < 3 * nb; ++i) key.push_back(glo_num_idx[i]);

@@ -482,13 +482,25 @@ __device__ __forceinline__ void raster_point(const SM& S, int j, int xi, int yi,
     nassigned++;
 }
 
-template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, bool FLAT>
+// PB: every block has its own grid (independent sets); otherwise all blocks
+// share the call's grid g
+template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, bool FLAT, bool PB>
 __global__ void __launch_bounds__(NW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
          int* fix_list, int* fix_count, Status* st, int t0)
 {
     typedef typename Vec4<T>::type T4;
+    BlockGrid gshared;   // the shared grid (read from the kernel's parameters)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+        gshared.gmin[d] = g.gmin[d];
+        gshared.step[d] = g.step[d];
+        gshared.inv_step[d] = g.inv_step[d];
+        gshared.n[d] = g.n[d];
+    }
+    gshared.off = 0;
     __shared__ RasterSmem<T, VAL64, COMPACT, FLAT> smem[NW];
     constexpr bool F32 = sizeof(T) == 4;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -652,7 +664,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         perm3(ra, ilo[0], ilo[1], ilo[2], ilo[0], ilo[1], ilo[2]);
                         perm3(ra, ihi[0], ihi[1], ihi[2], ihi[0], ihi[1], ihi[2]);
                         float gst[3], gmn[3], ginv[3];
-                        const BlockGrid& gb = blocks[b].grid;
+                        const BlockGrid& gb = PB ? blocks[b].grid : gshared;
                         S.BK[lane] = b;
                         perm3(ra, gb.step[0], gb.step[1], gb.step[2], gst[0], gst[1], gst[2]);
                         perm3(ra, gb.gmin[0], gb.gmin[1], gb.gmin[2], gmn[0], gmn[1], gmn[2]);
@@ -856,7 +868,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                     {
                         // the tet's axes: row axis ra, then y, z (see perm3)
                         const int ra = (I1.w >> 9) & 3;
-                        const BlockGrid& gb = blocks[S.BK[j]].grid;
+                        const BlockGrid& gb = PB ? blocks[S.BK[j]].grid : gshared;
                         float gst[3], gmn[3], ginv0;
                         perm3(ra, gb.step[0], gb.step[1], gb.step[2], gst[0], gst[1], gst[2]);
                         perm3(ra, gb.gmin[0], gb.gmin[1], gb.gmin[2], gmn[0], gmn[1], gmn[2]);
@@ -936,7 +948,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                         const float4 A0 = S.A0[jj], A1 = S.A1[jj];
                         const int4 I1 = S.I1[jj];
                         const int ra = (I1.w >> 9) & 3;
-                        const BlockGrid& gb = blocks[S.BK[jj]].grid;
+                        const BlockGrid& gb = PB ? blocks[S.BK[jj]].grid : gshared;
                         float gst[3], gmn[3];
                         perm3(ra, gb.step[0], gb.step[1], gb.step[2], gst[0], gst[1], gst[2]);
                         perm3(ra, gb.gmin[0], gb.gmin[1], gb.gmin[2], gmn[0], gmn[1], gmn[2]);
@@ -1015,15 +1027,23 @@ template <typename T, bool VAL64, bool LIST>
 static void raster_variant(int variant, long long work, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
                            const int* list, const int* list_count, const float4* pos, const int4* tv,
                            const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
-                           int* owner, int* fix_list, int* fix_count, Status* st, int t0 = 0)
+                           int* owner, int* fix_list, int* fix_count, Status* st, int t0 = 0, bool per_block = false)
 {
     // the double-precision tables need more shared memory: 3 warps per block
     constexpr int NW = (sizeof(T) == 4 && !VAL64) ? 4 : 3;
     const int nblk = grid_for(work, NW * 32, 16);
+    if (per_block)
+    {
+        // per-block grids: one launch configuration (5 blocks per SM)
+        k_raster<T, VAL64, LIST, 5, NW, false, false, true><<<nblk, NW * 32, 0, s>>>(
+            d_blocks, nb, total, list, list_count, pos, tv, rho32, rho64, g, tau, grid, owner, fix_list, fix_count, st,
+            t0);
+        return;
+    }
 #define TG_RASTER(MB, C, F)                                                                                        \
-    k_raster<T, VAL64, LIST, MB, NW, C, F><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, pos, tv, \
-                                                                      rho32, rho64, g, tau, grid, owner, fix_list,  \
-                                                                      fix_count, st, t0)
+    k_raster<T, VAL64, LIST, MB, NW, C, F, false><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, \
+                                                                             pos, tv, rho32, rho64, g, tau, grid,   \
+                                                                             owner, fix_list, fix_count, st, t0)
     switch (variant)
     {
     case 1: TG_RASTER(5, false, false); break;
@@ -1042,7 +1062,7 @@ int raster_variants() { return N_RASTER_VARIANTS; }
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                    int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s, const int* order,
-                   const int* order_count, int t0)
+                   const int* order_count, int t0, bool per_block)
 {
     if (total <= 0) return;
     const long long work = (long long)((total + 31) / 32) * 32 * 32;
@@ -1058,10 +1078,10 @@ void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int
     }
     if (mode == TESSGPU_MODE_FP64)
         raster_variant<double, true, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                            rho64, g, tau, grid, owner, nullptr, nullptr, st, t0);
+                                            rho64, g, tau, grid, owner, nullptr, nullptr, st, t0, per_block);
     else
         raster_variant<float, false, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                            rho64, g, tau, grid, owner, fix_list, fix_count, st, t0);
+                                            rho64, g, tau, grid, owner, fix_list, fix_count, st, t0, per_block);
 }
 
 // ---------------------------------------------------------------------------
@@ -1156,12 +1176,12 @@ void launch_tet_order(const float4* pos, const int4* tv, int total, const GridDe
 // possible list, the length is read on the device
 void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total, const float4* pos, const int4* tv,
                        const float* rho32, const double* rho64, const GridDesc& g, float* grid, int* owner,
-                       const int* fix_list, const int* fix_count, Status* st, cudaStream_t s)
+                       const int* fix_list, const int* fix_count, Status* st, cudaStream_t s, bool per_block)
 {
     if (total <= 0) return;
     const long long work = (long long)((total / 16 + 31) / 32) * 32 * 32;
     raster_variant<float, true, true>(0, work, s, d_blocks, nb, total, fix_list, fix_count, pos, tv, rho32, rho64, g,
-                                      0.0f, grid, owner, nullptr, nullptr, st);
+                                      0.0f, grid, owner, nullptr, nullptr, st, 0, per_block);
 }
 
 

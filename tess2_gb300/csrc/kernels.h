@@ -41,7 +41,8 @@ void launch_densities(const StarSum* W, int total_particles, float mass, double 
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                    int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s,
-                   const int* order = nullptr, const int* order_count = nullptr, int t0 = 0);
+                   const int* order = nullptr, const int* order_count = nullptr, int t0 = 0,
+                   bool per_block = false);
 int  raster_variants();
 void order_bricks(const GridDesc& g, int* nbx, int* nby, int* nbz);
 void launch_tet_order(const float4* pos, const int4* tv, int total, const GridDesc& g, int* key, int* hist,
@@ -80,6 +81,7 @@ void launch_raster_bricks(int mode, int variant, const BlockDesc* d_blocks, int 
                           cudaStream_t s);
 void launch_raster_fix(const BlockDesc* d_blocks, int nb, int total_tets, const float4* pos, const int4* tv,
                        const float* rho32, const double* rho64, const GridDesc& g, float* grid, int* owner,
-                       const int* fix_list, const int* fix_count, Status* st, cudaStream_t s);
+                       const int* fix_list, const int* fix_count, Status* st, cudaStream_t s,
+                       bool per_block = false);
 
 }
