@@ -60,8 +60,15 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64-mode and DENSE_TESS comparison runs")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip training and timing the DTFE surrogate network")
-    ap.add_argument("--surrogate-fields", type=int, default=24, help="training fields for the surrogate")
-    ap.add_argument("--surrogate-epochs", type=int, default=10)
+    ap.add_argument("--surrogate-train", action="store_true",
+                    help="instead of the DTFE benchmark: make fields of 2,097,152 particles -> 128^3 with the plain "
+                         "path, train the U-Net surrogate on them and validate it (one JSON line)")
+    ap.add_argument("--surrogate-fields", type=int, default=48, help="training fields for --surrogate-train")
+    ap.add_argument("--surrogate-val", type=int, default=16, help="validation fields for --surrogate-train")
+    ap.add_argument("--surrogate-epochs", type=int, default=12)
+    ap.add_argument("--surrogate-lr", type=float, default=3e-4)
+    ap.add_argument("--surrogate-particles", type=int, default=2097152,
+                    help="particles per field for --surrogate-train (configuration 4: 2,097,152)")
     ap.add_argument("--sets", type=int, default=0,
                     help="batched independent sets instead: this many particle sets, counts log-uniform in "
                          "[10,000, 500,000], each on its own grid of side 64/128/192/256, all in one call")
@@ -418,60 +425,62 @@ def time_rows(ctx, batch, blocks, gni, hbm, local):
 # ---------------------------------------------------------------------------
 # the surrogate network against the plain path
 # ---------------------------------------------------------------------------
-def time_surrogate(args, peaks, local):
-    """Trains the surrogate on fields the plain path makes (131,072 particles ->
-    64^3), then compares fields/s: the network (forward, CIC grid resident)
-    against the plain DTFE path on the GPU (star volumes + rasteriser, tets
-    resident) and against the plain path with its host Delaunay."""
+def time_surrogate(args, peaks, local, blocks, prep_s):
+    """The U-Net surrogate against the plain path at 128^3 (configuration 4's
+    grid): the network's forward pass and training step (random weights, CUDA
+    events), and the plain DTFE path on this run's own particles onto 128^3 --
+    the GPU pass with the tets resident, and with this run's host Delaunay time
+    added.  Its error against DTFE comes from --surrogate-train (fields of
+    2,097,152 particles; too long for this run)."""
     import torch
-    from tess2_gb300 import host
-    from tess2_gb300 import surrogate as S
+    from tess2_gb300 import unet as U
     from tess2_gb300.api import DENSE_DTFE, Context
-    npart, side = 131072, 64
-    r = S.train_and_evaluate(n_train=args.surrogate_fields, n_val=4, n_particles=npart, side=side,
-                             epochs=args.surrogate_epochs, lr=2e-3)
-    r.pop("net")
-    # the plain path on one such field: host Qhull, then the GPU DTFE pass
-    pts = host.mixture_particles(npart, 424242, frac_uniform=0.5, n_clumps=64, sigma=0.02)
-    t0 = time.time()
-    blk = host.tessellate([host.decompose(pts)[0]], processes=1)
-    t_qhull = time.time() - t0
+    side = 128
+    t = U.timings(side, reps=10)
     ctx = Context(local)
-    batch = ctx.upload(blk)
+    batch = ctx.upload(blocks)
     g = torch.empty(side ** 3, device=f"cuda:{local}")
     gni = [side] * 3
-    for _ in range(3):
-        batch.dense(DENSE_DTFE, gni, g.data_ptr(), want_info=False)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(10):
-        batch.dense(DENSE_DTFE, gni, g.data_ptr(), want_info=False)
-    e1.record()
-    torch.cuda.synchronize()
-    dtfe_ms = e0.elapsed_time(e1) / 10
+    dtfe_ms = U._events_ms(lambda: batch.dense(DENSE_DTFE, gni, g.data_ptr(), want_info=False), 10)
+    batch.free()
     bf16 = float(peaks.get("bf16_tflops", 1900.0))
-    # the network alone on a 256^3 grid (random weights and input): tcgen05 against mma.sync
-    big = {}
-    for eng, name in ((S.ENGINE_TCGEN05, "tcgen05"), (S.ENGINE_MMA_SYNC, "mma_sync")):
-        ms, tf = S.forward_throughput(256, engine=eng)
-        big[name] = dict(ms=ms, tflops=tf, frac_of_bf16_peak=tf / bf16,
-                         layers=[dict(c_in=ci, c_out=co, ms=lm, tflops=lt)
-                                 for ci, co, lm, lt in S.layer_times(256, engine=eng)])
-    r.update(forward_256=dict(grid=256, gflop=S.forward_flops((256, 256, 256)) / 1e9, **big))
-    r.update(plain_gpu_ms=dtfe_ms, plain_host_delaunay_s=t_qhull,
-             fields_per_s=1e3 / r["forward_ms"], plain_gpu_fields_per_s=1e3 / dtfe_ms,
-             plain_with_delaunay_fields_per_s=1.0 / (t_qhull + dtfe_ms * 1e-3),
-             speedup_vs_plain_gpu=dtfe_ms / r["forward_ms"],
-             fields_per_s_graph=1e3 / r["forward_graph_ms"],
-             speedup_vs_plain_gpu_graph=dtfe_ms / r["forward_graph_ms"],
-             speedup_vs_plain_with_delaunay=(t_qhull + dtfe_ms * 1e-3) / (r["forward_ms"] * 1e-3),
-             tensor_frac_of_bf16_peak=r["forward_tflops"] / bf16,
+    t.update(plain_gpu_ms=dtfe_ms, plain_host_delaunay_s=prep_s,
+             fields_per_s=1e3 / t["forward_ms"], plain_gpu_fields_per_s=1e3 / dtfe_ms,
+             plain_with_delaunay_fields_per_s=1.0 / (prep_s + dtfe_ms * 1e-3),
+             speedup_vs_plain_gpu=dtfe_ms / t["forward_ms"],
+             speedup_vs_plain_with_delaunay=(prep_s + dtfe_ms * 1e-3) / (t["forward_ms"] * 1e-3),
+             tensor_frac_of_bf16_peak=t["forward_tflops"] / bf16,
+             train_tensor_frac_of_bf16_peak=t["train_step_tflops"] / bf16,
              bf16_peak_source="measured MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
-             kernels="tcgen05 bf16 implicit GEMM with TMEM accumulators, TMA-fed (forward, data gradient); "
-                     "mma.sync m16n8k16 for other channel counts; FP32 weight gradient")
-    return r
+             network="U-Net, 4 levels, 32-256 channels, 3x3x3 convolutions, concatenated skips",
+             kernels="tcgen05 bf16 implicit GEMM with TMEM accumulators, TMA-fed (forward, data gradient, "
+                     "weight gradient)")
+    return t
+
+
+def train_surrogate(args):
+    """--surrogate-train: configuration 4 -- fields of 2,097,152 particles
+    (--surrogate-particles) -> 128^3 made by the plain path (host Qhull, GPU CIC and DTFE), the U-Net
+    trained on them, validated on held-out seeds; one JSON line."""
+    from tess2_gb300 import unet as U
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    log = lambda m: print("# " + m, flush=True)
+    r = U.train_and_evaluate(n_train=args.surrogate_fields, n_val=args.surrogate_val,
+                             n_particles=args.surrogate_particles, side=128,
+                             epochs=args.surrogate_epochs, lr=args.surrogate_lr, log=log)
+    r.pop("net")
+    bf16 = float(peaks.get("bf16_tflops", 1900.0))
+    r.update(metric="surrogate validation relative L2 of log(1 + rho / mean) vs DTFE, 128^3",
+             value=r["val_rel_l2"], unit="relative L2", higher_is_better=False,
+             tensor_frac_of_bf16_peak=r["forward_tflops"] / bf16,
+             fields_per_s=1e3 / r["forward_ms"],
+             plain_with_delaunay_fields_per_s=(args.surrogate_fields + args.surrogate_val) / r["fields_wall_s"],
+             data="synthetic: seeded particle sets, 50% uniform + 50% in 256 clumps sigma 0.01")
+    print(json.dumps(r), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -750,7 +759,7 @@ def run_gpu(args):
         rows = time_rows(ctx, batch, blocks, gni, hbm, local)
         extra["rows"] = rows
     if not args.no_surrogate:
-        extra["surrogate"] = time_surrogate(args, peaks, local)
+        extra["surrogate"] = time_surrogate(args, peaks, local, blocks, prep_s)
 
     parity = None
     if rank == 0 and not args.no_parity:
@@ -776,9 +785,10 @@ def run_gpu(args):
         print("# details " + json.dumps(details), flush=True)
         sur = extra.pop("surrogate", None)
         if sur:
-            extra["surrogate"] = {k: sur.get(k) for k in ("val_rel_l2", "cic_rel_l2", "fields_per_s",
-                                                          "speedup_vs_plain_gpu", "speedup_vs_plain_with_delaunay",
-                                                          "tensor_frac_of_bf16_peak", "train_step_ms")}
+            extra["surrogate"] = {k: sur.get(k) for k in ("forward_ms", "fields_per_s", "speedup_vs_plain_gpu",
+                                                          "speedup_vs_plain_with_delaunay", "forward_tflops",
+                                                          "tensor_frac_of_bf16_peak", "train_step_ms",
+                                                          "train_step_tflops")}
         cfg_short = {k: cfg[k] for k in ("workload", "particles", "particles_with_ghosts", "tets", "blocks", "mode",
                                          "l2")}
         line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
@@ -909,7 +919,9 @@ def run_sets(args):
 
 def main():
     args = parse()
-    if args.sets:
+    if args.surrogate_train:
+        train_surrogate(args)
+    elif args.sets:
         run_sets(args)
     elif args.impl == "reference":
         run_reference(args)

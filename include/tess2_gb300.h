@@ -393,6 +393,54 @@ tessgpu_status tessgpu_relu_grad(const float* g, const void* y, long long n, voi
 tessgpu_status tessgpu_adam(float* w, const float* g, float* m, float* v, int n, float lr, float beta1, float beta2,
                             float eps, int step, void* stream);
 
+/* ---- the surrogate's U-Net (tess2_gb300/unet.py) ----
+   Same chunk-planar bf16 layout: channel c of voxel v at ((c / 8) * V + v) * 8
+   + c % 8.  Grids: X a multiple of 128, or X in {16, 32, 64} with Y a multiple
+   of 128 / X; V = X * Y * Z.  A call writes only the planes it names; the
+   caller sizes the buffers.
+
+   y[planes y_plane0 .. y_plane0 + c_out / 8) = 3x3x3 convolution of x (c_in
+   channels, a multiple of 16) with the packed weights w, plus bias (may be
+   NULL), then ReLU when relu != 0, or, when mask is given (c_out channels),
+   set to 0 wherever mask <= 0 (the ReLU of a data gradient).  c_out a
+   multiple of 32.  tcgen05 implicit GEMM, FP32 accumulation in tensor memory,
+   bf16 output.  For the data gradient pass the packed data-gradient weights
+   with c_in and c_out exchanged. */
+tessgpu_status tessgpu_unet_conv(const void* x, int X, int Y, int Z, int c_in, const void* w, int c_out,
+                                 const float* bias, int relu, const void* mask, void* y, int y_plane0, void* stream);
+/* dw[tap][co][ci] += sum_v dy[v][co] x[v + tap][ci] (FP32 [27][c_out][c_in])
+   and db[co] += sum_v dy[v][co] (db may be NULL); tcgen05, K = voxels. */
+tessgpu_status tessgpu_unet_wgrad(const void* x, const void* dy, int X, int Y, int Z, int c_in, int c_out, float* dw,
+                                  float* db, void* stream);
+/* FP32 w[27][c_out][c_in] -> bf16 w_fwd[27][c_in/8][c_out][8] (forward) and
+   w_bwd[26 - tap][c_out/8][c_in][8] (data gradient) */
+tessgpu_status tessgpu_unet_pack_weights(const float* w, int c_out, int c_in, void* w_fwd, void* w_bwd, void* stream);
+/* y (X/2, Y/2, Z/2) = 2x2x2 means of x (X, Y, Z), c channels */
+tessgpu_status tessgpu_unet_pool(const void* x, int X, int Y, int Z, int c, void* y, void* stream);
+/* dx (X, Y, Z) = (act > 0) ? skip[planes skip_plane0 ..] + dy(coarse) / 8 : 0;
+   skip may be NULL (then 0) */
+tessgpu_status tessgpu_unet_pool_grad(const void* dy, const void* skip, int skip_plane0, const void* act, int X, int Y,
+                                      int Z, int c, void* dx, void* stream);
+/* y[planes y_plane0 ..] (X, Y, Z) = x (X/2, Y/2, Z/2) at the coarse voxel */
+tessgpu_status tessgpu_unet_upsample(const void* x, int X, int Y, int Z, int c, void* y, int y_plane0, void* stream);
+/* dx (X/2, Y/2, Z/2) = sum of dy[planes dy_plane0 ..] over the 8 fine voxels */
+tessgpu_status tessgpu_unet_upsample_grad(const void* dy, int dy_plane0, int X, int Y, int Z, int c, void* dx,
+                                          void* stream);
+/* x (16 channels, plane 1 already zero): channel 0 = field, channels 1-7 = 0 */
+tessgpu_status tessgpu_unet_input(const float* field, long long V, void* x, void* stream);
+/* pred = field + w[c] + sum_k w[k] act[k] (c <= 32 channels); with target
+   and loss, *loss += sum (pred - target)^2 (FP64) */
+tessgpu_status tessgpu_unet_head(const void* act, int c, const float* w, const float* field, long long V, float* pred,
+                                 const float* target, double* loss, void* stream);
+/* gradient of scale * sum (pred - target)^2 through the head: dact = (act >
+   0) ? w * g : 0 with g = 2 scale (pred - target); dw[k] += sum g act[k],
+   dw[c] += sum g */
+tessgpu_status tessgpu_unet_head_grad(const void* act, int c, const float* w, const float* pred, const float* target,
+                                      long long V, float scale, void* dact, float* dw, void* stream);
+/* Synchronises stream; TESSGPU_ERR_TIMEOUT (and the flag cleared) when a U-Net
+   tensor-core kernel gave up on a bounded wait since the last check. */
+tessgpu_status tessgpu_unet_check(void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,6 +26,7 @@ UNITS = {
     "api.cu": ["-fmad=false"],
     "noalloc.cu": ["-fmad=false"],
     "surrogate.cu": [],
+    "unet.cu": [],
 }
 
 

@@ -1,0 +1,1393 @@
+// The DTFE surrogate's U-Net kernels: 3x3x3 convolutions of any channel count
+// (multiples of 16 in, 32 out) on the 5th-generation tensor cores, for the
+// forward pass and the data gradient (tcgen05 implicit GEMM, bf16 x bf16 ->
+// FP32 in tensor memory), the weight gradient on the tensor cores too, and the
+// U-Net's other steps: 2x2x2 average pooling, nearest upsampling into a
+// concatenation buffer, their gradients, the 1x1 prediction head with its
+// loss, bias gradients.
+//
+// Layout.  Activations chunk-planar as the rest of the surrogate: channel c of
+// voxel v at ((c / 8) * V + v) * 8 + c % 8, voxel v = (z * Y + y) * X + x, bf16.
+// A concatenation [a | b] is one buffer whose first planes hold a and the
+// next ones b; producers write at a plane offset, so concatenating copies
+// nothing.  Weights: an FP32 master [tap][c_out][c_in] (tap = (dz * 3 + dy) * 3
+// + dx, offsets -1..1) packed to bf16 [tap][c_in / 8][c_out][8] for the
+// forward pass and to [26 - tap][c_out / 8][c_in][8] for the data gradient
+// (the same product with the weights flipped and transposed).
+//
+// Convolution (k_unet_conv): a tile is 128 consecutive voxels (M of one MMA)
+// x NT output channels (N).  Per stage the TMA warp copies one K chunk of KC
+// input channels for one (dz, dy) row of taps (SLAB: X a multiple of 128, the
+// tile inside one x row; one slab of positions x0 - 1 .. x0 + 128 serves
+// dx = -1, 0, 1 at start addresses 16 bytes apart) or for one tap (TAP: X of
+// 16, 32 or 64, the tile = 128 / X whole x rows; the box starts at x = dx), and
+// the matching weights, both by cp.async.bulk.tensor; positions outside the
+// grid arrive as zeros.  The MMA warp issues tcgen05.mma per 16 channels into
+// one of two tensor-memory accumulators; the four epilogue warps read the
+// other (tcgen05.ld, lane = voxel), add the bias, apply ReLU or the ReLU mask
+// of the data gradient, and store bf16 rows, consecutive threads on adjacent
+// 16-byte chunks.
+//
+// Weight gradient (k_unet_wgrad): dw[tap][co][ci] = sum_v dy[v][co] x[v+tap][ci]
+// with K = voxels: A = the output-gradient tile (M = 128 output channels,
+// zero past c_out), B = the input slab (N = NTW input channels), both
+// MN-major straight from the planes.  An item is (tap group, c_out tile,
+// c_in tile, voxel chunk); its accumulators (3 or 1 taps x NTW columns) stay
+// in tensor memory across the chunk's tiles and are added to dw once.
+//
+// Every wait is bounded (tc_common.cuh); a timed-out wait raises the CTA's
+// abort flag, every role leaves its loop, the CTA waits for its copies and
+// MMAs, frees its tensor memory and reports through tessgpu_unet_check.
+#include "../../include/tess2_gb300.h"
+#include "tc_common.cuh"
+
+namespace {
+
+using namespace tcg;
+
+constexpr int U_THREADS = 192;        // warps 0-3 epilogue, 4 TMA, 5 MMA (+ tensor-memory allocation)
+constexpr int U_SMEM = 227 * 1024;    // dynamic shared memory a CTA may opt into
+constexpr int U_M = 128;              // voxels per tile
+// every launch asks for at least this much shared memory, so that one CTA runs per SM:
+// a CTA's tensor-memory allocation (up to all 512 columns) then never waits for another's
+constexpr int U_MIN_SMEM = 116 * 1024;
+
+__device__ int g_unet_err;            // raised by a kernel whose bounded wait ran out
+
+__host__ __device__ constexpr int pow2_cols(int c)
+{
+    return c <= 32 ? 32 : (c <= 64 ? 64 : (c <= 128 ? 128 : (c <= 256 ? 256 : 512)));
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void tma5(uint32_t dst, uint64_t map, int c0, int c1, int c2, int c3, int c4, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+                 "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma4(uint32_t dst, uint64_t map, int c0, int c1, int c2, int c3, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+                 "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t dcol, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dcol),
+                 "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bar_init(uint32_t bar, int count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+// instruction descriptor: D f32, A and B bf16, M = 128, N = n; mn: both operands MN-major
+__host__ __device__ constexpr uint32_t idesc_f16(int n, bool mn)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | (mn ? (1u << 15) | (1u << 16) : 0u) | ((uint32_t)(n >> 3) << 17) |
+           ((uint32_t)(U_M >> 4) << 24);
+}
+
+// ---------------------------------------------------------------------------
+// convolution (forward and data gradient)
+// ---------------------------------------------------------------------------
+template <int NT, int KC, bool SLAB>
+struct ConvLayout
+{
+    static constexpr int TB = SLAB ? 3 : 1;                  // taps per stage
+    static constexpr int AROWS = SLAB ? 130 : U_M;           // positions per plane of the A stage
+    static constexpr int APLANE = AROWS * 16;
+    static constexpr int ABYTES = (KC / 8) * APLANE;
+    static constexpr int BPLANE = NT * 16;                   // one plane of KC/8 of a tap's weights
+    static constexpr int BTAP = (KC / 8) * BPLANE;
+    static constexpr int BBYTES = TB * BTAP;
+    static constexpr int BOFF = (ABYTES + 1023) / 1024 * 1024;
+    static constexpr int STAGE = (BOFF + BBYTES + 1023) / 1024 * 1024;
+    static constexpr int FIT = (U_SMEM - 1024) / STAGE;
+    static constexpr int STAGES = FIT < 8 ? FIT : 8;
+    static constexpr int BAR = STAGES * STAGE;
+    // full[S], empty[S], accf[2], acce[2], fin, tensor-memory address, abort flag, last[S]
+    static constexpr int OFF_FULL = BAR, OFF_EMPTY = BAR + 8 * STAGES, OFF_ACCF = BAR + 16 * STAGES,
+                         OFF_ACCE = OFF_ACCF + 16, OFF_FIN = OFF_ACCE + 16, OFF_TMEM = OFF_FIN + 8,
+                         OFF_ABORT = OFF_TMEM + 4, OFF_LAST = OFF_ABORT + 4;
+    static constexpr int TOTAL = OFF_LAST + 4 * STAGES;
+    static constexpr int TCOLS = pow2_cols(2 * NT);          // two accumulators of NT columns
+    static constexpr uint32_t TX = (uint32_t)(ABYTES + BBYTES);
+    static_assert(NT % 32 == 0 && NT >= 32 && NT <= 256, "N: a multiple of 32 up to 256");
+    static_assert(KC % 16 == 0 && KC <= 64, "K chunk");
+    static_assert(2 * NT <= 512, "tensor memory");
+    static_assert(STAGES >= 2, "shared memory");
+    static_assert(TOTAL <= U_SMEM, "shared memory");
+};
+
+struct ConvArgs
+{
+    int X, Y, Z;                    // grid (X a multiple of 128 for SLAB, X in {16, 32, 64} for TAP)
+    int cin, cout;                  // cin a multiple of KC, cout a multiple of NT
+    long long V;                    // X * Y * Z, a multiple of 128
+    const float* bias;              // [cout] or null
+    int relu;
+    const __nv_bfloat16* mask;      // chunk-planar, cout channels, or null: out = acc when mask > 0, else 0
+    __nv_bfloat16* y;               // chunk-planar output
+    int y_plane0;                   // plane of y that output channel 0 goes to
+    int* err;
+};
+
+template <int NT, int KC, bool SLAB>
+__global__ void __launch_bounds__(U_THREADS, 1)
+    k_unet_conv(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap, const ConvArgs p)
+{
+    using L = ConvLayout<NT, KC, SLAB>;
+    constexpr int S = L::STAGES;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int mtiles = (int)(p.V / U_M);
+    const int items = mtiles * (p.cout / NT);               // < 2^31 (launcher)
+    const int nkc = p.cin / KC;
+    const int steps = (SLAB ? 9 : 27) * nkc;                 // stages per item
+    const int NI = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const uint32_t s_base = smem_u32(smem);
+    const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY;
+    const uint32_t accf0 = s_base + L::OFF_ACCF, acce0 = s_base + L::OFF_ACCE, fin = s_base + L::OFF_FIN;
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
+    int* last = reinterpret_cast<int*>(smem + L::OFF_LAST);   // per slot: the last stage copied into it
+
+    for (int b = tid; b < S; b += U_THREADS) last[b] = -1;
+    if (tid == 0)
+    {
+        for (int b = 0; b < S; ++b)
+        {
+            bar_init(full0 + 8 * b, 1);    // expect_tx + the copies' bytes
+            bar_init(empty0 + 8 * b, 1);   // one commit of the MMAs that read the slot
+        }
+        for (int a = 0; a < 2; ++a)
+        {
+            bar_init(accf0 + 8 * a, 1);      // one commit per item
+            bar_init(acce0 + 8 * a, 128);    // the 128 epilogue threads
+        }
+        bar_init(fin, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 5)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_base + L::OFF_TMEM),
+                     "r"(L::TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
+
+    if (warp == 4)
+    {
+        // ---- TMA: per stage the input box and the weights of its taps ----
+        const bool leader = elect_one();
+        const uint64_t am = reinterpret_cast<uint64_t>(&amap), bm = reinterpret_cast<uint64_t>(&bmap);
+        if (leader)
+        {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(am) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(bm) : "memory");
+        }
+        bool stop = false;
+        int step = 0;
+        for (int k = 0; k < NI && !stop; ++k)
+        {
+            const int item = (int)blockIdx.x + k * (int)gridDim.x;
+            const int n = item / mtiles, m = item - n * mtiles;
+            const long long v0 = (long long)m * U_M;
+            const int x0 = (int)(v0 % p.X);
+            const long long r = v0 / p.X;
+            const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
+            for (int j = 0; j < steps; ++j, ++step)
+            {
+                const int b = step % S;
+                if (step >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((step / S - 1) & 1), abort))
+                {
+                    stop = true;
+                    break;
+                }
+                const int g = j / nkc, kc = j - g * nkc;
+                const int dz = SLAB ? g / 3 - 1 : g / 9 - 1;
+                const int dy = SLAB ? g % 3 - 1 : (g / 3) % 3 - 1;
+                const int xs = SLAB ? x0 - 1 : g % 3 - 1;          // the box's first x
+                const int tap0 = SLAB ? 3 * g : g;
+                if (leader)
+                {
+                    last[b] = step;
+                    expect_tx(full0 + 8 * b, L::TX);
+                    const uint32_t dst = s_base + b * L::STAGE;
+                    tma5(dst, am, 0, xs, y0 + dy, z + dz, kc * (KC / 8), full0 + 8 * b);
+                    tma4(dst + L::BOFF, bm, 0, n * NT, kc * (KC / 8), tap0, full0 + 8 * b);
+                }
+                __syncwarp();
+            }
+        }
+    }
+    else if (warp == 5)
+    {
+        // ---- MMA: the whole warp runs the loop (warp-uniform descriptors), one lane issues ----
+        constexpr uint32_t idesc = idesc_f16(NT, false);
+        const bool leader = elect_one();
+        bool go = true;
+        int step = 0;
+        for (int k = 0; k < NI && go; ++k)
+        {
+            const int a = k & 1;
+            // the epilogue has read this accumulator's item k - 2
+            if (k >= 2 && !warp_wait(acce0 + 8 * a, (uint32_t)(((k - 2) >> 1) & 1), abort)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const uint32_t dcol = tbase + (uint32_t)(a * NT);
+            for (int j = 0; j < steps; ++j, ++step)
+            {
+                const int b = step % S;
+                go = warp_wait(full0 + 8 * b, (uint32_t)((step / S) & 1), abort);
+                if (!go) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t abase = s_base + b * L::STAGE;
+                const uint64_t ad = umma_sdesc(abase, L::APLANE, 128);
+                const uint64_t bd = umma_sdesc(abase + L::BOFF, L::BPLANE, 128);
+#pragma unroll
+                for (int sh = 0; sh < L::TB; ++sh)
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ++ks)
+                    {
+                        const uint64_t da = ad + (uint64_t)((sh * 16 + ks * 2 * L::APLANE) >> 4);
+                        const uint64_t db = bd + (uint64_t)((sh * L::BTAP + ks * 2 * L::BPLANE) >> 4);
+                        if (leader) mma_f16(dcol, da, db, idesc, (j > 0 || sh > 0 || ks > 0) ? 1u : 0u);
+                    }
+                if (leader) commit(empty0 + 8 * b);
+                __syncwarp();
+            }
+            if (!go) break;
+            if (leader) commit(accf0 + 8 * a);
+            __syncwarp();
+        }
+        // every MMA issued has completed once fin's first phase does
+        if (leader) commit(fin);
+        __syncwarp();
+        if (!mbar_wait_bounded(fin, 0u)) *abort = 1;
+        __syncwarp();
+    }
+    else
+    {
+        // ---- epilogue (warps 0-3: tensor-memory lanes 32 warp .. 32 warp + 31 = voxels) ----
+        for (int k = 0; k < NI; ++k)
+        {
+            const int item = (int)blockIdx.x + k * (int)gridDim.x;
+            const int n = item / mtiles, m = item - n * mtiles;
+            const int a = k & 1;
+            bool ready = false;
+            if (lane == 0) ready = mbar_wait_or_abort(accf0 + 8 * a, (uint32_t)((k >> 1) & 1), abort);
+            if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const long long v = (long long)m * U_M + tid;
+            const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(a * NT);
+#pragma unroll 1
+            for (int c0 = 0; c0 < NT; c0 += 32)
+            {
+                uint32_t acc[32];
+                tmem_ld16(taddr + c0, acc);
+                tmem_ld16(taddr + c0 + 16, acc + 16);
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (c0 + 32 >= NT)
+                {
+                    // this thread has read all of the accumulator: hand it back to the MMA warp
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    mbar_arrive(acce0 + 8 * a);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                    const int ch = n * NT + c0 + 8 * q;   // first of the plane's 8 channels
+                    float f[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                    {
+                        f[e] = __uint_as_float(acc[8 * q + e]) + (p.bias ? __ldg(p.bias + ch + e) : 0.0f);
+                        if (p.relu) f[e] = fmaxf(f[e], 0.0f);
+                    }
+                    if (p.mask)
+                    {
+                        const uint4 mk = __ldg(reinterpret_cast<const uint4*>(p.mask + ((long long)(ch >> 3) * p.V + v) * 8));
+                        const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(&mk);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e)
+                            if (!(__bfloat162float(mb[e]) > 0.0f)) f[e] = 0.0f;
+                    }
+                    *reinterpret_cast<uint4*>(p.y + ((long long)(p.y_plane0 + (ch >> 3)) * p.V + v) * 8) =
+                        make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
+                                   pack_bf16(f[6], f[7]));
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // no copy may still be landing in shared memory when the CTA exits
+    for (int b = tid; b < S; b += U_THREADS)
+    {
+        const int s = last[b];
+        if (s >= 0) mbar_wait_bounded(full0 + 8 * b, (uint32_t)((s / S) & 1));
+    }
+    __syncthreads();
+    if (tid == 0 && *abort) atomicExch(p.err, 1);
+    if (warp == 5)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
+}
+
+// ---------------------------------------------------------------------------
+// weight gradient
+// ---------------------------------------------------------------------------
+template <int NTW, bool SLAB>
+struct WgradLayout
+{
+    static constexpr int TG = SLAB ? 3 : 1;                  // taps per item
+    static constexpr int APLANE = U_M * 16;                  // one plane of the output-gradient tile
+    static constexpr int ABYTES = 16 * APLANE;               // 16 planes: M = 128 output channels
+    static constexpr int XROWS = SLAB ? 130 : U_M;
+    static constexpr int XPLANE = XROWS * 16;
+    static constexpr int BBYTES = (NTW / 8) * XPLANE;
+    static constexpr int BOFF = ABYTES;
+    static constexpr int STAGE = (BOFF + BBYTES + 1023) / 1024 * 1024;
+    static constexpr int FIT = (U_SMEM - 1024) / STAGE;
+    static constexpr int STAGES = FIT < 4 ? FIT : 4;
+    static constexpr int BAR = STAGES * STAGE;
+    // full[S], empty[S], accf, acce, fin, tensor-memory address, abort flag, last[S]
+    static constexpr int OFF_FULL = BAR, OFF_EMPTY = BAR + 8 * STAGES, OFF_ACCF = BAR + 16 * STAGES,
+                         OFF_ACCE = OFF_ACCF + 8, OFF_FIN = OFF_ACCE + 8, OFF_TMEM = OFF_FIN + 8,
+                         OFF_ABORT = OFF_TMEM + 4, OFF_LAST = OFF_ABORT + 4;
+    static constexpr int TOTAL = OFF_LAST + 4 * STAGES;
+    static constexpr int TCOLS = pow2_cols(TG * NTW);
+    static constexpr uint32_t TX = (uint32_t)(ABYTES + BBYTES);
+    static_assert(NTW % 16 == 0 && NTW >= 16 && NTW <= 256, "N");
+    static_assert(TG * NTW <= 512, "tensor memory");
+    static_assert(STAGES >= 2, "shared memory");
+    static_assert(TOTAL <= U_SMEM, "shared memory");
+};
+
+struct WgradArgs
+{
+    int X, Y, Z;
+    int cin, cout;
+    long long V;
+    int nch;        // voxel chunks per (tap group, c_out tile, c_in tile); <= V / 128
+    float* dw;      // FP32 [27][cout][cin], accumulated into
+    int* err;
+};
+
+template <int NTW, bool SLAB>
+__global__ void __launch_bounds__(U_THREADS, 1)
+    k_unet_wgrad(const __grid_constant__ CUtensorMap dymap, const __grid_constant__ CUtensorMap xmap,
+                 const WgradArgs p)
+{
+    using L = WgradLayout<NTW, SLAB>;
+    constexpr int S = L::STAGES;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int mtiles = (int)(p.V / U_M);
+    const int CT = (p.cout + 127) / 128, NTN = p.cin / NTW, NG = SLAB ? 9 : 27;
+    const int items = NG * CT * NTN * p.nch;
+    const int NI = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const uint32_t s_base = smem_u32(smem);
+    const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY;
+    const uint32_t accf = s_base + L::OFF_ACCF, acce = s_base + L::OFF_ACCE, fin = s_base + L::OFF_FIN;
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
+    int* last = reinterpret_cast<int*>(smem + L::OFF_LAST);
+
+    for (int b = tid; b < S; b += U_THREADS) last[b] = -1;
+    if (tid == 0)
+    {
+        for (int b = 0; b < S; ++b)
+        {
+            bar_init(full0 + 8 * b, 1);
+            bar_init(empty0 + 8 * b, 1);
+        }
+        bar_init(accf, 1);
+        bar_init(acce, 128);
+        bar_init(fin, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 5)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_base + L::OFF_TMEM),
+                     "r"(L::TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
+
+    // item -> (tap group grp, c_out tile ct, c_in tile nt, chunk) and the chunk's tiles [m0, m1)
+    auto decode = [&](int item, int& grp, int& ct, int& nt, int& m0, int& m1) {
+        const int chunk = item % p.nch;
+        int rest = item / p.nch;
+        nt = rest % NTN;
+        rest /= NTN;
+        ct = rest % CT;
+        grp = rest / CT;
+        m0 = (int)((long long)chunk * mtiles / p.nch);
+        m1 = (int)((long long)(chunk + 1) * mtiles / p.nch);
+    };
+
+    if (warp == 4)
+    {
+        // ---- TMA: per tile the output-gradient planes of the c_out tile and the input box ----
+        const bool leader = elect_one();
+        const uint64_t dm = reinterpret_cast<uint64_t>(&dymap), xm = reinterpret_cast<uint64_t>(&xmap);
+        if (leader)
+        {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(dm) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(xm) : "memory");
+        }
+        bool stop = false;
+        int step = 0;
+        for (int k = 0; k < NI && !stop; ++k)
+        {
+            int grp, ct, nt, m0, m1;
+            decode((int)blockIdx.x + k * (int)gridDim.x, grp, ct, nt, m0, m1);
+            const int dz = SLAB ? grp / 3 - 1 : grp / 9 - 1;
+            const int dy = SLAB ? grp % 3 - 1 : (grp / 3) % 3 - 1;
+            for (int m = m0; m < m1; ++m, ++step)
+            {
+                const int b = step % S;
+                if (step >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((step / S - 1) & 1), abort))
+                {
+                    stop = true;
+                    break;
+                }
+                const long long v0 = (long long)m * U_M;
+                const int x0 = (int)(v0 % p.X);
+                const long long r = v0 / p.X;
+                const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
+                if (leader)
+                {
+                    last[b] = step;
+                    expect_tx(full0 + 8 * b, L::TX);
+                    const uint32_t dst = s_base + b * L::STAGE;
+                    tma5(dst, dm, 0, x0, y0, z, ct * 16, full0 + 8 * b);
+                    tma5(dst + L::BOFF, xm, 0, SLAB ? x0 - 1 : grp % 3 - 1, y0 + dy, z + dz, nt * (NTW / 8),
+                         full0 + 8 * b);
+                }
+                __syncwarp();
+            }
+        }
+    }
+    else if (warp == 5)
+    {
+        // ---- MMA: D[tap][co][ci] += dyT x, 8 MMAs of 16 voxels per tap and tile ----
+        constexpr uint32_t idesc = idesc_f16(NTW, true);
+        const bool leader = elect_one();
+        bool go = true;
+        int step = 0;
+        for (int k = 0; k < NI && go; ++k)
+        {
+            int grp, ct, nt, m0, m1;
+            decode((int)blockIdx.x + k * (int)gridDim.x, grp, ct, nt, m0, m1);
+            // the epilogue has read item k - 1's accumulators
+            if (k >= 1 && !warp_wait(acce, (uint32_t)((k - 1) & 1), abort)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int m = m0; m < m1; ++m, ++step)
+            {
+                const int b = step % S;
+                go = warp_wait(full0 + 8 * b, (uint32_t)((step / S) & 1), abort);
+                if (!go) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t abase = s_base + b * L::STAGE;
+                const uint64_t ad = umma_sdesc(abase, 128, L::APLANE);
+                const uint64_t bd = umma_sdesc(abase + L::BOFF, 128, L::XPLANE);
+#pragma unroll
+                for (int sh = 0; sh < L::TG; ++sh)
+#pragma unroll
+                    for (int ks = 0; ks < U_M / 16; ++ks)
+                    {
+                        const uint64_t da = ad + (uint64_t)((ks * 256) >> 4);
+                        const uint64_t db = bd + (uint64_t)((sh * 16 + ks * 256) >> 4);
+                        if (leader)
+                            mma_f16(tbase + (uint32_t)(sh * NTW), da, db, idesc, (m > m0 || ks > 0) ? 1u : 0u);
+                    }
+                if (leader) commit(empty0 + 8 * b);
+                __syncwarp();
+            }
+            if (!go) break;
+            if (leader) commit(accf);
+            __syncwarp();
+        }
+        if (leader) commit(fin);
+        __syncwarp();
+        if (!mbar_wait_bounded(fin, 0u)) *abort = 1;
+        __syncwarp();
+    }
+    else
+    {
+        // ---- epilogue: lane 32 warp + l = output channel of the c_out tile; add to dw ----
+        for (int k = 0; k < NI; ++k)
+        {
+            int grp, ct, nt, m0, m1;
+            decode((int)blockIdx.x + k * (int)gridDim.x, grp, ct, nt, m0, m1);
+            bool ready = false;
+            if (lane == 0) ready = mbar_wait_or_abort(accf, (uint32_t)(k & 1), abort);
+            if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const int co = ct * 128 + tid;
+#pragma unroll 1
+            for (int sh = 0; sh < L::TG; ++sh)
+            {
+                const int tap = SLAB ? 3 * grp + sh : grp;
+#pragma unroll 1
+                for (int c0 = 0; c0 < NTW; c0 += 16)
+                {
+                    uint32_t v[16];
+                    tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(sh * NTW + c0), v);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;");
+                    if (co < p.cout)
+                    {
+                        float* out = p.dw + ((long long)tap * p.cout + co) * p.cin + nt * NTW + c0;
+#pragma unroll
+                        for (int c = 0; c < 16; ++c) atomicAdd(out + c, __uint_as_float(v[c]));
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(acce);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    for (int b = tid; b < S; b += U_THREADS)
+    {
+        const int s = last[b];
+        if (s >= 0) mbar_wait_bounded(full0 + 8 * b, (uint32_t)((s / S) & 1));
+    }
+    __syncthreads();
+    if (tid == 0 && *abort) atomicExch(p.err, 1);
+    if (warp == 5)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
+}
+
+// Weight gradient with taps stacked along M, for c_out in {16, 32, 64}: with
+// u = v + s_t, dw[t][co][ci] = sum_u dy[u - s_t][co] x[u][ci], so the input tile
+// is the same for every tap and the output gradient is shifted instead.  A =
+// TS = 128 / c_out shifted copies of the output-gradient tile (rows j * c_out
+// + co for tap g * TS + j), B = the input tile; one MMA per 16 voxels then
+// feeds TS taps, every row of M = 128 a real output channel.  The last group's
+// slots past tap 26 load tap 26 again and are not written back.
+template <int NTW, int TS>
+__global__ void __launch_bounds__(U_THREADS, 1)
+    k_unet_wgrad_stacked(const __grid_constant__ CUtensorMap dymap, const __grid_constant__ CUtensorMap xmap,
+                         const WgradArgs p)
+{
+    using L = WgradLayout<NTW, false>;
+    constexpr int S = L::STAGES;
+    constexpr int CO = 128 / TS;                 // = c_out
+    constexpr int NG = (27 + TS - 1) / TS;       // tap groups
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int mtiles = (int)(p.V / U_M);
+    const int NTN = p.cin / NTW;
+    const int items = NG * NTN * p.nch;
+    const int NI = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const bool slab = p.X % U_M == 0;           // tile = part of one x row; else 128 / X whole rows
+    const uint32_t s_base = smem_u32(smem);
+    const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY;
+    const uint32_t accf = s_base + L::OFF_ACCF, acce = s_base + L::OFF_ACCE, fin = s_base + L::OFF_FIN;
+    volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
+    int* last = reinterpret_cast<int*>(smem + L::OFF_LAST);
+
+    for (int b = tid; b < S; b += U_THREADS) last[b] = -1;
+    if (tid == 0)
+    {
+        for (int b = 0; b < S; ++b)
+        {
+            bar_init(full0 + 8 * b, 1);
+            bar_init(empty0 + 8 * b, 1);
+        }
+        bar_init(accf, 1);
+        bar_init(acce, 128);
+        bar_init(fin, 1);
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (warp == 5)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_base + L::OFF_TMEM),
+                     "r"(L::TCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
+
+    auto decode = [&](int item, int& grp, int& nt, int& m0, int& m1) {
+        const int chunk = item % p.nch;
+        const int rest = item / p.nch;
+        nt = rest % NTN;
+        grp = rest / NTN;
+        m0 = (int)((long long)chunk * mtiles / p.nch);
+        m1 = (int)((long long)(chunk + 1) * mtiles / p.nch);
+    };
+
+    if (warp == 4)
+    {
+        // ---- TMA: per tile TS shifted output-gradient boxes and the input box ----
+        const bool leader = elect_one();
+        const uint64_t dm = reinterpret_cast<uint64_t>(&dymap), xm = reinterpret_cast<uint64_t>(&xmap);
+        if (leader)
+        {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(dm) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(xm) : "memory");
+        }
+        bool stop = false;
+        int step = 0;
+        for (int k = 0; k < NI && !stop; ++k)
+        {
+            int grp, nt, m0, m1;
+            decode((int)blockIdx.x + k * (int)gridDim.x, grp, nt, m0, m1);
+            for (int m = m0; m < m1; ++m, ++step)
+            {
+                const int b = step % S;
+                if (step >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((step / S - 1) & 1), abort))
+                {
+                    stop = true;
+                    break;
+                }
+                const long long v0 = (long long)m * U_M;
+                const int x0 = (int)(v0 % p.X);
+                const long long r = v0 / p.X;
+                const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
+                if (leader)
+                {
+                    last[b] = step;
+                    expect_tx(full0 + 8 * b, L::TX);
+                    const uint32_t dst = s_base + b * L::STAGE;
+#pragma unroll 1
+                    for (int j = 0; j < TS; ++j)
+                    {
+                        const int t = min(grp * TS + j, 26);
+                        const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+                        tma5(dst + j * (CO / 8) * L::APLANE, dm, 0, (slab ? x0 : 0) - dx, y0 - dy, z - dz, 0,
+                             full0 + 8 * b);
+                    }
+                    tma5(dst + L::BOFF, xm, 0, slab ? x0 : 0, y0, z, nt * (NTW / 8), full0 + 8 * b);
+                }
+                __syncwarp();
+            }
+        }
+    }
+    else if (warp == 5)
+    {
+        // ---- MMA: D[slot, co][ci] += A (stacked, MN-major) x B (MN-major), 8 MMAs per tile ----
+        constexpr uint32_t idesc = idesc_f16(NTW, true);
+        const bool leader = elect_one();
+        bool go = true;
+        int step = 0;
+        for (int k = 0; k < NI && go; ++k)
+        {
+            int grp, nt, m0, m1;
+            decode((int)blockIdx.x + k * (int)gridDim.x, grp, nt, m0, m1);
+            if (k >= 1 && !warp_wait(acce, (uint32_t)((k - 1) & 1), abort)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            for (int m = m0; m < m1; ++m, ++step)
+            {
+                const int b = step % S;
+                go = warp_wait(full0 + 8 * b, (uint32_t)((step / S) & 1), abort);
+                if (!go) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t abase = s_base + b * L::STAGE;
+                const uint64_t ad = umma_sdesc(abase, 128, L::APLANE);
+                const uint64_t bd = umma_sdesc(abase + L::BOFF, 128, L::XPLANE);
+#pragma unroll
+                for (int ks = 0; ks < U_M / 16; ++ks)
+                    if (leader)
+                        mma_f16(tbase, ad + (uint64_t)((ks * 256) >> 4), bd + (uint64_t)((ks * 256) >> 4), idesc,
+                                (m > m0 || ks > 0) ? 1u : 0u);
+                if (leader) commit(empty0 + 8 * b);
+                __syncwarp();
+            }
+            if (!go) break;
+            if (leader) commit(accf);
+            __syncwarp();
+        }
+        if (leader) commit(fin);
+        __syncwarp();
+        if (!mbar_wait_bounded(fin, 0u)) *abort = 1;
+        __syncwarp();
+    }
+    else
+    {
+        // ---- epilogue: lane 32 warp + l = row (tap slot l / c_out, output channel l % c_out) ----
+        for (int k = 0; k < NI; ++k)
+        {
+            int grp, nt, m0, m1;
+            decode((int)blockIdx.x + k * (int)gridDim.x, grp, nt, m0, m1);
+            bool ready = false;
+            if (lane == 0) ready = mbar_wait_or_abort(accf, (uint32_t)(k & 1), abort);
+            if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            const int tap = grp * TS + tid / CO, co = tid % CO;
+#pragma unroll 1
+            for (int c0 = 0; c0 < NTW; c0 += 16)
+            {
+                uint32_t v[16];
+                tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (tap < 27)
+                {
+                    float* out = p.dw + ((long long)tap * CO + co) * p.cin + nt * NTW + c0;
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) atomicAdd(out + c, __uint_as_float(v[c]));
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(acce);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    for (int b = tid; b < S; b += U_THREADS)
+    {
+        const int s = last[b];
+        if (s >= 0) mbar_wait_bounded(full0 + 8 * b, (uint32_t)((s / S) & 1));
+    }
+    __syncthreads();
+    if (tid == 0 && *abort) atomicExch(p.err, 1);
+    if (warp == 5)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
+}
+
+// ---------------------------------------------------------------------------
+// the other steps (CUDA cores; HBM-bound)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void unpack8(const uint4& u, float* f)
+{
+    const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&u);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) f[e] = __bfloat162float(h[e]);
+}
+
+__device__ __forceinline__ uint4 pack8(const float* f)
+{
+    return make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), pack_bf16(f[6], f[7]));
+}
+
+// the coarse voxel of fine voxel v, and the fine voxels of coarse voxel u
+__device__ __forceinline__ long long coarse_of(long long v, int X, int Y)
+{
+    const int x = (int)(v % X);
+    const long long r = v / X;
+    const int y = (int)(r % Y), z = (int)(r / Y);
+    return ((long long)(z >> 1) * (Y >> 1) + (y >> 1)) * (X >> 1) + (x >> 1);
+}
+
+__device__ __forceinline__ long long fine_of(long long u, int X, int Y, int child)
+{
+    const int hx = X >> 1, hy = Y >> 1;
+    const int x = (int)(u % hx);
+    const long long r = u / hx;
+    const int y = (int)(r % hy), z = (int)(r / hy);
+    return ((long long)(2 * z + (child >> 2)) * Y + 2 * y + ((child >> 1) & 1)) * X + 2 * x + (child & 1);
+}
+
+// y[u] = mean of x over the 8 fine voxels of u (X, Y, Z: the fine grid)
+__global__ void k_pool(const __nv_bfloat16* __restrict__ x, int X, int Y, int Z, int planes,
+                       __nv_bfloat16* __restrict__ y)
+{
+    const long long V = (long long)X * Y * Z, U = V / 8, n = U * planes;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    {
+        const int pl = (int)(i / U);
+        const long long u = i - (long long)pl * U;
+        float s[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+        {
+            float f[8];
+            unpack8(__ldg(reinterpret_cast<const uint4*>(x + ((long long)pl * V + fine_of(u, X, Y, c)) * 8)), f);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) s[e] += f[e];
+        }
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] *= 0.125f;
+        reinterpret_cast<uint4*>(y)[(long long)pl * U + u] = pack8(s);
+    }
+}
+
+// dx[v] = (act[v] > 0) ? skip[v] + dy[coarse(v)] / 8 : 0 (skip: planes skip_plane0.. of a
+// concatenation gradient, or null); X, Y, Z: the fine grid
+__global__ void k_pool_grad(const __nv_bfloat16* __restrict__ dy, const __nv_bfloat16* __restrict__ skip,
+                            int skip_plane0, const __nv_bfloat16* __restrict__ act, int X, int Y, int Z, int planes,
+                            __nv_bfloat16* __restrict__ dx)
+{
+    const long long V = (long long)X * Y * Z, U = V / 8, n = V * planes;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    {
+        const int pl = (int)(i / V);
+        const long long v = i - (long long)pl * V;
+        float g[8], a[8];
+        unpack8(__ldg(reinterpret_cast<const uint4*>(dy) + (long long)pl * U + coarse_of(v, X, Y)), g);
+        unpack8(__ldg(reinterpret_cast<const uint4*>(act) + i), a);
+        float s[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+        if (skip) unpack8(__ldg(reinterpret_cast<const uint4*>(skip) + (long long)(skip_plane0 + pl) * V + v), s);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) s[e] = a[e] > 0.0f ? s[e] + 0.125f * g[e] : 0.0f;
+        reinterpret_cast<uint4*>(dx)[i] = pack8(s);
+    }
+}
+
+// y[planes y_plane0 ..][v] = x[coarse(v)] (X, Y, Z: the fine grid)
+__global__ void k_upsample(const __nv_bfloat16* __restrict__ x, int X, int Y, int Z, int planes,
+                           __nv_bfloat16* __restrict__ y, int y_plane0)
+{
+    const long long V = (long long)X * Y * Z, U = V / 8, n = V * planes;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    {
+        const int pl = (int)(i / V);
+        const long long v = i - (long long)pl * V;
+        reinterpret_cast<uint4*>(y)[(long long)(y_plane0 + pl) * V + v] =
+            __ldg(reinterpret_cast<const uint4*>(x) + (long long)pl * U + coarse_of(v, X, Y));
+    }
+}
+
+// dx[u] = sum of dy (planes dy_plane0 ..) over the 8 fine voxels of u (X, Y, Z: the fine grid)
+__global__ void k_upsample_grad(const __nv_bfloat16* __restrict__ dy, int dy_plane0, int X, int Y, int Z, int planes,
+                                __nv_bfloat16* __restrict__ dx)
+{
+    const long long V = (long long)X * Y * Z, U = V / 8, n = U * planes;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    {
+        const int pl = (int)(i / U);
+        const long long u = i - (long long)pl * U;
+        float s[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+        {
+            float f[8];
+            unpack8(__ldg(reinterpret_cast<const uint4*>(dy) + (long long)(dy_plane0 + pl) * V + fine_of(u, X, Y, c)), f);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) s[e] += f[e];
+        }
+        reinterpret_cast<uint4*>(dx)[i] = pack8(s);
+    }
+}
+
+// the network's input: channel 0 of 16 = field, the rest 0 (plane 1 must be zero already)
+__global__ void k_input(const float* __restrict__ field, long long V, __nv_bfloat16* __restrict__ x)
+{
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    {
+        const float f[8] = { field[v], 0, 0, 0, 0, 0, 0, 0 };
+        reinterpret_cast<uint4*>(x)[v] = pack8(f);
+    }
+}
+
+// pred[v] = field[v] + b + sum_c w[c] act[c][v]; with a target: loss += sum (pred - target)^2 (block
+// partial sums, one atomic per block)
+__global__ void __launch_bounds__(256) k_head(const __nv_bfloat16* __restrict__ act, int c, const float* __restrict__ w,
+                                              const float* __restrict__ field, long long V, float* __restrict__ pred,
+                                              const float* __restrict__ target, double* loss)
+{
+    __shared__ double part[8];
+    double l = 0.0;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    {
+        float s = field[v] + w[c];
+        for (int pl = 0; pl < c / 8; ++pl)
+        {
+            float f[8];
+            unpack8(__ldg(reinterpret_cast<const uint4*>(act) + (long long)pl * V + v), f);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) s = fmaf(w[8 * pl + e], f[e], s);
+        }
+        pred[v] = s;
+        if (target)
+        {
+            const double d = (double)s - (double)target[v];
+            l += d * d;
+        }
+    }
+    if (!target || !loss) return;
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        double t = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += part[i];
+        atomicAdd(loss, t);
+    }
+}
+
+// gradient of scale * sum (pred - target)^2 through the head: g = 2 scale (pred - target);
+// dact[c][v] = (act > 0) ? w[c] g : 0; dw[c] += sum_v g act[c][v], dw[c_count] += sum_v g
+__global__ void __launch_bounds__(256) k_head_grad(const __nv_bfloat16* __restrict__ act, int c,
+                                                   const float* __restrict__ w, const float* __restrict__ pred,
+                                                   const float* __restrict__ target, long long V, float scale,
+                                                   __nv_bfloat16* __restrict__ dact, float* dw)
+{
+    __shared__ float part[8][33];
+    float acc[33];
+    for (int i = 0; i <= 32; ++i) acc[i] = 0.0f;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    {
+        const float g = 2.0f * scale * (pred[v] - target[v]);
+        acc[32] += g;
+        for (int pl = 0; pl < c / 8; ++pl)
+        {
+            float f[8], d[8];
+            unpack8(__ldg(reinterpret_cast<const uint4*>(act) + (long long)pl * V + v), f);
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+            {
+                acc[8 * pl + e] += g * f[e];
+                d[e] = f[e] > 0.0f ? w[8 * pl + e] * g : 0.0f;
+            }
+            reinterpret_cast<uint4*>(dact)[(long long)pl * V + v] = pack8(d);
+        }
+    }
+    const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+    for (int i = 0; i <= 32; ++i)
+    {
+        float s = acc[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (ln == 0) part[wid][i] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x <= 32 && (threadIdx.x < c || threadIdx.x == 32))
+    {
+        float s = 0.0f;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += part[i][threadIdx.x];
+        atomicAdd(dw + (threadIdx.x == 32 ? c : threadIdx.x), s);
+    }
+}
+
+// db[co] += sum_v dy[v][co]: one block per (plane, voxel slice), one atomic per channel and block
+__global__ void __launch_bounds__(256) k_unet_bias_grad(const __nv_bfloat16* __restrict__ dy, long long V, float* db)
+{
+    __shared__ float part[8][8];
+    const int pl = blockIdx.y;
+    float acc[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    {
+        float f[8];
+        unpack8(__ldg(reinterpret_cast<const uint4*>(dy) + (long long)pl * V + v), f);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) acc[e] += f[e];
+    }
+    const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+    {
+        float s = acc[e];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (ln == 0) part[wid][e] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8)
+    {
+        float s = 0.0f;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += part[i][threadIdx.x];
+        atomicAdd(db + 8 * pl + threadIdx.x, s);
+    }
+}
+
+// FP32 master [tap][co][ci] -> bf16 forward [tap][ci/8][co][8] and data-gradient [26-tap][co/8][ci][8]
+__global__ void k_pack_weights(const float* __restrict__ w, int cout, int cin, __nv_bfloat16* __restrict__ wf,
+                               __nv_bfloat16* __restrict__ wb)
+{
+    const int n = 27 * cout * cin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const int tap = i / (cout * cin), co = (i / cin) % cout, ci = i % cin;
+        const __nv_bfloat16 v = __float2bfloat16_rn(w[i]);
+        wf[(((long long)tap * (cin / 8) + ci / 8) * cout + co) * 8 + ci % 8] = v;
+        wb[(((long long)(26 - tap) * (cout / 8) + co / 8) * cin + ci) * 8 + co % 8] = v;
+    }
+}
+
+int grid_1d(long long n, int t)
+{
+    long long b = (n + t - 1) / t;
+    return (int)(b < 1 ? 1 : (b > 152LL * 32 ? 152LL * 32 : b));
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+int smem_of(int total)
+{
+    return total > U_MIN_SMEM ? total : U_MIN_SMEM;
+}
+
+int sm_count()
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+// a chunk-planar activation of c channels as (8 channels, X, Y, Z, c / 8), box (8, bx, by, 1, bp)
+bool act_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int bx, int by, int bp)
+{
+    const EncodeTiled encode = tensor_map_encoder();
+    if (!encode || ((uintptr_t)base & 15)) return false;
+    const cuuint64_t dims[5] = { 8, (cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(c / 8) };
+    const cuuint64_t strides[4] = { 16, (cuuint64_t)X * 16, (cuuint64_t)X * Y * 16, (cuuint64_t)X * Y * Z * 16 };
+    const cuuint32_t box[5] = { 8, (cuuint32_t)bx, (cuuint32_t)by, 1, (cuuint32_t)bp };
+    const cuuint32_t estride[5] = { 1, 1, 1, 1, 1 };
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// packed weights [27][cin/8][cout][8] as (8, cout, cin / 8, 27), box (8, nt, kc / 8, tb)
+bool weight_map(CUtensorMap* map, const void* base, int cin, int cout, int nt, int kc, int tb)
+{
+    const EncodeTiled encode = tensor_map_encoder();
+    if (!encode || ((uintptr_t)base & 15)) return false;
+    const cuuint64_t dims[4] = { 8, (cuuint64_t)cout, (cuuint64_t)(cin / 8), 27 };
+    const cuuint64_t strides[3] = { 16, (cuuint64_t)cout * 16, (cuuint64_t)(cin / 8) * cout * 16 };
+    const cuuint32_t box[4] = { 8, (cuuint32_t)nt, (cuuint32_t)(kc / 8), (cuuint32_t)tb };
+    const cuuint32_t estride[4] = { 1, 1, 1, 1 };
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NT, int KC, bool SLAB>
+tessgpu_status launch_conv(const void* x, const void* w, const ConvArgs& a, cudaStream_t s)
+{
+    using L = ConvLayout<NT, KC, SLAB>;
+    static bool ready[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
+    if (!ready[dev])
+    {
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (optin < smem_of(L::TOTAL)) return TESSGPU_ERR_UNSUPPORTED;
+        if (cudaFuncSetAttribute(k_unet_conv<NT, KC, SLAB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_of(L::TOTAL)) != cudaSuccess)
+            return TESSGPU_ERR_CUDA;
+        ready[dev] = true;
+    }
+    CUtensorMap amap, bmap;
+    if (!act_map(&amap, x, a.X, a.Y, a.Z, a.cin, SLAB ? 130 : a.X, SLAB ? 1 : U_M / a.X, KC / 8) ||
+        !weight_map(&bmap, w, a.cin, a.cout, NT, KC, L::TB))
+        return TESSGPU_ERR_UNSUPPORTED;
+    const long long items = a.V / U_M * (a.cout / NT);
+    const int sms = sm_count();
+    const int grid = (int)(items < sms ? items : sms);
+    k_unet_conv<NT, KC, SLAB><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(amap, bmap, a);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+template <int NTW, bool SLAB>
+tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStream_t s)
+{
+    using L = WgradLayout<NTW, SLAB>;
+    static bool ready[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
+    if (!ready[dev])
+    {
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (optin < smem_of(L::TOTAL)) return TESSGPU_ERR_UNSUPPORTED;
+        if (cudaFuncSetAttribute(k_unet_wgrad<NTW, SLAB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_of(L::TOTAL)) != cudaSuccess)
+            return TESSGPU_ERR_CUDA;
+        ready[dev] = true;
+    }
+    CUtensorMap dymap, xmap;
+    if (!act_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, SLAB ? U_M : a.X, SLAB ? 1 : U_M / a.X, 16) ||
+        !act_map(&xmap, x, a.X, a.Y, a.Z, a.cin, SLAB ? 130 : a.X, SLAB ? 1 : U_M / a.X, NTW / 8))
+        return TESSGPU_ERR_UNSUPPORTED;
+    const int sms = sm_count();
+    const long long mt = a.V / U_M;
+    const long long base = (long long)(SLAB ? 9 : 27) * ((a.cout + 127) / 128) * (a.cin / NTW);
+    long long nch = (2LL * sms + base - 1) / base;
+    if (nch > mt) nch = mt;
+    if (nch < 1) nch = 1;
+    a.nch = (int)nch;
+    const long long items = base * nch;
+    const int grid = (int)(items < sms ? items : sms);
+    k_unet_wgrad<NTW, SLAB><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(dymap, xmap, a);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+template <int NTW, int TS>
+tessgpu_status launch_wgrad_stacked(const void* x, const void* dy, WgradArgs a, cudaStream_t s)
+{
+    using L = WgradLayout<NTW, false>;
+    static bool ready[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
+    if (!ready[dev])
+    {
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (optin < smem_of(L::TOTAL)) return TESSGPU_ERR_UNSUPPORTED;
+        if (cudaFuncSetAttribute(k_unet_wgrad_stacked<NTW, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_of(L::TOTAL)) != cudaSuccess)
+            return TESSGPU_ERR_CUDA;
+        ready[dev] = true;
+    }
+    const bool slab = a.X % U_M == 0;
+    CUtensorMap dymap, xmap;
+    if (!act_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, slab ? U_M : a.X, slab ? 1 : U_M / a.X, a.cout / 8) ||
+        !act_map(&xmap, x, a.X, a.Y, a.Z, a.cin, slab ? U_M : a.X, slab ? 1 : U_M / a.X, NTW / 8))
+        return TESSGPU_ERR_UNSUPPORTED;
+    const int sms = sm_count();
+    const long long mt = a.V / U_M;
+    const long long base = (long long)((27 + TS - 1) / TS) * (a.cin / NTW);
+    long long nch = (2LL * sms + base - 1) / base;
+    if (nch > mt) nch = mt;
+    if (nch < 1) nch = 1;
+    a.nch = (int)nch;
+    const long long items = base * nch;
+    const int grid = (int)(items < sms ? items : sms);
+    k_unet_wgrad_stacked<NTW, TS><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(dymap, xmap, a);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+bool unet_grid_ok(int X, int Y, int Z)
+{
+    if (X <= 0 || Y <= 0 || Z <= 0) return false;
+    if (X % 128 == 0) return true;   // slab tiles (one x row)
+    return (X == 16 || X == 32 || X == 64) && Y % (U_M / X) == 0;   // tiles of whole x rows
+}
+
+int* err_flag()
+{
+    int* e = nullptr;
+    return cudaGetSymbolAddress((void**)&e, g_unet_err) == cudaSuccess ? e : nullptr;
+}
+
+}  // namespace
+
+extern "C" tessgpu_status tessgpu_unet_conv(const void* x, int X, int Y, int Z, int cin, const void* w, int cout,
+                                            const float* bias, int relu, const void* mask, void* y, int y_plane0,
+                                            void* stream)
+{
+    if (!x || !w || !y || !unet_grid_ok(X, Y, Z) || cin <= 0 || cin % 16 || cout <= 0 || cout % 32 || y_plane0 < 0 ||
+        (long long)X * Y * Z / U_M * (cout / 32) >= (1LL << 31))
+        return TESSGPU_ERR_INVALID;
+    int* err = err_flag();
+    if (!err) return TESSGPU_ERR_CUDA;
+    ConvArgs a;
+    a.X = X; a.Y = Y; a.Z = Z;
+    a.cin = cin; a.cout = cout;
+    a.V = (long long)X * Y * Z;
+    a.bias = bias; a.relu = relu;
+    a.mask = (const __nv_bfloat16*)mask;
+    a.y = (__nv_bfloat16*)y;
+    a.y_plane0 = y_plane0;
+    a.err = err;
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool slab = X % 128 == 0;
+    // N tile: all output channels up to 256, else the largest of 256, 192, 128, 96, 64, 32 dividing c_out
+    int nt = 32;
+    for (int c : { 256, 192, 128, 96, 64 })
+        if (cout % c == 0)
+        {
+            nt = c;
+            break;
+        }
+    const int kc = cin % 64 == 0 && !slab ? 64 : (cin % 32 == 0 ? 32 : 16);
+#define UC(NT_, KC_, SL_)                                                                                              \
+    if (nt == NT_ && kc == KC_ && slab == SL_) return launch_conv<NT_, KC_, SL_>(x, w, a, s);
+    UC(32, 16, true) UC(32, 32, true) UC(64, 32, true) UC(96, 32, true) UC(128, 32, true) UC(192, 32, true)
+    UC(256, 32, true)
+    UC(32, 16, false) UC(32, 32, false) UC(64, 32, false) UC(96, 32, false) UC(128, 32, false) UC(192, 32, false)
+    UC(256, 32, false)
+    UC(32, 64, false) UC(64, 64, false) UC(96, 64, false) UC(128, 64, false) UC(192, 64, false) UC(256, 64, false)
+#undef UC
+    return TESSGPU_ERR_UNSUPPORTED;
+}
+
+extern "C" tessgpu_status tessgpu_unet_wgrad(const void* x, const void* dy, int X, int Y, int Z, int cin, int cout,
+                                             float* dw, float* db, void* stream)
+{
+    if (!x || !dy || !dw || !unet_grid_ok(X, Y, Z) || cin <= 0 || cin % 16 || cout <= 0 || cout % 8)
+        return TESSGPU_ERR_INVALID;
+    int* err = err_flag();
+    if (!err) return TESSGPU_ERR_CUDA;
+    WgradArgs a;
+    a.X = X; a.Y = Y; a.Z = Z;
+    a.cin = cin; a.cout = cout;
+    a.V = (long long)X * Y * Z;
+    a.nch = 1;
+    a.dw = dw;
+    a.err = err;
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool slab = X % 128 == 0;
+    // N tile over the input channels: all of them up to 128 (slab: three taps share tensor memory) or 256
+    int ntw = 16;
+    const int cap = slab ? 128 : 256;
+    for (int c : { 256, 192, 128, 96, 64, 32, 16 })
+        if (c <= cap && cin % c == 0)
+        {
+            ntw = c;
+            break;
+        }
+    tessgpu_status st = TESSGPU_ERR_UNSUPPORTED;
+    if (cout == 16 || cout == 32 || cout == 64)
+    {
+        // taps stacked along M: the input's N tile up to 256 channels
+        int nts = 16;
+        for (int c : { 256, 192, 128, 96, 64, 32, 16 })
+            if (cin % c == 0)
+            {
+                nts = c;
+                break;
+            }
+#define US(N_, T_) else if (nts == N_ && cout == 128 / T_) st = launch_wgrad_stacked<N_, T_>(x, dy, a, s);
+        if (false) {}
+        US(16, 8) US(32, 8) US(64, 8) US(96, 8) US(128, 8) US(192, 8) US(256, 8)
+        US(16, 4) US(32, 4) US(64, 4) US(96, 4) US(128, 4) US(192, 4) US(256, 4)
+        US(16, 2) US(32, 2) US(64, 2) US(96, 2) US(128, 2) US(192, 2) US(256, 2)
+#undef US
+    }
+#define UW(N_, SL_)                                                                                                    \
+    else if (ntw == N_ && slab == SL_) st = launch_wgrad<N_, SL_>(x, dy, a, s);
+    if (st != TESSGPU_ERR_UNSUPPORTED) {}
+    UW(16, true) UW(32, true) UW(64, true) UW(96, true) UW(128, true)
+    UW(16, false) UW(32, false) UW(64, false) UW(96, false) UW(128, false) UW(192, false) UW(256, false)
+#undef UW
+    if (st != TESSGPU_OK || !db) return st;
+    const long long V = a.V;
+    long long nb = (V + 255) / 256;
+    if (nb > 128) nb = 128;
+    k_unet_bias_grad<<<dim3((unsigned)nb, (unsigned)(cout / 8)), 256, 0, s>>>((const __nv_bfloat16*)dy, V, db);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_pack_weights(const float* w, int cout, int cin, void* w_fwd, void* w_bwd,
+                                                    void* stream)
+{
+    if (!w || !w_fwd || !w_bwd || cout <= 0 || cin <= 0 || cout % 8 || cin % 8) return TESSGPU_ERR_INVALID;
+    const int n = 27 * cout * cin;
+    k_pack_weights<<<grid_1d(n, 256), 256, 0, (cudaStream_t)stream>>>(w, cout, cin, (__nv_bfloat16*)w_fwd,
+                                                                      (__nv_bfloat16*)w_bwd);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_pool(const void* x, int X, int Y, int Z, int c, void* y, void* stream)
+{
+    if (!x || !y || X <= 0 || Y <= 0 || Z <= 0 || X % 2 || Y % 2 || Z % 2 || c <= 0 || c % 8)
+        return TESSGPU_ERR_INVALID;
+    const long long n = (long long)X * Y * Z / 8 * (c / 8);
+    k_pool<<<grid_1d(n, 256), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)x, X, Y, Z, c / 8,
+                                                               (__nv_bfloat16*)y);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_pool_grad(const void* dy, const void* skip, int skip_plane0, const void* act,
+                                                 int X, int Y, int Z, int c, void* dx, void* stream)
+{
+    if (!dy || !act || !dx || X <= 0 || Y <= 0 || Z <= 0 || X % 2 || Y % 2 || Z % 2 || c <= 0 || c % 8 ||
+        skip_plane0 < 0)
+        return TESSGPU_ERR_INVALID;
+    const long long n = (long long)X * Y * Z * (c / 8);
+    k_pool_grad<<<grid_1d(n, 256), 256, 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16*)dy, (const __nv_bfloat16*)skip, skip_plane0, (const __nv_bfloat16*)act, X, Y, Z, c / 8,
+        (__nv_bfloat16*)dx);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_upsample(const void* x, int X, int Y, int Z, int c, void* y, int y_plane0,
+                                                void* stream)
+{
+    if (!x || !y || X <= 0 || Y <= 0 || Z <= 0 || X % 2 || Y % 2 || Z % 2 || c <= 0 || c % 8 || y_plane0 < 0)
+        return TESSGPU_ERR_INVALID;
+    const long long n = (long long)X * Y * Z * (c / 8);
+    k_upsample<<<grid_1d(n, 256), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)x, X, Y, Z, c / 8,
+                                                                  (__nv_bfloat16*)y, y_plane0);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_upsample_grad(const void* dy, int dy_plane0, int X, int Y, int Z, int c,
+                                                     void* dx, void* stream)
+{
+    if (!dy || !dx || X <= 0 || Y <= 0 || Z <= 0 || X % 2 || Y % 2 || Z % 2 || c <= 0 || c % 8 || dy_plane0 < 0)
+        return TESSGPU_ERR_INVALID;
+    const long long n = (long long)X * Y * Z / 8 * (c / 8);
+    k_upsample_grad<<<grid_1d(n, 256), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)dy, dy_plane0, X, Y, Z,
+                                                                       c / 8, (__nv_bfloat16*)dx);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_input(const float* field, long long V, void* x, void* stream)
+{
+    if (!field || !x || V <= 0) return TESSGPU_ERR_INVALID;
+    k_input<<<grid_1d(V, 256), 256, 0, (cudaStream_t)stream>>>(field, V, (__nv_bfloat16*)x);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_head(const void* act, int c, const float* w, const float* field, long long V,
+                                            float* pred, const float* target, double* loss, void* stream)
+{
+    if (!act || !w || !field || !pred || V <= 0 || c <= 0 || c % 8 || c > 32) return TESSGPU_ERR_INVALID;
+    k_head<<<grid_1d(V, 256), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)act, c, w, field, V, pred, target,
+                                                              loss);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_head_grad(const void* act, int c, const float* w, const float* pred,
+                                                 const float* target, long long V, float scale, void* dact, float* dw,
+                                                 void* stream)
+{
+    if (!act || !w || !pred || !target || !dact || !dw || V <= 0 || c <= 0 || c % 8 || c > 32)
+        return TESSGPU_ERR_INVALID;
+    k_head_grad<<<grid_1d(V, 256), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)act, c, w, pred, target, V,
+                                                                   scale, (__nv_bfloat16*)dact, dw);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_check(void* stream)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    int h = 0;
+    const int zero = 0;
+    if (cudaMemcpyFromSymbolAsync(&h, g_unet_err, sizeof(int), 0, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return TESSGPU_ERR_CUDA;
+    if (!h) return TESSGPU_OK;
+    if (cudaMemcpyToSymbolAsync(g_unet_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return TESSGPU_ERR_CUDA;
+    return TESSGPU_ERR_TIMEOUT;
+}
