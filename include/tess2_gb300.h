@@ -272,7 +272,8 @@ long long      tessgpu_sets_grid_floats(int nsets, const int* glo_num_idx, long 
    (src/dense.cpp:130-164); here all sets share each stage's launch, and one
    rasteriser launch covers every set: the row kernel over all sets' tets, or,
    in a context made with TESSGPU_RASTER=bricks, the persistent brick kernel
-   whose CTAs take (brick, chunk) items of every set from one device counter.  graph != 0: the step is recorded into
+   whose CTAs take (brick, chunk) items of every set from one device counter.
+   graph != 0: the step is recorded into
    a CUDA graph on the first call with these sets, grids and output, and
    replayed by later calls (the brick shape is autotuned on the first call of
    a context, outside the graph).  The batch's descriptors must not change

@@ -38,6 +38,8 @@
 // Every wait is bounded (tc_common.cuh); a timed-out wait raises the CTA's
 // abort flag, every role leaves its loop, the CTA waits for its copies and
 // MMAs, frees its tensor memory and reports through tessgpu_unet_check.
+#include <cstdlib>
+
 #include "../../include/tess2_gb300.h"
 #include "tc_common.cuh"
 
@@ -113,17 +115,18 @@ __host__ __device__ constexpr uint32_t idesc_f16(int n, bool mn)
 // ---------------------------------------------------------------------------
 // convolution (forward and data gradient)
 // ---------------------------------------------------------------------------
-template <int NT, int KC, bool SLAB>
+template <int NT, int KC, bool SLAB, int MT>
 struct ConvLayout
 {
     static constexpr int TB = SLAB ? 3 : 1;                  // taps per stage
-    static constexpr int AROWS = SLAB ? 130 : U_M;           // positions per plane of the A stage
+    static constexpr int AROWS = SLAB ? 130 : U_M;           // positions per plane of an A box
     static constexpr int APLANE = AROWS * 16;
-    static constexpr int ABYTES = (KC / 8) * APLANE;
+    static constexpr int ABYTES = (KC / 8) * APLANE;         // one tile's A box
+    static constexpr int ASTRIDE = (ABYTES + 1023) / 1024 * 1024;
     static constexpr int BPLANE = NT * 16;                   // one plane of KC/8 of a tap's weights
     static constexpr int BTAP = (KC / 8) * BPLANE;
     static constexpr int BBYTES = TB * BTAP;
-    static constexpr int BOFF = (ABYTES + 1023) / 1024 * 1024;
+    static constexpr int BOFF = MT * ASTRIDE;
     static constexpr int STAGE = (BOFF + BBYTES + 1023) / 1024 * 1024;
     static constexpr int FIT = (U_SMEM - 1024) / STAGE;
     static constexpr int STAGES = FIT < 8 ? FIT : 8;
@@ -133,11 +136,12 @@ struct ConvLayout
                          OFF_ACCE = OFF_ACCF + 16, OFF_FIN = OFF_ACCE + 16, OFF_TMEM = OFF_FIN + 8,
                          OFF_ABORT = OFF_TMEM + 4, OFF_LAST = OFF_ABORT + 4;
     static constexpr int TOTAL = OFF_LAST + 4 * STAGES;
-    static constexpr int TCOLS = pow2_cols(2 * NT);          // two accumulators of NT columns
-    static constexpr uint32_t TX = (uint32_t)(ABYTES + BBYTES);
+    static constexpr int TCOLS = pow2_cols(2 * MT * NT);     // two sets of MT accumulators of NT columns
+    static constexpr int THREADS = 32 * (5 + MT);            // epilogue 0-3, TMA 4, MMA 5 .. 4 + MT
+    static constexpr uint32_t TX = (uint32_t)(MT * ABYTES + BBYTES);
     static_assert(NT % 32 == 0 && NT >= 32 && NT <= 256, "N: a multiple of 32 up to 256");
     static_assert(KC % 16 == 0 && KC <= 64, "K chunk");
-    static_assert(2 * NT <= 512, "tensor memory");
+    static_assert(2 * MT * NT <= 512, "tensor memory");
     static_assert(STAGES >= 2, "shared memory");
     static_assert(TOTAL <= U_SMEM, "shared memory");
 };
@@ -155,16 +159,16 @@ struct ConvArgs
     int* err;
 };
 
-template <int NT, int KC, bool SLAB>
-__global__ void __launch_bounds__(U_THREADS, 1)
+template <int NT, int KC, bool SLAB, int MT>
+__global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
     k_unet_conv(const __grid_constant__ CUtensorMap amap, const __grid_constant__ CUtensorMap bmap, const ConvArgs p)
 {
-    using L = ConvLayout<NT, KC, SLAB>;
+    using L = ConvLayout<NT, KC, SLAB, MT>;
     constexpr int S = L::STAGES;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int mtiles = (int)(p.V / U_M);
-    const int items = mtiles * (p.cout / NT);               // < 2^31 (launcher)
+    const int mgroups = (int)(p.V / (U_M * MT));             // items of MT consecutive tiles
+    const int items = mgroups * (p.cout / NT);               // < 2^31 (launcher)
     const int nkc = p.cin / KC;
     const int steps = (SLAB ? 9 : 27) * nkc;                 // stages per item
     const int NI = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -174,20 +178,20 @@ __global__ void __launch_bounds__(U_THREADS, 1)
     volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
     int* last = reinterpret_cast<int*>(smem + L::OFF_LAST);   // per slot: the last stage copied into it
 
-    for (int b = tid; b < S; b += U_THREADS) last[b] = -1;
+    for (int b = tid; b < S; b += L::THREADS) last[b] = -1;
     if (tid == 0)
     {
         for (int b = 0; b < S; ++b)
         {
-            bar_init(full0 + 8 * b, 1);    // expect_tx + the copies' bytes
-            bar_init(empty0 + 8 * b, 1);   // one commit of the MMAs that read the slot
+            bar_init(full0 + 8 * b, 1);     // expect_tx + the copies' bytes
+            bar_init(empty0 + 8 * b, MT);   // one commit per MMA warp that read the slot
         }
         for (int a = 0; a < 2; ++a)
         {
-            bar_init(accf0 + 8 * a, 1);      // one commit per item
+            bar_init(accf0 + 8 * a, MT);     // one commit per MMA warp and item
             bar_init(acce0 + 8 * a, 128);    // the 128 epilogue threads
         }
-        bar_init(fin, 1);
+        bar_init(fin, MT);
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
@@ -205,7 +209,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
 
     if (warp == 4)
     {
-        // ---- TMA: per stage the input box and the weights of its taps ----
+        // ---- TMA: per stage the MT tiles' input boxes and the weights of their taps ----
         const bool leader = elect_one();
         const uint64_t am = reinterpret_cast<uint64_t>(&amap), bm = reinterpret_cast<uint64_t>(&bmap);
         if (leader)
@@ -218,11 +222,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
         for (int k = 0; k < NI && !stop; ++k)
         {
             const int item = (int)blockIdx.x + k * (int)gridDim.x;
-            const int n = item / mtiles, m = item - n * mtiles;
-            const long long v0 = (long long)m * U_M;
-            const int x0 = (int)(v0 % p.X);
-            const long long r = v0 / p.X;
-            const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
+            const int n = item / mgroups, mg = item - n * mgroups;
             for (int j = 0; j < steps; ++j, ++step)
             {
                 const int b = step % S;
@@ -234,34 +234,44 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                 const int g = j / nkc, kc = j - g * nkc;
                 const int dz = SLAB ? g / 3 - 1 : g / 9 - 1;
                 const int dy = SLAB ? g % 3 - 1 : (g / 3) % 3 - 1;
-                const int xs = SLAB ? x0 - 1 : g % 3 - 1;          // the box's first x
                 const int tap0 = SLAB ? 3 * g : g;
                 if (leader)
                 {
                     last[b] = step;
                     expect_tx(full0 + 8 * b, L::TX);
                     const uint32_t dst = s_base + b * L::STAGE;
-                    tma5(dst, am, 0, xs, y0 + dy, z + dz, kc * (KC / 8), full0 + 8 * b);
+#pragma unroll
+                    for (int t = 0; t < MT; ++t)
+                    {
+                        const long long v0 = ((long long)mg * MT + t) * U_M;
+                        const int x0 = (int)(v0 % p.X);
+                        const long long r = v0 / p.X;
+                        const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
+                        const int xs = SLAB ? x0 - 1 : g % 3 - 1;          // the box's first x
+                        tma5(dst + t * L::ASTRIDE, am, 0, xs, y0 + dy, z + dz, kc * (KC / 8), full0 + 8 * b);
+                    }
                     tma4(dst + L::BOFF, bm, 0, n * NT, kc * (KC / 8), tap0, full0 + 8 * b);
                 }
                 __syncwarp();
             }
         }
     }
-    else if (warp == 5)
+    else if (warp >= 5)
     {
-        // ---- MMA: the whole warp runs the loop (warp-uniform descriptors), one lane issues ----
+        // ---- MMA (warp 5 + t: tile t of each item): the whole warp runs the loop (warp-uniform
+        // descriptors), one lane issues ----
         constexpr uint32_t idesc = idesc_f16(NT, false);
+        const int t = warp - 5;
         const bool leader = elect_one();
         bool go = true;
         int step = 0;
         for (int k = 0; k < NI && go; ++k)
         {
             const int a = k & 1;
-            // the epilogue has read this accumulator's item k - 2
+            // the epilogue has read this accumulator set's item k - 2
             if (k >= 2 && !warp_wait(acce0 + 8 * a, (uint32_t)(((k - 2) >> 1) & 1), abort)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint32_t dcol = tbase + (uint32_t)(a * NT);
+            const uint32_t dcol = tbase + (uint32_t)((a * MT + t) * NT);
             for (int j = 0; j < steps; ++j, ++step)
             {
                 const int b = step % S;
@@ -269,7 +279,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                 if (!go) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t abase = s_base + b * L::STAGE;
-                const uint64_t ad = umma_sdesc(abase, L::APLANE, 128);
+                const uint64_t ad = umma_sdesc(abase + t * L::ASTRIDE, L::APLANE, 128);
                 const uint64_t bd = umma_sdesc(abase + L::BOFF, L::BPLANE, 128);
 #pragma unroll
                 for (int sh = 0; sh < L::TB; ++sh)
@@ -287,7 +297,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
             if (leader) commit(accf0 + 8 * a);
             __syncwarp();
         }
-        // every MMA issued has completed once fin's first phase does
+        // every MMA this warp issued has completed once fin's first phase does
         if (leader) commit(fin);
         __syncwarp();
         if (!mbar_wait_bounded(fin, 0u)) *abort = 1;
@@ -299,49 +309,54 @@ __global__ void __launch_bounds__(U_THREADS, 1)
         for (int k = 0; k < NI; ++k)
         {
             const int item = (int)blockIdx.x + k * (int)gridDim.x;
-            const int n = item / mtiles, m = item - n * mtiles;
+            const int n = item / mgroups, mg = item - n * mgroups;
             const int a = k & 1;
             bool ready = false;
             if (lane == 0) ready = mbar_wait_or_abort(accf0 + 8 * a, (uint32_t)((k >> 1) & 1), abort);
             if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const long long v = (long long)m * U_M + tid;
-            const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(a * NT);
 #pragma unroll 1
-            for (int c0 = 0; c0 < NT; c0 += 32)
+            for (int t = 0; t < MT; ++t)
             {
-                uint32_t acc[32];
-                tmem_ld16(taddr + c0, acc);
-                tmem_ld16(taddr + c0 + 16, acc + 16);
-                asm volatile("tcgen05.wait::ld.sync.aligned;");
-                if (c0 + 32 >= NT)
+                const long long v = ((long long)mg * MT + t) * U_M + tid;
+                const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)((a * MT + t) * NT);
+#pragma unroll 1
+                for (int c0 = 0; c0 < NT; c0 += 32)
                 {
-                    // this thread has read all of the accumulator: hand it back to the MMA warp
-                    asm volatile("tcgen05.fence::before_thread_sync;");
-                    mbar_arrive(acce0 + 8 * a);
-                }
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                {
-                    const int ch = n * NT + c0 + 8 * q;   // first of the plane's 8 channels
-                    float f[8];
-#pragma unroll
-                    for (int e = 0; e < 8; ++e)
+                    uint32_t acc[32];
+                    tmem_ld16(taddr + c0, acc);
+                    tmem_ld16(taddr + c0 + 16, acc + 16);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;");
+                    if (t == MT - 1 && c0 + 32 >= NT)
                     {
-                        f[e] = __uint_as_float(acc[8 * q + e]) + (p.bias ? __ldg(p.bias + ch + e) : 0.0f);
-                        if (p.relu) f[e] = fmaxf(f[e], 0.0f);
+                        // this thread has read all of the set: hand it back to the MMA warps
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                        mbar_arrive(acce0 + 8 * a);
                     }
-                    if (p.mask)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
                     {
-                        const uint4 mk = __ldg(reinterpret_cast<const uint4*>(p.mask + ((long long)(ch >> 3) * p.V + v) * 8));
-                        const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(&mk);
+                        const int ch = n * NT + c0 + 8 * q;   // first of the plane's 8 channels
+                        float f[8];
 #pragma unroll
                         for (int e = 0; e < 8; ++e)
-                            if (!(__bfloat162float(mb[e]) > 0.0f)) f[e] = 0.0f;
+                        {
+                            f[e] = __uint_as_float(acc[8 * q + e]) + (p.bias ? __ldg(p.bias + ch + e) : 0.0f);
+                            if (p.relu) f[e] = fmaxf(f[e], 0.0f);
+                        }
+                        if (p.mask)
+                        {
+                            const uint4 mk =
+                                __ldg(reinterpret_cast<const uint4*>(p.mask + ((long long)(ch >> 3) * p.V + v) * 8));
+                            const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(&mk);
+#pragma unroll
+                            for (int e = 0; e < 8; ++e)
+                                if (!(__bfloat162float(mb[e]) > 0.0f)) f[e] = 0.0f;
+                        }
+                        *reinterpret_cast<uint4*>(p.y + ((long long)(p.y_plane0 + (ch >> 3)) * p.V + v) * 8) =
+                            make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
+                                       pack_bf16(f[6], f[7]));
                     }
-                    *reinterpret_cast<uint4*>(p.y + ((long long)(p.y_plane0 + (ch >> 3)) * p.V + v) * 8) =
-                        make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
-                                   pack_bf16(f[6], f[7]));
                 }
             }
         }
@@ -350,7 +365,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     // no copy may still be landing in shared memory when the CTA exits
-    for (int b = tid; b < S; b += U_THREADS)
+    for (int b = tid; b < S; b += L::THREADS)
     {
         const int s = last[b];
         if (s >= 0) mbar_wait_bounded(full0 + 8 * b, (uint32_t)((s / S) & 1));
@@ -1086,10 +1101,10 @@ bool weight_map(CUtensorMap* map, const void* base, int cin, int cout, int nt, i
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NT, int KC, bool SLAB>
+template <int NT, int KC, bool SLAB, int MT>
 tessgpu_status launch_conv(const void* x, const void* w, const ConvArgs& a, cudaStream_t s)
 {
-    using L = ConvLayout<NT, KC, SLAB>;
+    using L = ConvLayout<NT, KC, SLAB, MT>;
     static bool ready[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
@@ -1098,7 +1113,7 @@ tessgpu_status launch_conv(const void* x, const void* w, const ConvArgs& a, cuda
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (optin < smem_of(L::TOTAL)) return TESSGPU_ERR_UNSUPPORTED;
-        if (cudaFuncSetAttribute(k_unet_conv<NT, KC, SLAB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(k_unet_conv<NT, KC, SLAB, MT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem_of(L::TOTAL)) != cudaSuccess)
             return TESSGPU_ERR_CUDA;
         ready[dev] = true;
@@ -1107,10 +1122,10 @@ tessgpu_status launch_conv(const void* x, const void* w, const ConvArgs& a, cuda
     if (!act_map(&amap, x, a.X, a.Y, a.Z, a.cin, SLAB ? 130 : a.X, SLAB ? 1 : U_M / a.X, KC / 8) ||
         !weight_map(&bmap, w, a.cin, a.cout, NT, KC, L::TB))
         return TESSGPU_ERR_UNSUPPORTED;
-    const long long items = a.V / U_M * (a.cout / NT);
+    const long long items = a.V / (U_M * MT) * (a.cout / NT);
     const int sms = sm_count();
     const int grid = (int)(items < sms ? items : sms);
-    k_unet_conv<NT, KC, SLAB><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(amap, bmap, a);
+    k_unet_conv<NT, KC, SLAB, MT><<<grid, L::THREADS, smem_of(L::TOTAL), s>>>(amap, bmap, a);
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
@@ -1190,6 +1205,12 @@ bool unet_grid_ok(int X, int Y, int Z)
     return (X == 16 || X == 32 || X == 64) && Y % (U_M / X) == 0;   // tiles of whole x rows
 }
 
+int unet_tiles_env()
+{
+    const char* e = getenv("TESSGPU_UNET_TILES");
+    return e ? atoi(e) : 0;
+}
+
 int* err_flag()
 {
     int* e = nullptr;
@@ -1227,13 +1248,21 @@ extern "C" tessgpu_status tessgpu_unet_conv(const void* x, int X, int Y, int Z, 
             break;
         }
     const int kc = cin % 64 == 0 && !slab ? 64 : (cin % 32 == 0 ? 32 : 16);
-#define UC(NT_, KC_, SL_)                                                                                              \
-    if (nt == NT_ && kc == KC_ && slab == SL_) return launch_conv<NT_, KC_, SL_>(x, w, a, s);
-    UC(32, 16, true) UC(32, 32, true) UC(64, 32, true) UC(96, 32, true) UC(128, 32, true) UC(192, 32, true)
-    UC(256, 32, true)
-    UC(32, 16, false) UC(32, 32, false) UC(64, 32, false) UC(96, 32, false) UC(128, 32, false) UC(192, 32, false)
-    UC(256, 32, false)
-    UC(32, 64, false) UC(64, 64, false) UC(96, 64, false) UC(128, 64, false) UC(192, 64, false) UC(256, 64, false)
+    // tiles per item: four (N = 32) or two (N = 64) MMA-issuing warps on tiles that share the weights'
+    // stage, when the tile count divides; TESSGPU_UNET_TILES=1 forces one
+    const long long mtiles = a.V / U_M;
+    int mt = nt == 32 ? 4 : (nt == 64 ? 2 : 1);
+    if (mtiles % mt || unet_tiles_env() == 1) mt = 1;
+#define UC(NT_, KC_, SL_, MT_)                                                                                         \
+    if (nt == NT_ && kc == KC_ && slab == SL_ && mt == MT_) return launch_conv<NT_, KC_, SL_, MT_>(x, w, a, s);
+    UC(32, 16, true, 4) UC(32, 32, true, 4) UC(64, 32, true, 2) UC(96, 32, true, 1) UC(128, 32, true, 1)
+    UC(192, 32, true, 1) UC(256, 32, true, 1)
+    UC(32, 16, false, 4) UC(32, 32, false, 4) UC(64, 32, false, 2) UC(96, 32, false, 1) UC(128, 32, false, 1)
+    UC(192, 32, false, 1) UC(256, 32, false, 1)
+    UC(32, 64, false, 4) UC(64, 64, false, 2) UC(96, 64, false, 1) UC(128, 64, false, 1) UC(192, 64, false, 1)
+    UC(256, 64, false, 1)
+    UC(32, 16, true, 1) UC(32, 32, true, 1) UC(64, 32, true, 1) UC(32, 16, false, 1) UC(32, 32, false, 1)
+    UC(64, 32, false, 1) UC(32, 64, false, 1) UC(64, 64, false, 1)
 #undef UC
     return TESSGPU_ERR_UNSUPPORTED;
 }

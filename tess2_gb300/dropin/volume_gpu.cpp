@@ -19,6 +19,7 @@
 
 #include "tess/volume.h"
 #include "tess2_gb300.h"
+#include "dropin_common.h"
 
 namespace {
 
@@ -50,15 +51,6 @@ void check(tessgpu_status s, const char* what)
     }
 }
 
-int vertex_count(const tet_t* tets, int num_tets)
-{
-    int n = 0;
-    for (int t = 0; t < num_tets; ++t)
-        for (int k = 0; k < 4; ++k)
-            if (tets[t].verts[k] + 1 > n) n = tets[t].verts[k] + 1;
-    return n;
-}
-
 }  // namespace
 
 extern "C" void tess2_gb300_forget_volumes()
@@ -73,7 +65,7 @@ void fill_circumcenters(std::vector<float>& circumcenters, tet_t* tets, int num_
     std::lock_guard<std::mutex> lock(g_mutex);
     circumcenters.resize(3 * (size_t)num_tets);
     if (num_tets <= 0) return;
-    check(tessgpu_fill_circumcenters(context(), particles, vertex_count(tets, num_tets),
+    check(tessgpu_fill_circumcenters(context(), particles, tess2_gb300_vertex_count(tets, num_tets),
                                      reinterpret_cast<const int*>(tets), num_tets, circumcenters.data()),
           "fill_circumcenters");
 }
@@ -86,7 +78,7 @@ float volume(int v, int* verts_to_tets, tet_t* tets, int num_tets, float* partic
     if (g_kept.tets != tets || g_kept.num_tets != num_tets || g_kept.particles != particles ||
         g_kept.v2t != verts_to_tets || g_kept.cc != circumcenters.data())
     {
-        const int n = vertex_count(tets, num_tets);
+        const int n = tess2_gb300_vertex_count(tets, num_tets);
         g_kept.vol.assign(n > 0 ? n : 1, -1.0f);
         if (n > 0)
             check(tessgpu_volumes(context(), particles, n, reinterpret_cast<const int*>(tets), num_tets,

@@ -13,7 +13,7 @@ ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libdropin_test.so")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
-SRCS = [os.path.join(ROOT, "tess2_gb300", "dropin", f) for f in ("dense_gpu.cpp", "volume_gpu.cpp")]
+SRCS = [os.path.join(ROOT, "tess2_gb300", "dropin", f) for f in ("dense_gpu.cpp", "volume_gpu.cpp", "topology_gpu.cpp")]
 
 
 def _flags(tess_include):

@@ -7,6 +7,8 @@
 #include <cstring>
 #include <vector>
 #include "tess/dense.hpp"
+#include "tess/tess.h"
+#include "tess/tet-neighbors.h"
 #include "tess/volume.h"
 
 struct tess_shim_reduce_log tess_shim_reduce_record;
@@ -94,6 +96,23 @@ int dropin_dense(int alg_type, int nb, const drop_block* blocks, const int* glo_
 }
 
 // fill_circumcenters() then volume() of every vertex, as tools/draw.cpp calls them
+// complete() for every vertex, then fill_vert_to_tet() on a block made from the arrays
+void dropin_topology(const float* particles, int np, const int* tets, int nt, const int* v2t, int* complete_out,
+                     int* v2t_out)
+{
+    for (int v = 0; v < np; ++v) complete_out[v] = v2t[v] < 0 ? 0 : complete(v, (tet_t*)tets, nt, v2t[v]);
+    dblock_t b;
+    std::memset(&b, 0, sizeof(b));
+    b.num_particles = np;
+    b.particles = (float*)particles;
+    b.num_tets = nt;
+    b.tets = (tet_t*)tets;
+    b.vert_to_tet = (int*)std::malloc(sizeof(int));   // fill_vert_to_tet reallocs it, as the reference does
+    fill_vert_to_tet(&b);
+    std::memcpy(v2t_out, b.vert_to_tet, sizeof(int) * (size_t)np);
+    std::free(b.vert_to_tet);
+}
+
 void dropin_volumes(const float* particles, int np, const int* tets, int nt, const int* v2t, float* cc_out,
                     float* vol_out)
 {

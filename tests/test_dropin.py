@@ -1,6 +1,7 @@
-"""The compiled drop-in (tess2_gb300/dropin/dense_gpu.cpp, volume_gpu.cpp):
-tess2's own signatures -- dense(), WriteGrid(), dense_stats(), volume(),
-fill_circumcenters() -- over the GPU library.
+"""The compiled drop-in (tess2_gb300/dropin/dense_gpu.cpp, volume_gpu.cpp,
+topology_gpu.cpp): tess2's own signatures -- dense(), WriteGrid(),
+dense_stats(), volume(), fill_circumcenters(), and complete() and
+fill_vert_to_tet() with C linkage -- over the GPU library.
 
 CPU: the sources compile against tess2's own headers where a tess2 checkout
 is present (TESS2_REF, or a "reference" directory beside this repository),
@@ -43,7 +44,7 @@ def test_dropin_compiles_against_reference_headers():
     m = _build_mod()
     m.compile_against(inc)
     syms = []
-    for f in ("dense_gpu.cpp.ref.o", "volume_gpu.cpp.ref.o"):
+    for f in ("dense_gpu.cpp.ref.o", "volume_gpu.cpp.ref.o", "topology_gpu.cpp.ref.o"):
         out = subprocess.run(["nm", "-C", "--defined-only", os.path.join(m.OUT, f)], capture_output=True, text=True)
         syms += out.stdout.splitlines()
     text = "\n".join(syms)
@@ -55,6 +56,10 @@ def test_dropin_compiles_against_reference_headers():
                 "fill_circumcenters(std::vector<float, std::allocator<float> >&, tet_t*, int, float*)",
                 "volume(int, int*, tet_t*, int, float*, std::vector<float, std::allocator<float> > const&)"):
         assert sig in text, sig
+    # C linkage, as tess2 declares them (tet-neighbors.h, tess.h): unmangled symbols
+    raw = subprocess.run(["nm", "--defined-only", os.path.join(m.OUT, "topology_gpu.cpp.ref.o")], capture_output=True,
+                         text=True).stdout.split()
+    assert "complete" in raw and "fill_vert_to_tet" in raw
 
 
 @pytest.fixture(scope="module")
@@ -129,3 +134,22 @@ def test_dropin_volume_and_circumcenters(dropin, name):
                           cc.ctypes.data, vol.ctypes.data)
     assert np.array_equal(cc.view(np.uint32), np.ascontiguousarray(d["circumcenters"], np.float32).view(np.uint32))
     assert np.array_equal(vol.view(np.uint32), np.ascontiguousarray(d["volumes"], np.float32).view(np.uint32))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c1_uniform4096_seed1", "mix2048_seed7"])
+def test_dropin_complete_and_vert_to_tet(dropin, name):
+    """complete() per vertex equals the reference's (goldens); fill_vert_to_tet()
+    reallocs and fills vert_to_tet exactly as the reference (the last tet wins)."""
+    from tess2_gb300 import host
+    d = load_single(name)
+    p = np.ascontiguousarray(d["particles"], np.float32)
+    t = np.ascontiguousarray(d["tets"], np.int32)
+    v2t = np.ascontiguousarray(d["vert_to_tet"], np.int32)
+    comp = np.zeros(len(p), np.int32)
+    v2t_out = np.full(len(p), -7, np.int32)
+    dropin.dropin_topology(p.ctypes.data, ctypes.c_int(len(p)), t.ctypes.data, ctypes.c_int(len(t)), v2t.ctypes.data,
+                           comp.ctypes.data, v2t_out.ctypes.data)
+    assert np.array_equal(comp, np.ascontiguousarray(d["complete"], np.int32))
+    assert np.array_equal(v2t_out, host.vert_to_tet_host(len(p), t))
+    assert np.array_equal(v2t_out, v2t)

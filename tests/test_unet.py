@@ -127,6 +127,37 @@ def test_unet_conv_matches_oracle(grid, cin, cout):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("grid,cin,cout", [((128, 4, 3), 16, 32), ((128, 2, 2), 96, 64), ((64, 4, 2), 192, 64),
+                                           ((32, 8, 4), 64, 32)])
+def test_unet_conv_tiles_per_item_same_bits(grid, cin, cout):
+    """Several tiles per item (one MMA warp each, sharing the weights' stage)
+    give the same bits as one tile per item (TESSGPU_UNET_TILES=1)."""
+    import os
+    import torch
+    from tess2_gb300 import unet as U
+    X, Y, Z = grid
+    V = X * Y * Z
+    rng = np.random.default_rng(cin + 3 * cout)
+    x = _dev(_planar(_bf16(rng.standard_normal((Z, Y, X, cin)))), torch.bfloat16)
+    w = _dev((rng.standard_normal((27, cout, cin)) / np.sqrt(27 * cin)).astype(np.float32), torch.float32)
+    wf = torch.empty(27 * cout * cin, dtype=torch.bfloat16, device="cuda:0")
+    wb = torch.empty_like(wf)
+    U.pack_weights(w, cout, cin, wf, wb)
+    out = []
+    for tiles in (None, "1"):
+        if tiles:
+            os.environ["TESSGPU_UNET_TILES"] = tiles
+        try:
+            y = torch.zeros((cout // 8, V, 8), dtype=torch.bfloat16, device="cuda:0")
+            U.conv(x, grid, cin, wf, cout, y, relu=True)
+            U.check()
+            out.append(y.view(torch.int16).cpu().numpy())
+        finally:
+            os.environ.pop("TESSGPU_UNET_TILES", None)
+    assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("grid,cin,cout", [((128, 4, 3), 32, 96), ((64, 4, 2), 64, 192), ((32, 4, 2), 128, 384),
                                            ((16, 8, 4), 256, 128)])
 def test_unet_data_gradient_matches_oracle(grid, cin, cout):
