@@ -305,13 +305,16 @@ __device__ __noinline__ bool inside_exact(float a00, float a01, float a02, float
 //   T=float,  VAL64=true,  LIST=true   mixed fix-up pass over fix_list: the same
 //       exact classification, values from an FP64 evaluation
 //   T=double, VAL64=true,  LIST=false  FP64 mode: everything in FP64
-constexpr int SLICES = 16;  // tets with at most this many z slices visit only their cross-section rows
+// tets with at most SLICES z slices visit only their cross-section rows (the
+// launch variants with SL = 0 visit every row of the box and let the rows'
+// x intervals drop the empty ones: no per-slice set-up)
+constexpr int SLICES = 16;
 
 template <typename T> struct Vec4;
 template <> struct Vec4<float> { typedef float4 type; };
 template <> struct Vec4<double> { typedef double4_32a type; };
 
-template <typename T, bool VAL64, bool COMPACT, bool FLAT = false>
+template <typename T, bool VAL64, bool COMPACT, bool FLAT = false, int SL = SLICES>
 struct __align__(32) RasterSmem
 {
     typedef typename Vec4<T>::type T4;
@@ -324,7 +327,7 @@ struct __align__(32) RasterSmem
     float4 XA[32], XB[32], XG[32];           // face k's x bound on row (dy, dz): XA_k + XB_k dy + XG_k dz
     int4   I0[32];                           // ix0, ix1, iy0, ny
     int4   I1[32];                           // iz0, s, local tet index, face masks | sliced flag | row axis
-    int    SLC[SLICES][32];                  // per z slice: first row dy << 16 | rows
+    int    SLC[SL > 0 ? SL : 1][32];         // per z slice: first row dy << 16 | rows
     int    pre[33];                          // prefix of the tets' row counts
     // FLAT: a round's points spread over the lanes (per row of the round)
     T      RN[4][FLAT ? 32 : 1];             // the row's R_k
@@ -401,17 +404,25 @@ __device__ __forceinline__ void unperm3(int ra, V n0, V n1, V n2, V& x, V& y, V&
     z = ra == 2 ? n0 : n2;
 }
 
+// flat index of grid point (xi, yi, zi) given in the tet's row-axis order
+__device__ __forceinline__ size_t grid_index(const BlockGrid& g, int ra, int xi, int yi, int zi)
+{
+    int gx_, gy_, gz_;
+    unperm3(ra, xi, yi, zi, gx_, gy_, gz_);
+    return g.off + ((size_t)gz_ * g.n[1] + gy_) * g.n[0] + gx_;
+}
+
 // one grid point of a row: classify against the tet's four numerator planes
 // (exact arithmetic when the filter cannot decide) and write the
 // interpolated density when it is inside
 // xi, yi, zi and pyf, pzf are in the tet's row-axis order; hx, gx the row
 // axis' grid step and origin
 template <typename T, bool VAL64, typename SM>
-__device__ __forceinline__ void raster_point(const SM& S, int j, int xi, int yi, int zi, float pyf,
-                                             float pzf, const float4& A0, const float4& A1, const int4& I1,
-                                             const T* cx, const T* RN, const T* Bk, float hx, float gx, int ra,
-                                             const BlockGrid& g, const int4* tv, const float4* pos, float* grid,
-                                             int* owner, unsigned long long& nexact, unsigned long long& nassigned)
+__device__ __forceinline__ void raster_point(const SM& S, int j, int xi, float pyf, float pzf, const float4& A0,
+                                             const float4& A1, const int4& I1, const T* cx, const T* RN, const T* Bk,
+                                             float hx, float gx, int ra, size_t gi, const int4* tv,
+                                             const float4* pos, float* grid, int* owner,
+                                             unsigned long long& nexact, unsigned long long& nassigned)
 {
     typedef typename Vec4<T>::type T4;
     constexpr bool F32 = sizeof(T) == 4;
@@ -473,9 +484,6 @@ __device__ __forceinline__ void raster_point(const SM& S, int j, int xi, int yi,
         }
         f = (float)acc;
     }
-    int gx_, gy_, gz_;
-    unperm3(ra, xi, yi, zi, gx_, gy_, gz_);
-    const size_t gi = g.off + ((size_t)gz_ * g.n[1] + gy_) * g.n[0] + gx_;
     grid[gi] = f;
     if (owner)
         owner[gi] = I1.z;
@@ -484,7 +492,7 @@ __device__ __forceinline__ void raster_point(const SM& S, int j, int xi, int yi,
 
 // PB: every block has its own grid (independent sets); otherwise all blocks
 // share the call's grid g
-template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, bool FLAT, bool PB>
+template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, bool FLAT, bool PB, int SL = SLICES>
 __global__ void __launch_bounds__(NW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
@@ -501,10 +509,10 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
         gshared.n[d] = g.n[d];
     }
     gshared.off = 0;
-    __shared__ RasterSmem<T, VAL64, COMPACT, FLAT> smem[NW];
+    __shared__ RasterSmem<T, VAL64, COMPACT, FLAT, SL> smem[NW];
     constexpr bool F32 = sizeof(T) == 4;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    RasterSmem<T, VAL64, COMPACT, FLAT>& S = smem[wid];
+    RasterSmem<T, VAL64, COMPACT, FLAT, SL>& S = smem[wid];
     unsigned long long nexact = 0, nassigned = 0, nfix = 0, nrows = 0, ncand = 0;
     const int n = LIST ? *list_count : total;
     const int nchunks = (n + 31) / 32;
@@ -732,7 +740,7 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                             S.XG[lane] = make_float4(xg[0], xg[1], xg[2], xg[3]);
                         }
                         S.I0[lane] = make_int4(ilo[0], ihi[0], ilo[1], nyb);
-                        if (nzb <= SLICES)
+                        if (nzb <= SL)
                         {
                             // rows of slice z: the y range of the tet's cross-section there,
                             // from the edges that cross the plane, widened by a rounding
@@ -919,9 +927,15 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                                 cnt = i1 - i0 + 1;
                             }
                             else
-                                for (int xi = i0; xi <= i1; ++xi)
-                                    raster_point<T, VAL64>(S, j, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0],
-                                                           gmn[0], ra, gb, tv, pos, grid, owner, nexact, nassigned);
+                            {
+                                // the row's grid index advances by the row axis' stride
+                                const size_t stride = ra == 0 ? 1 : (ra == 1 ? (size_t)gb.n[0]
+                                                                             : (size_t)gb.n[0] * gb.n[1]);
+                                size_t gi = grid_index(gb, ra, i0, yi, zi);
+                                for (int xi = i0; xi <= i1; ++xi, gi += stride)
+                                    raster_point<T, VAL64>(S, j, xi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0], gmn[0],
+                                                           ra, gi, tv, pos, grid, owner, nexact, nassigned);
+                            }
                         }
                     }
                 }
@@ -963,8 +977,9 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
                             Bk[k] = ck.w;
                             RN[k] = S.RN[k][rs];
                         }
-                        raster_point<T, VAL64>(S, jj, xi, yi, zi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0], gmn[0], ra,
-                                               gb, tv, pos, grid, owner, nexact, nassigned);
+                        raster_point<T, VAL64>(S, jj, xi, pyf, pzf, A0, A1, I1, cx, RN, Bk, gst[0], gmn[0], ra,
+                                               grid_index(gb, ra, xi, yi, zi), tv, pos, grid, owner, nexact,
+                                               nassigned);
                     }
                 }
                 __syncwarp();
@@ -1021,7 +1036,8 @@ void launch_densities(const StarSum* W, int n, float mass, double inv_scale, flo
 // the caller times them.
 //   0..2: per-lane rows, 4/5/6 blocks per SM    3: compact, 5 blocks
 //   4..5: compact + flat, 4/5 blocks per SM
-constexpr int N_RASTER_VARIANTS = 6;
+//   6..7: per-lane rows, 4/5 blocks per SM, every row of the box (no slices)
+constexpr int N_RASTER_VARIANTS = 8;
 
 template <typename T, bool VAL64, bool LIST>
 static void raster_variant(int variant, long long work, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
@@ -1040,18 +1056,19 @@ static void raster_variant(int variant, long long work, cudaStream_t s, const Bl
             t0);
         return;
     }
-#define TG_RASTER(MB, C, F)                                                                                        \
-    k_raster<T, VAL64, LIST, MB, NW, C, F, false><<<nblk, NW * 32, 0, s>>>(d_blocks, nb, total, list, list_count, \
-                                                                             pos, tv, rho32, rho64, g, tau, grid,   \
-                                                                             owner, fix_list, fix_count, st, t0)
+#define TG_RASTER(MB, C, F, SL_)                                                                                   \
+    k_raster<T, VAL64, LIST, MB, NW, C, F, false, SL_><<<nblk, NW * 32, 0, s>>>(                                   \
+        d_blocks, nb, total, list, list_count, pos, tv, rho32, rho64, g, tau, grid, owner, fix_list, fix_count, st, t0)
     switch (variant)
     {
-    case 1: TG_RASTER(5, false, false); break;
-    case 2: TG_RASTER(6, false, false); break;
-    case 3: TG_RASTER(5, true, false); break;
-    case 4: TG_RASTER(4, true, true); break;
-    case 5: TG_RASTER(5, true, true); break;
-    default: TG_RASTER(4, false, false); break;
+    case 1: TG_RASTER(5, false, false, SLICES); break;
+    case 2: TG_RASTER(6, false, false, SLICES); break;
+    case 3: TG_RASTER(5, true, false, SLICES); break;
+    case 4: TG_RASTER(4, true, true, SLICES); break;
+    case 5: TG_RASTER(5, true, true, SLICES); break;
+    case 6: TG_RASTER(4, false, false, 0); break;
+    case 7: TG_RASTER(5, false, false, 0); break;
+    default: TG_RASTER(4, false, false, SLICES); break;
     }
 #undef TG_RASTER
 }

@@ -556,6 +556,33 @@ def _dtfe_batch(ctx, blocks, gni, mode, want_owner=True):
     return g, owner, info
 
 
+_ROW_VARIANT_GRIDS = {}
+
+
+@pytest.mark.parametrize("variant", ["0", "1", "2", "3", "4", "5", "6", "7"])
+@pytest.mark.parametrize("mode,tol", [(0, 1e-6), (1, 1e-12)])
+def test_dtfe_row_variants_vs_oracle(oracle, variant, mode, tol):
+    """Every launch variant of the row rasteriser the autotuner may pick
+    (blocks per SM, compact, flat, with and without per-slice rows): owners
+    equal to the FP64 oracle's, values within the mode's bound, and the same
+    grid bits as variant 0."""
+    d, blocks = load_blocks("blocks8_mix8192_seed3")
+    gni = [int(x) for x in d["glo_num_idx"]]
+    ref = oracle.dtfe(blocks, gni)
+    ctx, old = _fresh_ctx({"TESSGPU_RASTER": "rows", "TESSGPU_RASTER_VARIANT": variant})
+    try:
+        g, owner, info = _dtfe_batch(ctx, blocks, gni, mode)
+    finally:
+        _restore(old)
+    assert info["raster_variant"] == int(variant)
+    assert np.array_equal(owner, ref["owner"])
+    assert info["grid_pts_assigned"] == ref["assigned"]
+    assert rel_l2(g, ref["grid"]) < tol
+    assert np.all(g[ref["owner"] < 0] == 0)
+    first = _ROW_VARIANT_GRIDS.setdefault(mode, g)
+    assert np.array_equal(g.view(np.uint32), first.view(np.uint32))
+
+
 @pytest.mark.parametrize("variant", ["0", "1", "2", "3"])
 @pytest.mark.parametrize("mode,tol", [(0, 1e-6), (1, 1e-12)])
 def test_dtfe_brick_variants_vs_oracle(oracle, variant, mode, tol):
