@@ -119,9 +119,11 @@ template <int NT, int KC, bool SLAB, int MT>
 struct ConvLayout
 {
     static constexpr int TB = SLAB ? 3 : 1;                  // taps per stage
-    static constexpr int AROWS = SLAB ? 130 : U_M;           // positions per plane of an A box
-    static constexpr int APLANE = AROWS * 16;
-    static constexpr int ABYTES = (KC / 8) * APLANE;         // one tile's A box
+    // one plane of a tile's input: TAP, 128 rows of 16 bytes; SLAB, the 128 rows x0 .. x0 + 127 at
+    // byte 128 (a 128-byte-aligned box) with the halo rows x0 - 1 at 112 and x0 + 128 at 2176
+    static constexpr int APLANE = SLAB ? 2304 : U_M * 16;
+    static constexpr int AROW0 = SLAB ? 112 : 0;             // byte of the A operand's first row
+    static constexpr int ABYTES = (KC / 8) * APLANE;         // one tile's input
     static constexpr int ASTRIDE = (ABYTES + 1023) / 1024 * 1024;
     static constexpr int BPLANE = NT * 16;                   // one plane of KC/8 of a tap's weights
     static constexpr int BTAP = (KC / 8) * BPLANE;
@@ -138,9 +140,11 @@ struct ConvLayout
     static constexpr int TOTAL = OFF_LAST + 4 * STAGES;
     static constexpr int TCOLS = pow2_cols(2 * MT * NT);     // two sets of MT accumulators of NT columns
     static constexpr int THREADS = 32 * (5 + MT);            // epilogue 0-3, TMA 4, MMA 5 .. 4 + MT
-    static constexpr uint32_t TX = (uint32_t)(MT * ABYTES + BBYTES);
+    // bytes the copies deliver per stage (the halo rows are stored by the TMA warp's lanes)
+    static constexpr uint32_t TX = (uint32_t)(MT * (KC / 8) * U_M * 16 + BBYTES);
     static_assert(NT % 32 == 0 && NT >= 32 && NT <= 256, "N: a multiple of 32 up to 256");
     static_assert(KC % 16 == 0 && KC <= 64, "K chunk");
+    static_assert(!SLAB || MT * (KC / 8) * 2 <= 32, "one halo row per lane");
     static_assert(2 * MT * NT <= 512, "tensor memory");
     static_assert(STAGES >= 2, "shared memory");
     static_assert(TOTAL <= U_SMEM, "shared memory");
@@ -148,6 +152,7 @@ struct ConvLayout
 
 struct ConvArgs
 {
+    const __nv_bfloat16* x;         // the input (cin channels), for the slab's halo rows
     int X, Y, Z;                    // grid (X a multiple of 128 for SLAB, X in {16, 32, 64} for TAP)
     int cin, cout;                  // cin a multiple of KC, cout a multiple of NT
     long long V;                    // X * Y * Z, a multiple of 128
@@ -171,6 +176,7 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
     const int items = mgroups * (p.cout / NT);               // < 2^31 (launcher)
     const int nkc = p.cin / KC;
     const int steps = (SLAB ? 9 : 27) * nkc;                 // stages per item
+    const bool split = !SLAB && p.X == 64;                   // tile rows copied as two halves
     const int NI = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const uint32_t s_base = smem_u32(smem);
     const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY;
@@ -183,8 +189,8 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
     {
         for (int b = 0; b < S; ++b)
         {
-            bar_init(full0 + 8 * b, 1);     // expect_tx + the copies' bytes
-            bar_init(empty0 + 8 * b, MT);   // one commit per MMA warp that read the slot
+            bar_init(full0 + 8 * b, SLAB ? 2 : 1);   // expect_tx + the copies' bytes (+ the halo rows)
+            bar_init(empty0 + 8 * b, MT);            // one commit per MMA warp that read the slot
         }
         for (int a = 0; a < 2; ++a)
         {
@@ -217,12 +223,34 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
             asm volatile("prefetch.tensormap [%0];" ::"l"(am) : "memory");
             asm volatile("prefetch.tensormap [%0];" ::"l"(bm) : "memory");
         }
+        // SLAB: lane l < 2 MT KC/8 keeps one halo row (tile t, plane q, side) in a register, loaded a
+        // stage ahead so that its latency overlaps the wait for the next ring slot
+        const int nh = MT * (KC / 8) * 2;
+        const int ht = lane / (2 * (KC / 8)), hq = (lane >> 1) % (KC / 8), hside = lane & 1;
+        auto halo_load = [&](int mg, int j) {
+            uint4 h = make_uint4(0, 0, 0, 0);
+            if (lane < nh)
+            {
+                const int g = j / nkc, kc = j - g * nkc;
+                const long long v0 = ((long long)mg * MT + ht) * U_M;
+                const int x0 = (int)(v0 % p.X);
+                const long long r = v0 / p.X;
+                const int y = (int)(r % p.Y) + g % 3 - 1, z = (int)(r / p.Y) + g / 3 - 1;
+                const int x = hside ? x0 + U_M : x0 - 1;
+                if (x >= 0 && x < p.X && y >= 0 && y < p.Y && z >= 0 && z < p.Z)
+                    h = __ldg(reinterpret_cast<const uint4*>(p.x) + (long long)(kc * (KC / 8) + hq) * p.V +
+                              ((long long)z * p.Y + y) * p.X + x);
+            }
+            return h;
+        };
         bool stop = false;
         int step = 0;
         for (int k = 0; k < NI && !stop; ++k)
         {
             const int item = (int)blockIdx.x + k * (int)gridDim.x;
             const int n = item / mgroups, mg = item - n * mgroups;
+            uint4 hrow = make_uint4(0, 0, 0, 0);
+            if (SLAB) hrow = halo_load(mg, 0);
             for (int j = 0; j < steps; ++j, ++step)
             {
                 const int b = step % S;
@@ -234,12 +262,13 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
                 const int g = j / nkc, kc = j - g * nkc;
                 const int dz = SLAB ? g / 3 - 1 : g / 9 - 1;
                 const int dy = SLAB ? g % 3 - 1 : (g / 3) % 3 - 1;
+                const int dx = SLAB ? 0 : g % 3 - 1;
                 const int tap0 = SLAB ? 3 * g : g;
+                const uint32_t dst = s_base + b * L::STAGE;
                 if (leader)
                 {
                     last[b] = step;
                     expect_tx(full0 + 8 * b, L::TX);
-                    const uint32_t dst = s_base + b * L::STAGE;
 #pragma unroll
                     for (int t = 0; t < MT; ++t)
                     {
@@ -247,10 +276,41 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
                         const int x0 = (int)(v0 % p.X);
                         const long long r = v0 / p.X;
                         const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
-                        const int xs = SLAB ? x0 - 1 : g % 3 - 1;          // the box's first x
-                        tma5(dst + t * L::ASTRIDE, am, 0, xs, y0 + dy, z + dz, kc * (KC / 8), full0 + 8 * b);
+                        const uint32_t ta = dst + t * L::ASTRIDE;
+                        if (SLAB)
+                        {
+                            // per plane one box of 4 rows of 32 voxels (512 bytes each)
+#pragma unroll
+                            for (int q = 0; q < KC / 8; ++q)
+                                tma5(ta + q * L::APLANE + 128, am, 0, x0 >> 5, y0 + dy, z + dz, kc * (KC / 8) + q,
+                                     full0 + 8 * b);
+                        }
+                        else if (split)
+                        {
+                            // X = 64: each plane as two boxes of 32 voxels a row (M order: half, row, x)
+                            for (int q = 0; q < KC / 8; ++q)
+                                for (int h = 0; h < 2; ++h)
+                                    tma4(ta + q * L::APLANE + h * 1024, am, 8 * dx + 256 * h, y0 + dy, z + dz,
+                                         kc * (KC / 8) + q, full0 + 8 * b);
+                        }
+                        else
+                            // X of 16 or 32: rows of X voxels x 8 channels; the box starts at x = dx and the
+                            // x halo comes back as zeros
+                            tma4(ta, am, 8 * dx, y0 + dy, z + dz, kc * (KC / 8), full0 + 8 * b);
                     }
-                    tma4(dst + L::BOFF, bm, 0, n * NT, kc * (KC / 8), tap0, full0 + 8 * b);
+                    tma4(dst + L::BOFF, bm, 0, n * (NT / 32), kc * (KC / 8), tap0, full0 + 8 * b);
+                }
+                if (SLAB)
+                {
+                    // the halo rows x0 - 1 and x0 + 128 of every tile and plane (zero outside the
+                    // grid), made visible to the tensor cores; then the next stage's rows are loaded
+                    if (lane < nh)
+                        *reinterpret_cast<uint4*>(smem + (dst - s_base) + ht * L::ASTRIDE + hq * L::APLANE +
+                                                  (hside ? 128 + U_M * 16 : 112)) = hrow;
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(full0 + 8 * b);
+                    if (j + 1 < steps) hrow = halo_load(mg, j + 1);
                 }
                 __syncwarp();
             }
@@ -279,7 +339,7 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
                 if (!go) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t abase = s_base + b * L::STAGE;
-                const uint64_t ad = umma_sdesc(abase + t * L::ASTRIDE, L::APLANE, 128);
+                const uint64_t ad = umma_sdesc(abase + t * L::ASTRIDE + L::AROW0, L::APLANE, 128);
                 const uint64_t bd = umma_sdesc(abase + L::BOFF, L::BPLANE, 128);
 #pragma unroll
                 for (int sh = 0; sh < L::TB; ++sh)
@@ -318,7 +378,9 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
 #pragma unroll 1
             for (int t = 0; t < MT; ++t)
             {
-                const long long v = ((long long)mg * MT + t) * U_M + tid;
+                // tensor-memory lane tid = the tile's row tid: voxel tid, or for X = 64 (half, row, x)
+                const int vt = split ? ((tid >> 5) & 1) * 64 + (tid >> 6) * 32 + (tid & 31) : tid;
+                const long long v = ((long long)mg * MT + t) * U_M + vt;
                 const uint32_t taddr = tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)((a * MT + t) * NT);
 #pragma unroll 1
                 for (int c0 = 0; c0 < NT; c0 += 32)
@@ -385,8 +447,10 @@ struct WgradLayout
     static constexpr int TG = SLAB ? 3 : 1;                  // taps per item
     static constexpr int APLANE = U_M * 16;                  // one plane of the output-gradient tile
     static constexpr int ABYTES = 16 * APLANE;               // 16 planes: M = 128 output channels
-    static constexpr int XROWS = SLAB ? 130 : U_M;
-    static constexpr int XPLANE = XROWS * 16;
+    // one plane of the input: SLAB, voxels x0 .. x0 + 127 at byte 128 (a 128-byte-aligned box) with the
+    // halo rows x0 - 1 at 112 and x0 + 128 at 2176; otherwise 128 rows from byte 0
+    static constexpr int XPLANE = SLAB ? 2304 : U_M * 16;
+    static constexpr int XROW0 = SLAB ? 112 : 0;
     static constexpr int BBYTES = (NTW / 8) * XPLANE;
     static constexpr int BOFF = ABYTES;
     static constexpr int STAGE = (BOFF + BBYTES + 1023) / 1024 * 1024;
@@ -399,8 +463,9 @@ struct WgradLayout
                          OFF_ABORT = OFF_TMEM + 4, OFF_LAST = OFF_ABORT + 4;
     static constexpr int TOTAL = OFF_LAST + 4 * STAGES;
     static constexpr int TCOLS = pow2_cols(TG * NTW);
-    static constexpr uint32_t TX = (uint32_t)(ABYTES + BBYTES);
+    static constexpr uint32_t TX = (uint32_t)(ABYTES + (NTW / 8) * U_M * 16);   // the copies' bytes
     static_assert(NTW % 16 == 0 && NTW >= 16 && NTW <= 256, "N");
+    static_assert(!SLAB || NTW / 8 * 2 <= 32, "one halo row per lane");
     static_assert(TG * NTW <= 512, "tensor memory");
     static_assert(STAGES >= 2, "shared memory");
     static_assert(TOTAL <= U_SMEM, "shared memory");
@@ -408,6 +473,8 @@ struct WgradLayout
 
 struct WgradArgs
 {
+    const __nv_bfloat16* x;   // the input, for the slab's halo rows
+    int merged;               // not SLAB: 1 = boxes of whole x rows (X <= 32), 0 = 16-byte rows (X = 64)
     int X, Y, Z;
     int cin, cout;
     long long V;
@@ -440,7 +507,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
     {
         for (int b = 0; b < S; ++b)
         {
-            bar_init(full0 + 8 * b, 1);
+            bar_init(full0 + 8 * b, SLAB ? 2 : 1);   // expect_tx + the copies (+ the halo rows)
             bar_init(empty0 + 8 * b, 1);
         }
         bar_init(accf, 1);
@@ -462,13 +529,15 @@ __global__ void __launch_bounds__(U_THREADS, 1)
     const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
 
     // item -> (tap group grp, c_out tile ct, c_in tile nt, chunk) and the chunk's tiles [m0, m1)
+    // the tap group varies fastest: CTAs running at the same time read the same voxel chunk
+    // (from L2 after the first), each for its own taps
     auto decode = [&](int item, int& grp, int& ct, int& nt, int& m0, int& m1) {
-        const int chunk = item % p.nch;
-        int rest = item / p.nch;
-        nt = rest % NTN;
-        rest /= NTN;
+        grp = item % NG;
+        int rest = item / NG;
         ct = rest % CT;
-        grp = rest / CT;
+        rest /= CT;
+        nt = rest % NTN;
+        const int chunk = rest / NTN;
         m0 = (int)((long long)chunk * mtiles / p.nch);
         m1 = (int)((long long)(chunk + 1) * mtiles / p.nch);
     };
@@ -483,6 +552,23 @@ __global__ void __launch_bounds__(U_THREADS, 1)
             asm volatile("prefetch.tensormap [%0];" ::"l"(dm) : "memory");
             asm volatile("prefetch.tensormap [%0];" ::"l"(xm) : "memory");
         }
+        // SLAB: lane l < 2 NTW/8 keeps one halo row (plane l / 2, side l % 2) of the input slab in a
+        // register, loaded a tile ahead so that its latency overlaps the wait for the next slot
+        const int nh = SLAB ? (NTW / 8) * 2 : 0, hq = lane >> 1, hside = lane & 1;
+        auto halo_load = [&](int m, int nt, int dy, int dz) {
+            uint4 h = make_uint4(0, 0, 0, 0);
+            if (lane < nh)
+            {
+                const long long v0 = (long long)m * U_M;
+                const int x0 = (int)(v0 % p.X);
+                const long long r = v0 / p.X;
+                const int y = (int)(r % p.Y) + dy, z = (int)(r / p.Y) + dz, x = hside ? x0 + U_M : x0 - 1;
+                if (x >= 0 && x < p.X && y >= 0 && y < p.Y && z >= 0 && z < p.Z)
+                    h = __ldg(reinterpret_cast<const uint4*>(p.x) + (long long)(nt * (NTW / 8) + hq) * p.V +
+                              ((long long)z * p.Y + y) * p.X + x);
+            }
+            return h;
+        };
         bool stop = false;
         int step = 0;
         for (int k = 0; k < NI && !stop; ++k)
@@ -491,6 +577,9 @@ __global__ void __launch_bounds__(U_THREADS, 1)
             decode((int)blockIdx.x + k * (int)gridDim.x, grp, ct, nt, m0, m1);
             const int dz = SLAB ? grp / 3 - 1 : grp / 9 - 1;
             const int dy = SLAB ? grp % 3 - 1 : (grp / 3) % 3 - 1;
+            const int dx = SLAB ? 0 : grp % 3 - 1;
+            uint4 hrow = make_uint4(0, 0, 0, 0);
+            if (SLAB) hrow = halo_load(m0, nt, dy, dz);
             for (int m = m0; m < m1; ++m, ++step)
             {
                 const int b = step % S;
@@ -503,14 +592,43 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                 const int x0 = (int)(v0 % p.X);
                 const long long r = v0 / p.X;
                 const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
+                const uint32_t dst = s_base + b * L::STAGE;
                 if (leader)
                 {
                     last[b] = step;
                     expect_tx(full0 + 8 * b, L::TX);
-                    const uint32_t dst = s_base + b * L::STAGE;
-                    tma5(dst, dm, 0, x0, y0, z, ct * 16, full0 + 8 * b);
-                    tma5(dst + L::BOFF, xm, 0, SLAB ? x0 - 1 : grp % 3 - 1, y0 + dy, z + dz, nt * (NTW / 8),
-                         full0 + 8 * b);
+                    if (SLAB)
+                    {
+                        // the output-gradient planes (16, those past c_out read as zeros) and each input
+                        // plane as boxes of 4 rows of 32 voxels (512-byte rows)
+                        tma5(dst, dm, 0, x0 >> 5, y0, z, ct * 16, full0 + 8 * b);
+#pragma unroll
+                        for (int q = 0; q < NTW / 8; ++q)
+                            tma5(dst + L::BOFF + q * L::XPLANE + 128, xm, 0, x0 >> 5, y0 + dy, z + dz,
+                                 nt * (NTW / 8) + q, full0 + 8 * b);
+                    }
+                    else if (p.merged)
+                    {
+                        // whole x rows (x and channel merged); the input box starts at x = dx, its x halo
+                        // reads as zeros
+                        tma4(dst, dm, 0, y0, z, ct * 16, full0 + 8 * b);
+                        tma4(dst + L::BOFF, xm, 8 * dx, y0 + dy, z + dz, nt * (NTW / 8), full0 + 8 * b);
+                    }
+                    else
+                    {
+                        tma5(dst, dm, 0, x0, y0, z, ct * 16, full0 + 8 * b);
+                        tma5(dst + L::BOFF, xm, 0, dx, y0 + dy, z + dz, nt * (NTW / 8), full0 + 8 * b);
+                    }
+                }
+                if (SLAB)
+                {
+                    if (lane < nh)
+                        *reinterpret_cast<uint4*>(smem + (dst - s_base) + L::BOFF + hq * L::XPLANE +
+                                                  (hside ? 128 + U_M * 16 : 112)) = hrow;
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(full0 + 8 * b);
+                    if (m + 1 < m1) hrow = halo_load(m + 1, nt, dy, dz);
                 }
                 __syncwarp();
             }
@@ -538,7 +656,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t abase = s_base + b * L::STAGE;
                 const uint64_t ad = umma_sdesc(abase, 128, L::APLANE);
-                const uint64_t bd = umma_sdesc(abase + L::BOFF, 128, L::XPLANE);
+                const uint64_t bd = umma_sdesc(abase + L::BOFF + L::XROW0, 128, L::XPLANE);
 #pragma unroll
                 for (int sh = 0; sh < L::TG; ++sh)
 #pragma unroll
@@ -664,11 +782,12 @@ __global__ void __launch_bounds__(U_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
 
+    // the tap group varies fastest (CTAs running together share the voxel chunk in L2)
     auto decode = [&](int item, int& grp, int& nt, int& m0, int& m1) {
-        const int chunk = item % p.nch;
-        const int rest = item / p.nch;
+        grp = item % NG;
+        const int rest = item / NG;
         nt = rest % NTN;
-        grp = rest / NTN;
+        const int chunk = rest / NTN;
         m0 = (int)((long long)chunk * mtiles / p.nch);
         m1 = (int)((long long)(chunk + 1) * mtiles / p.nch);
     };
@@ -1087,14 +1206,47 @@ bool act_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// packed weights [27][cin/8][cout][8] as (8, cout, cin / 8, 27), box (8, nt, kc / 8, tb)
+// an activation (X a multiple of 32) as (256 = 32 voxels x 8 channels, X / 32, Y, Z, c / 8), box
+// (256, 4, 1, 1, bp): bp planes of 128 voxels of an x row in 512-byte rows
+bool row_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int bp = 1)
+{
+    const EncodeTiled encode = tensor_map_encoder();
+    if (!encode || ((uintptr_t)base & 15) || X % 32) return false;
+    const cuuint64_t dims[5] = { 256, (cuuint64_t)(X / 32), (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(c / 8) };
+    const cuuint64_t strides[4] = { 512, (cuuint64_t)X * 16, (cuuint64_t)X * Y * 16, (cuuint64_t)X * Y * Z * 16 };
+    const cuuint32_t box[5] = { 256, 4, 1, 1, (cuuint32_t)bp };
+    const cuuint32_t estride[5] = { 1, 1, 1, 1, 1 };
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// an activation with X of 16, 32 or 64 as (8 X = x and channel merged, Y, Z, c / 8): a box of
+// 128 / X rows (X <= 32: all of a row, bp planes; X = 64: half a row, one plane); a box starting at
+// x = -1 or ending at x = X reads zeros there (the x halo)
+bool merged_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int bp)
+{
+    const EncodeTiled encode = tensor_map_encoder();
+    if (!encode || ((uintptr_t)base & 15) || (X != 16 && X != 32 && X != 64)) return false;
+    const cuuint64_t dims[4] = { (cuuint64_t)(8 * X), (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(c / 8) };
+    const cuuint64_t strides[3] = { (cuuint64_t)X * 16, (cuuint64_t)X * Y * 16, (cuuint64_t)X * Y * Z * 16 };
+    const cuuint32_t box[4] = { (cuuint32_t)(X == 64 ? 256 : 8 * X), (cuuint32_t)(U_M / X), 1,
+                                (cuuint32_t)(X == 64 ? 1 : bp) };
+    const cuuint32_t estride[4] = { 1, 1, 1, 1 };
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// packed weights [27][cin/8][cout][8] as (256 = 32 output channels x 8, cout / 32, cin / 8, 27), box
+// (256, nt / 32, kc / 8, tb): 512-byte rows, landing as [tap][plane][nt][8] like a box of 16-byte rows
 bool weight_map(CUtensorMap* map, const void* base, int cin, int cout, int nt, int kc, int tb)
 {
     const EncodeTiled encode = tensor_map_encoder();
-    if (!encode || ((uintptr_t)base & 15)) return false;
-    const cuuint64_t dims[4] = { 8, (cuuint64_t)cout, (cuuint64_t)(cin / 8), 27 };
-    const cuuint64_t strides[3] = { 16, (cuuint64_t)cout * 16, (cuuint64_t)(cin / 8) * cout * 16 };
-    const cuuint32_t box[4] = { 8, (cuuint32_t)nt, (cuuint32_t)(kc / 8), (cuuint32_t)tb };
+    if (!encode || ((uintptr_t)base & 15) || cout % 32 || nt % 32) return false;
+    const cuuint64_t dims[4] = { 256, (cuuint64_t)(cout / 32), (cuuint64_t)(cin / 8), 27 };
+    const cuuint64_t strides[3] = { 512, (cuuint64_t)cout * 16, (cuuint64_t)(cin / 8) * cout * 16 };
+    const cuuint32_t box[4] = { 256, (cuuint32_t)(nt / 32), (cuuint32_t)(kc / 8), (cuuint32_t)tb };
     const cuuint32_t estride[4] = { 1, 1, 1, 1 };
     return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, estride,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1119,7 +1271,7 @@ tessgpu_status launch_conv(const void* x, const void* w, const ConvArgs& a, cuda
         ready[dev] = true;
     }
     CUtensorMap amap, bmap;
-    if (!act_map(&amap, x, a.X, a.Y, a.Z, a.cin, SLAB ? 130 : a.X, SLAB ? 1 : U_M / a.X, KC / 8) ||
+    if (!(SLAB ? row_map(&amap, x, a.X, a.Y, a.Z, a.cin) : merged_map(&amap, x, a.X, a.Y, a.Z, a.cin, KC / 8)) ||
         !weight_map(&bmap, w, a.cin, a.cout, NT, KC, L::TB))
         return TESSGPU_ERR_UNSUPPORTED;
     const long long items = a.V / (U_M * MT) * (a.cout / NT);
@@ -1147,9 +1299,16 @@ tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStre
         ready[dev] = true;
     }
     CUtensorMap dymap, xmap;
-    if (!act_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, SLAB ? U_M : a.X, SLAB ? 1 : U_M / a.X, 16) ||
-        !act_map(&xmap, x, a.X, a.Y, a.Z, a.cin, SLAB ? 130 : a.X, SLAB ? 1 : U_M / a.X, NTW / 8))
-        return TESSGPU_ERR_UNSUPPORTED;
+    a.merged = !SLAB && a.X <= 32;
+    bool ok;
+    if (SLAB)
+        ok = row_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16) && row_map(&xmap, x, a.X, a.Y, a.Z, a.cin, 1);
+    else if (a.merged)
+        ok = merged_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16) && merged_map(&xmap, x, a.X, a.Y, a.Z, a.cin, NTW / 8);
+    else
+        ok = act_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, a.X, U_M / a.X, 16) &&
+             act_map(&xmap, x, a.X, a.Y, a.Z, a.cin, a.X, U_M / a.X, NTW / 8);
+    if (!ok) return TESSGPU_ERR_UNSUPPORTED;
     const int sms = sm_count();
     const long long mt = a.V / U_M;
     const long long base = (long long)(SLAB ? 9 : 27) * ((a.cout + 127) / 128) * (a.cin / NTW);
@@ -1229,6 +1388,7 @@ extern "C" tessgpu_status tessgpu_unet_conv(const void* x, int X, int Y, int Z, 
     int* err = err_flag();
     if (!err) return TESSGPU_ERR_CUDA;
     ConvArgs a;
+    a.x = (const __nv_bfloat16*)x;
     a.X = X; a.Y = Y; a.Z = Z;
     a.cin = cin; a.cout = cout;
     a.V = (long long)X * Y * Z;
@@ -1293,7 +1453,11 @@ extern "C" tessgpu_status tessgpu_unet_wgrad(const void* x, const void* dy, int 
             break;
         }
     tessgpu_status st = TESSGPU_ERR_UNSUPPORTED;
-    if (cout == 16 || cout == 32 || cout == 64)
+    a.x = (const __nv_bfloat16*)x;
+    a.merged = 0;
+    // taps stacked along M where the per-tap-group kernel would read its operands in 16-byte rows
+    // (X = 64) and M = 128 would be mostly padding
+    if (!slab && X == 64 && (cout == 16 || cout == 32 || cout == 64))
     {
         // taps stacked along M: the input's N tile up to 256 channels
         int nts = 16;
