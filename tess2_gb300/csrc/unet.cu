@@ -483,7 +483,7 @@ struct WgradArgs
     int* err;
 };
 
-template <int NTW, bool SLAB>
+template <int NTW, bool SLAB, int TS>
 __global__ void __launch_bounds__(U_THREADS, 1)
     k_unet_wgrad(const __grid_constant__ CUtensorMap dymap, const __grid_constant__ CUtensorMap xmap,
                  const WgradArgs p)
@@ -493,7 +493,9 @@ __global__ void __launch_bounds__(U_THREADS, 1)
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int mtiles = (int)(p.V / U_M);
-    const int CT = (p.cout + 127) / 128, NTN = p.cin / NTW, NG = SLAB ? 9 : 27;
+    // SLAB: TS (dz, dy) pairs share M (128 / TS output channels each); otherwise one tap per group
+    constexpr int CO_S = U_M / TS;           // rows of M per pair
+    const int CT = (p.cout + 127) / 128, NTN = p.cin / NTW, NG = SLAB ? (9 + TS - 1) / TS : 27;
     const int items = NG * CT * NTN * p.nch;
     const int NI = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const uint32_t s_base = smem_u32(smem);
@@ -575,11 +577,9 @@ __global__ void __launch_bounds__(U_THREADS, 1)
         {
             int grp, ct, nt, m0, m1;
             decode((int)blockIdx.x + k * (int)gridDim.x, grp, ct, nt, m0, m1);
-            const int dz = SLAB ? grp / 3 - 1 : grp / 9 - 1;
-            const int dy = SLAB ? grp % 3 - 1 : (grp / 3) % 3 - 1;
-            const int dx = SLAB ? 0 : grp % 3 - 1;
+            const int dz = grp / 9 - 1, dy = (grp / 3) % 3 - 1, dx = grp % 3 - 1;   // not SLAB: the tap
             uint4 hrow = make_uint4(0, 0, 0, 0);
-            if (SLAB) hrow = halo_load(m0, nt, dy, dz);
+            if (SLAB) hrow = halo_load(m0, nt, 0, 0);
             for (int m = m0; m < m1; ++m, ++step)
             {
                 const int b = step % S;
@@ -599,13 +599,21 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                     expect_tx(full0 + 8 * b, L::TX);
                     if (SLAB)
                     {
-                        // the output-gradient planes (16, those past c_out read as zeros) and each input
-                        // plane as boxes of 4 rows of 32 voxels (512-byte rows)
-                        tma5(dst, dm, 0, x0 >> 5, y0, z, ct * 16, full0 + 8 * b);
+                        // with u = v + (dz, dy): dW[dz, dy, dx] = sum_u dy[u - (dz, dy)] x[u + dx].  Per pair
+                        // of the group the output gradient shifted by whole rows (16 / TS planes, those past
+                        // c_out read as zeros); the input slab of the tile's own row (its dx taps 16 bytes
+                        // apart); both as boxes of 4 rows of 32 voxels (512-byte rows)
+#pragma unroll
+                        for (int jj = 0; jj < TS; ++jj)
+                        {
+                            const int pr = min(grp * TS + jj, 8);   // pairs past the ninth load the ninth again
+                            tma5(dst + jj * (16 / TS) * L::APLANE, dm, 0, x0 >> 5, y0 - (pr % 3 - 1),
+                                 z - (pr / 3 - 1), ct * 16, full0 + 8 * b);
+                        }
 #pragma unroll
                         for (int q = 0; q < NTW / 8; ++q)
-                            tma5(dst + L::BOFF + q * L::XPLANE + 128, xm, 0, x0 >> 5, y0 + dy, z + dz,
-                                 nt * (NTW / 8) + q, full0 + 8 * b);
+                            tma5(dst + L::BOFF + q * L::XPLANE + 128, xm, 0, x0 >> 5, y0, z, nt * (NTW / 8) + q,
+                                 full0 + 8 * b);
                     }
                     else if (p.merged)
                     {
@@ -628,7 +636,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
                     if (lane == 0) mbar_arrive(full0 + 8 * b);
-                    if (m + 1 < m1) hrow = halo_load(m + 1, nt, dy, dz);
+                    if (m + 1 < m1) hrow = halo_load(m + 1, nt, 0, 0);
                 }
                 __syncwarp();
             }
@@ -690,18 +698,20 @@ __global__ void __launch_bounds__(U_THREADS, 1)
             if (lane == 0) ready = mbar_wait_or_abort(accf, (uint32_t)(k & 1), abort);
             if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const int co = ct * 128 + tid;
+            // lane tid: SLAB, pair grp * TS + tid / CO_S and output channel ct * 128 + tid % CO_S
+            const int pr = SLAB ? grp * TS + tid / CO_S : 0;
+            const int co = ct * 128 + tid % CO_S;
 #pragma unroll 1
             for (int sh = 0; sh < L::TG; ++sh)
             {
-                const int tap = SLAB ? 3 * grp + sh : grp;
+                const int tap = SLAB ? 3 * pr + sh : grp;
 #pragma unroll 1
                 for (int c0 = 0; c0 < NTW; c0 += 16)
                 {
                     uint32_t v[16];
                     tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)(sh * NTW + c0), v);
                     asm volatile("tcgen05.wait::ld.sync.aligned;");
-                    if (co < p.cout)
+                    if (co < p.cout && (!SLAB || pr < 9))
                     {
                         float* out = p.dw + ((long long)tap * p.cout + co) * p.cin + nt * NTW + c0;
 #pragma unroll
@@ -1281,7 +1291,7 @@ tessgpu_status launch_conv(const void* x, const void* w, const ConvArgs& a, cuda
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
-template <int NTW, bool SLAB>
+template <int NTW, bool SLAB, int TS>
 tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStream_t s)
 {
     using L = WgradLayout<NTW, SLAB>;
@@ -1293,7 +1303,7 @@ tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStre
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (optin < smem_of(L::TOTAL)) return TESSGPU_ERR_UNSUPPORTED;
-        if (cudaFuncSetAttribute(k_unet_wgrad<NTW, SLAB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(k_unet_wgrad<NTW, SLAB, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem_of(L::TOTAL)) != cudaSuccess)
             return TESSGPU_ERR_CUDA;
         ready[dev] = true;
@@ -1302,7 +1312,7 @@ tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStre
     a.merged = !SLAB && a.X <= 32;
     bool ok;
     if (SLAB)
-        ok = row_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16) && row_map(&xmap, x, a.X, a.Y, a.Z, a.cin, 1);
+        ok = row_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16 / TS) && row_map(&xmap, x, a.X, a.Y, a.Z, a.cin, 1);
     else if (a.merged)
         ok = merged_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16) && merged_map(&xmap, x, a.X, a.Y, a.Z, a.cin, NTW / 8);
     else
@@ -1311,14 +1321,14 @@ tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStre
     if (!ok) return TESSGPU_ERR_UNSUPPORTED;
     const int sms = sm_count();
     const long long mt = a.V / U_M;
-    const long long base = (long long)(SLAB ? 9 : 27) * ((a.cout + 127) / 128) * (a.cin / NTW);
+    const long long base = (long long)(SLAB ? (9 + TS - 1) / TS : 27) * ((a.cout + 127) / 128) * (a.cin / NTW);
     long long nch = (2LL * sms + base - 1) / base;
     if (nch > mt) nch = mt;
     if (nch < 1) nch = 1;
     a.nch = (int)nch;
     const long long items = base * nch;
     const int grid = (int)(items < sms ? items : sms);
-    k_unet_wgrad<NTW, SLAB><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(dymap, xmap, a);
+    k_unet_wgrad<NTW, SLAB, TS><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(dymap, xmap, a);
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
@@ -1444,6 +1454,8 @@ extern "C" tessgpu_status tessgpu_unet_wgrad(const void* x, const void* dy, int 
     cudaStream_t s = (cudaStream_t)stream;
     const bool slab = X % 128 == 0;
     // N tile over the input channels: all of them up to 128 (slab: three taps share tensor memory) or 256
+    // slab grids: output channels of 16, 32 or 64 leave room in M for 8, 4 or 2 (dz, dy) pairs
+    const int ts = slab && (cout == 16 || cout == 32 || cout == 64) ? 128 / cout : 1;
     int ntw = 16;
     const int cap = slab ? 128 : 256;
     for (int c : { 256, 192, 128, 96, 64, 32, 16 })
@@ -1474,11 +1486,15 @@ extern "C" tessgpu_status tessgpu_unet_wgrad(const void* x, const void* dy, int 
         US(16, 2) US(32, 2) US(64, 2) US(96, 2) US(128, 2) US(192, 2) US(256, 2)
 #undef US
     }
-#define UW(N_, SL_)                                                                                                    \
-    else if (ntw == N_ && slab == SL_) st = launch_wgrad<N_, SL_>(x, dy, a, s);
+#define UW(N_, SL_, T_)                                                                                            \
+    else if (ntw == N_ && slab == SL_ && ts == T_) st = launch_wgrad<N_, SL_, T_>(x, dy, a, s);
     if (st != TESSGPU_ERR_UNSUPPORTED) {}
-    UW(16, true) UW(32, true) UW(64, true) UW(96, true) UW(128, true)
-    UW(16, false) UW(32, false) UW(64, false) UW(96, false) UW(128, false) UW(192, false) UW(256, false)
+    UW(16, true, 1) UW(32, true, 1) UW(64, true, 1) UW(96, true, 1) UW(128, true, 1)
+    UW(16, true, 2) UW(32, true, 2) UW(64, true, 2) UW(96, true, 2) UW(128, true, 2)
+    UW(16, true, 4) UW(32, true, 4) UW(64, true, 4) UW(96, true, 4) UW(128, true, 4)
+    UW(16, true, 8) UW(32, true, 8) UW(64, true, 8) UW(96, true, 8) UW(128, true, 8)
+    UW(16, false, 1) UW(32, false, 1) UW(64, false, 1) UW(96, false, 1) UW(128, false, 1) UW(192, false, 1)
+    UW(256, false, 1)
 #undef UW
     if (st != TESSGPU_OK || !db) return st;
     const long long V = a.V;
