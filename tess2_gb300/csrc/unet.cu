@@ -441,16 +441,22 @@ __global__ void __launch_bounds__(ConvLayout<NT, KC, SLAB, MT>::THREADS, 1)
 // ---------------------------------------------------------------------------
 // weight gradient
 // ---------------------------------------------------------------------------
-template <int NTW, bool SLAB>
+// SLAB with RPT = 1: the tile is 128 voxels of one x row (X a multiple of 128); RPT = 2: two whole
+// rows of X = 64.  The input slab keeps each row with a halo row before and after it; a 16-voxel
+// K chunk never straddles two rows, so each MMA starts at its own row.
+template <int NTW, bool SLAB, int RPT = 1>
 struct WgradLayout
 {
     static constexpr int TG = SLAB ? 3 : 1;                  // taps per item
     static constexpr int APLANE = U_M * 16;                  // one plane of the output-gradient tile
     static constexpr int ABYTES = 16 * APLANE;               // 16 planes: M = 128 output channels
-    // one plane of the input: SLAB, voxels x0 .. x0 + 127 at byte 128 (a 128-byte-aligned box) with the
-    // halo rows x0 - 1 at 112 and x0 + 128 at 2176; otherwise 128 rows from byte 0
-    static constexpr int XPLANE = SLAB ? 2304 : U_M * 16;
-    static constexpr int XROW0 = SLAB ? 112 : 0;
+    static constexpr int RBYTES = U_M / RPT * 16;            // one row of the tile, 16 bytes a voxel
+    // row i of an input plane at byte ROWM0 + i ROWSTEP (128-byte aligned), its halo rows 16 bytes
+    // before it and RBYTES after its start
+    static constexpr int ROWSTEP = (RBYTES + 32 + 127) / 128 * 128;
+    static constexpr int ROWM0 = 128;
+    static constexpr int XPLANE =
+        SLAB ? (ROWM0 + (RPT - 1) * ROWSTEP + RBYTES + 16 + 127) / 128 * 128 : U_M * 16;
     static constexpr int BBYTES = (NTW / 8) * XPLANE;
     static constexpr int BOFF = ABYTES;
     static constexpr int STAGE = (BOFF + BBYTES + 1023) / 1024 * 1024;
@@ -465,7 +471,8 @@ struct WgradLayout
     static constexpr int TCOLS = pow2_cols(TG * NTW);
     static constexpr uint32_t TX = (uint32_t)(ABYTES + (NTW / 8) * U_M * 16);   // the copies' bytes
     static_assert(NTW % 16 == 0 && NTW >= 16 && NTW <= 256, "N");
-    static_assert(!SLAB || NTW / 8 * 2 <= 32, "one halo row per lane");
+    static_assert(RPT == 1 || RPT == 2, "rows per tile");
+    static_assert(!SLAB || RPT == 2 || NTW / 8 * 2 <= 32, "one halo row per lane");
     static_assert(TG * NTW <= 512, "tensor memory");
     static_assert(STAGES >= 2, "shared memory");
     static_assert(TOTAL <= U_SMEM, "shared memory");
@@ -483,12 +490,13 @@ struct WgradArgs
     int* err;
 };
 
-template <int NTW, bool SLAB, int TS>
+template <int NTW, bool SLAB, int TS, int RPT>
 __global__ void __launch_bounds__(U_THREADS, 1)
     k_unet_wgrad(const __grid_constant__ CUtensorMap dymap, const __grid_constant__ CUtensorMap xmap,
                  const WgradArgs p)
 {
-    using L = WgradLayout<NTW, SLAB>;
+    using L = WgradLayout<NTW, SLAB, RPT>;
+    constexpr bool HALO = SLAB && RPT == 1;   // halo rows from the grid; RPT = 2: whole rows, halos zero
     constexpr int S = L::STAGES;
     extern __shared__ __align__(1024) uint8_t smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -509,7 +517,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
     {
         for (int b = 0; b < S; ++b)
         {
-            bar_init(full0 + 8 * b, SLAB ? 2 : 1);   // expect_tx + the copies (+ the halo rows)
+            bar_init(full0 + 8 * b, HALO ? 2 : 1);   // expect_tx + the copies (+ the halo rows)
             bar_init(empty0 + 8 * b, 1);
         }
         bar_init(accf, 1);
@@ -517,6 +525,16 @@ __global__ void __launch_bounds__(U_THREADS, 1)
         bar_init(fin, 1);
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    if (SLAB && RPT == 2)
+    {
+        // whole rows: every halo row lies outside the grid, zero for the whole kernel
+        for (int i = tid; i < S * (NTW / 8) * RPT * 2; i += U_THREADS)
+        {
+            const int side = i & 1, r = (i >> 1) % RPT, q = (i >> 1) / RPT % (NTW / 8), b = (i >> 1) / RPT / (NTW / 8);
+            *reinterpret_cast<uint4*>(smem + b * L::STAGE + L::BOFF + q * L::XPLANE + L::ROWM0 + r * L::ROWSTEP +
+                                      (side ? L::RBYTES : -16)) = make_uint4(0, 0, 0, 0);
+        }
     }
     if (warp == 5)
     {
@@ -556,7 +574,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
         }
         // SLAB: lane l < 2 NTW/8 keeps one halo row (plane l / 2, side l % 2) of the input slab in a
         // register, loaded a tile ahead so that its latency overlaps the wait for the next slot
-        const int nh = SLAB ? (NTW / 8) * 2 : 0, hq = lane >> 1, hside = lane & 1;
+        const int nh = HALO ? (NTW / 8) * 2 : 0, hq = lane >> 1, hside = lane & 1;
         auto halo_load = [&](int m, int nt, int dy, int dz) {
             uint4 h = make_uint4(0, 0, 0, 0);
             if (lane < nh)
@@ -579,7 +597,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
             decode((int)blockIdx.x + k * (int)gridDim.x, grp, ct, nt, m0, m1);
             const int dz = grp / 9 - 1, dy = (grp / 3) % 3 - 1, dx = grp % 3 - 1;   // not SLAB: the tap
             uint4 hrow = make_uint4(0, 0, 0, 0);
-            if (SLAB) hrow = halo_load(m0, nt, 0, 0);
+            if (HALO) hrow = halo_load(m0, nt, 0, 0);
             for (int m = m0; m < m1; ++m, ++step)
             {
                 const int b = step % S;
@@ -612,8 +630,10 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                         }
 #pragma unroll
                         for (int q = 0; q < NTW / 8; ++q)
-                            tma5(dst + L::BOFF + q * L::XPLANE + 128, xm, 0, x0 >> 5, y0, z, nt * (NTW / 8) + q,
-                                 full0 + 8 * b);
+#pragma unroll
+                            for (int i = 0; i < RPT; ++i)
+                                tma5(dst + L::BOFF + q * L::XPLANE + L::ROWM0 + i * L::ROWSTEP, xm, 0, x0 >> 5, y0 + i,
+                                     z, nt * (NTW / 8) + q, full0 + 8 * b);
                     }
                     else if (p.merged)
                     {
@@ -628,7 +648,7 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                         tma5(dst + L::BOFF, xm, 0, dx, y0 + dy, z + dz, nt * (NTW / 8), full0 + 8 * b);
                     }
                 }
-                if (SLAB)
+                if (HALO)
                 {
                     if (lane < nh)
                         *reinterpret_cast<uint4*>(smem + (dst - s_base) + L::BOFF + hq * L::XPLANE +
@@ -664,14 +684,18 @@ __global__ void __launch_bounds__(U_THREADS, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint32_t abase = s_base + b * L::STAGE;
                 const uint64_t ad = umma_sdesc(abase, 128, L::APLANE);
-                const uint64_t bd = umma_sdesc(abase + L::BOFF + L::XROW0, 128, L::XPLANE);
+                // SLAB: K chunk ks (16 voxels) lies in row ks / (8 / RPT) of the tile; its slab rows start
+                // at that row's halo row, plus 16 bytes per dx
+                const uint64_t bd = umma_sdesc(abase + L::BOFF + (SLAB ? L::ROWM0 - 16 : 0), 128, L::XPLANE);
 #pragma unroll
                 for (int sh = 0; sh < L::TG; ++sh)
 #pragma unroll
                     for (int ks = 0; ks < U_M / 16; ++ks)
                     {
+                        constexpr int KPR = 8 / RPT;   // K chunks per row
+                        const int boff = SLAB ? (ks / KPR) * L::ROWSTEP + (ks % KPR) * 256 : ks * 256;
                         const uint64_t da = ad + (uint64_t)((ks * 256) >> 4);
-                        const uint64_t db = bd + (uint64_t)((sh * 16 + ks * 256) >> 4);
+                        const uint64_t db = bd + (uint64_t)((sh * 16 + boff) >> 4);
                         if (leader)
                             mma_f16(tbase + (uint32_t)(sh * NTW), da, db, idesc, (m > m0 || ks > 0) ? 1u : 0u);
                     }
@@ -717,200 +741,6 @@ __global__ void __launch_bounds__(U_THREADS, 1)
 #pragma unroll
                         for (int c = 0; c < 16; ++c) atomicAdd(out + c, __uint_as_float(v[c]));
                     }
-                }
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(acce);
-        }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    for (int b = tid; b < S; b += U_THREADS)
-    {
-        const int s = last[b];
-        if (s >= 0) mbar_wait_bounded(full0 + 8 * b, (uint32_t)((s / S) & 1));
-    }
-    __syncthreads();
-    if (tid == 0 && *abort) atomicExch(p.err, 1);
-    if (warp == 5)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(L::TCOLS));
-}
-
-// Weight gradient with taps stacked along M, for c_out in {16, 32, 64}: with
-// u = v + s_t, dw[t][co][ci] = sum_u dy[u - s_t][co] x[u][ci], so the input tile
-// is the same for every tap and the output gradient is shifted instead.  A =
-// TS = 128 / c_out shifted copies of the output-gradient tile (rows j * c_out
-// + co for tap g * TS + j), B = the input tile; one MMA per 16 voxels then
-// feeds TS taps, every row of M = 128 a real output channel.  The last group's
-// slots past tap 26 load tap 26 again and are not written back.
-template <int NTW, int TS>
-__global__ void __launch_bounds__(U_THREADS, 1)
-    k_unet_wgrad_stacked(const __grid_constant__ CUtensorMap dymap, const __grid_constant__ CUtensorMap xmap,
-                         const WgradArgs p)
-{
-    using L = WgradLayout<NTW, false>;
-    constexpr int S = L::STAGES;
-    constexpr int CO = 128 / TS;                 // = c_out
-    constexpr int NG = (27 + TS - 1) / TS;       // tap groups
-    extern __shared__ __align__(1024) uint8_t smem[];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int mtiles = (int)(p.V / U_M);
-    const int NTN = p.cin / NTW;
-    const int items = NG * NTN * p.nch;
-    const int NI = (int)blockIdx.x < items ? (items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const bool slab = p.X % U_M == 0;           // tile = part of one x row; else 128 / X whole rows
-    const uint32_t s_base = smem_u32(smem);
-    const uint32_t full0 = s_base + L::OFF_FULL, empty0 = s_base + L::OFF_EMPTY;
-    const uint32_t accf = s_base + L::OFF_ACCF, acce = s_base + L::OFF_ACCE, fin = s_base + L::OFF_FIN;
-    volatile int* abort = reinterpret_cast<volatile int*>(smem + L::OFF_ABORT);
-    int* last = reinterpret_cast<int*>(smem + L::OFF_LAST);
-
-    for (int b = tid; b < S; b += U_THREADS) last[b] = -1;
-    if (tid == 0)
-    {
-        for (int b = 0; b < S; ++b)
-        {
-            bar_init(full0 + 8 * b, 1);
-            bar_init(empty0 + 8 * b, 1);
-        }
-        bar_init(accf, 1);
-        bar_init(acce, 128);
-        bar_init(fin, 1);
-        *abort = 0;
-        asm volatile("fence.mbarrier_init.release.cluster;");
-    }
-    if (warp == 5)
-    {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(s_base + L::OFF_TMEM),
-                     "r"(L::TCOLS));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t tbase = *reinterpret_cast<const volatile uint32_t*>(smem + L::OFF_TMEM);
-
-    // the tap group varies fastest (CTAs running together share the voxel chunk in L2)
-    auto decode = [&](int item, int& grp, int& nt, int& m0, int& m1) {
-        grp = item % NG;
-        const int rest = item / NG;
-        nt = rest % NTN;
-        const int chunk = rest / NTN;
-        m0 = (int)((long long)chunk * mtiles / p.nch);
-        m1 = (int)((long long)(chunk + 1) * mtiles / p.nch);
-    };
-
-    if (warp == 4)
-    {
-        // ---- TMA: per tile TS shifted output-gradient boxes and the input box ----
-        const bool leader = elect_one();
-        const uint64_t dm = reinterpret_cast<uint64_t>(&dymap), xm = reinterpret_cast<uint64_t>(&xmap);
-        if (leader)
-        {
-            asm volatile("prefetch.tensormap [%0];" ::"l"(dm) : "memory");
-            asm volatile("prefetch.tensormap [%0];" ::"l"(xm) : "memory");
-        }
-        bool stop = false;
-        int step = 0;
-        for (int k = 0; k < NI && !stop; ++k)
-        {
-            int grp, nt, m0, m1;
-            decode((int)blockIdx.x + k * (int)gridDim.x, grp, nt, m0, m1);
-            for (int m = m0; m < m1; ++m, ++step)
-            {
-                const int b = step % S;
-                if (step >= S && !warp_wait(empty0 + 8 * b, (uint32_t)((step / S - 1) & 1), abort))
-                {
-                    stop = true;
-                    break;
-                }
-                const long long v0 = (long long)m * U_M;
-                const int x0 = (int)(v0 % p.X);
-                const long long r = v0 / p.X;
-                const int y0 = (int)(r % p.Y), z = (int)(r / p.Y);
-                if (leader)
-                {
-                    last[b] = step;
-                    expect_tx(full0 + 8 * b, L::TX);
-                    const uint32_t dst = s_base + b * L::STAGE;
-#pragma unroll 1
-                    for (int j = 0; j < TS; ++j)
-                    {
-                        const int t = min(grp * TS + j, 26);
-                        const int dz = t / 9 - 1, dy = (t / 3) % 3 - 1, dx = t % 3 - 1;
-                        tma5(dst + j * (CO / 8) * L::APLANE, dm, 0, (slab ? x0 : 0) - dx, y0 - dy, z - dz, 0,
-                             full0 + 8 * b);
-                    }
-                    tma5(dst + L::BOFF, xm, 0, slab ? x0 : 0, y0, z, nt * (NTW / 8), full0 + 8 * b);
-                }
-                __syncwarp();
-            }
-        }
-    }
-    else if (warp == 5)
-    {
-        // ---- MMA: D[slot, co][ci] += A (stacked, MN-major) x B (MN-major), 8 MMAs per tile ----
-        constexpr uint32_t idesc = idesc_f16(NTW, true);
-        const bool leader = elect_one();
-        bool go = true;
-        int step = 0;
-        for (int k = 0; k < NI && go; ++k)
-        {
-            int grp, nt, m0, m1;
-            decode((int)blockIdx.x + k * (int)gridDim.x, grp, nt, m0, m1);
-            if (k >= 1 && !warp_wait(acce, (uint32_t)((k - 1) & 1), abort)) break;
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            for (int m = m0; m < m1; ++m, ++step)
-            {
-                const int b = step % S;
-                go = warp_wait(full0 + 8 * b, (uint32_t)((step / S) & 1), abort);
-                if (!go) break;
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t abase = s_base + b * L::STAGE;
-                const uint64_t ad = umma_sdesc(abase, 128, L::APLANE);
-                const uint64_t bd = umma_sdesc(abase + L::BOFF, 128, L::XPLANE);
-#pragma unroll
-                for (int ks = 0; ks < U_M / 16; ++ks)
-                    if (leader)
-                        mma_f16(tbase, ad + (uint64_t)((ks * 256) >> 4), bd + (uint64_t)((ks * 256) >> 4), idesc,
-                                (m > m0 || ks > 0) ? 1u : 0u);
-                if (leader) commit(empty0 + 8 * b);
-                __syncwarp();
-            }
-            if (!go) break;
-            if (leader) commit(accf);
-            __syncwarp();
-        }
-        if (leader) commit(fin);
-        __syncwarp();
-        if (!mbar_wait_bounded(fin, 0u)) *abort = 1;
-        __syncwarp();
-    }
-    else
-    {
-        // ---- epilogue: lane 32 warp + l = row (tap slot l / c_out, output channel l % c_out) ----
-        for (int k = 0; k < NI; ++k)
-        {
-            int grp, nt, m0, m1;
-            decode((int)blockIdx.x + k * (int)gridDim.x, grp, nt, m0, m1);
-            bool ready = false;
-            if (lane == 0) ready = mbar_wait_or_abort(accf, (uint32_t)(k & 1), abort);
-            if (!__shfl_sync(0xffffffffu, ready ? 1 : 0, 0)) break;
-            asm volatile("tcgen05.fence::after_thread_sync;");
-            const int tap = grp * TS + tid / CO, co = tid % CO;
-#pragma unroll 1
-            for (int c0 = 0; c0 < NTW; c0 += 16)
-            {
-                uint32_t v[16];
-                tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-                asm volatile("tcgen05.wait::ld.sync.aligned;");
-                if (tap < 27)
-                {
-                    float* out = p.dw + ((long long)tap * CO + co) * p.cin + nt * NTW + c0;
-#pragma unroll
-                    for (int c = 0; c < 16; ++c) atomicAdd(out + c, __uint_as_float(v[c]));
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
@@ -1217,14 +1047,14 @@ bool act_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int
 }
 
 // an activation (X a multiple of 32) as (256 = 32 voxels x 8 channels, X / 32, Y, Z, c / 8), box
-// (256, 4, 1, 1, bp): bp planes of 128 voxels of an x row in 512-byte rows
-bool row_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int bp = 1)
+// (256, min(X, 128) / 32, by, 1, bp): bp planes of by rows of up to 128 voxels, in 512-byte rows
+bool row_map(CUtensorMap* map, const void* base, int X, int Y, int Z, int c, int bp = 1, int by = 1)
 {
     const EncodeTiled encode = tensor_map_encoder();
     if (!encode || ((uintptr_t)base & 15) || X % 32) return false;
     const cuuint64_t dims[5] = { 256, (cuuint64_t)(X / 32), (cuuint64_t)Y, (cuuint64_t)Z, (cuuint64_t)(c / 8) };
     const cuuint64_t strides[4] = { 512, (cuuint64_t)X * 16, (cuuint64_t)X * Y * 16, (cuuint64_t)X * Y * Z * 16 };
-    const cuuint32_t box[5] = { 256, 4, 1, 1, (cuuint32_t)bp };
+    const cuuint32_t box[5] = { 256, (cuuint32_t)(X < 128 ? X / 32 : 4), (cuuint32_t)by, 1, (cuuint32_t)bp };
     const cuuint32_t estride[5] = { 1, 1, 1, 1, 1 };
     return encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, estride,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1291,10 +1121,10 @@ tessgpu_status launch_conv(const void* x, const void* w, const ConvArgs& a, cuda
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
-template <int NTW, bool SLAB, int TS>
+template <int NTW, bool SLAB, int TS, int RPT>
 tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStream_t s)
 {
-    using L = WgradLayout<NTW, SLAB>;
+    using L = WgradLayout<NTW, SLAB, RPT>;
     static bool ready[64];
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
@@ -1303,7 +1133,7 @@ tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStre
         int optin = 0;
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (optin < smem_of(L::TOTAL)) return TESSGPU_ERR_UNSUPPORTED;
-        if (cudaFuncSetAttribute(k_unet_wgrad<NTW, SLAB, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(k_unet_wgrad<NTW, SLAB, TS, RPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem_of(L::TOTAL)) != cudaSuccess)
             return TESSGPU_ERR_CUDA;
         ready[dev] = true;
@@ -1312,7 +1142,7 @@ tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStre
     a.merged = !SLAB && a.X <= 32;
     bool ok;
     if (SLAB)
-        ok = row_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16 / TS) && row_map(&xmap, x, a.X, a.Y, a.Z, a.cin, 1);
+        ok = row_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16 / TS, RPT) && row_map(&xmap, x, a.X, a.Y, a.Z, a.cin, 1, 1);
     else if (a.merged)
         ok = merged_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, 16) && merged_map(&xmap, x, a.X, a.Y, a.Z, a.cin, NTW / 8);
     else
@@ -1328,42 +1158,7 @@ tessgpu_status launch_wgrad(const void* x, const void* dy, WgradArgs a, cudaStre
     a.nch = (int)nch;
     const long long items = base * nch;
     const int grid = (int)(items < sms ? items : sms);
-    k_unet_wgrad<NTW, SLAB, TS><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(dymap, xmap, a);
-    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
-}
-
-template <int NTW, int TS>
-tessgpu_status launch_wgrad_stacked(const void* x, const void* dy, WgradArgs a, cudaStream_t s)
-{
-    using L = WgradLayout<NTW, false>;
-    static bool ready[64];
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return TESSGPU_ERR_CUDA;
-    if (!ready[dev])
-    {
-        int optin = 0;
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (optin < smem_of(L::TOTAL)) return TESSGPU_ERR_UNSUPPORTED;
-        if (cudaFuncSetAttribute(k_unet_wgrad_stacked<NTW, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem_of(L::TOTAL)) != cudaSuccess)
-            return TESSGPU_ERR_CUDA;
-        ready[dev] = true;
-    }
-    const bool slab = a.X % U_M == 0;
-    CUtensorMap dymap, xmap;
-    if (!act_map(&dymap, dy, a.X, a.Y, a.Z, a.cout, slab ? U_M : a.X, slab ? 1 : U_M / a.X, a.cout / 8) ||
-        !act_map(&xmap, x, a.X, a.Y, a.Z, a.cin, slab ? U_M : a.X, slab ? 1 : U_M / a.X, NTW / 8))
-        return TESSGPU_ERR_UNSUPPORTED;
-    const int sms = sm_count();
-    const long long mt = a.V / U_M;
-    const long long base = (long long)((27 + TS - 1) / TS) * (a.cin / NTW);
-    long long nch = (2LL * sms + base - 1) / base;
-    if (nch > mt) nch = mt;
-    if (nch < 1) nch = 1;
-    a.nch = (int)nch;
-    const long long items = base * nch;
-    const int grid = (int)(items < sms ? items : sms);
-    k_unet_wgrad_stacked<NTW, TS><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(dymap, xmap, a);
+    k_unet_wgrad<NTW, SLAB, TS, RPT><<<grid, U_THREADS, smem_of(L::TOTAL), s>>>(dymap, xmap, a);
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 
@@ -1452,9 +1247,11 @@ extern "C" tessgpu_status tessgpu_unet_wgrad(const void* x, const void* dy, int 
     a.dw = dw;
     a.err = err;
     cudaStream_t s = (cudaStream_t)stream;
-    const bool slab = X % 128 == 0;
+    // slab form: X a multiple of 128 (a tile in one x row) or X = 64 (a tile of two whole rows)
+    const bool slab = X % 128 == 0 || X == 64;
+    const int rpt = X == 64 ? 2 : 1;
     // N tile over the input channels: all of them up to 128 (slab: three taps share tensor memory) or 256
-    // slab grids: output channels of 16, 32 or 64 leave room in M for 8, 4 or 2 (dz, dy) pairs
+    // slab form: output channels of 16, 32 or 64 leave room in M for 8, 4 or 2 (dz, dy) pairs
     const int ts = slab && (cout == 16 || cout == 32 || cout == 64) ? 128 / cout : 1;
     int ntw = 16;
     const int cap = slab ? 128 : 256;
@@ -1467,34 +1264,19 @@ extern "C" tessgpu_status tessgpu_unet_wgrad(const void* x, const void* dy, int 
     tessgpu_status st = TESSGPU_ERR_UNSUPPORTED;
     a.x = (const __nv_bfloat16*)x;
     a.merged = 0;
-    // taps stacked along M where the per-tap-group kernel would read its operands in 16-byte rows
-    // (X = 64) and M = 128 would be mostly padding
-    if (!slab && X == 64 && (cout == 16 || cout == 32 || cout == 64))
-    {
-        // taps stacked along M: the input's N tile up to 256 channels
-        int nts = 16;
-        for (int c : { 256, 192, 128, 96, 64, 32, 16 })
-            if (cin % c == 0)
-            {
-                nts = c;
-                break;
-            }
-#define US(N_, T_) else if (nts == N_ && cout == 128 / T_) st = launch_wgrad_stacked<N_, T_>(x, dy, a, s);
-        if (false) {}
-        US(16, 8) US(32, 8) US(64, 8) US(96, 8) US(128, 8) US(192, 8) US(256, 8)
-        US(16, 4) US(32, 4) US(64, 4) US(96, 4) US(128, 4) US(192, 4) US(256, 4)
-        US(16, 2) US(32, 2) US(64, 2) US(96, 2) US(128, 2) US(192, 2) US(256, 2)
-#undef US
-    }
-#define UW(N_, SL_, T_)                                                                                            \
-    else if (ntw == N_ && slab == SL_ && ts == T_) st = launch_wgrad<N_, SL_, T_>(x, dy, a, s);
-    if (st != TESSGPU_ERR_UNSUPPORTED) {}
-    UW(16, true, 1) UW(32, true, 1) UW(64, true, 1) UW(96, true, 1) UW(128, true, 1)
-    UW(16, true, 2) UW(32, true, 2) UW(64, true, 2) UW(96, true, 2) UW(128, true, 2)
-    UW(16, true, 4) UW(32, true, 4) UW(64, true, 4) UW(96, true, 4) UW(128, true, 4)
-    UW(16, true, 8) UW(32, true, 8) UW(64, true, 8) UW(96, true, 8) UW(128, true, 8)
-    UW(16, false, 1) UW(32, false, 1) UW(64, false, 1) UW(96, false, 1) UW(128, false, 1) UW(192, false, 1)
-    UW(256, false, 1)
+#define UW(N_, SL_, T_, R_)                                                                                        \
+    else if (ntw == N_ && slab == SL_ && ts == T_ && rpt == R_) st = launch_wgrad<N_, SL_, T_, R_>(x, dy, a, s);
+    if (false) {}
+    UW(16, true, 1, 1) UW(32, true, 1, 1) UW(64, true, 1, 1) UW(96, true, 1, 1) UW(128, true, 1, 1)
+    UW(16, true, 2, 1) UW(32, true, 2, 1) UW(64, true, 2, 1) UW(96, true, 2, 1) UW(128, true, 2, 1)
+    UW(16, true, 4, 1) UW(32, true, 4, 1) UW(64, true, 4, 1) UW(96, true, 4, 1) UW(128, true, 4, 1)
+    UW(16, true, 8, 1) UW(32, true, 8, 1) UW(64, true, 8, 1) UW(96, true, 8, 1) UW(128, true, 8, 1)
+    UW(16, true, 1, 2) UW(32, true, 1, 2) UW(64, true, 1, 2) UW(96, true, 1, 2) UW(128, true, 1, 2)
+    UW(16, true, 2, 2) UW(32, true, 2, 2) UW(64, true, 2, 2) UW(96, true, 2, 2) UW(128, true, 2, 2)
+    UW(16, true, 4, 2) UW(32, true, 4, 2) UW(64, true, 4, 2) UW(96, true, 4, 2) UW(128, true, 4, 2)
+    UW(16, true, 8, 2) UW(32, true, 8, 2) UW(64, true, 8, 2) UW(96, true, 8, 2) UW(128, true, 8, 2)
+    UW(16, false, 1, 1) UW(32, false, 1, 1) UW(64, false, 1, 1) UW(96, false, 1, 1) UW(128, false, 1, 1)
+    UW(192, false, 1, 1) UW(256, false, 1, 1)
 #undef UW
     if (st != TESSGPU_OK || !db) return st;
     const long long V = a.V;

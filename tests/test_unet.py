@@ -182,10 +182,12 @@ def test_unet_data_gradient_matches_oracle(grid, cin, cout):
 @pytest.mark.gpu
 @pytest.mark.parametrize("grid,cin,cout", [((128, 4, 3), 16, 32), ((128, 4, 3), 96, 32), ((128, 2, 2), 32, 96),
                                            ((64, 4, 4), 192, 64), ((32, 4, 2), 384, 128), ((16, 8, 8), 128, 256),
-                                           ((32, 8, 4), 64, 16), ((16, 8, 8), 32, 64), ((128, 2, 2), 128, 128)])
+                                           ((32, 8, 4), 64, 16), ((16, 8, 8), 32, 64), ((128, 2, 2), 128, 128),
+                                           ((64, 4, 2), 32, 32), ((64, 2, 2), 64, 128), ((64, 2, 2), 16, 16)])
 def test_unet_wgrad_matches_oracle(grid, cin, cout):
-    """Weight and bias gradients (FP32 sums of bf16 products); c_out of 16, 32 or 64
-    takes the tap-stacked kernel, the others the per-tap-group one."""
+    """Weight and bias gradients (FP32 sums of bf16 products): slab grids (X a
+    multiple of 128, or X = 64 with two rows a tile) with 1, 2, 4 or 8 (dz, dy)
+    pairs stacked in M, and the per-tap form for X of 16 or 32."""
     import torch
     from oracle.surrogate_oracle import conv3d_wgrad
     from tess2_gb300 import unet as U
