@@ -390,7 +390,9 @@ __device__ __forceinline__ int warp_walk(int axis, float fixed_a, float fixed_b,
 // call per position, the first position of the left walk probed twice)
 struct ScanOut { int tot; int nrows; bool overflow; int deposited; int probes; };
 
-__device__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cmin_pos, WarpSmem& S, int nf,
+// out of line: called twice per cell (count, then deposit), and one copy keeps the cell kernel's
+// code small enough for the instruction cache (118 -> 98 ms at 2M -> 512^3)
+__device__ __noinline__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cmin_pos, WarpSmem& S, int nf,
                             const GridDesc& g, int lane, bool rec, float inc, float* grid)
 {
     ScanOut o = { 0, 0, false, 0, 0 };
