@@ -327,8 +327,9 @@ __device__ void distribute_cic(const float* pt, float scalar, int* idx, float* w
 // (coordinate `axis` = cmin_pos[axis] + (start + (k0 + q) d) step[axis], the
 // other two fixed), each lane every 8th face.  The same per-face arithmetic as
 // warp_pt_in_cell, so each answer is the one a single probe gives.  Bit q of
-// the result is the answer at point q (q < npts).
-__device__ __forceinline__ unsigned warp_pt_in_cell4(int axis, float fixed_a, float fixed_b, int start, int d, int k0,
+// the result is the answer at point q (q < npts).  Out of line: the walks call it from three
+// places, and one copy keeps the cell kernel's code smaller (see scanline).
+__device__ __noinline__ unsigned warp_pt_in_cell4(int axis, float fixed_a, float fixed_b, int start, int d, int k0,
                                                      int npts, const float* cmin_pos, const GridDesc& g,
                                                      const WarpSmem& S, int nf, float eps, int lane)
 {
@@ -390,8 +391,9 @@ __device__ __forceinline__ int warp_walk(int axis, float fixed_a, float fixed_b,
 // call per position, the first position of the left walk probed twice)
 struct ScanOut { int tot; int nrows; bool overflow; int deposited; int probes; };
 
-// out of line: called twice per cell (count, then deposit), and one copy keeps the cell kernel's
-// code small enough for the instruction cache (118 -> 98 ms at 2M -> 512^3)
+// out of line, like warp_pt_in_cell4: called twice per cell (count, then deposit), and one copy
+// keeps the cell kernel's code small enough for the instruction cache (the two: 118 -> 91 ms at
+// 2M -> 512^3)
 __device__ __noinline__ ScanOut scanline(const int* cgp, const int* cmin_idx, const float* cmin_pos, WarpSmem& S, int nf,
                             const GridDesc& g, int lane, bool rec, float inc, float* grid)
 {
