@@ -60,6 +60,7 @@ struct tessgpu_ctx
     long long                pair_cap_hint = 0;
     bool                     in_retry = false;
     bool                     rows = true;           // the row kernel for dense() (raster_rows() when made)
+    int                      pageable_access = -1;  // the device reads and writes pageable host memory (-1: not asked)
     int                      sets_variant[2] = { -1, -1 };   // brick shape of tessgpu_batch_dense_sets, per mode
 };
 
@@ -1147,6 +1148,12 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         }
         if (var < 0)
         {
+            // the tuning launches count into the status; keep what the stages
+            // before the rasteriser counted (star volumes' FP64 tets, errors)
+            // and put it back afterwards
+            Status saved;
+            CK(cudaMemcpyAsync(&saved, ctx->d_status, sizeof(Status), cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
             float best = 1e30f;
             cudaEvent_t e0, e1;
             cudaEventCreate(&e0);
@@ -1174,7 +1181,8 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             cudaEventDestroy(e1);
             ctx->raster_variant[p->mode] = var;
             CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
-            CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
+            CK(cudaMemcpyAsync(ctx->d_status, &saved, sizeof(Status), cudaMemcpyHostToDevice, s));
+            CK(cudaStreamSynchronize(s));
             CK(cudaMemsetAsync(target, 0, sizeof(float) * G, s));
             if (owner) CK(cudaMemsetAsync(owner, 0xff, sizeof(int) * G, s));
         }
@@ -1950,6 +1958,28 @@ __global__ void k_pack_block(const float* raw, int np, float4* pos)
         pos[p] = make_float4(raw[3 * (size_t)p], raw[3 * (size_t)p + 1], raw[3 * (size_t)p + 2], 0.0f);
 }
 
+// A box of the global grid (x fastest, nx * ny per z plane) into the same box of a host array
+// the device addresses directly (pageable memory on a host whose GPU shares its page tables):
+// one CTA per row of the box
+__global__ void k_store_box(const float* __restrict__ grid, float* host, int nx, int ny, int x0, int y0, int z0,
+                            int bx, int by, int bz)
+{
+    const long long rows = (long long)by * bz;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x)
+    {
+        const int y = y0 + (int)(r % by), z = z0 + (int)(r / by);
+        const size_t base = ((size_t)z * ny + y) * nx + x0;
+        for (int x = threadIdx.x; x < bx; x += blockDim.x) host[base + x] = grid[base + x];
+    }
+}
+
+// n floats into a host array the device addresses directly
+__global__ void k_store_run(const float* __restrict__ src, float* dst, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
 // one block's tet_t vertices -> batch-wide particle indices, checked
 __global__ void k_ingest_verts(const int4* raw, int nt, int np, int p_off, int4* tv, Status* st)
 {
@@ -1973,6 +2003,32 @@ __global__ void k_ingest_verts(const int4* raw, int nt, int np, int p_off, int4*
 // copy stream as soon as the last block that writes into it is done.  Same
 // kernels and results as the batch path; it needs the rasteriser's launch
 // variant chosen already.
+// true when the device reads and writes pageable host memory directly (its page tables shared with
+// the host's); asked once per context
+static bool pageable_access(tessgpu_ctx* ctx)
+{
+    if (ctx->pageable_access < 0)
+    {
+        int a = 0;
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, ctx->device) != cudaSuccess) a = 0;
+        cudaGetLastError();
+        ctx->pageable_access = a ? 1 : 0;
+    }
+    return ctx->pageable_access == 1;
+}
+
+// host memory that is neither pinned nor registered with CUDA
+static bool is_pageable(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+
 static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessgpu_block* blocks,
                                            const tessgpu_dense_params* p, int variant, float* host_grid,
                                            tessgpu_dense_info* info, float** d_grid_out)
@@ -2085,6 +2141,17 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     // when the blocks' grid boxes tile the grid (the usual case), each box
     // goes down as soon as its block is done, so only the last box trails
     const bool tiles = boxes_tile(hb, p->glo_num_idx);
+    // pageable host arrays on a device that addresses them: the ingest kernels read the caller's
+    // particles and tets in place, and the grid boxes are stored into the caller's array by a kernel on
+    // the download stream (a copy from or to pageable memory would wait on the host thread, stalling
+    // the pipeline); pinned or registered arrays go through the copy engines
+    bool direct_in = pageable_access(ctx);
+    for (int i = 0; i < nb && direct_in; ++i)
+        if ((blocks[i].num_particles && !is_pageable(blocks[i].particles)) ||
+            (blocks[i].num_tets && !is_pageable(blocks[i].tets)) ||
+            (blocks[i].num_tets && ((uintptr_t)blocks[i].tets & 15)))
+            direct_in = false;
+    const bool direct_out = host_grid && pageable_access(ctx) && is_pageable(host_grid);
 
     const double scale = star_sum_scale(dmin, dmax, p->mode == TESSGPU_MODE_FP64);
 
@@ -2108,6 +2175,14 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         const int b = order[k];
         const BlockDesc& d = hb[b];
         const int eu0 = smark(ctx, ctx->h2d);
+        if (direct_in)
+        {
+            // nothing to copy: the events complete at once
+            if (k == 0)
+                for (int i = 0; i < 1 + kFirstParts; ++i) CK(cudaEventRecord(ctx->first_ev[i], ctx->h2d));
+            CK(cudaEventRecord(ctx->pipe_ev[k], ctx->h2d));
+            continue;
+        }
         if (k == 0)
         {
             if (d.np)
@@ -2160,7 +2235,8 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         const int ec0 = smark(ctx, s);
         if (d.np)
         {
-            k_pack_block<<<grid_small(d.np), 256, 0, s>>>(stage_xyz + 3 * (size_t)d.p_off, d.np, pos + d.p_off);
+            k_pack_block<<<grid_small(d.np), 256, 0, s>>>(direct_in ? blocks[b].particles : stage_xyz + 3 * (size_t)d.p_off,
+                                                          d.np, pos + d.p_off);
             CK(cudaMemsetAsync(W + d.p_off, 0, sizeof(StarSum) * d.np, s));
             ctx->launches++;
         }
@@ -2173,8 +2249,10 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             if (k == 0)
                 CK(cudaStreamWaitEvent(s, ctx->first_ev[1 + i], 0));
             if (t1 <= t0) continue;
-            k_ingest_verts<<<grid_small(t1 - t0), 256, 0, s>>>(stage_tets + 2 * ((size_t)d.t_off + t0), (int)(t1 - t0),
-                                                                d.np, d.p_off, tv + d.t_off + t0, ctx->d_status);
+            const int4* src = direct_in ? reinterpret_cast<const int4*>(blocks[b].tets) + 2 * (size_t)t0
+                                        : stage_tets + 2 * ((size_t)d.t_off + t0);
+            k_ingest_verts<<<grid_small(t1 - t0), 256, 0, s>>>(src, (int)(t1 - t0), d.np, d.p_off, tv + d.t_off + t0,
+                                                                ctx->d_status);
             ctx->launches++;
             if (bricks)
                 bricks_star(ctx, p->mode, variant, d_blocks, nb, d.t_off + t0, t1 - t0, pos, tv, W, scale, g, bins, s);
@@ -2225,7 +2303,20 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
                                          d.gmax_idx[1] - d.gmin_idx[1] + 1, d.gmax_idx[2] - d.gmin_idx[2] + 1);
             prm.kind = cudaMemcpyDeviceToHost;
             const int e0 = smark(ctx, ctx->d2h);
-            CK(cudaMemcpy3DAsync(&prm, ctx->d2h));
+            if (direct_out)
+            {
+                const int bx = d.gmax_idx[0] - d.gmin_idx[0] + 1, by = d.gmax_idx[1] - d.gmin_idx[1] + 1,
+                          bz = d.gmax_idx[2] - d.gmin_idx[2] + 1;
+                const long long rows = (long long)by * bz;
+                if (rows > 0 && bx > 0)
+                {
+                    k_store_box<<<(unsigned)std::min(rows, 2LL * 152), 256, 0, ctx->d2h>>>(
+                        grid, host_grid, nx, ny, d.gmin_idx[0], d.gmin_idx[1], d.gmin_idx[2], bx, by, bz);
+                    ctx->launches++;
+                }
+            }
+            else
+                CK(cudaMemcpy3DAsync(&prm, ctx->d2h));
             span(ctx, "download", e0, smark(ctx, ctx->d2h));
         }
         for (int l = 0; l < L && !tiles; ++l)
@@ -2234,8 +2325,14 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
                 for (int kk = std::max(0, k - 1); kk <= k; ++kk)   // this block and the one on the other stream
                     CK(cudaStreamWaitEvent(ctx->d2h, ctx->pipe_ev[nb + kk], 0));
                 const size_t off = (size_t)slab_lo[l] * area, n = (size_t)(slab_hi[l] - slab_lo[l] + 1) * area;
-                CK(cudaMemcpyAsync(host_grid + off, grid + off, sizeof(float) * n, cudaMemcpyDeviceToHost,
-                                   ctx->d2h));
+                if (direct_out)
+                {
+                    k_store_run<<<2 * 152, 256, 0, ctx->d2h>>>(grid + off, host_grid + off, n);
+                    ctx->launches++;
+                }
+                else
+                    CK(cudaMemcpyAsync(host_grid + off, grid + off, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                                       ctx->d2h));
             }
     }
     // the second compute stream's last block, before the statistics

@@ -396,6 +396,21 @@ def test_dtfe_host_pipeline_matches_batch(gpu_ctx, dims):
         finally:
             del os.environ["TESSGPU_PIPELINE"]
         assert np.array_equal(r0["grid"], ref)
+        # pinned host arrays go through the copy engines; pageable ones (above) are read and
+        # written in place by the kernels where the device addresses pageable memory
+        keep, pblocks = [], []
+        for b in blocks:
+            nb = dict(b)
+            for k in ("particles", "tets"):
+                a = np.ascontiguousarray(b[k])
+                t = torch.empty(a.shape, dtype=torch.from_numpy(a[:0]).dtype, pin_memory=True)
+                t.numpy()[...] = a
+                keep.append(t)
+                nb[k] = t.numpy()
+            pblocks.append(nb)
+        out = torch.empty((gni[2], gni[1], gni[0]), dtype=torch.float32, pin_memory=True).numpy()
+        gpu_ctx.dense(DENSE_DTFE, pblocks, gni, mode=mode, out=out)
+        assert np.array_equal(out, ref)
 
 
 def test_dtfe_brick_order_same_grid(gpu_ctx):
