@@ -69,3 +69,39 @@ def test_dense_tess_sampled_cell_counts(gpu_ctx, mix_blocks):
     for blk, c, r in zip(mix_blocks, cells, ref):
         assert np.array_equal(counts[off + c], r)
         off += int(blk["num_orig"])
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_dtfe_star_sums_batch_vs_noalloc(gpu_ctx, mix_blocks, mode):
+    """Vertex densities of the mixture, block by block: the batch path (all
+    blocks' tets in one star-volume launch) against the allocation-free entry
+    point (its own kernel, one block per call).  Both sum the star volumes as
+    fixed-point integers at the scale of the same data bounds, so the
+    densities agree bit for bit whatever order the atomics land in."""
+    import ctypes
+    import torch
+    from tess2_gb300.api import DENSE_DTFE, lib
+    b = gpu_ctx.upload(mix_blocks)
+    b.keep_debug(True)
+    g = torch.zeros(int(np.prod(GNI)), dtype=torch.float32, device="cuda")
+    b.dense(DENSE_DTFE, GNI, g.data_ptr(), mode=mode)
+    total = sum(len(x["particles"]) for x in mix_blocks)
+    _, _, rho = b.debug_outputs(particles=total)
+    b.free()
+    mn = np.min([x["bounds_min"] for x in mix_blocks], axis=0)
+    mx = np.max([x["bounds_max"] for x in mix_blocks], axis=0)
+    bounds = (ctypes.c_float * 6)(*[float(v) for v in mn], *[float(v) for v in mx])
+    off = 0
+    for blk in mix_blocks:
+        p = torch.from_numpy(np.ascontiguousarray(blk["particles"], np.float32)).cuda()
+        t = torch.from_numpy(np.ascontiguousarray(blk["tets"], np.int32)).cuda()   # tet_t records
+        assert t.dim() == 2 and t.shape[1] == 8
+        out = torch.full((p.shape[0],), -1.0, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        s = lib().tessgpu_dtfe_densities_noalloc(p.data_ptr(), p.shape[0], t.data_ptr(), t.shape[0], bounds, 1.0,
+                                                 mode, out.data_ptr(), None)
+        assert s == 0
+        got = rho[off:off + p.shape[0]]
+        assert np.array_equal(got.view(np.uint32), out.cpu().numpy().view(np.uint32))
+        off += p.shape[0]
+    assert off == total
