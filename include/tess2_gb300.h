@@ -429,6 +429,19 @@ tessgpu_status tessgpu_unet_upsample_grad(const void* dy, int dy_plane0, int X, 
                                           void* stream);
 /* x (16 channels, plane 1 already zero): channel 0 = field, channels 1-7 = 0 */
 tessgpu_status tessgpu_unet_input(const float* field, long long V, void* x, void* stream);
+/* Where the particles sit in the voxels of an X x Y x Z grid of points
+   grid_min + i * grid_step (host arrays of 3): moments (device, 10 planes of
+   X*Y*Z floats, zeroed by the call) receives per voxel, over the particles
+   whose nearest grid point it is, with u = (p - point) / grid_step: the
+   count, the sums of u_x, u_y, u_z and of u_x u_x, u_y u_y, u_z u_z,
+   u_x u_y, u_x u_z, u_y u_z.  xyz: device, 3 floats per particle. */
+tessgpu_status tessgpu_unet_cell_moments(const float* xyz, long long n, const float* grid_min, const float* grid_step,
+                                         int X, int Y, int Z, float* moments, void* stream);
+/* x (16 channels) from the field and those moments: 0 field, 1 log(1 + count),
+   2-4 twice the mean offset, 5-10 twelve times the offsets' central second
+   moments (xx, yy, zz, xy, xz, yz; zero below two particles), 11-15 zero */
+tessgpu_status tessgpu_unet_input_moments(const float* field, const float* moments, long long V, void* x,
+                                          void* stream);
 /* pred = field + w[c] + sum_k w[k] act[k] (c <= 32 channels); with target
    and loss, *loss += sum (pred - target)^2 (FP64) */
 tessgpu_status tessgpu_unet_head(const void* act, int c, const float* w, const float* field, long long V, float* pred,

@@ -138,3 +138,47 @@ def flat_grads(G):
         parts += [G[name][0].ravel(), np.ravel(G[name][1])]
     parts += [np.ravel(G["head"][0]), np.ravel(G["head"][1])]
     return np.concatenate(parts)
+
+
+def cell_moments(xyz, grid_min, grid_step, dims, f32=False):
+    """The particles' voxel moments (tessgpu_unet_cell_moments): each particle
+    at its nearest grid point g (round half to even, as the kernel's
+    float-to-int rounding), u = (p - g) / step; planes (10, Z, Y, X): count,
+    sums of u_x, u_y, u_z, of u_x^2, u_y^2, u_z^2, u_x u_y, u_x u_z, u_y u_z,
+    summed in FP64.  Particles whose nearest point is outside the grid are
+    left out.  f32: the grid coordinate (p - min) * (1 / step) in FP32, as the
+    kernel computes it, so that particles at a voxel boundary fall the same
+    way; otherwise FP64."""
+    X, Y, Z = (int(d) for d in dims)
+    if f32:
+        inv = (np.float32(1.0) / np.asarray(grid_step, np.float32)).astype(np.float32)
+        f = ((np.asarray(xyz, np.float32) - np.asarray(grid_min, np.float32)) * inv).astype(np.float64)
+    else:
+        f = (np.asarray(xyz, np.float64) - np.asarray(grid_min, np.float64)) / np.asarray(grid_step, np.float64)
+    i = np.rint(f).astype(np.int64)
+    ok = np.all((i >= 0) & (i < np.array([X, Y, Z])), axis=1)
+    f, i = f[ok], i[ok]
+    u = f - i
+    v = (i[:, 2] * Y + i[:, 1]) * X + i[:, 0]
+    terms = [np.ones(len(u)), u[:, 0], u[:, 1], u[:, 2], u[:, 0] ** 2, u[:, 1] ** 2, u[:, 2] ** 2,
+             u[:, 0] * u[:, 1], u[:, 0] * u[:, 2], u[:, 1] * u[:, 2]]
+    m = np.zeros((10, X * Y * Z))
+    for k, t in enumerate(terms):
+        np.add.at(m[k], v, t)
+    return m.reshape(10, Z, Y, X)
+
+
+def input_features(field, m):
+    """The 16 input channels tessgpu_unet_input_moments makes, FP64, (Z, Y, X, 16)."""
+    n = m[0]
+    safe = np.maximum(n, 1.0)
+    f = np.zeros(n.shape + (16,))
+    f[..., 0] = field
+    f[..., 1] = np.log1p(n)
+    mean = [np.where(n > 0, m[1 + a] / safe, 0.0) for a in range(3)]
+    for a in range(3):
+        f[..., 2 + a] = 2.0 * mean[a]
+    pairs = [(4, 0, 0), (5, 1, 1), (6, 2, 2), (7, 0, 1), (8, 0, 2), (9, 1, 2)]
+    for k, (plane, a, b) in enumerate(pairs):
+        f[..., 5 + k] = np.where(n > 1, 12.0 * (m[plane] / safe - mean[a] * mean[b]), 0.0)
+    return f

@@ -886,6 +886,75 @@ __global__ void k_input(const float* __restrict__ field, long long V, __nv_bfloa
     }
 }
 
+// Where the particles sit inside the voxels: each particle goes to its nearest
+// grid point g (x fastest), u = (p - g) / step in [-1/2, 1/2] per axis, and
+// the voxel sums MOMENT_PLANES planes of V floats: [0] the count, [1..3] the
+// sums of u_x, u_y, u_z, [4..9] of u_x u_x, u_y u_y, u_z u_z, u_x u_y,
+// u_x u_z, u_y u_z.  A cloud-in-cell grid cannot tell where in a voxel its
+// particles are; the DTFE field between them depends on it.
+constexpr int MOMENT_PLANES = 10;
+
+__global__ void k_cell_moments(const float* __restrict__ xyz, long long n, float3 g0, float3 inv, int X, int Y, int Z,
+                               float* __restrict__ m)
+{
+    const long long V = (long long)X * Y * Z;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    {
+        const float fx = (xyz[3 * i] - g0.x) * inv.x;
+        const float fy = (xyz[3 * i + 1] - g0.y) * inv.y;
+        const float fz = (xyz[3 * i + 2] - g0.z) * inv.z;
+        const int ix = __float2int_rn(fx), iy = __float2int_rn(fy), iz = __float2int_rn(fz);
+        if (ix < 0 || ix >= X || iy < 0 || iy >= Y || iz < 0 || iz >= Z)
+            continue;   // nearest grid point outside the grid
+        const float ux = fx - ix, uy = fy - iy, uz = fz - iz;
+        float* c = m + ((long long)iz * Y + iy) * X + ix;
+        atomicAdd(c, 1.0f);
+        atomicAdd(c + V, ux);
+        atomicAdd(c + 2 * V, uy);
+        atomicAdd(c + 3 * V, uz);
+        atomicAdd(c + 4 * V, ux * ux);
+        atomicAdd(c + 5 * V, uy * uy);
+        atomicAdd(c + 6 * V, uz * uz);
+        atomicAdd(c + 7 * V, ux * uy);
+        atomicAdd(c + 8 * V, ux * uz);
+        atomicAdd(c + 9 * V, uy * uz);
+    }
+}
+
+// The network's 16 input channels from the field and the voxel moments:
+// 0 field, 1 log(1 + count), 2-4 twice the mean offset, 5-10 twelve times the
+// offsets' central second moments (xx, yy, zz, xy, xz, yz; a uniform spread
+// over the voxel gives 1 on the diagonal), 11-15 zero.  Empty voxels give
+// zeros, a single particle zero second moments.
+__global__ void k_input_moments(const float* __restrict__ field, const float* __restrict__ m, long long V,
+                                __nv_bfloat16* __restrict__ x)
+{
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < V; v += (long long)gridDim.x * blockDim.x)
+    {
+        const float n = m[v];
+        float f[16] = { field[v], log1pf(n) };
+        if (n > 0.0f)
+        {
+            const float r = 1.0f / n;
+            const float mx = m[V + v] * r, my = m[2 * V + v] * r, mz = m[3 * V + v] * r;
+            f[2] = 2.0f * mx;
+            f[3] = 2.0f * my;
+            f[4] = 2.0f * mz;
+            if (n > 1.0f)
+            {
+                f[5] = 12.0f * (m[4 * V + v] * r - mx * mx);
+                f[6] = 12.0f * (m[5 * V + v] * r - my * my);
+                f[7] = 12.0f * (m[6 * V + v] * r - mz * mz);
+                f[8] = 12.0f * (m[7 * V + v] * r - mx * my);
+                f[9] = 12.0f * (m[8 * V + v] * r - mx * mz);
+                f[10] = 12.0f * (m[9 * V + v] * r - my * mz);
+            }
+        }
+        reinterpret_cast<uint4*>(x)[v] = pack8(f);
+        reinterpret_cast<uint4*>(x)[V + v] = pack8(f + 8);
+    }
+}
+
 // pred[v] = field[v] + b + sum_c w[c] act[c][v]; with a target: loss += sum (pred - target)^2 (block
 // partial sums, one atomic per block)
 __global__ void __launch_bounds__(256) k_head(const __nv_bfloat16* __restrict__ act, int c, const float* __restrict__ w,
@@ -1345,6 +1414,32 @@ extern "C" tessgpu_status tessgpu_unet_input(const float* field, long long V, vo
 {
     if (!field || !x || V <= 0) return TESSGPU_ERR_INVALID;
     k_input<<<grid_1d(V, 256), 256, 0, (cudaStream_t)stream>>>(field, V, (__nv_bfloat16*)x);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_cell_moments(const float* xyz, long long n, const float* grid_min,
+                                                    const float* grid_step, int X, int Y, int Z, float* moments,
+                                                    void* stream)
+{
+    if ((n > 0 && !xyz) || n < 0 || !grid_min || !grid_step || !moments || X <= 0 || Y <= 0 || Z <= 0)
+        return TESSGPU_ERR_INVALID;
+    for (int d = 0; d < 3; ++d)
+        if (!(grid_step[d] > 0.0f)) return TESSGPU_ERR_INVALID;
+    const long long V = (long long)X * Y * Z;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (cudaMemsetAsync(moments, 0, sizeof(float) * MOMENT_PLANES * V, s) != cudaSuccess) return TESSGPU_ERR_CUDA;
+    if (n > 0)
+        k_cell_moments<<<grid_1d(n, 256), 256, 0, s>>>(
+            xyz, n, make_float3(grid_min[0], grid_min[1], grid_min[2]),
+            make_float3(1.0f / grid_step[0], 1.0f / grid_step[1], 1.0f / grid_step[2]), X, Y, Z, moments);
+    return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
+}
+
+extern "C" tessgpu_status tessgpu_unet_input_moments(const float* field, const float* moments, long long V, void* x,
+                                                     void* stream)
+{
+    if (!field || !moments || !x || V <= 0) return TESSGPU_ERR_INVALID;
+    k_input_moments<<<grid_1d(V, 256), 256, 0, (cudaStream_t)stream>>>(field, moments, V, (__nv_bfloat16*)x);
     return cudaGetLastError() == cudaSuccess ? TESSGPU_OK : TESSGPU_ERR_CUDA;
 }
 

@@ -6,7 +6,9 @@ Four levels, 32 channels doubling per level (grid S -> S/2 -> S/4 -> S/8),
 3x3x3 convolutions with ReLU, 2x2x2 average pooling down, nearest
 upsampling up, the skips concatenated:
 
-  e0a 16->32, e0b 32->32            level 0  (input: log CIC in channel 0 of 16)
+  e0a 16->32, e0b 32->32            level 0  (input: log CIC in channel 0 of 16,
+                                              optionally the particles' voxel
+                                              moments in channels 1-10)
   e1a 32->64, e1b 64->64            level 1  (pooled e0b)
   e2a 64->128, e2b 128->128         level 2  (pooled e1b)
   bt 128->256                       level 3  (pooled e2b)
@@ -39,6 +41,7 @@ CONVS = [  # name, c_in, c_out, level
     ("d2", 384, 128, 2), ("d1", 192, 64, 1), ("d0", 96, 32, 0),
 ]
 HEAD_C = 32
+MOMENT_PLANES = 10   # tessgpu_unet_cell_moments: count, 3 first and 6 second moments
 
 
 def _lib():
@@ -53,6 +56,8 @@ def _lib():
         "tessgpu_unet_upsample": [vp, i, i, i, i, vp, i, vp],
         "tessgpu_unet_upsample_grad": [vp, i, i, i, i, i, vp, vp],
         "tessgpu_unet_input": [vp, ll, vp, vp],
+        "tessgpu_unet_cell_moments": [vp, ll, vp, vp, i, i, i, vp, vp],
+        "tessgpu_unet_input_moments": [vp, vp, ll, vp, vp],
         "tessgpu_unet_head": [vp, i, vp, vp, ll, vp, vp, vp, vp],
         "tessgpu_unet_head_grad": [vp, i, vp, vp, vp, ll, f, vp, vp, vp],
         "tessgpu_unet_check": [vp],
@@ -115,7 +120,7 @@ class UNet:
     by 8; X at level 0 a multiple of 128, and X / 2^l in {16, 32, 64} or a
     multiple of 128 at the other levels)."""
 
-    def __init__(self, grid, seed=0, device="cuda:0"):
+    def __init__(self, grid, seed=0, device="cuda:0", in_channels=1):
         import torch
         self.dev = torch.device(device)
         X, Y, Z = grid
@@ -136,10 +141,11 @@ class UNet:
         p = np.zeros(off, np.float32)
         for name, ci, co, _ in CONVS:
             a, b, _ = self.slices[name]
-            fan = 27 * (1 if name == "e0a" else ci)   # e0a sees one nonzero input channel
+            # e0a sees in_channels nonzero input channels (1: the CIC grid; 11 with the moments)
+            fan = 27 * (in_channels if name == "e0a" else ci)
             w = rng.standard_normal((27, co, ci)).astype(np.float32) * math.sqrt(2.0 / fan)
             if name == "e0a":
-                w[:, :, 1:] = 0.0
+                w[:, :, in_channels:] = 0.0
             p[a:b] = w.ravel()
         f32, bf = torch.float32, torch.bfloat16
         self.params = torch.from_numpy(p).to(self.dev)
@@ -217,15 +223,20 @@ class UNet:
         ci, co, l = next((c[1], c[2], c[3]) for c in CONVS if c[0] == name)
         conv(x, self.grids[l], ci, self.wf[name], co, y, y_plane0, bias=self.b(name), relu=True, stream=stream)
 
-    def forward(self, field=None, target=None, stream=None):
+    def forward(self, field=None, target=None, stream=None, moments=None):
         """Prediction (FP32, V0) for the field (FP32 log CIC, V0) -- by default the
-        resident self.field; with a target the squared error is summed into self.loss."""
+        resident self.field; with a target the squared error is summed into self.loss.
+        moments: the particles' voxel moments (cell_moments) as further input channels."""
         L = _lib()
         s = _stream(stream)
         A, V, G3 = self.a, self.V, self.grids
         if field is not None:
             self.field.copy_(field)
-        _ok(L.tessgpu_unet_input(_ptr(self.field), V[0], _ptr(A["x0"]), s), "tessgpu_unet_input")
+        if moments is not None:
+            _ok(L.tessgpu_unet_input_moments(_ptr(self.field), _ptr(moments), V[0], _ptr(A["x0"]), s),
+                "tessgpu_unet_input_moments")
+        else:
+            _ok(L.tessgpu_unet_input(_ptr(self.field), V[0], _ptr(A["x0"]), s), "tessgpu_unet_input")
         self._conv("e0a", A["x0"], A["e0a"], stream=s)
         self._conv("e0b", A["e0a"], A["cat0"], 8, stream=s)
         _ok(L.tessgpu_unet_pool(_ptr(A["cat0"], 8, V[0]), *G3[0], 32, _ptr(A["p0"]), s), "pool")
@@ -296,10 +307,10 @@ class UNet:
                                 lr, b1, b2, eps, self.step, s), "tessgpu_adam")
         self._pack(s)
 
-    def train_step(self, field, target, lr=1e-3, stream=None):
+    def train_step(self, field, target, lr=1e-3, stream=None, moments=None):
         """One Adam step on one field; returns nothing (the summed squared error
         accumulates in self.loss, read it when convenient)."""
-        self.forward(field, target, stream)
+        self.forward(field, target, stream, moments)
         self.backward(stream)
         self.adam(lr, stream=stream)
 
@@ -307,6 +318,47 @@ class UNet:
 # ---------------------------------------------------------------------------
 # fields, training, evaluation
 # ---------------------------------------------------------------------------
+def cell_moments(xyz, grid_min, grid_step, dims, out=None, stream=None):
+    """The particles' voxel moments (MOMENT_PLANES x V FP32, device): xyz a
+    device tensor of (n, 3) float32, the grid's points grid_min + i * grid_step,
+    dims (X, Y, Z)."""
+    import torch
+    X, Y, Z = (int(d) for d in dims)
+    if out is None:
+        out = torch.empty(MOMENT_PLANES * X * Y * Z, dtype=torch.float32, device=xyz.device)
+    gmin = (ctypes.c_float * 3)(*[float(v) for v in grid_min])
+    gstep = (ctypes.c_float * 3)(*[float(v) for v in grid_step])
+    _ok(_lib().tessgpu_unet_cell_moments(_ptr(xyz), int(xyz.shape[0]), gmin, gstep, X, Y, Z, _ptr(out),
+                                         _stream(stream)), "tessgpu_unet_cell_moments")
+    return out
+
+
+_PAIR = {(0, 1): 7, (1, 0): 7, (0, 2): 8, (2, 0): 8, (1, 2): 9, (2, 1): 9}
+
+
+def transform_moments(m, S, perm, flips):
+    """The voxel moments of the particle set mapped by a symmetry of the cube,
+    given as the (z, y, x) array's dimension permutation and the flipped
+    dimensions of the permuted array (as applied to the grids): the planes are
+    permuted and flipped like the grids, the offsets' components permuted and
+    negated along flipped axes, the second moments transformed as R M R^T."""
+    import torch
+    t = m.view(MOMENT_PLANES, S, S, S).permute(0, *[p + 1 for p in perm])
+    if flips:
+        t = torch.flip(t, [f + 1 for f in flips])
+    # array dimension d is physical axis 2 - d
+    src = [2 - perm[2 - a] for a in range(3)]           # new axis a <- old axis src[a]
+    sign = [-1.0 if (2 - a) in flips else 1.0 for a in range(3)]
+    out = torch.empty((MOMENT_PLANES, S, S, S), dtype=m.dtype, device=m.device)
+    out[0] = t[0]
+    for a in range(3):
+        out[1 + a] = sign[a] * t[1 + src[a]]
+        out[4 + a] = t[4 + src[a]]
+    for a, b in ((0, 1), (0, 2), (1, 2)):
+        out[_PAIR[(a, b)]] = sign[a] * sign[b] * t[_PAIR[(src[a], src[b])]]
+    return out.view(-1)
+
+
 def rel_l2(a, b):
     a = np.asarray(a, np.float64).ravel()
     b = np.asarray(b, np.float64).ravel()
@@ -342,15 +394,16 @@ def log_density(grid):
     return np.log1p(g / max(g.mean(), 1e-30)).astype(np.float32)
 
 
-def make_fields(seeds, n_particles, side, processes=None, device=0, log=None):
-    """(x, y) per seed: log densities of the CIC and the DTFE grid (side^3, one
-    block in the unit box) of the seed's particle set (50 % uniform + 50 % in 256
-    Gaussian clumps, sigma 0.01).  Host Qhull in spawned worker processes, the
-    CIC and DTFE passes on the GPU as each set arrives.  Returns the fields and
-    the seconds spent: Qhull (summed over workers is not known; wall time of
-    the whole run), and the GPU passes."""
+def make_fields(seeds, n_particles, side, processes=None, device=0, log=None, moments=False):
+    """(x, y[, m]) per seed: log densities of the CIC and the DTFE grid (side^3,
+    one block in the unit box) of the seed's particle set (50 % uniform + 50 %
+    in 256 Gaussian clumps, sigma 0.01), and with moments the particles' voxel
+    moments on the DTFE grid's points (a device tensor).  Host Qhull in spawned
+    worker processes, the GPU passes as each set arrives.  Returns the fields,
+    the wall time of the whole run and the seconds of the GPU passes."""
     import multiprocessing as mp
     import os
+    import torch
     from .api import DENSE_CIC, DENSE_DTFE, Context
     procs = processes or min(len(seeds), os.cpu_count() or 1)
     out = []
@@ -364,9 +417,15 @@ def make_fields(seeds, n_particles, side, processes=None, device=0, log=None):
             g0 = time.time()
             gni = [side] * 3
             cic = ctx.dense(DENSE_CIC, [blk], gni)["grid"]
-            dtfe = ctx.dense(DENSE_DTFE, [blk], gni)["grid"]
+            r = ctx.dense(DENSE_DTFE, [blk], gni)
+            item = (log_density(cic).ravel(), log_density(r["grid"]).ravel())
+            if moments:
+                xyz = torch.from_numpy(np.ascontiguousarray(blk["particles"], np.float32)).to(f"cuda:{device}")
+                m = cell_moments(xyz, r["info"]["grid_phys_mins"], r["info"]["grid_step_size"], gni)
+                torch.cuda.synchronize()
+                item = item + (m,)
             gpu_s += time.time() - g0
-            out.append((log_density(cic).ravel(), log_density(dtfe).ravel()))
+            out.append(item)
             if log and (i + 1) % 8 == 0:
                 log(f"fields: {i + 1}/{len(seeds)} after {time.time() - t0:.0f} s")
     return out, time.time() - t0, gpu_s
@@ -438,76 +497,99 @@ def layer_times(side=128, reps=5, seed=0):
     return out
 
 
-def train_and_evaluate(n_train=48, n_val=16, n_particles=2097152, side=128, epochs=12, lr=3e-4, seed=7,
-                       processes=None, bound=0.05, log=None):
-    """Trains the U-Net on fields the plain path makes (each step on one field
-    under a random symmetry of the cube), then per validation
-    field: relative L2 of the log density against DTFE, the density-PDF error,
-    the CIC input's own error (the method without the network).  Fallback:
-    a predicted error per field (a least-squares fit, on the training fields,
-    of the network's error against statistics of its input), and the fields
-    whose prediction exceeds `bound` recomputed exactly by the plain path."""
+def _train(net, fields, side, epochs, lr, seed, use_moments, log=None):
+    """Adam over the fields, one field a step under a random one of the cube's
+    48 symmetries (DTFE commutes with them: axis flips and a permutation; the
+    voxel moments transform with them), cosine learning-rate decay.  Returns
+    the per-epoch mean squared errors, the seconds and the steps."""
     import torch
-    tr, t_tr, g_tr = make_fields(range(10_000 + seed * 1000, 10_000 + seed * 1000 + n_train), n_particles, side,
-                                 processes, log=log)
-    va, t_va, g_va = make_fields(range(900_000 + seed * 1000, 900_000 + seed * 1000 + n_val), n_particles, side,
-                                 processes, log=log)
-    net = UNet((side, side, side), seed=seed)
-    dev = net.dev
-    tx = [(torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)) for x, y in tr]
-    vx = [(torch.from_numpy(x).to(dev), torch.from_numpy(y).to(dev)) for x, y in va]
+    S = side
+    aug = np.random.default_rng(seed)
     losses = []
     torch.cuda.synchronize()
     t0 = time.time()
-    steps = 0
-    total = epochs * len(tx)
-    S = side
-    aug = np.random.default_rng(seed)
+    steps, total = 0, epochs * len(fields)
     for ep in range(epochs):
-        order = np.random.default_rng(seed + ep).permutation(len(tx))
+        order = np.random.default_rng(seed + ep).permutation(len(fields))
         net.loss.zero_()
         for k in order:
-            # one of the cube's 48 symmetries (DTFE commutes with them): axis flips and a permutation
             flips = [d for d in range(3) if aug.integers(2)]
             perm = [int(a) for a in aug.permutation(3)]
-            x, y = (t.view(S, S, S).permute(*perm) for t in tx[k])
+            x, y = (t.view(S, S, S).permute(*perm) for t in fields[k][:2])
             if flips:
                 x, y = torch.flip(x, flips), torch.flip(y, flips)
             x, y = x.contiguous().view(-1), y.contiguous().view(-1)
-            # cosine learning-rate decay over the run
-            net.train_step(x, y, lr=lr * 0.5 * (1 + math.cos(math.pi * steps / total)))
+            m = transform_moments(fields[k][2], S, perm, flips) if use_moments else None
+            net.train_step(x, y, lr=lr * 0.5 * (1 + math.cos(math.pi * steps / total)), moments=m)
             steps += 1
-        losses.append(net.loss.item() / (len(tx) * net.V[0]))
+        losses.append(net.loss.item() / (len(fields) * net.V[0]))
         if log:
-            log(f"epoch {ep}: train mse {losses[-1]:.5f}")
+            log(f"epoch {ep}: train mse {losses[-1]:.5f}" + (" (moments)" if use_moments else " (CIC only)"))
     torch.cuda.synchronize()
-    t_train = time.time() - t0
-    check()
+    return losses, time.time() - t0, steps
 
-    def stats(x):
+
+def _evaluate(net, fields, use_moments):
+    out = []
+    for f in fields:
+        x, y = f[0], f[1]
+        p = net.forward(x, moments=f[2] if use_moments else None).cpu().numpy()
+        yh = y.cpu().numpy()
         a = x.cpu().numpy().astype(np.float64)
-        return [1.0, float(a.std()), float((a == 0).mean()), float(a.max())]
+        out.append(dict(err=rel_l2(p, yh), pdf=pdf_error(p, yh), cic=rel_l2(x.cpu().numpy(), yh),
+                        s=[1.0, float(a.std()), float((a == 0).mean()), float(a.max())]))
+    return out
 
-    def evaluate(pairs):
-        out = []
-        for x, y in pairs:
-            p = net.forward(x).cpu().numpy()
-            yh = y.cpu().numpy()
-            out.append(dict(err=rel_l2(p, yh), pdf=pdf_error(p, yh), cic=rel_l2(x.cpu().numpy(), yh),
-                            s=stats(x)))
-        return out
 
-    etr, eva = evaluate(tx), evaluate(vx)
+def train_and_evaluate(n_train=48, n_val=16, n_particles=2097152, side=128, epochs=12, lr=3e-4, seed=7,
+                       processes=None, bound=0.05, log=None, moments=True, compare=True):
+    """Trains the U-Net on fields the plain path makes, then per validation
+    field: relative L2 of the log density against DTFE, the density-PDF error,
+    the CIC input's own error (the method without the network).  moments: the
+    network also sees the particles' voxel moments (input channels 1-10);
+    compare: a second network on the same fields with the CIC grid alone, for
+    the difference the moments make.  Fallback: a predicted error per field
+    (a least-squares fit, on the training fields, of the network's error
+    against statistics of its input), and the fields whose prediction exceeds
+    `bound` recomputed exactly by the plain path."""
+    import torch
+    tr, t_tr, g_tr = make_fields(range(10_000 + seed * 1000, 10_000 + seed * 1000 + n_train), n_particles, side,
+                                 processes, log=log, moments=moments)
+    va, t_va, g_va = make_fields(range(900_000 + seed * 1000, 900_000 + seed * 1000 + n_val), n_particles, side,
+                                 processes, log=log, moments=moments)
+    dev = torch.device("cuda:0")
+    tx = [tuple(torch.from_numpy(a).to(dev) if isinstance(a, np.ndarray) else a for a in f) for f in tr]
+    vx = [tuple(torch.from_numpy(a).to(dev) if isinstance(a, np.ndarray) else a for a in f) for f in va]
+    extra = {}
+    if moments and compare:
+        base = UNet((side, side, side), seed=seed, in_channels=1)
+        _train(base, tx, side, epochs, lr, seed, False, log)
+        eb = _evaluate(base, vx, False)
+        extra = dict(val_rel_l2_cic_only=float(np.mean([e["err"] for e in eb])),
+                     val_pdf_error_cic_only=float(np.mean([e["pdf"] for e in eb])))
+        del base
+    net = UNet((side, side, side), seed=seed, in_channels=11 if moments else 1)
+    losses, t_train, steps = _train(net, tx, side, epochs, lr, seed, moments, log)
+    check()
+    etr, eva = _evaluate(net, tx, moments), _evaluate(net, vx, moments)
     # the error predictor: least squares on the training fields' input statistics
     A = np.array([e["s"] for e in etr])
     coef, *_ = np.linalg.lstsq(A, np.array([e["err"] for e in etr]), rcond=None)
     pred_err = [float(np.dot(coef, e["s"])) for e in eva]
     fallback = [i for i, pe in enumerate(pred_err) if pe > bound]
     served = [0.0 if i in fallback else e["err"] for i, e in enumerate(eva)]
-    fwd_ms = _events_ms(lambda: net.forward(vx[0][0]), 10)
+    m0 = vx[0][2] if moments else None
+    fwd_ms = _events_ms(lambda: net.forward(vx[0][0], moments=m0), 10)
+    mom_ms = None
+    if moments:
+        # the moments' own cost at serving time: the deposit of the field's particles
+        pts = torch.rand(n_particles, 3, device=dev)
+        mbuf = torch.empty_like(m0)
+        mom_ms = _events_ms(lambda: cell_moments(pts, [0.0] * 3, [1.0 / (side - 1)] * 3, [side] * 3, out=mbuf), 10)
     check()
     return dict(n_train=n_train, n_val=n_val, particles=n_particles, grid=side, epochs=epochs, steps=steps,
-                params=net.nparams, train_mse=losses, train_s=t_train, train_step_ms=1e3 * t_train / max(steps, 1),
+                params=net.nparams, inputs="log CIC + voxel moments" if moments else "log CIC",
+                train_mse=losses, train_s=t_train, train_step_ms=1e3 * t_train / max(steps, 1),
                 fields_wall_s=t_tr + t_va, fields_gpu_s=g_tr + g_va,
                 val_rel_l2=float(np.mean([e["err"] for e in eva])),
                 val_rel_l2_max=float(np.max([e["err"] for e in eva])),
@@ -516,4 +598,5 @@ def train_and_evaluate(n_train=48, n_val=16, n_particles=2097152, side=128, epoc
                 train_rel_l2=float(np.mean([e["err"] for e in etr])),
                 predicted_error=pred_err, actual_error=[e["err"] for e in eva], bound=bound,
                 fallback_fields=len(fallback), served_rel_l2=float(np.mean(served)),
-                forward_ms=fwd_ms, forward_tflops=net.flops_forward() / (fwd_ms * 1e-3) / 1e12, net=net)
+                forward_ms=fwd_ms, moments_ms=mom_ms,
+                forward_tflops=net.flops_forward() / (fwd_ms * 1e-3) / 1e12, net=net, **extra)

@@ -326,3 +326,59 @@ def test_unet_training_lowers_loss():
     U.check()
     assert np.all(np.isfinite(losses))
     assert losses[-1] < 0.5 * losses[0], losses
+
+
+def _sym_particles(p, perm, flips):
+    """particles under the symmetry that permute(perm) then flip(flips) applies to
+    a (z, y, x) grid array of the unit cube: new axis a <- old axis 2 - perm[2 - a],
+    mirrored when array dimension 2 - a is flipped"""
+    q = np.empty_like(p)
+    for a in range(3):
+        c = p[:, 2 - perm[2 - a]]
+        q[:, a] = 1.0 - c if (2 - a) in flips else c
+    return q
+
+
+@pytest.mark.parametrize("perm,flips", [([0, 1, 2], [0]), ([2, 1, 0], []), ([1, 2, 0], [1, 2]),
+                                        ([0, 2, 1], [0, 1, 2])])
+def test_moments_follow_cube_symmetries(perm, flips):
+    """transform_moments (the training augmentation) on the moments of a particle
+    set equals the moments of the transformed particles (FP64 oracle both ways)."""
+    import torch
+    from oracle.unet_oracle import cell_moments
+    from tess2_gb300.unet import transform_moments
+    S = 8
+    rng = np.random.default_rng(3)
+    p = rng.random((3000, 3))
+    step = [1.0 / (S - 1)] * 3
+    m = cell_moments(p, [0.0] * 3, step, [S] * 3)
+    want = cell_moments(_sym_particles(p, perm, flips), [0.0] * 3, step, [S] * 3)
+    got = transform_moments(torch.from_numpy(m.ravel()), S, perm, flips).view(10, S, S, S).numpy()
+    assert np.allclose(got, want, atol=1e-9)
+
+
+@pytest.mark.gpu
+def test_unet_cell_moments_and_input_match_oracle():
+    """tessgpu_unet_cell_moments (FP32 atomics) and tessgpu_unet_input_moments
+    (bf16 channels) against the FP64 oracle on a clustered particle set."""
+    import torch
+    from oracle.unet_oracle import cell_moments, input_features
+    from tess2_gb300 import host
+    from tess2_gb300 import unet as U
+    X, Y, Z = 16, 8, 12
+    pts = host.mixture_particles(20000, 5).astype(np.float32)
+    gmin, step = [0.01, -0.02, 0.0], [0.9 / (X - 1), 1.1 / (Y - 1), 1.0 / (Z - 1)]
+    ref = cell_moments(pts, gmin, step, (X, Y, Z), f32=True)
+    m = U.cell_moments(torch.from_numpy(pts).cuda(), gmin, step, (X, Y, Z))
+    got = m.view(10, Z, Y, X).cpu().numpy()
+    assert np.array_equal(got[0], ref[0])                       # counts exact
+    assert np.allclose(got[1:], ref[1:], atol=2e-4 * max(1.0, ref[0].max()))
+    field = np.random.default_rng(1).standard_normal((Z, Y, X)).astype(np.float32)
+    x = torch.zeros(2 * X * Y * Z * 8, dtype=torch.bfloat16, device="cuda")
+    L = U._lib()
+    assert L.tessgpu_unet_input_moments(torch.from_numpy(field.ravel()).cuda().data_ptr(), m.data_ptr(), X * Y * Z,
+                                        x.data_ptr(), None) == 0
+    feats = _unplanar(x.float().cpu().numpy().reshape(2, X * Y * Z, 8), (X, Y, Z))
+    want = input_features(field, ref)
+    assert np.allclose(feats, want, rtol=1e-2, atol=2e-2)
+    assert np.all(feats[..., 11:] == 0)
