@@ -63,6 +63,7 @@ struct Status
     unsigned long long candidates;  // DTFE: grid points tested
     unsigned long long probes;      // DENSE_TESS: PtInCell calls of the scanline
     unsigned long long face_tests;  // DENSE_TESS: probes x faces of the cell
+    int cell_next;                  // k_cells: the next cell a warp takes (zeroed per launch)
 };
 
 __device__ __forceinline__ void fail(Status* st, int code, int detail)

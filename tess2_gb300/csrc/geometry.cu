@@ -19,6 +19,7 @@
 //                     evaluated by all lanes at once (a lane per face, two ballots)
 //   k_cic           one thread per particle (DENSE_CIC)
 #include "kernels.h"
+#include <algorithm>
 #include <float.h>
 #include <math.h>
 
@@ -524,8 +525,18 @@ k_cells(const BlockDesc* blocks, const int* c_off, int nb, int total_cells, cons
     double acc_mass = 0.0;
     unsigned long long acc_cells = 0, acc_probes = 0, acc_faces = 0;
 
-    for (int c = blockIdx.x * CELL_WARPS + w; c < total_cells; c += gridDim.x * CELL_WARPS)
+    // persistent warps take cells in order from a counter: cells differ in
+    // cost by orders of magnitude (a background cell's scanline against a
+    // clump cell's CIC fallback), and a fixed share per warp left SMs idle
+    // while the last blocks ran
+    for (;;)
     {
+        int c = 0;
+        if (lane == 0)
+            c = atomicAdd(&st->cell_next, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= total_cells)
+            break;
         const int b = find_block_c(c_off, nb, c);
         const int p_off = blocks[b].p_off;
         const int v = p_off + (c - c_off[b]);
@@ -1229,8 +1240,23 @@ void launch_cells(int mode, const BlockDesc* d_blocks, const int* d_c_off, int n
                   int* cell_counts, Status* st, cudaStream_t s)
 {
     if (total <= 0) return;
-    const int nblk = grid1d((long long)total * 32, CELL_WARPS * 32, 16);
+    // one resident wave of persistent blocks (the kernel's occupancy per SM)
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int nt = CELL_WARPS * 32;
+    switch (mode)
+    {
+    case CELL_COMPLETE: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cells<CELL_COMPLETE>, nt, 0); break;
+    case CELL_VOLUME: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cells<CELL_VOLUME>, nt, 0); break;
+    case CELL_VOLUME_F64:
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cells<CELL_VOLUME_F64>, nt, 0);
+        break;
+    default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cells<CELL_DENSE_TESS>, nt, 0); break;
+    }
+    const long long need = ((long long)total + CELL_WARPS - 1) / CELL_WARPS;
+    const int nblk = (int)std::min<long long>(need, (long long)sms * std::max(per_sm, 1));
+    cudaMemsetAsync(&st->cell_next, 0, sizeof(int), s);
     switch (mode)
     {
     case CELL_COMPLETE:
