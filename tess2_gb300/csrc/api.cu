@@ -1009,7 +1009,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             BALLOC(SLOT_RHO32, sizeof(float) * (bt->N ? bt->N : 1), bt->rho32);
             BALLOC(SLOT_RHO64, sizeof(double) * (bt->N ? bt->N : 1), bt->rho64);
             BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
-            BALLOC(SLOT_FIXN, sizeof(int) * (nb + 1), bt->fix_count);
+            BALLOC(SLOT_FIXN, sizeof(int) * 2 * (nb + 1), bt->fix_count);
         }
         int* owner = nullptr;
         if (bt->keep_debug)
@@ -1021,7 +1021,10 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             owner = bt->d_owner;
         }
         CK(cudaMemsetAsync(bt->W, 0, sizeof(StarSum) * bt->N, s));
-        CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int) * (nb + 1), s));
+        // fix_count: the FP64 fix-up list length per block, then the
+        // rasteriser's chunk counter per block (persistent launches)
+        int* next = bt->fix_count + (nb + 1);
+        CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int) * 2 * (nb + 1), s));
         // fixed-point scale of the star-volume sums: any star volume is below
         // the volume of the particles' bounding box; allow 8x the data box
         const double scale = star_sum_scale(dmin, dmax, p->mode == TESSGPU_MODE_FP64);
@@ -1062,7 +1065,7 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
                     {
                         launch_raster(p->mode, known, bt->d_blocks, nb, d.nt, bt->pos, bt->tv, bt->rho32, bt->rho64,
                                       g, kTau, target, owner, bt->fix_list + d.t_off, bt->fix_count + k,
-                                      ctx->d_status, sk, nullptr, nullptr, d.t_off);
+                                      ctx->d_status, sk, nullptr, nullptr, d.t_off, false, next + k);
                         t3 = smark(ctx, sk);
                         if (p->mode != TESSGPU_MODE_FP64)
                         {
@@ -1164,9 +1167,11 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
                 for (int rep = 0; rep < 2; ++rep)
                 {
                     CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
+                    CK(cudaMemsetAsync(next, 0, sizeof(int), s));
                     cudaEventRecord(e0, s);
                     launch_raster(p->mode, v, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g,
-                                  kTau, target, owner, bt->fix_list, bt->fix_count, ctx->d_status, s, order, order_n);
+                                  kTau, target, owner, bt->fix_list, bt->fix_count, ctx->d_status, s, order, order_n,
+                                  0, false, next);
                     cudaEventRecord(e1, s);
                     ctx->launches++;
                     CK(cudaEventSynchronize(e1));
@@ -1181,13 +1186,14 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
             cudaEventDestroy(e1);
             ctx->raster_variant[p->mode] = var;
             CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), s));
+            CK(cudaMemsetAsync(next, 0, sizeof(int), s));
             CK(cudaMemcpyAsync(ctx->d_status, &saved, sizeof(Status), cudaMemcpyHostToDevice, s));
             CK(cudaStreamSynchronize(s));
             CK(cudaMemsetAsync(target, 0, sizeof(float) * G, s));
             if (owner) CK(cudaMemsetAsync(owner, 0xff, sizeof(int) * G, s));
         }
         launch_raster(p->mode, var, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g, kTau,
-                      target, owner, bt->fix_list, bt->fix_count, ctx->d_status, s, order, order_n);
+                      target, owner, bt->fix_list, bt->fix_count, ctx->d_status, s, order, order_n, 0, false, next);
         mark(ctx, "raster");
         if (p->mode != TESSGPU_MODE_FP64)
         {
@@ -1492,7 +1498,7 @@ static tessgpu_status dense_sets_rows(tessgpu_ctx* ctx, tessgpu_batch* bt, const
     if (!bt->fix_list || bt->pooled)
     {
         BALLOC(SLOT_FIX, sizeof(int) * (bt->T ? bt->T : 1), bt->fix_list);
-        BALLOC(SLOT_FIXN, sizeof(int) * (nb + 1), bt->fix_count);
+        BALLOC(SLOT_FIXN, sizeof(int) * 2 * (nb + 1), bt->fix_count);
     }
     StarSum* W = bt->W;
     CK(cudaMemcpyAsync(bt->d_blocks, bt->hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
@@ -2108,7 +2114,8 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     float* rho32 = (float*)get(SLOT_RHO32, sizeof(float) * std::max(N, 1LL));
     double* rho64 = (double*)get(SLOT_RHO64, sizeof(double) * std::max(N, 1LL));
     int* fix = bricks ? nullptr : (int*)get(SLOT_FIX, sizeof(int) * std::max(T, 1LL));
-    int* fixn = (int*)get(SLOT_FIXN, sizeof(int) * nb);   // one fix-list length per block (row kernel)
+    // per block: the FP64 fix-up list length, then the rasteriser's chunk counter
+    int* fixn = (int*)get(SLOT_FIXN, sizeof(int) * 2 * nb);
     float* grid = (float*)get(SLOT_GRID, sizeof(float) * G);
     CK(e);
     *d_grid_out = grid;
@@ -2215,7 +2222,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     // the brick rasteriser writes every point of the blocks' boxes
     if (!bricks || !tiles)
         CK(cudaMemsetAsync(grid, 0, sizeof(float) * G, s));
-    CK(cudaMemsetAsync(fixn, 0, sizeof(int) * nb, s));
+    CK(cudaMemsetAsync(fixn, 0, sizeof(int) * 2 * nb, s));
     if (bricks)
         CK(cudaMemsetAsync(bins.pair_cursor, 0, sizeof(unsigned long long), s));
     // blocks alternate between two compute streams, so one block's launches
@@ -2278,7 +2285,8 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         {
             // the block's FP64 fix-up list: its own segment of the list buffer
             launch_raster(p->mode, variant, d_blocks, nb, d.nt, pos, tv, rho32, rho64, g, kTau, grid, nullptr,
-                          fix + d.t_off, fixn + k, ctx->d_status, s, nullptr, nullptr, d.t_off);
+                          fix + d.t_off, fixn + k, ctx->d_status, s, nullptr, nullptr, d.t_off, false,
+                          fixn + nb + k);
             ctx->launches++;
             if (mixed)
             {

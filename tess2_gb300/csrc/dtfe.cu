@@ -496,7 +496,7 @@ template <typename T, bool VAL64, bool LIST, int MINB, int NW, bool COMPACT, boo
 __global__ void __launch_bounds__(NW * 32, MINB)
 k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int* list_count, const float4* pos,
          const int4* tv, const float* rho32, const double* rho64, GridDesc g, float tau, float* grid, int* owner,
-         int* fix_list, int* fix_count, Status* st, int t0)
+         int* fix_list, int* fix_count, Status* st, int t0, int* next)
 {
     typedef typename Vec4<T>::type T4;
     BlockGrid gshared;   // the shared grid (read from the kernel's parameters)
@@ -517,8 +517,21 @@ k_raster(const BlockDesc* blocks, int nb, int total, const int* list, const int*
     const int n = LIST ? *list_count : total;
     const int nchunks = (n + 31) / 32;
     int qn = 0;   // queued tets (warp-uniform)
-    for (int chunk = blockIdx.x * NW + wid;; chunk += gridDim.x * NW)
+    // next: persistent warps take chunks of 32 tets in order from a counter
+    // (a chunk of background tets costs far more than one of clump tets);
+    // otherwise a fixed grid-stride share per warp
+    int chunk = blockIdx.x * NW + wid;
+    for (bool first = true;; first = false)
     {
+        if (next)
+        {
+            int c = 0;
+            if (lane == 0)
+                c = atomicAdd(next, 1);
+            chunk = __shfl_sync(FULL, c, 0);
+        }
+        else if (!first)
+            chunk += gridDim.x * NW;
         const bool more = chunk < nchunks;
         if (COMPACT && more)
         {
@@ -1039,26 +1052,48 @@ void launch_densities(const StarSum* W, int n, float mass, double inv_scale, flo
 //   6..7: per-lane rows, 4/5 blocks per SM, every row of the box (no slices)
 constexpr int N_RASTER_VARIANTS = 8;
 
+// Blocks of a rasteriser launch: with a chunk counter, one resident wave of
+// persistent blocks (the kernel's occupancy per SM); otherwise up to 16 per SM
+// with a fixed share of the chunks each.
+template <typename K>
+static int raster_grid(K kernel, int threads, long long work, bool persistent)
+{
+    if (!persistent)
+        return grid_for(work, threads, 16);
+    int dev = 0, sms = 152, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+    const long long need = (work + threads - 1) / threads;
+    const long long cap = (long long)sms * (per_sm > 0 ? per_sm : 1);
+    return (int)(need < 1 ? 1 : (need < cap ? need : cap));
+}
+
 template <typename T, bool VAL64, bool LIST>
 static void raster_variant(int variant, long long work, cudaStream_t s, const BlockDesc* d_blocks, int nb, int total,
                            const int* list, const int* list_count, const float4* pos, const int4* tv,
                            const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
-                           int* owner, int* fix_list, int* fix_count, Status* st, int t0 = 0, bool per_block = false)
+                           int* owner, int* fix_list, int* fix_count, Status* st, int t0 = 0, bool per_block = false,
+                           int* next = nullptr)
 {
     // the double-precision tables need more shared memory: 3 warps per block
     constexpr int NW = (sizeof(T) == 4 && !VAL64) ? 4 : 3;
-    const int nblk = grid_for(work, NW * 32, 16);
     if (per_block)
     {
         // per-block grids: one launch configuration (5 blocks per SM)
-        k_raster<T, VAL64, LIST, 5, NW, false, false, true><<<nblk, NW * 32, 0, s>>>(
+        auto kfn = k_raster<T, VAL64, LIST, 5, NW, false, false, true>;
+        kfn<<<raster_grid(kfn, NW * 32, work, next != nullptr), NW * 32, 0, s>>>(
             d_blocks, nb, total, list, list_count, pos, tv, rho32, rho64, g, tau, grid, owner, fix_list, fix_count, st,
-            t0);
+            t0, next);
         return;
     }
 #define TG_RASTER(MB, C, F, SL_)                                                                                   \
-    k_raster<T, VAL64, LIST, MB, NW, C, F, false, SL_><<<nblk, NW * 32, 0, s>>>(                                   \
-        d_blocks, nb, total, list, list_count, pos, tv, rho32, rho64, g, tau, grid, owner, fix_list, fix_count, st, t0)
+    {                                                                                                              \
+        auto kfn = k_raster<T, VAL64, LIST, MB, NW, C, F, false, SL_>;                                             \
+        kfn<<<raster_grid(kfn, NW * 32, work, next != nullptr), NW * 32, 0, s>>>(                                  \
+            d_blocks, nb, total, list, list_count, pos, tv, rho32, rho64, g, tau, grid, owner, fix_list, fix_count, \
+            st, t0, next);                                                                                         \
+    }
     switch (variant)
     {
     case 1: TG_RASTER(5, false, false, SLICES); break;
@@ -1079,7 +1114,7 @@ int raster_variants() { return N_RASTER_VARIANTS; }
 void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int total, const float4* pos,
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                    int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s, const int* order,
-                   const int* order_count, int t0, bool per_block)
+                   const int* order_count, int t0, bool per_block, int* next)
 {
     if (total <= 0) return;
     const long long work = (long long)((total + 31) / 32) * 32 * 32;
@@ -1095,10 +1130,10 @@ void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int
     }
     if (mode == TESSGPU_MODE_FP64)
         raster_variant<double, true, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                            rho64, g, tau, grid, owner, nullptr, nullptr, st, t0, per_block);
+                                            rho64, g, tau, grid, owner, nullptr, nullptr, st, t0, per_block, next);
     else
         raster_variant<float, false, false>(variant, work, s, d_blocks, nb, total, nullptr, nullptr, pos, tv, rho32,
-                                            rho64, g, tau, grid, owner, fix_list, fix_count, st, t0, per_block);
+                                            rho64, g, tau, grid, owner, fix_list, fix_count, st, t0, per_block, next);
 }
 
 // ---------------------------------------------------------------------------

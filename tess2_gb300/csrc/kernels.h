@@ -42,7 +42,7 @@ void launch_raster(int mode, int variant, const BlockDesc* d_blocks, int nb, int
                    const int4* tv, const float* rho32, const double* rho64, const GridDesc& g, float tau, float* grid,
                    int* owner, int* fix_list, int* fix_count, Status* st, cudaStream_t s,
                    const int* order = nullptr, const int* order_count = nullptr, int t0 = 0,
-                   bool per_block = false);
+                   bool per_block = false, int* next = nullptr);   // next: zeroed chunk counter (persistent)
 int  raster_variants();
 void order_bricks(const GridDesc& g, int* nbx, int* nby, int* nbz);
 void launch_tet_order(const float4* pos, const int4* tv, int total, const GridDesc& g, int* key, int* hist,
