@@ -1028,14 +1028,17 @@ extern "C" tessgpu_status tessgpu_batch_dense(tessgpu_ctx* ctx, tessgpu_batch* b
         // fixed-point scale of the star-volume sums: any star volume is below
         // the volume of the particles' bounding box; allow 8x the data box
         const double scale = star_sum_scale(dmin, dmax, p->mode == TESSGPU_MODE_FP64);
-        // once the launch variant is known, blocks run their stages on two
-        // streams in turn (as the host pipeline does), so one block's star
-        // volumes overlap another's rasteriser
+        // TESSGPU_BATCH_OVERLAP=1: once the launch variant is known, blocks run
+        // their stages on two streams in turn, so one block's star volumes
+        // overlap another's rasteriser.  Off by default: the rasteriser's
+        // persistent launches fill every SM, and two of them side by side
+        // (4.49 ms a step at 2M -> 512^3) lose to each stage over all blocks
+        // in one launch (4.37 ms).
         {
             const char* ov = getenv("TESSGPU_BATCH_OVERLAP");
             const char* oenv = getenv("TESSGPU_RASTER_ORDER");
             int known = bt->raster_variant[p->mode] >= 0 ? bt->raster_variant[p->mode] : ctx->raster_variant[p->mode];
-            if (!(ov && *ov && atoi(ov) == 0) && known >= 0 && !(oenv && atoi(oenv) == 1) && !p->project)
+            if ((ov && *ov && atoi(ov) == 1) && known >= 0 && !(oenv && atoi(oenv) == 1) && !p->project)
             {
                 bt->raster_variant[p->mode] = known;
                 if (!ctx->cs2) CK(cudaStreamCreateWithFlags(&ctx->cs2, cudaStreamNonBlocking));
@@ -2233,11 +2236,14 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     CK(cudaEventRecord(ev_setup, s));
     CK(cudaStreamWaitEvent(ctx->cs2, ev_setup, 0));
     const bool mixed = p->mode != TESSGPU_MODE_FP64;
+    // TESSGPU_PIPELINE_STREAMS=1: every block's compute on one stream
+    const char* psenv = getenv("TESSGPU_PIPELINE_STREAMS");
+    const bool two_streams = !(psenv && *psenv && atoi(psenv) == 1);
     for (int k = 0; k < nb; ++k)
     {
         const int b = order[k];
         const BlockDesc& d = hb[b];
-        cudaStream_t s = (k & 1) ? ctx->cs2 : ctx->stream;
+        cudaStream_t s = (two_streams && (k & 1)) ? ctx->cs2 : ctx->stream;
         CK(cudaStreamWaitEvent(s, k == 0 ? ctx->first_ev[0] : ctx->pipe_ev[k], 0));
         const int ec0 = smark(ctx, s);
         if (d.np)

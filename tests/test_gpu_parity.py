@@ -396,6 +396,13 @@ def test_dtfe_host_pipeline_matches_batch(gpu_ctx, dims):
         finally:
             del os.environ["TESSGPU_PIPELINE"]
         assert np.array_equal(r0["grid"], ref)
+        os.environ["TESSGPU_PIPELINE_STREAMS"] = "1"   # every block's kernels on one stream
+        try:
+            r2 = gpu_ctx.dense(DENSE_DTFE, blocks, gni, mode=mode)
+        finally:
+            del os.environ["TESSGPU_PIPELINE_STREAMS"]
+        assert np.array_equal(r2["grid"], ref)
+        assert r2["info"]["fp64_tets"] == ib["fp64_tets"]
         # pinned host arrays go through the copy engines; pageable ones (above) are read and
         # written in place by the kernels where the device addresses pageable memory
         keep, pblocks = [], []
@@ -438,8 +445,8 @@ def test_dtfe_brick_order_same_grid(gpu_ctx):
 
 
 def test_dtfe_batch_overlap_same_grid(gpu_ctx):
-    """The batch path with blocks on two streams (the default once the launch
-    variant is known) and TESSGPU_BATCH_OVERLAP=0 (stages one after the other
+    """The batch path with blocks on two streams (TESSGPU_BATCH_OVERLAP=1, once
+    the launch variant is known) and by default (stages one after the other
     over all blocks): the same grid bit for bit and the same counts."""
     import os
     import torch
@@ -448,7 +455,7 @@ def test_dtfe_batch_overlap_same_grid(gpu_ctx):
     gni = [50, 46, 54]
     for mode in (MODE_MIXED, MODE_FP64):
         out = []
-        for env in ("0", None):
+        for env in ("1", None):
             if env:
                 os.environ["TESSGPU_BATCH_OVERLAP"] = env
             try:
