@@ -1517,8 +1517,11 @@ static tessgpu_status dense_sets_rows(tessgpu_ctx* ctx, tessgpu_batch* bt, const
     auto raster = [&](cudaStream_t rs, int v) {
         CK(cudaMemsetAsync(d_out, 0, sizeof(float) * Gtot, rs));
         CK(cudaMemsetAsync(bt->fix_count, 0, sizeof(int), rs));
+        int* next = bt->fix_count + (nb + 1);   // the persistent rasteriser's chunk counter
+        CK(cudaMemsetAsync(next, 0, sizeof(int), rs));
         launch_raster(mode, v, bt->d_blocks, nb, (int)bt->T, bt->pos, bt->tv, bt->rho32, bt->rho64, g0, kTau,
-                      d_out, nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs, nullptr, nullptr, 0, true);
+                      d_out, nullptr, bt->fix_list, bt->fix_count, ctx->d_status, rs, nullptr, nullptr, 0, true,
+                      next);
         ctx->launches += bt->T ? 1 : 0;
         if (mode != TESSGPU_MODE_FP64)
         {
