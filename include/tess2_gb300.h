@@ -135,7 +135,10 @@ typedef struct tessgpu_dense_info
 /* ---- context ---------------------------------------------------------- */
 
 /* Create a context on a CUDA device; stream may be NULL (the legacy default
-   stream) or a cudaStream_t the caller owns. */
+   stream) or a cudaStream_t the caller owns.  A context and its batches are
+   used by one host thread at a time: its calls share a status word and
+   scratch buffers on the device (threads that work concurrently make one
+   context each). */
 tessgpu_status tessgpu_create(int device, void* stream, tessgpu_ctx** out);
 void           tessgpu_destroy(tessgpu_ctx* ctx);
 const char*    tessgpu_last_error(const tessgpu_ctx* ctx);
