@@ -149,11 +149,10 @@ long long      tessgpu_launch_count(const tessgpu_ctx* ctx);
 /* Stage timing: when on, every dense call records CUDA events on the
    context's stream between its stages; tessgpu_stage_times then returns up to
    cap (name, milliseconds) pairs of the last call (after it has finished).
-   When a DTFE batch runs its blocks on two streams (the default once the
-   rasteriser's launch variant is chosen; TESSGPU_BATCH_OVERLAP=0 runs the
-   stages one after the other over all blocks instead), the per-stage entries
-   are sums over the blocks of spans timed on each block's stream, which
-   overlap one another; the pipelined host-buffer DTFE call reports its
+   When a DTFE batch runs its blocks on two streams (TESSGPU_BATCH_OVERLAP=1;
+   by default each stage runs over all blocks in one launch), the per-stage
+   entries are sums over the blocks of spans timed on each block's stream,
+   which overlap one another; the pipelined host-buffer DTFE call reports its
    upload, compute and download spans the same way. */
 tessgpu_status tessgpu_set_timing(tessgpu_ctx* ctx, int on);
 int            tessgpu_stage_times(tessgpu_ctx* ctx, const char** names, float* ms, int cap);
