@@ -1977,19 +1977,49 @@ __global__ void k_store_box(const float* __restrict__ grid, float* host, int nx,
                             int bx, int by, int bz)
 {
     const long long rows = (long long)by * bz;
+    // 16-byte accesses when every row starts on a 16-byte boundary at both ends
+    const bool v4 = ((x0 | bx | nx) & 3) == 0 && (((size_t)host | (size_t)grid) & 15) == 0;
     for (long long r = blockIdx.x; r < rows; r += gridDim.x)
     {
         const int y = y0 + (int)(r % by), z = z0 + (int)(r / by);
         const size_t base = ((size_t)z * ny + y) * nx + x0;
-        for (int x = threadIdx.x; x < bx; x += blockDim.x) host[base + x] = grid[base + x];
+        if (v4)
+        {
+            const float4* src = reinterpret_cast<const float4*>(grid + base);
+            float4* dst = reinterpret_cast<float4*>(host + base);
+            for (int x = threadIdx.x; x < (bx >> 2); x += blockDim.x) dst[x] = __ldg(src + x);
+        }
+        else
+            for (int x = threadIdx.x; x < bx; x += blockDim.x) host[base + x] = grid[base + x];
     }
 }
 
 // n floats into a host array the device addresses directly
 __global__ void k_store_run(const float* __restrict__ src, float* dst, size_t n)
 {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if ((((size_t)src | (size_t)dst) & 15) == 0)
+    {
+        const size_t n4 = n >> 2;
+        for (size_t i = i0; i < n4; i += stride)
+            reinterpret_cast<float4*>(dst)[i] = __ldg(reinterpret_cast<const float4*>(src) + i);
+        i0 += n4 << 2;
+    }
+    for (size_t i = i0; i < n; i += stride)
         dst[i] = src[i];
+}
+
+// CTAs of a kernel that reads or writes host memory directly: each waits on
+// the host link for most of its life, so a few keep the link busy and leave
+// the SMs to the compute streams (TESSGPU_HOSTIO_CTAS overrides).  At 2M ->
+// 512^3 from pageable arrays: 304 CTAs 8.2 ms a call, 192 7.3-7.5, 128
+// 7.3-7.4, 96 7.5, 64 8.9 (the download then waits on the link).
+static int hostio_ctas()
+{
+    const char* e = getenv("TESSGPU_HOSTIO_CTAS");
+    const int n = e && *e ? atoi(e) : 0;
+    return n > 0 ? n : 128;
 }
 
 // one block's tet_t vertices -> batch-wide particle indices, checked
@@ -2190,10 +2220,33 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         const int eu0 = smark(ctx, ctx->h2d);
         if (direct_in)
         {
-            // nothing to copy: the events complete at once
+            // the block's arrays are read where they lie, by kernels on this
+            // stream (the copy engines' place when the arrays are pinned), so
+            // they run ahead of the compute streams as the copies do; few CTAs,
+            // since each mostly waits on the host link
+            if (d.np)
+            {
+                k_pack_block<<<std::min(grid_small(d.np), hostio_ctas()), 256, 0, ctx->h2d>>>(blocks[b].particles,
+                                                                                               d.np, pos + d.p_off);
+                ctx->launches++;
+            }
             if (k == 0)
-                for (int i = 0; i < 1 + kFirstParts; ++i) CK(cudaEventRecord(ctx->first_ev[i], ctx->h2d));
+                CK(cudaEventRecord(ctx->first_ev[0], ctx->h2d));
+            for (int i = 0; i < (k == 0 ? kFirstParts : 1); ++i)
+            {
+                const long long t0 = k == 0 ? part(d, i) : 0, t1 = k == 0 ? part(d, i + 1) : d.nt;
+                if (t1 > t0)
+                {
+                    k_ingest_verts<<<std::min(grid_small(t1 - t0), hostio_ctas()), 256, 0, ctx->h2d>>>(
+                        reinterpret_cast<const int4*>(blocks[b].tets) + 2 * (size_t)t0, (int)(t1 - t0), d.np, d.p_off,
+                        tv + d.t_off + t0, ctx->d_status);
+                    ctx->launches++;
+                }
+                if (k == 0)
+                    CK(cudaEventRecord(ctx->first_ev[1 + i], ctx->h2d));
+            }
             CK(cudaEventRecord(ctx->pipe_ev[k], ctx->h2d));
+            span(ctx, "upload", eu0, smark(ctx, ctx->h2d));
             continue;
         }
         if (k == 0)
@@ -2251,10 +2304,12 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         const int ec0 = smark(ctx, s);
         if (d.np)
         {
-            k_pack_block<<<grid_small(d.np), 256, 0, s>>>(direct_in ? blocks[b].particles : stage_xyz + 3 * (size_t)d.p_off,
-                                                          d.np, pos + d.p_off);
+            if (!direct_in)   // (direct: packed on the upload stream)
+            {
+                k_pack_block<<<grid_small(d.np), 256, 0, s>>>(stage_xyz + 3 * (size_t)d.p_off, d.np, pos + d.p_off);
+                ctx->launches++;
+            }
             CK(cudaMemsetAsync(W + d.p_off, 0, sizeof(StarSum) * d.np, s));
-            ctx->launches++;
         }
         if (bricks)
             bricks_reset(ctx, hb, b, b + 1, nbricks, bins, s);
@@ -2265,11 +2320,13 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
             if (k == 0)
                 CK(cudaStreamWaitEvent(s, ctx->first_ev[1 + i], 0));
             if (t1 <= t0) continue;
-            const int4* src = direct_in ? reinterpret_cast<const int4*>(blocks[b].tets) + 2 * (size_t)t0
-                                        : stage_tets + 2 * ((size_t)d.t_off + t0);
-            k_ingest_verts<<<grid_small(t1 - t0), 256, 0, s>>>(src, (int)(t1 - t0), d.np, d.p_off, tv + d.t_off + t0,
-                                                                ctx->d_status);
-            ctx->launches++;
+            if (!direct_in)   // (direct: ingested on the upload stream)
+            {
+                k_ingest_verts<<<grid_small(t1 - t0), 256, 0, s>>>(stage_tets + 2 * ((size_t)d.t_off + t0),
+                                                                    (int)(t1 - t0), d.np, d.p_off, tv + d.t_off + t0,
+                                                                    ctx->d_status);
+                ctx->launches++;
+            }
             if (bricks)
                 bricks_star(ctx, p->mode, variant, d_blocks, nb, d.t_off + t0, t1 - t0, pos, tv, W, scale, g, bins, s);
             else
@@ -2327,7 +2384,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
                 const long long rows = (long long)by * bz;
                 if (rows > 0 && bx > 0)
                 {
-                    k_store_box<<<(unsigned)std::min(rows, 2LL * 152), 256, 0, ctx->d2h>>>(
+                    k_store_box<<<(unsigned)std::min(rows, (long long)hostio_ctas()), 256, 0, ctx->d2h>>>(
                         grid, host_grid, nx, ny, d.gmin_idx[0], d.gmin_idx[1], d.gmin_idx[2], bx, by, bz);
                     ctx->launches++;
                 }
@@ -2344,7 +2401,7 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
                 const size_t off = (size_t)slab_lo[l] * area, n = (size_t)(slab_hi[l] - slab_lo[l] + 1) * area;
                 if (direct_out)
                 {
-                    k_store_run<<<2 * 152, 256, 0, ctx->d2h>>>(grid + off, host_grid + off, n);
+                    k_store_run<<<hostio_ctas(), 256, 0, ctx->d2h>>>(grid + off, host_grid + off, n);
                     ctx->launches++;
                 }
                 else
