@@ -2202,6 +2202,9 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
     ctx->nsev = 0;
     ctx->spans.clear();
     mark(ctx, "start");
+    // the status word is zeroed first: the upload stream's ingest kernels may
+    // report into it (pageable arrays read in place)
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
     // the copy streams start after whatever the compute stream was doing with the pool
     cudaEvent_t ev0 = ctx->pipe_ev[2 * nb];
     CK(cudaEventRecord(ev0, s));
@@ -2277,7 +2280,6 @@ static tessgpu_status dense_dtfe_pipelined(tessgpu_ctx* ctx, int nb, const tessg
         span(ctx, "upload", eu0, smark(ctx, ctx->h2d));
     }
     CK(cudaMemcpyAsync(d_blocks, hb.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(Status), s));
     // the brick rasteriser writes every point of the blocks' boxes
     if (!bricks || !tiles)
         CK(cudaMemsetAsync(grid, 0, sizeof(float) * G, s));
