@@ -56,6 +56,9 @@ def parse():
                     help="clump sigmas log-uniform in [lo, hi] instead of --sigma")
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-spans", action="store_true",
+                    help="print the host-buffer call's per-stream spans (upload, compute, download), pinned and "
+                         "pageable arrays, on a '# e2e spans' line")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the FP64-mode and DENSE_TESS comparison runs")
     ap.add_argument("--no-surrogate", action="store_true",
@@ -748,6 +751,20 @@ def run_gpu(args):
         for _ in range(ke):
             ctx.dense(DENSE_DTFE, pblocks, gni, out=pout)
         tp = (time.perf_counter() - t0) / ke
+        if args.e2e_spans:
+            spans = {}
+            for name, bl, o in (("pinned", hblocks, out), ("pageable", pblocks, pout),
+                                ("pageable in, pinned out", pblocks, out), ("pinned in, pageable out", hblocks, pout)):
+                ctx.dense(DENSE_DTFE, bl, gni, out=o)
+                runs = []
+                ctx.set_timing(True)
+                for _ in range(5):   # the call with the median time to the last block
+                    ctx.dense(DENSE_DTFE, bl, gni, out=o)
+                    runs.append({k: round(v, 3) for k, v in ctx.stage_times()})
+                ctx.set_timing(False)
+                runs.sort(key=lambda r: r.get("blocks_done", 0.0) + r.get("downloads_done", 0.0))
+                spans[name] = runs[len(runs) // 2]
+            print("# e2e spans " + json.dumps(spans), flush=True)
         e2e = dict(value=G / te, unit=UNIT, ms_per_step=te * 1e3, h2d_bytes_per_step=int(h2d),
                    d2h_bytes_per_step=int(4 * G), api="tessgpu_dense (host buffers, pinned)",
                    pageable=dict(value=G / tp, ms_per_step=tp * 1e3,
