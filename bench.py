@@ -675,6 +675,20 @@ def run_gpu(args):
                                        achieved_gbs=tb / (mst * 1e-3) / 1e9, hbm_frac=tb / (mst * 1e-3) / 1e9 / hbm,
                                        achieved_gflops=tf / (mst * 1e-3) / 1e9,
                                        fp32_frac_of_nominal=tf / (mst * 1e-3) / fp32_nominal)
+        # Voronoi cell volumes as the reference computes them (float,
+        # bit-identical to its volume()) against FP64 cell volumes, for
+        # block 0's own particles
+        b0 = blocks[0]
+        n0 = int(b0["num_orig"])
+        v32 = ctx.volume(b0["vert_to_tet"], b0["tets"], b0["particles"], n=n0)
+        v64 = ctx.volume_f64(b0["vert_to_tet"], b0["tets"], b0["particles"], n=n0)
+        fin = (v32 > 0) & (v64 > 0)
+        dv = v32[fin].astype(np.float64) - v64[fin]
+        extra["cell_volume_vs_fp64"] = dict(
+            cells=n0, finite=int(fin.sum()), rel_l2=float(np.linalg.norm(dv) / max(np.linalg.norm(v64[fin]), 1e-300)),
+            max_rel=float(np.max(np.abs(dv) / v64[fin])) if fin.any() else 0.0,
+            infinite_cells_agree=bool(np.array_equal(v32 < 0, v64 < 0)),
+            sample="block 0's own particles; float volumes bit-identical to the reference's volume()")
 
     # roofline of the dominant kernel: the mixed rasteriser.  Algorithmic bytes
     # per launch of the brick kernel: the pair list 4 B per (tet, brick) pair,
